@@ -1,0 +1,1097 @@
+/*
+ * espic_oracle.c -- CPU restatement of the ES-PIC hot path of "Plasma
+ * Simulations by Example".  TEST INFRASTRUCTURE ONLY: the parity checker for
+ * the CUDA path, never part of the product.  See espic_oracle.h for the data
+ * conventions.  Each function cites the reference code it restates.
+ *
+ * Deliberate, documented departures from the reference (the CUDA path makes
+ * the same ones, so the two agree):
+ *  - gather/scatter clamp the cell index to [0, n-2] per axis.  The reference
+ *    reads and writes index n when a particle sits exactly on the max face
+ *    after a one-bounce reflection (ch2/Species.cpp:32-36 with
+ *    ch2/Field.h:164-208); the clamp keeps the same interpolation weights
+ *    (di = 1) without the out-of-bounds access.
+ *  - node volumes are allocated (ni,nj,nk); the reference allocates
+ *    (ni,nk,nk) (ch2/World.cpp:16) which is only safe when nj <= nk.
+ */
+#include "espic_oracle.h"
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NODE(g, i, j, k) ((int64_t)(k) * (g)->ni * (g)->nj + (int64_t)(j) * (g)->ni + (i))
+
+/* ------------------------------------------------------------------------ */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11).  Counter = (index/2 lo, hi, stream lo, hi),
+ * key = seed.  Each block gives two 53-bit uniforms in [0,1).             */
+void eo_philox4x32(uint32_t c[4], const uint32_t key[2]) {
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c[1] ^ k0;
+        uint32_t n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+static double u53(uint32_t a, uint32_t b) {
+    uint64_t x = (((uint64_t)a << 32) | b) >> 11;
+    return (double)x * (1.0 / 9007199254740992.0);
+}
+
+double eo_philox_uniform(uint64_t seed, uint64_t stream, uint64_t index) {
+    uint64_t blk = index >> 1;
+    uint32_t c[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), (uint32_t)stream,
+                     (uint32_t)(stream >> 32)};
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    eo_philox4x32(c, key);
+    return (index & 1) ? u53(c[2], c[3]) : u53(c[0], c[1]);
+}
+
+void eo_philox_uniforms(uint64_t seed, uint64_t stream, uint64_t first, int64_t n, double *out) {
+    for (int64_t i = 0; i < n; i++) out[i] = eo_philox_uniform(seed, stream, first + (uint64_t)i);
+}
+
+/* ------------------------------------------------------------------------ */
+/* World::setExtents, ch2/World.cpp:22-36 */
+void eo_grid_set(eo_grid *g, int ni, int nj, int nk, const double x0[3], const double xm[3]) {
+    int nn[3] = {ni, nj, nk};
+    g->ni = ni;
+    g->nj = nj;
+    g->nk = nk;
+    g->pad = 0;
+    for (int d = 0; d < 3; d++) {
+        g->x0[d] = x0[d];
+        g->xm[d] = xm[d];
+        g->dh[d] = (xm[d] - x0[d]) / (nn[d] - 1);
+    }
+}
+
+/* World::computeNodeVolumes, ch2/World.cpp:58-69 */
+void eo_node_volumes(const eo_grid *g, double *vol) {
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                double V = g->dh[0] * g->dh[1] * g->dh[2];
+                if (i == 0 || i == g->ni - 1) V *= 0.5;
+                if (j == 0 || j == g->nj - 1) V *= 0.5;
+                if (k == 0 || k == g->nk - 1) V *= 0.5;
+                vol[NODE(g, i, j, k)] = V;
+            }
+}
+
+/* World::XtoL, ch2/World.h:72-78 */
+void eo_xtol(const eo_grid *g, const double x[3], double lc[3]) {
+    for (int d = 0; d < 3; d++) lc[d] = (x[d] - g->x0[d]) / g->dh[d];
+}
+
+/* World::inBounds, ch2/World.h:59-63 */
+int eo_in_bounds(const eo_grid *g, const double x[3]) {
+    for (int d = 0; d < 3; d++)
+        if (x[d] < g->x0[d] || x[d] >= g->xm[d]) return 0;
+    return 1;
+}
+
+static inline int clampi(int i, int n) {
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    return i;
+}
+
+/* Cell index and in-cell fraction: (int) truncation as in Field_::gather,
+ * ch2/Field.h:188-196, plus the index clamp described at the top. */
+static inline void cell_of(const eo_grid *g, const double lc[3], int ijk[3], double f[3]) {
+    int n[3] = {g->ni, g->nj, g->nk};
+    for (int d = 0; d < 3; d++) {
+        int i = clampi((int)lc[d], n[d]);
+        ijk[d] = i;
+        f[d] = lc[d] - i;
+    }
+}
+
+/* Field_<double3>::gather, ch2/Field.h:186-208: 8 terms in the reference's
+ * corner order, each term ((E*(1-di))*(1-dj))*(1-dk), summed left to right. */
+void eo_gather3(const eo_grid *g, const double *ef, const double lc[3], double out[3]) {
+    int c[3];
+    double f[3];
+    cell_of(g, lc, c, f);
+    double di = f[0], dj = f[1], dk = f[2];
+    int64_t n000 = NODE(g, c[0], c[1], c[2]);
+    int64_t sx = 1, sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    int64_t idx[8] = {n000,           n000 + sx,           n000 + sx + sy,      n000 + sy,
+                      n000 + sz,      n000 + sx + sz,      n000 + sx + sy + sz, n000 + sy + sz};
+    for (int d = 0; d < 3; d++) {
+        double v = ef[idx[0] * 3 + d] * (1 - di) * (1 - dj) * (1 - dk) +
+                   ef[idx[1] * 3 + d] * (di) * (1 - dj) * (1 - dk) +
+                   ef[idx[2] * 3 + d] * (di) * (dj) * (1 - dk) +
+                   ef[idx[3] * 3 + d] * (1 - di) * (dj) * (1 - dk) +
+                   ef[idx[4] * 3 + d] * (1 - di) * (1 - dj) * (dk) +
+                   ef[idx[5] * 3 + d] * (di) * (1 - dj) * (dk) +
+                   ef[idx[6] * 3 + d] * (di) * (dj) * (dk) +
+                   ef[idx[7] * 3 + d] * (1 - di) * (dj) * (dk);
+        out[d] = v;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Species::advance (box), ch2/Species.cpp:7-38: gather, v += E*(dt*q/m),
+ * x += v*dt, one-bounce mirror reflection on every wall. */
+void eo_push_box(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                 double *P, int64_t stride, int64_t n) {
+    double s = dt * charge / mass;
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        double lc[3], e[3];
+        eo_xtol(g, x, lc);
+        eo_gather3(g, ef, lc, e);
+        for (int d = 0; d < 3; d++) v[d] += e[d] * s;
+        for (int d = 0; d < 3; d++) x[d] += v[d] * dt;
+        for (int d = 0; d < 3; d++) {
+            if (x[d] < g->x0[d]) {
+                x[d] = 2 * g->x0[d] - x[d];
+                v[d] *= -1.0;
+            } else if (x[d] >= g->xm[d]) {
+                x[d] = 2 * g->xm[d] - x[d];
+                v[d] *= -1.0;
+            }
+        }
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + p] = x[d];
+            P[(3 + d) * stride + p] = v[d];
+        }
+    }
+}
+
+/* World::inSphere, ch3/ver2/World.cpp:119-126.  sphere = {cx, cy, cz, r^2}. */
+static inline int in_sphere(const double sphere[4], const double x[3]) {
+    double r0 = x[0] - sphere[0], r1 = x[1] - sphere[1], r2 = x[2] - sphere[2];
+    double rm2 = r0 * r0 + r1 * r1 + r2 * r2;
+    return rm2 <= sphere[3];
+}
+
+/* Species::advance (sphere), ch3/ver2/Species.cpp:7-33: same push; a particle
+ * inside the sphere or out of the domain gets mpw = 0.  Returns the number
+ * killed.  Compaction is a separate call. */
+int64_t eo_push_sphere(const eo_grid *g, const double *ef, const double sphere[4], double charge,
+                       double mass, double dt, double *P, int64_t stride, int64_t n) {
+    double s = dt * charge / mass;
+    int64_t killed = 0;
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        double lc[3], e[3];
+        eo_xtol(g, x, lc);
+        eo_gather3(g, ef, lc, e);
+        for (int d = 0; d < 3; d++) v[d] += e[d] * s;
+        for (int d = 0; d < 3; d++) x[d] += v[d] * dt;
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + p] = x[d];
+            P[(3 + d) * stride + p] = v[d];
+        }
+        if (in_sphere(sphere, x) || !eo_in_bounds(g, x)) {
+            P[6 * stride + p] = 0;
+            killed++;
+        }
+    }
+    return killed;
+}
+
+static inline void copy_particle(double *P, int64_t stride, int64_t dst, int64_t src) {
+    for (int c = 0; c < 7; c++) P[c * stride + dst] = P[c * stride + src];
+}
+
+/* Removal step of ch3/ver2/Species.cpp:35-46: a dead slot (mpw <= 0) is
+ * filled with the last particle and re-checked. */
+int64_t eo_compact_swap_last(double *P, int64_t stride, int64_t n) {
+    int64_t np = n;
+    for (int64_t p = 0; p < np; p++) {
+        if (P[6 * stride + p] > 0) continue;
+        copy_particle(P, stride, p, np - 1);
+        np--;
+        p--;
+    }
+    return np;
+}
+
+/* The CUDA path's deterministic in-place compaction: with n_new live
+ * particles, the r-th dead slot below n_new (in index order) receives the
+ * r-th live particle at or above n_new.  Same survivors as the reference,
+ * different order. */
+int64_t eo_compact_holes(double *P, int64_t stride, int64_t n) {
+    int64_t alive = 0;
+    for (int64_t p = 0; p < n; p++) alive += P[6 * stride + p] > 0;
+    int64_t hole = 0;
+    for (int64_t src = alive; src < n; src++) {
+        if (!(P[6 * stride + src] > 0)) continue;
+        while (P[6 * stride + hole] > 0) hole++;
+        copy_particle(P, stride, hole, src);
+        hole++;
+    }
+    return alive;
+}
+
+/* Species::addParticle, ch2/Species.cpp:55-71: reject outside [x0,xm),
+ * rewind v by (q/m)*E*(dt/2), append. */
+int64_t eo_add_particles(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                         const double *pos3, const double *vel3, const double *w, int64_t n,
+                         double *P, int64_t stride, int64_t np0, int64_t cap) {
+    int64_t np = np0;
+    double qm = charge / mass;
+    for (int64_t p = 0; p < n; p++) {
+        const double *x = pos3 + 3 * p;
+        if (!eo_in_bounds(g, x)) continue;
+        if (np >= cap) return -1;
+        double lc[3], e[3], v[3];
+        eo_xtol(g, x, lc);
+        eo_gather3(g, ef, lc, e);
+        for (int d = 0; d < 3; d++) v[d] = vel3[3 * p + d] - e[d] * qm * (0.5 * dt);
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + np] = x[d];
+            P[(3 + d) * stride + np] = v[d];
+        }
+        P[6 * stride + np] = w[p];
+        np++;
+    }
+    return np;
+}
+
+/* Species::loadParticlesBox, ch2/Species.cpp:74-97, with the uniforms given
+ * explicitly (3 per particle, x then y then z). */
+int64_t eo_load_box(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                    const double x1[3], const double x2[3], double num_den, int64_t num_mp,
+                    const double *u, double *P, int64_t stride, int64_t np0, int64_t cap) {
+    double box_vol = (x2[0] - x1[0]) * (x2[1] - x1[1]) * (x2[2] - x1[2]);
+    double num_real = num_den * box_vol;
+    double mpw = num_real / (double)num_mp;
+    int64_t np = np0;
+    for (int64_t p = 0; p < num_mp; p++) {
+        double pos[3], vel[3] = {0, 0, 0};
+        for (int d = 0; d < 3; d++) pos[d] = x1[d] + u[3 * p + d] * (x2[d] - x1[d]);
+        np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &mpw, 1, P, stride, np, cap);
+        if (np < 0) return -1;
+    }
+    return np;
+}
+
+/* Species::loadParticlesBoxQS, ch2/Species.cpp:101-141 */
+int64_t eo_load_box_qs(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       const double x1[3], const double x2[3], double num_den, const int num_mp[3],
+                       double *P, int64_t stride, int64_t np0, int64_t cap) {
+    double box_vol = (x2[0] - x1[0]) * (x2[1] - x1[1]) * (x2[2] - x1[2]);
+    int num_mp_tot = (num_mp[0] - 1) * (num_mp[1] - 1) * (num_mp[2] - 1);
+    double num_real = num_den * box_vol;
+    double mpw = num_real / num_mp_tot;
+    double di = (x2[0] - x1[0]) / (num_mp[0] - 1);
+    double dj = (x2[1] - x1[1]) / (num_mp[1] - 1);
+    double dk = (x2[2] - x1[2]) / (num_mp[2] - 1);
+    int64_t np = np0;
+    for (int i = 0; i < num_mp[0]; i++)
+        for (int j = 0; j < num_mp[1]; j++)
+            for (int k = 0; k < num_mp[2]; k++) {
+                double pos[3], vel[3] = {0, 0, 0};
+                pos[0] = x1[0] + i * di;
+                pos[1] = x1[1] + j * dj;
+                pos[2] = x1[2] + k * dk;
+                if (pos[0] == x2[0]) pos[0] -= 1e-4 * di;
+                if (pos[1] == x2[1]) pos[1] -= 1e-4 * dj;
+                if (pos[2] == x2[2]) pos[2] -= 1e-4 * dk;
+                double w = 1;
+                if (i == 0 || i == num_mp[0] - 1) w *= 0.5;
+                if (j == 0 || j == num_mp[1] - 1) w *= 0.5;
+                if (k == 0 || k == num_mp[2] - 1) w *= 0.5;
+                double ww = mpw * w;
+                np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &ww, 1, P, stride, np, cap);
+                if (np < 0) return -1;
+            }
+    return np;
+}
+
+/* Number of macroparticles a beam source creates this step,
+ * ch3/ver2/Source.cpp:7-18: (int)(n*v*A*dt/mpw0 + U). */
+int eo_inject_count(const eo_grid *g, double dt, double mpw0, double v_drift, double den,
+                    double u0) {
+    double Lx = g->dh[0] * (g->ni - 1);
+    double Ly = g->dh[1] * (g->nj - 1);
+    double A = Lx * Ly;
+    double num_real = den * v_drift * A * dt;
+    return (int)(num_real / mpw0 + u0);
+}
+
+/* ColdBeamSource::sample, ch3/ver2/Source.cpp:4-27.  Uniform order: count,
+ * then (x, y) per particle. */
+int64_t eo_inject_cold(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, const double *u, int64_t *u_used,
+                       double *P, int64_t stride, int64_t np0, int64_t cap) {
+    double Lx = g->dh[0] * (g->ni - 1);
+    double Ly = g->dh[1] * (g->nj - 1);
+    int num_sim = eo_inject_count(g, dt, mpw0, v_drift, den, u[0]);
+    int64_t np = np0;
+    for (int i = 0; i < num_sim; i++) {
+        double pos[3] = {g->x0[0] + u[1 + 2 * i] * Lx, g->x0[1] + u[2 + 2 * i] * Ly, g->x0[2]};
+        double vel[3] = {0, 0, v_drift};
+        np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &mpw0, 1, P, stride, np, cap);
+        if (np < 0) return -1;
+    }
+    if (u_used) *u_used = 1 + 2 * (int64_t)num_sim;
+    return np;
+}
+
+/* Species::sampleVth and Species::sampleIsotropicVel, ch4/Species.cpp:149-175.
+ * u: theta, r, then 9 uniforms for the three speed components. */
+static void isotropic_vel(double mass, double temp, const double *u, double out[3]) {
+    double theta = 2 * EO_PI * u[0];
+    double r = -1.0 + 2 * u[1];
+    double a = sqrt(1 - r * r);
+    double d[3] = {r, cos(theta) * a, sin(theta) * a};
+    double v_th = sqrt(2 * EO_K * temp / mass);
+    double v1 = v_th * (u[2] + u[3] + u[4] - 1.5);
+    double v2 = v_th * (u[5] + u[6] + u[7] - 1.5);
+    double v3 = v_th * (u[8] + u[9] + u[10] - 1.5);
+    double speed = 3 / sqrt(2 + 2 + 2) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    for (int c = 0; c < 3; c++) out[c] = d[c] * speed;
+}
+
+/* WarmBeamSource::sample, ch4/Source.cpp:31-55: cold-beam positions plus an
+ * isotropic thermal velocity, drift added to z.  13 uniforms per particle. */
+int64_t eo_inject_warm(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, double temp, const double *u,
+                       int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap) {
+    double Lx = g->dh[0] * (g->ni - 1);
+    double Ly = g->dh[1] * (g->nj - 1);
+    int num_sim = eo_inject_count(g, dt, mpw0, v_drift, den, u[0]);
+    int64_t np = np0;
+    for (int i = 0; i < num_sim; i++) {
+        const double *ui = u + 1 + 13 * (int64_t)i;
+        double pos[3] = {g->x0[0] + ui[0] * Lx, g->x0[1] + ui[1] * Ly, g->x0[2]};
+        double vel[3];
+        isotropic_vel(mass, temp, ui + 2, vel);
+        vel[2] += v_drift;
+        np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &mpw0, 1, P, stride, np, cap);
+        if (np < 0) return -1;
+    }
+    if (u_used) *u_used = 1 + 13 * (int64_t)num_sim;
+    return np;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Corner weights of Field_::scatter, ch2/Field.h:164-183, in the reference's
+ * corner order: value*(1-di)*(1-dj)*(1-dk) evaluated left to right. */
+static inline void cic_weights(double value, double di, double dj, double dk, double w[8]) {
+    w[0] = value * (1 - di) * (1 - dj) * (1 - dk);
+    w[1] = value * (di) * (1 - dj) * (1 - dk);
+    w[2] = value * (di) * (dj) * (1 - dk);
+    w[3] = value * (1 - di) * (dj) * (1 - dk);
+    w[4] = value * (1 - di) * (1 - dj) * (dk);
+    w[5] = value * (di) * (1 - dj) * (dk);
+    w[6] = value * (di) * (dj) * (dk);
+    w[7] = value * (1 - di) * (dj) * (dk);
+}
+
+static inline void cic_nodes(const eo_grid *g, const int c[3], int64_t idx[8]) {
+    int64_t n000 = NODE(g, c[0], c[1], c[2]);
+    int64_t sx = 1, sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    idx[0] = n000;
+    idx[1] = n000 + sx;
+    idx[2] = n000 + sx + sy;
+    idx[3] = n000 + sy;
+    idx[4] = n000 + sz;
+    idx[5] = n000 + sx + sz;
+    idx[6] = n000 + sx + sy + sz;
+    idx[7] = n000 + sy + sz;
+}
+
+/* Species::computeNumberDensity scatter loop, ch2/Species.cpp:41-49, FP64 sum
+ * in particle order (the reference's own arithmetic). */
+void eo_deposit_fp64(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *acc) {
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double lc[3], f[3], w[8];
+        int c[3];
+        int64_t idx[8];
+        eo_xtol(g, x, lc);
+        cell_of(g, lc, c, f);
+        cic_weights(P[6 * stride + p], f[0], f[1], f[2], w);
+        cic_nodes(g, c, idx);
+        for (int m = 0; m < 8; m++) acc[idx[m]] += w[m];
+    }
+}
+
+/* The CUDA path's deposit: each corner weight is rounded once to a 64-bit
+ * integer in units of 1/fx (fx a power of two) and summed exactly, so the
+ * total does not depend on particle order. */
+void eo_deposit_fixed(const eo_grid *g, const double *P, int64_t stride, int64_t n, double fx,
+                      int64_t *acc) {
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double lc[3], f[3], w[8];
+        int c[3];
+        int64_t idx[8];
+        eo_xtol(g, x, lc);
+        cell_of(g, lc, c, f);
+        cic_weights(P[6 * stride + p], f[0], f[1], f[2], w);
+        cic_nodes(g, c, idx);
+        for (int m = 0; m < 8; m++) acc[idx[m]] += (int64_t)llrint(w[m] * fx);
+    }
+}
+
+/* Field_::operator/=, ch2/Field.h:125-134: divide, or 0 where vol == 0. */
+void eo_divide_volume(int64_t nn, double *den, const double *vol) {
+    for (int64_t u = 0; u < nn; u++) {
+        if (vol[u] != 0)
+            den[u] /= vol[u];
+        else
+            den[u] = 0;
+    }
+}
+
+void eo_density_from_fixed(int64_t nn, const int64_t *acc, double inv_fx, const double *vol,
+                           double *den) {
+    for (int64_t u = 0; u < nn; u++) den[u] = (double)acc[u] * inv_fx;
+    eo_divide_volume(nn, den, vol);
+}
+
+/* World::computeChargeDensity, ch2/World.cpp:46-54: rho = 0; rho += q_s*den_s
+ * for each charged species.  dens is [ns][nn]. */
+void eo_charge_density(int64_t nn, int ns, const double *charges, const double *dens, double *rho) {
+    for (int64_t u = 0; u < nn; u++) rho[u] = 0;
+    for (int s = 0; s < ns; s++) {
+        if (charges[s] == 0) continue;
+        const double *d = dens + (int64_t)s * nn;
+        for (int64_t u = 0; u < nn; u++) rho[u] += d[u] * charges[s];
+    }
+}
+
+/* Exponent S of the fixed-point scale fx = 2^S: the largest S with
+ * capacity * weight_bound * 2^S <= 2^62, so that no node total can overflow
+ * a signed 64-bit integer; capped at 52. */
+int eo_fixed_scale_exponent(double weight_bound, int64_t capacity) {
+    if (capacity < 1) capacity = 1;
+    if (!(weight_bound > 0)) weight_bound = 1;
+    double lim = ldexp(1.0, 62) / ((double)capacity * weight_bound);
+    int e;
+    frexp(lim, &e); /* lim = m*2^e, m in [0.5,1) -> 2^(e-1) <= lim */
+    int S = e - 1;
+    if (S > 52) S = 52;
+    return S;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Residual of PotentialSolver::solve, ch2/PotentialSolver.cpp:44-61. */
+double eo_residual_box(const eo_grid *g, const double *phi, const double *rho) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    double sum = 0;
+    for (int i = 1; i < g->ni - 1; i++)
+        for (int j = 1; j < g->nj - 1; j++)
+            for (int k = 1; k < g->nk - 1; k++) {
+                int64_t u = NODE(g, i, j, k);
+                double R = -phi[u] * (2 * idx2 + 2 * idy2 + 2 * idz2) + rho[u] / EO_EPS_0 +
+                           idx2 * (phi[u - 1] + phi[u + 1]) + idy2 * (phi[u - sy] + phi[u + sy]) +
+                           idz2 * (phi[u - sz] + phi[u + sz]);
+                sum += R * R;
+            }
+    return sqrt(sum / (g->ni * g->nj * g->nk));
+}
+
+static inline void sor_box_node(const eo_grid *g, double *phi, const double *rho, int64_t u,
+                                double idx2, double idy2, double idz2) {
+    int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    double phi_new = (rho[u] / EO_EPS_0 + idx2 * (phi[u - 1] + phi[u + 1]) +
+                      idy2 * (phi[u - sy] + phi[u + sy]) + idz2 * (phi[u - sz] + phi[u + sz])) /
+                     (2 * idx2 + 2 * idy2 + 2 * idz2);
+    phi[u] = phi[u] + 1.4 * (phi_new - phi[u]);
+}
+
+/* PotentialSolver::solve, ch2/PotentialSolver.cpp:11-67: lexicographic
+ * SOR (omega 1.4) over interior nodes, residual every 25 iterations. */
+int eo_sor_box_lex(const eo_grid *g, double *phi, const double *rho, int max_it, double tol,
+                   double *l2_out, int *it_out) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    double L2 = 0;
+    int conv = 0, it;
+    for (it = 0; it < max_it; it++) {
+        for (int i = 1; i < g->ni - 1; i++)
+            for (int j = 1; j < g->nj - 1; j++)
+                for (int k = 1; k < g->nk - 1; k++)
+                    sor_box_node(g, phi, rho, NODE(g, i, j, k), idx2, idy2, idz2);
+        if (it % 25 == 0) {
+            L2 = eo_residual_box(g, phi, rho);
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (l2_out) *l2_out = L2;
+    if (it_out) *it_out = conv ? it + 1 : it;
+    return conv;
+}
+
+/* The CUDA path's red-black ordering of the same SOR: colour (i+j+k)&1, red
+ * (0) then black (1), same node formula, same residual schedule. */
+int eo_sor_box_rb(const eo_grid *g, double *phi, const double *rho, int max_it, double tol,
+                  double *l2_out, int *it_out) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    double L2 = 0;
+    int conv = 0, it;
+    for (it = 0; it < max_it; it++) {
+        for (int colour = 0; colour < 2; colour++)
+            for (int k = 1; k < g->nk - 1; k++)
+                for (int j = 1; j < g->nj - 1; j++)
+                    for (int i = 1; i < g->ni - 1; i++)
+                        if (((i + j + k) & 1) == colour)
+                            sor_box_node(g, phi, rho, NODE(g, i, j, k), idx2, idy2, idz2);
+        if (it % 25 == 0) {
+            L2 = eo_residual_box(g, phi, rho);
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (l2_out) *l2_out = L2;
+    if (it_out) *it_out = conv ? it + 1 : it;
+    return conv;
+}
+
+/* World::addSphere, ch3/ver2/World.cpp:88-106: node position x0 + dh*(i,j,k);
+ * nodes inside or on the sphere get object_id 1 and the sphere potential. */
+void eo_objects_sphere(const eo_grid *g, const double c[3], double radius, double phi_s, int *obj,
+                       double *phi) {
+    double sphere[4] = {c[0], c[1], c[2], radius * radius};
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                double l[3] = {(double)i, (double)j, (double)k};
+                double x[3];
+                for (int d = 0; d < 3; d++) x[d] = g->x0[d] + g->dh[d] * l[d];
+                if (in_sphere(sphere, x)) {
+                    obj[NODE(g, i, j, k)] = 1;
+                    phi[NODE(g, i, j, k)] = phi_s;
+                }
+            }
+}
+
+/* World::addInlet, ch3/ver2/World.cpp:109-116: k = 0 plane is Dirichlet 0 V. */
+void eo_objects_inlet(const eo_grid *g, int *obj, double *phi) {
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++) {
+            obj[NODE(g, i, j, 0)] = 2;
+            phi[NODE(g, i, j, 0)] = 0;
+        }
+}
+
+/* Immediate Neumann neighbour of a boundary node, in the precedence of
+ * PotentialSolver::solveGS, ch3/ver2/PotentialSolver.cpp:359-370; -1 for an
+ * interior node. */
+static int64_t neumann_next(const eo_grid *g, int i, int j, int k) {
+    if (i == 0) return NODE(g, i + 1, j, k);
+    if (i == g->ni - 1) return NODE(g, i - 1, j, k);
+    if (j == 0) return NODE(g, i, j + 1, k);
+    if (j == g->nj - 1) return NODE(g, i, j - 1, k);
+    if (k == 0) return NODE(g, i, j, k + 1);
+    if (k == g->nk - 1) return NODE(g, i, j, k - 1);
+    return -1;
+}
+
+/* For each non-Dirichlet boundary node, the end of its chain of Neumann
+ * copies (an interior or a Dirichlet node); -1 elsewhere.  At the fixed
+ * point of solveGS every boundary node equals its chain end. */
+void eo_neumann_targets(const eo_grid *g, const int *obj, int *target) {
+    for (int k = 0; k < g->nk; k++)
+        for (int j = 0; j < g->nj; j++)
+            for (int i = 0; i < g->ni; i++) {
+                int64_t u = NODE(g, i, j, k);
+                target[u] = -1;
+                if (obj[u] > 0) continue;
+                int64_t nx = neumann_next(g, i, j, k);
+                if (nx < 0) continue;
+                int64_t t = nx;
+                for (int guard = 0; guard < 8; guard++) {
+                    if (obj[t] > 0) break;
+                    int ti = (int)(t % g->ni), tj = (int)((t / g->ni) % g->nj),
+                        tk = (int)(t / ((int64_t)g->ni * g->nj));
+                    int64_t n2 = neumann_next(g, ti, tj, tk);
+                    if (n2 < 0) break;
+                    t = n2;
+                }
+                target[u] = (int)t;
+            }
+}
+
+/* Residual of solveGS, ch3/ver2/PotentialSolver.cpp:394-424. */
+double eo_residual_sphere(const eo_grid *g, const double *phi, const double *rho, const int *obj,
+                          double phi0, double te0, double n0) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    double sum = 0;
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                int64_t u = NODE(g, i, j, k);
+                if (obj[u] > 0) continue;
+                int64_t nb = neumann_next(g, i, j, k);
+                double R;
+                if (nb >= 0)
+                    R = phi[u] - phi[nb];
+                else {
+                    double ne = n0 * exp((phi[u] - phi0) / te0);
+                    R = -phi[u] * (2 * idx2 + 2 * idy2 + 2 * idz2) + (rho[u] - EO_QE * ne) / EO_EPS_0 +
+                        idx2 * (phi[u - 1] + phi[u + 1]) + idy2 * (phi[u - sy] + phi[u + sy]) +
+                        idz2 * (phi[u - sz] + phi[u + sz]);
+                }
+                sum += R * R;
+            }
+    return sqrt(sum / (g->ni * g->nj * g->nk));
+}
+
+static inline void gs_sphere_node(const eo_grid *g, double *phi, const double *rho, int64_t u,
+                                  double idx2, double idy2, double idz2, double phi0, double te0,
+                                  double n0) {
+    int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    double ne = n0 * exp((phi[u] - phi0) / te0);
+    double phi_new = ((rho[u] - EO_QE * ne) / EO_EPS_0 + idx2 * (phi[u - 1] + phi[u + 1]) +
+                      idy2 * (phi[u - sy] + phi[u + sy]) + idz2 * (phi[u - sz] + phi[u + sz])) /
+                     (2 * idx2 + 2 * idy2 + 2 * idz2);
+    phi[u] = phi[u] + 1.4 * (phi_new - phi[u]);
+}
+
+/* PotentialSolver::solveGS, ch3/ver2/PotentialSolver.cpp:334-430:
+ * lexicographic nonlinear SOR with Boltzmann electrons. */
+int eo_gs_sphere_lex(const eo_grid *g, double *phi, const double *rho, const int *obj, double phi0,
+                     double te0, double n0, int max_it, double tol, double *l2_out, int *it_out) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    double L2 = 0;
+    int conv = 0, it;
+    for (it = 0; it < max_it; it++) {
+        for (int i = 0; i < g->ni; i++)
+            for (int j = 0; j < g->nj; j++)
+                for (int k = 0; k < g->nk; k++) {
+                    int64_t u = NODE(g, i, j, k);
+                    if (obj[u] > 0) continue;
+                    int64_t nb = neumann_next(g, i, j, k);
+                    if (nb >= 0)
+                        phi[u] = phi[nb];
+                    else
+                        gs_sphere_node(g, phi, rho, u, idx2, idy2, idz2, phi0, te0, n0);
+                }
+        if (it % 25 == 0) {
+            L2 = eo_residual_sphere(g, phi, rho, obj, phi0, te0, n0);
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (l2_out) *l2_out = L2;
+    if (it_out) *it_out = conv ? it + 1 : it;
+    return conv;
+}
+
+/* The CUDA path's red-black form of solveGS: red then black interior
+ * non-Dirichlet nodes, then every Neumann node copies its chain end. */
+int eo_sor_sphere_rb(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                     const int *target, double phi0, double te0, double n0, int max_it, double tol,
+                     double *l2_out, int *it_out) {
+    double idx2 = 1.0 / (g->dh[0] * g->dh[0]);
+    double idy2 = 1.0 / (g->dh[1] * g->dh[1]);
+    double idz2 = 1.0 / (g->dh[2] * g->dh[2]);
+    int64_t nn = (int64_t)g->ni * g->nj * g->nk;
+    double L2 = 0;
+    int conv = 0, it;
+    for (it = 0; it < max_it; it++) {
+        for (int colour = 0; colour < 2; colour++)
+            for (int k = 1; k < g->nk - 1; k++)
+                for (int j = 1; j < g->nj - 1; j++)
+                    for (int i = 1; i < g->ni - 1; i++) {
+                        int64_t u = NODE(g, i, j, k);
+                        if (((i + j + k) & 1) != colour || obj[u] > 0) continue;
+                        gs_sphere_node(g, phi, rho, u, idx2, idy2, idz2, phi0, te0, n0);
+                    }
+        for (int64_t u = 0; u < nn; u++)
+            if (target[u] >= 0) phi[u] = phi[target[u]];
+        if (it % 25 == 0) {
+            L2 = eo_residual_sphere(g, phi, rho, obj, phi0, te0, n0);
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (l2_out) *l2_out = L2;
+    if (it_out) *it_out = conv ? it + 1 : it;
+    return conv;
+}
+
+/* PotentialSolver::solveQN, ch3/ver2/PotentialSolver.cpp:204-222 */
+void eo_qn(const eo_grid *g, double *phi, const double *rho, const int *obj, double phi0,
+           double te0, double n0) {
+    double rho0 = n0 * EO_QE;
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                int64_t u = NODE(g, i, j, k);
+                if (obj[u] > 0) continue;
+                double ratio = rho[u] / rho0;
+                if (ratio < 1e-6) ratio = 1e-6;
+                phi[u] = phi0 + te0 * log(ratio);
+            }
+}
+
+/* ---- matrix-free Newton / Jacobi-PCG on the symmetric form of the
+ * discrete problem of solveGS (the CUDA path's algorithm).  Unknowns are
+ * interior nodes with obj == 0.  L = -Laplacian with Dirichlet neighbours
+ * moved to the right-hand side and Neumann neighbours mirrored (a boundary
+ * neighbour of an interior node always copies that node), so L is SPD.
+ * F(x) = L x - bD + (qe n0/eps0) e^{(x-phi0)/Te} - rho/eps0,
+ * J = L + diag((qe n0/(eps0 Te)) e^{(x-phi0)/Te}).  The reference's own
+ * Newton-PCG (ch3/ver2/PotentialSolver.cpp:225-331) uses a non-symmetric
+ * matrix on which CG breaks down; this form solves the same equations. */
+typedef struct {
+    const eo_grid *g;
+    const int *obj;
+    double c[3];
+} nk_ctx;
+
+static inline int is_unknown(const nk_ctx *K, int i, int j, int k) {
+    const eo_grid *g = K->g;
+    if (i < 1 || j < 1 || k < 1 || i > g->ni - 2 || j > g->nj - 2 || k > g->nk - 2) return 0;
+    return K->obj[NODE(g, i, j, k)] == 0;
+}
+
+/* neighbour kind: 0 unknown, 1 Dirichlet, 2 Neumann boundary */
+static inline int nb_kind(const nk_ctx *K, int i, int j, int k) {
+    const eo_grid *g = K->g;
+    int64_t u = NODE(g, i, j, k);
+    if (K->obj[u] > 0) return 1;
+    if (i == 0 || j == 0 || k == 0 || i == g->ni - 1 || j == g->nj - 1 || k == g->nk - 1) return 2;
+    return 0;
+}
+
+static const int NB_OFF[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+
+/* y = L x on unknowns (x zero elsewhere); diag gets the diagonal of L. */
+static void apply_L(const nk_ctx *K, const double *x, double *y, double *diag) {
+    const eo_grid *g = K->g;
+    for (int k = 1; k < g->nk - 1; k++)
+        for (int j = 1; j < g->nj - 1; j++)
+            for (int i = 1; i < g->ni - 1; i++) {
+                int64_t u = NODE(g, i, j, k);
+                if (K->obj[u] != 0) continue;
+                double s = 0, d = 0;
+                for (int m = 0; m < 6; m++) {
+                    int a = i + NB_OFF[m][0], b = j + NB_OFF[m][1], c = k + NB_OFF[m][2];
+                    double cm = K->c[m >> 1];
+                    int kind = nb_kind(K, a, b, c);
+                    if (kind == 0) {
+                        d += cm;
+                        s -= cm * x[NODE(g, a, b, c)];
+                    } else if (kind == 1) {
+                        d += cm;
+                    }
+                }
+                y[u] = d * x[u] + s;
+                if (diag) diag[u] = d;
+            }
+}
+
+int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                  const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
+                  int pcg_max, double pcg_tol, int *nr_it_out, int *pcg_it_out) {
+    int64_t nn = (int64_t)g->ni * g->nj * g->nk;
+    nk_ctx K = {g, obj, {1.0 / (g->dh[0] * g->dh[0]), 1.0 / (g->dh[1] * g->dh[1]),
+                         1.0 / (g->dh[2] * g->dh[2])}};
+    double *bD = calloc(nn, sizeof(double)), *F = calloc(nn, sizeof(double));
+    double *diagL = calloc(nn, sizeof(double)), *Pd = calloc(nn, sizeof(double));
+    double *y = calloc(nn, sizeof(double)), *r = calloc(nn, sizeof(double));
+    double *z = calloc(nn, sizeof(double)), *p = calloc(nn, sizeof(double));
+    double *q = calloc(nn, sizeof(double)), *xu = calloc(nn, sizeof(double));
+    /* Dirichlet contributions */
+    for (int k = 1; k < g->nk - 1; k++)
+        for (int j = 1; j < g->nj - 1; j++)
+            for (int i = 1; i < g->ni - 1; i++) {
+                int64_t u = NODE(g, i, j, k);
+                if (obj[u] != 0) continue;
+                double s = 0;
+                for (int m = 0; m < 6; m++) {
+                    int a = i + NB_OFF[m][0], b = j + NB_OFF[m][1], c = k + NB_OFF[m][2];
+                    if (nb_kind(&K, a, b, c) == 1) s += K.c[m >> 1] * phi[NODE(g, a, b, c)];
+                }
+                bD[u] = s;
+            }
+    const double A0 = EO_QE * n0 / EO_EPS_0;
+    int conv = 0, nr, pcg_total = 0;
+    for (nr = 0; nr < nr_max; nr++) {
+        for (int64_t u = 0; u < nn; u++) xu[u] = (obj[u] == 0) ? phi[u] : 0;
+        apply_L(&K, xu, F, diagL);
+        double fn = 0;
+        for (int k = 1; k < g->nk - 1; k++)
+            for (int j = 1; j < g->nj - 1; j++)
+                for (int i = 1; i < g->ni - 1; i++) {
+                    int64_t u = NODE(g, i, j, k);
+                    if (obj[u] != 0) continue;
+                    double e = exp((phi[u] - phi0) / te0);
+                    F[u] = F[u] - bD[u] + A0 * e - rho[u] / EO_EPS_0;
+                    Pd[u] = A0 / te0 * e;
+                    fn += F[u] * F[u];
+                }
+        /* PCG on J y = F from y = 0 */
+        double rz = 0;
+        for (int64_t u = 0; u < nn; u++) {
+            y[u] = 0;
+            r[u] = F[u];
+            double dg = diagL[u] + Pd[u];
+            z[u] = (dg != 0) ? r[u] / dg : 0;
+            p[u] = z[u];
+            rz += r[u] * z[u];
+        }
+        double stop2 = pcg_tol * pcg_tol * fn;
+        int it = 0;
+        if (fn > 0) {
+            for (it = 0; it < pcg_max; it++) {
+                apply_L(&K, p, q, NULL);
+                double pq = 0;
+                for (int64_t u = 0; u < nn; u++) {
+                    q[u] += Pd[u] * p[u];
+                    pq += p[u] * q[u];
+                }
+                double alpha = rz / pq;
+                double rr = 0;
+                for (int64_t u = 0; u < nn; u++) {
+                    y[u] += alpha * p[u];
+                    r[u] -= alpha * q[u];
+                    rr += r[u] * r[u];
+                }
+                if (rr <= stop2) {
+                    it++;
+                    break;
+                }
+                double rz_new = 0;
+                for (int64_t u = 0; u < nn; u++) {
+                    double dg = diagL[u] + Pd[u];
+                    z[u] = (dg != 0) ? r[u] / dg : 0;
+                    rz_new += r[u] * z[u];
+                }
+                double beta = rz_new / rz;
+                rz = rz_new;
+                for (int64_t u = 0; u < nn; u++) p[u] = z[u] + beta * p[u];
+            }
+        }
+        pcg_total += it;
+        double yn = 0;
+        for (int64_t u = 0; u < nn; u++) {
+            if (obj[u] != 0) continue;
+            phi[u] -= y[u];
+            yn += y[u] * y[u];
+        }
+        double norm = sqrt(yn / nn);
+        if (norm < nr_tol) {
+            conv = 1;
+            nr++;
+            break;
+        }
+    }
+    for (int64_t u = 0; u < nn; u++)
+        if (target[u] >= 0) phi[u] = phi[target[u]];
+    free(bD);
+    free(F);
+    free(diagL);
+    free(Pd);
+    free(y);
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    free(xu);
+    if (nr_it_out) *nr_it_out = nr;
+    if (pcg_it_out) *pcg_it_out = pcg_total;
+    return conv;
+}
+
+/* PotentialSolver::computeEF, ch2/PotentialSolver.cpp:70-110 (identical in
+ * ch3/ver2/PotentialSolver.cpp:465-504). */
+void eo_efield(const eo_grid *g, const double *phi, double *ef) {
+    double dx = g->dh[0], dy = g->dh[1], dz = g->dh[2];
+    int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                int64_t u = NODE(g, i, j, k);
+                double *e = ef + 3 * u;
+                if (i == 0)
+                    e[0] = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]) / (2 * dx);
+                else if (i == g->ni - 1)
+                    e[0] = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]) / (2 * dx);
+                else
+                    e[0] = -(phi[u + 1] - phi[u - 1]) / (2 * dx);
+                if (j == 0)
+                    e[1] = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]) / (2 * dy);
+                else if (j == g->nj - 1)
+                    e[1] = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]) / (2 * dy);
+                else
+                    e[1] = -(phi[u + sy] - phi[u - sy]) / (2 * dy);
+                if (k == 0)
+                    e[2] = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]) / (2 * dz);
+                else if (k == g->nk - 1)
+                    e[2] = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]) / (2 * dz);
+                else
+                    e[2] = -(phi[u + sz] - phi[u - sz]) / (2 * dz);
+            }
+}
+
+/* Species::getRealCount / getMomentum / getKE, ch2/Species.cpp:144-168.
+ * out = {real count, px, py, pz, KE}. */
+void eo_species_diag(const double *P, int64_t stride, int64_t n, double mass, double out[5]) {
+    double cnt = 0, m[3] = {0, 0, 0}, ke = 0;
+    for (int64_t p = 0; p < n; p++) {
+        double w = P[6 * stride + p];
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        cnt += w;
+        for (int d = 0; d < 3; d++) m[d] += v[d] * w;
+        double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        ke += w * v2;
+    }
+    out[0] = cnt;
+    for (int d = 0; d < 3; d++) out[1 + d] = m[d] * mass;
+    out[4] = 0.5 * mass * ke;
+}
+
+/* World::getPE, ch2/World.cpp:72-84 */
+double eo_potential_energy(const eo_grid *g, const double *ef, const double *vol) {
+    double pe = 0;
+    for (int i = 0; i < g->ni; i++)
+        for (int j = 0; j < g->nj; j++)
+            for (int k = 0; k < g->nk; k++) {
+                int64_t u = NODE(g, i, j, k);
+                const double *e = ef + 3 * u;
+                double ef2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+                pe += ef2 * vol[u];
+            }
+    return 0.5 * EO_EPS_0 * pe;
+}
+
+/* Field_::updateAverage, ch3/ver2/Field.h:214-220 */
+void eo_update_average(int64_t nn, double *ave, const double *inst, int samples) {
+    for (int64_t u = 0; u < nn; u++) ave[u] = (inst[u] + samples * ave[u]) / (samples + 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Threaded CPU baseline: the per-thread particle ranges and private deposit
+ * buffers of ch9/MT (Species.cpp:9-110), for the sphere push + compaction +
+ * fixed-point deposit.  Returns seconds of wall time. */
+#include <time.h>
+typedef struct {
+    const eo_grid *g;
+    const double *ef;
+    const double *sphere;
+    double charge, mass, dt, fx;
+    double *P;
+    int64_t stride, p0, p1;
+    int64_t *acc;
+    int mode;
+} bench_job;
+
+static void *bench_worker(void *arg) {
+    bench_job *J = (bench_job *)arg;
+    if (J->mode == 0) {
+        double *P = J->P;
+        int64_t s = J->stride;
+        /* push this range in place */
+        double tmp_sph[4];
+        memcpy(tmp_sph, J->sphere, sizeof tmp_sph);
+        for (int64_t p = J->p0; p < J->p1; p++) {
+            double q = J->dt * J->charge / J->mass;
+            double x[3] = {P[p], P[s + p], P[2 * s + p]};
+            double v[3] = {P[3 * s + p], P[4 * s + p], P[5 * s + p]};
+            double lc[3], e[3];
+            eo_xtol(J->g, x, lc);
+            eo_gather3(J->g, J->ef, lc, e);
+            for (int d = 0; d < 3; d++) v[d] += e[d] * q;
+            for (int d = 0; d < 3; d++) x[d] += v[d] * J->dt;
+            for (int d = 0; d < 3; d++) {
+                P[d * s + p] = x[d];
+                P[(3 + d) * s + p] = v[d];
+            }
+            if (in_sphere(tmp_sph, x) || !eo_in_bounds(J->g, x)) P[6 * s + p] = 0;
+        }
+    } else {
+        eo_deposit_fixed(J->g, J->P + J->p0, J->stride, J->p1 - J->p0, J->fx, J->acc);
+    }
+    return NULL;
+}
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],
+                             double charge, double mass, double dt, double fx, double *P,
+                             int64_t stride, int64_t n, int threads, int steps, int64_t *n_out,
+                             int64_t *acc) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    int64_t nn = (int64_t)g->ni * g->nj * g->nk;
+    int64_t **bufs = calloc(threads, sizeof(int64_t *));
+    for (int t = 0; t < threads; t++) bufs[t] = calloc(nn, sizeof(int64_t));
+    pthread_t th[256];
+    bench_job jobs[256];
+    double t0 = now_s();
+    for (int st = 0; st < steps; st++) {
+        for (int mode = 0; mode < 2; mode++) {
+            int64_t per = n / threads;
+            for (int t = 0; t < threads; t++) {
+                bench_job *J = &jobs[t];
+                J->g = g;
+                J->ef = ef;
+                J->sphere = sphere;
+                J->charge = charge;
+                J->mass = mass;
+                J->dt = dt;
+                J->fx = fx;
+                J->P = P;
+                J->stride = stride;
+                J->p0 = t * per;
+                J->p1 = (t == threads - 1) ? n : (t + 1) * per;
+                J->acc = bufs[t];
+                J->mode = mode;
+                if (mode == 1) memset(bufs[t], 0, nn * sizeof(int64_t));
+                pthread_create(&th[t], NULL, bench_worker, J);
+            }
+            for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+            if (mode == 0) n = eo_compact_swap_last(P, stride, n);
+        }
+        for (int64_t u = 0; u < nn; u++) {
+            int64_t s = 0;
+            for (int t = 0; t < threads; t++) s += bufs[t][u];
+            acc[u] = s;
+        }
+    }
+    double el = now_s() - t0;
+    for (int t = 0; t < threads; t++) free(bufs[t]);
+    free(bufs);
+    if (n_out) *n_out = n;
+    return el;
+}

@@ -1,0 +1,129 @@
+/*
+ * espic_oracle.h -- CPU restatement of the electrostatic PIC time step of
+ * "Plasma Simulations by Example" (ch2 grounded box, ch3/ver2 sphere, ch4
+ * warm-beam injector).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the CUDA
+ * path: only the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark may load it.  The product library (libespic) never calls it and
+ * has no CPU fallback.
+ *
+ * Parity is pinned: tests/golden/ holds vectors produced by the reference's
+ * own CPU code (compiled from its sources by oracle/build_ref.py) and the
+ * tests check every function here against them.
+ *
+ * Conventions
+ *  - Node fields are linear arrays in the reference's U order
+ *    (ch3/ver2/Field.h:161): u = k*ni*nj + j*ni + i, i fastest.
+ *  - Vector node fields (ef) are interleaved [u][3].
+ *  - Particles are a structure-of-arrays block P with row stride `stride`:
+ *    P[c*stride + p], c = 0..6 for x, y, z, vx, vy, vz, mpw.
+ *  - Every expression keeps the reference's operand order; build with
+ *    -ffp-contract=off so that no multiply-add is fused.
+ */
+#ifndef ESPIC_ORACLE_H
+#define ESPIC_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int ni, nj, nk, pad;
+    double x0[3], xm[3], dh[3];
+} eo_grid;
+
+/* Physical constants of the reference, Const:: in ch2/World.h:12-21. */
+#define EO_EPS_0 8.85418782e-12
+#define EO_QE 1.602176565e-19
+#define EO_AMU 1.660538921e-27
+#define EO_ME 9.10938215e-31
+#define EO_K 1.380648e-23
+#define EO_PI 3.141592653
+
+/* ---- counter-based RNG (Philox4x32-10, Salmon et al., SC'11) ---------- */
+void eo_philox4x32(uint32_t ctr[4], const uint32_t key[2]);
+double eo_philox_uniform(uint64_t seed, uint64_t stream, uint64_t index);
+void eo_philox_uniforms(uint64_t seed, uint64_t stream, uint64_t first, int64_t n, double *out);
+
+/* ---- geometry: World::setExtents ch2/World.cpp:22-36 ---------------------- */
+void eo_grid_set(eo_grid *g, int ni, int nj, int nk, const double x0[3], const double xm[3]);
+void eo_node_volumes(const eo_grid *g, double *vol);
+void eo_xtol(const eo_grid *g, const double x[3], double lc[3]);
+void eo_gather3(const eo_grid *g, const double *ef, const double lc[3], double out[3]);
+int eo_in_bounds(const eo_grid *g, const double x[3]);
+
+/* ---- particles ------------------------------------------------------- */
+void eo_push_box(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                 double *P, int64_t stride, int64_t n);
+int64_t eo_push_sphere(const eo_grid *g, const double *ef, const double sphere[4], double charge,
+                       double mass, double dt, double *P, int64_t stride, int64_t n);
+int64_t eo_compact_swap_last(double *P, int64_t stride, int64_t n);
+int64_t eo_compact_holes(double *P, int64_t stride, int64_t n);
+int64_t eo_add_particles(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                         const double *pos3, const double *vel3, const double *w, int64_t n,
+                         double *P, int64_t stride, int64_t np0, int64_t cap);
+int64_t eo_load_box(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                    const double x1[3], const double x2[3], double num_den, int64_t num_mp,
+                    const double *u, double *P, int64_t stride, int64_t np0, int64_t cap);
+int64_t eo_load_box_qs(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       const double x1[3], const double x2[3], double num_den, const int num_mp[3],
+                       double *P, int64_t stride, int64_t np0, int64_t cap);
+int64_t eo_inject_cold(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, const double *u, int64_t *u_used,
+                       double *P, int64_t stride, int64_t np0, int64_t cap);
+int64_t eo_inject_warm(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, double temp, const double *u,
+                       int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap);
+int eo_inject_count(const eo_grid *g, double dt, double mpw0, double v_drift, double den, double u0);
+
+/* ---- deposit --------------------------------------------------------- */
+void eo_deposit_fp64(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *acc);
+void eo_deposit_fixed(const eo_grid *g, const double *P, int64_t stride, int64_t n, double fx,
+                      int64_t *acc);
+void eo_divide_volume(int64_t nn, double *den, const double *vol);
+void eo_density_from_fixed(int64_t nn, const int64_t *acc, double inv_fx, const double *vol,
+                           double *den);
+void eo_charge_density(int64_t nn, int ns, const double *charges, const double *dens, double *rho);
+int eo_fixed_scale_exponent(double weight_bound, int64_t capacity);
+
+/* ---- field solve ----------------------------------------------------- */
+double eo_residual_box(const eo_grid *g, const double *phi, const double *rho);
+int eo_sor_box_lex(const eo_grid *g, double *phi, const double *rho, int max_it, double tol,
+                   double *l2_out, int *it_out);
+int eo_sor_box_rb(const eo_grid *g, double *phi, const double *rho, int max_it, double tol,
+                  double *l2_out, int *it_out);
+void eo_objects_sphere(const eo_grid *g, const double c[3], double radius, double phi_s,
+                       int *obj, double *phi);
+void eo_objects_inlet(const eo_grid *g, int *obj, double *phi);
+void eo_neumann_targets(const eo_grid *g, const int *obj, int *target);
+double eo_residual_sphere(const eo_grid *g, const double *phi, const double *rho, const int *obj,
+                          double phi0, double te0, double n0);
+int eo_gs_sphere_lex(const eo_grid *g, double *phi, const double *rho, const int *obj, double phi0,
+                     double te0, double n0, int max_it, double tol, double *l2_out, int *it_out);
+int eo_sor_sphere_rb(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                     const int *target, double phi0, double te0, double n0, int max_it, double tol,
+                     double *l2_out, int *it_out);
+void eo_qn(const eo_grid *g, double *phi, const double *rho, const int *obj, double phi0,
+           double te0, double n0);
+int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                  const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
+                  int pcg_max, double pcg_tol, int *nr_it_out, int *pcg_it_out);
+void eo_efield(const eo_grid *g, const double *phi, double *ef);
+
+/* ---- diagnostics ----------------------------------------------------- */
+void eo_species_diag(const double *P, int64_t stride, int64_t n, double mass, double out[5]);
+double eo_potential_energy(const eo_grid *g, const double *ef, const double *vol);
+void eo_update_average(int64_t nn, double *ave, const double *inst, int samples);
+
+/* ---- CPU baseline (threaded like ch9/MT) ------------------------------ */
+double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],
+                             double charge, double mass, double dt, double fx, double *P,
+                             int64_t stride, int64_t n, int threads, int steps, int64_t *n_out,
+                             int64_t *acc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

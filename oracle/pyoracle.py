@@ -1,0 +1,378 @@
+"""ctypes view of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loaded by the tests, the smoke check and the CPU-baseline leg of bench.py,
+as the checker; the product library never imports it.  Arrays follow the
+oracle's conventions: node fields in U order (i fastest), ef as [nn, 3],
+particles as a (7, n) float64 block x, y, z, vx, vy, vz, mpw.
+"""
+import ctypes as C
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+from . import build_ref
+
+_lib = None
+
+D = C.c_double
+I64 = C.c_int64
+PD = C.POINTER(C.c_double)
+PI = C.POINTER(C.c_int)
+PI64 = C.POINTER(C.c_int64)
+
+
+class Grid(C.Structure):
+    _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("pad", C.c_int),
+                ("x0", D * 3), ("xm", D * 3), ("dh", D * 3)]
+
+    @property
+    def nn(self):
+        return self.ni * self.nj * self.nk
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_ref.build_oracle()
+        _lib = C.CDLL(path)
+        _sig(_lib)
+    return _lib
+
+
+def _sig(L):
+    L.eo_philox_uniform.restype = D
+    L.eo_philox_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
+    L.eo_philox_uniforms.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, I64, PD]
+    L.eo_grid_set.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, C.c_int, PD, PD]
+    L.eo_node_volumes.argtypes = [C.POINTER(Grid), PD]
+    L.eo_push_box.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, I64, I64]
+    L.eo_push_sphere.restype = I64
+    L.eo_push_sphere.argtypes = [C.POINTER(Grid), PD, PD, D, D, D, PD, I64, I64]
+    L.eo_compact_swap_last.restype = I64
+    L.eo_compact_swap_last.argtypes = [PD, I64, I64]
+    L.eo_compact_holes.restype = I64
+    L.eo_compact_holes.argtypes = [PD, I64, I64]
+    L.eo_add_particles.restype = I64
+    L.eo_add_particles.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, PD, I64, PD, I64, I64, I64]
+    L.eo_load_box.restype = I64
+    L.eo_load_box.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, D, I64, PD, PD, I64, I64, I64]
+    L.eo_load_box_qs.restype = I64
+    L.eo_load_box_qs.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, D, PI, PD, I64, I64, I64]
+    L.eo_inject_count.restype = C.c_int
+    L.eo_inject_count.argtypes = [C.POINTER(Grid), D, D, D, D, D]
+    L.eo_inject_cold.restype = I64
+    L.eo_inject_cold.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, PD, PI64, PD, I64, I64, I64]
+    L.eo_inject_warm.restype = I64
+    L.eo_inject_warm.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, PD, PI64, PD, I64, I64,
+                                 I64]
+    L.eo_deposit_fp64.argtypes = [C.POINTER(Grid), PD, I64, I64, PD]
+    L.eo_deposit_fixed.argtypes = [C.POINTER(Grid), PD, I64, I64, D, PI64]
+    L.eo_divide_volume.argtypes = [I64, PD, PD]
+    L.eo_density_from_fixed.argtypes = [I64, PI64, D, PD, PD]
+    L.eo_charge_density.argtypes = [I64, C.c_int, PD, PD, PD]
+    L.eo_fixed_scale_exponent.restype = C.c_int
+    L.eo_fixed_scale_exponent.argtypes = [D, I64]
+    L.eo_residual_box.restype = D
+    L.eo_residual_box.argtypes = [C.POINTER(Grid), PD, PD]
+    for f in (L.eo_sor_box_lex, L.eo_sor_box_rb):
+        f.restype = C.c_int
+        f.argtypes = [C.POINTER(Grid), PD, PD, C.c_int, D, PD, PI]
+    L.eo_objects_sphere.argtypes = [C.POINTER(Grid), PD, D, D, PI, PD]
+    L.eo_objects_inlet.argtypes = [C.POINTER(Grid), PI, PD]
+    L.eo_neumann_targets.argtypes = [C.POINTER(Grid), PI, PI]
+    L.eo_residual_sphere.restype = D
+    L.eo_residual_sphere.argtypes = [C.POINTER(Grid), PD, PD, PI, D, D, D]
+    L.eo_gs_sphere_lex.restype = C.c_int
+    L.eo_gs_sphere_lex.argtypes = [C.POINTER(Grid), PD, PD, PI, D, D, D, C.c_int, D, PD, PI]
+    L.eo_sor_sphere_rb.restype = C.c_int
+    L.eo_sor_sphere_rb.argtypes = [C.POINTER(Grid), PD, PD, PI, PI, D, D, D, C.c_int, D, PD, PI]
+    L.eo_qn.argtypes = [C.POINTER(Grid), PD, PD, PI, D, D, D]
+    L.eo_newton_pcg.restype = C.c_int
+    L.eo_newton_pcg.argtypes = [C.POINTER(Grid), PD, PD, PI, PI, D, D, D, C.c_int, D, C.c_int, D,
+                                PI, PI]
+    L.eo_efield.argtypes = [C.POINTER(Grid), PD, PD]
+    L.eo_species_diag.argtypes = [PD, I64, I64, D, PD]
+    L.eo_potential_energy.restype = D
+    L.eo_potential_energy.argtypes = [C.POINTER(Grid), PD, PD]
+    L.eo_update_average.argtypes = [I64, PD, PD, C.c_int]
+    L.eo_bench_push_deposit.restype = D
+    L.eo_bench_push_deposit.argtypes = [C.POINTER(Grid), PD, PD, D, D, D, D, PD, I64, I64, C.c_int,
+                                        C.c_int, PI64, PI64]
+
+
+def pd(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(PD)
+
+
+def pi(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(PI)
+
+
+def pi64(a):
+    assert a.dtype == np.int64 and a.flags.c_contiguous
+    return a.ctypes.data_as(PI64)
+
+
+def arr3(v):
+    return (D * 3)(*[float(x) for x in v])
+
+
+def grid(n, x0, xm):
+    g = Grid()
+    lib().eo_grid_set(C.byref(g), int(n[0]), int(n[1]), int(n[2]), arr3(x0), arr3(xm))
+    return g
+
+
+def node_volumes(g):
+    v = np.zeros(g.nn)
+    lib().eo_node_volumes(C.byref(g), pd(v))
+    return v
+
+
+def philox_uniforms(seed, stream, first, n):
+    out = np.zeros(int(n))
+    lib().eo_philox_uniforms(seed, stream, first, int(n), pd(out))
+    return out
+
+
+def push_box(g, ef, charge, mass, dt, P):
+    P = np.ascontiguousarray(P, dtype=np.float64).copy()
+    lib().eo_push_box(C.byref(g), pd(ef), charge, mass, dt, pd(P), P.shape[1], P.shape[1])
+    return P
+
+
+def push_sphere(g, ef, sphere4, charge, mass, dt, P, compact="swap_last"):
+    P = np.ascontiguousarray(P, dtype=np.float64).copy()
+    n = P.shape[1]
+    s = np.asarray(sphere4, dtype=np.float64)
+    L = lib()
+    L.eo_push_sphere(C.byref(g), pd(ef), pd(s), charge, mass, dt, pd(P), n, n)
+    if compact == "swap_last":
+        m = L.eo_compact_swap_last(pd(P), n, n)
+    elif compact == "holes":
+        m = L.eo_compact_holes(pd(P), n, n)
+    else:
+        return P
+    return np.ascontiguousarray(P[:, :m])
+
+
+def add_particles(g, ef, charge, mass, dt, pos3, vel3, w, P=None, cap=None):
+    pos3 = np.ascontiguousarray(pos3, dtype=np.float64)
+    vel3 = np.ascontiguousarray(vel3, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    n = pos3.shape[0]
+    np0 = 0 if P is None else P.shape[1]
+    cap = cap or (np0 + n)
+    B = np.zeros((7, cap))
+    if P is not None:
+        B[:, :np0] = P
+    m = lib().eo_add_particles(C.byref(g), pd(ef), charge, mass, dt, pd(pos3), pd(vel3), pd(w), n,
+                               pd(B), cap, np0, cap)
+    return np.ascontiguousarray(B[:, :m])
+
+
+def load_box(g, ef, charge, mass, dt, x1, x2, num_den, num_mp, u):
+    B = np.zeros((7, num_mp))
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    m = lib().eo_load_box(C.byref(g), pd(ef), charge, mass, dt, arr3(x1), arr3(x2), num_den, num_mp,
+                          pd(u), pd(B), num_mp, 0, num_mp)
+    return np.ascontiguousarray(B[:, :m])
+
+
+def load_box_qs(g, ef, charge, mass, dt, x1, x2, num_den, num_mp):
+    cap = int(np.prod(num_mp))
+    B = np.zeros((7, cap))
+    nm = np.asarray(num_mp, dtype=np.int32)
+    m = lib().eo_load_box_qs(C.byref(g), pd(ef), charge, mass, dt, arr3(x1), arr3(x2), num_den,
+                             pi(nm), pd(B), cap, 0, cap)
+    return np.ascontiguousarray(B[:, :m])
+
+
+def inject(g, ef, charge, mass, dt, mpw0, v_drift, den, u, temp=None, P=None):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    L = lib()
+    cnt = L.eo_inject_count(C.byref(g), dt, mpw0, v_drift, den, float(u[0]))
+    np0 = 0 if P is None else P.shape[1]
+    cap = np0 + max(cnt, 0)
+    B = np.zeros((7, max(cap, 1)))
+    if P is not None:
+        B[:, :np0] = P
+    used = C.c_int64(0)
+    if temp is None:
+        m = L.eo_inject_cold(C.byref(g), pd(ef), charge, mass, dt, mpw0, v_drift, den, pd(u),
+                             C.byref(used), pd(B), B.shape[1], np0, B.shape[1])
+    else:
+        m = L.eo_inject_warm(C.byref(g), pd(ef), charge, mass, dt, mpw0, v_drift, den, temp, pd(u),
+                             C.byref(used), pd(B), B.shape[1], np0, B.shape[1])
+    return np.ascontiguousarray(B[:, :m]), used.value
+
+
+def deposit_fp64(g, P):
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    acc = np.zeros(g.nn)
+    lib().eo_deposit_fp64(C.byref(g), pd(P), P.shape[1], P.shape[1], pd(acc))
+    return acc
+
+
+def deposit_fixed(g, P, fx):
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    acc = np.zeros(g.nn, dtype=np.int64)
+    lib().eo_deposit_fixed(C.byref(g), pd(P), P.shape[1], P.shape[1], fx, pi64(acc))
+    return acc
+
+
+def divide_volume(den, vol):
+    den = np.ascontiguousarray(den, dtype=np.float64).copy()
+    lib().eo_divide_volume(den.size, pd(den), pd(vol))
+    return den
+
+
+def density_from_fixed(acc, fx, vol):
+    den = np.zeros(acc.size)
+    lib().eo_density_from_fixed(acc.size, pi64(acc), 1.0 / fx, pd(vol), pd(den))
+    return den
+
+
+def charge_density(charges, dens):
+    dens = np.ascontiguousarray(dens, dtype=np.float64)
+    ch = np.ascontiguousarray(charges, dtype=np.float64)
+    rho = np.zeros(dens.shape[1])
+    lib().eo_charge_density(dens.shape[1], dens.shape[0], pd(ch), pd(dens), pd(rho))
+    return rho
+
+
+def fixed_scale_exponent(weight_bound, capacity):
+    return lib().eo_fixed_scale_exponent(weight_bound, capacity)
+
+
+def sor_box(g, phi, rho, max_it, tol, order="rb"):
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    l2 = C.c_double(0)
+    it = C.c_int(0)
+    f = lib().eo_sor_box_rb if order == "rb" else lib().eo_sor_box_lex
+    conv = f(C.byref(g), pd(phi), pd(rho), max_it, tol, C.byref(l2), C.byref(it))
+    return phi, bool(conv), l2.value, it.value
+
+
+def residual_box(g, phi, rho):
+    return lib().eo_residual_box(C.byref(g), pd(phi), pd(rho))
+
+
+def objects(g, center, radius, phi_s, inlet=True):
+    obj = np.zeros(g.nn, dtype=np.int32)
+    phi = np.zeros(g.nn)
+    if radius is not None:
+        lib().eo_objects_sphere(C.byref(g), arr3(center), radius, phi_s, pi(obj), pd(phi))
+    if inlet:
+        lib().eo_objects_inlet(C.byref(g), pi(obj), pd(phi))
+    return obj, phi
+
+
+def neumann_targets(g, obj):
+    t = np.zeros(g.nn, dtype=np.int32)
+    lib().eo_neumann_targets(C.byref(g), pi(obj), pi(t))
+    return t
+
+
+def residual_sphere(g, phi, rho, obj, phi0, te0, n0):
+    return lib().eo_residual_sphere(C.byref(g), pd(phi), pd(rho), pi(obj), phi0, te0, n0)
+
+
+def gs_sphere(g, phi, rho, obj, phi0, te0, n0, max_it, tol, order="rb"):
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    l2 = C.c_double(0)
+    it = C.c_int(0)
+    if order == "rb":
+        t = neumann_targets(g, obj)
+        conv = lib().eo_sor_sphere_rb(C.byref(g), pd(phi), pd(rho), pi(obj), pi(t), phi0, te0, n0,
+                                      max_it, tol, C.byref(l2), C.byref(it))
+    else:
+        conv = lib().eo_gs_sphere_lex(C.byref(g), pd(phi), pd(rho), pi(obj), phi0, te0, n0, max_it,
+                                      tol, C.byref(l2), C.byref(it))
+    return phi, bool(conv), l2.value, it.value
+
+
+def qn(g, phi, rho, obj, phi0, te0, n0):
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    lib().eo_qn(C.byref(g), pd(phi), pd(rho), pi(obj), phi0, te0, n0)
+    return phi
+
+
+def newton_pcg(g, phi, rho, obj, phi0, te0, n0, nr_max=20, nr_tol=1e-6, pcg_max=10000,
+               pcg_tol=1e-8):
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    t = neumann_targets(g, obj)
+    a = C.c_int(0)
+    b = C.c_int(0)
+    conv = lib().eo_newton_pcg(C.byref(g), pd(phi), pd(rho), pi(obj), pi(t), phi0, te0, n0, nr_max,
+                               nr_tol, pcg_max, pcg_tol, C.byref(a), C.byref(b))
+    return phi, bool(conv), a.value, b.value
+
+
+def efield(g, phi):
+    ef = np.zeros((g.nn, 3))
+    lib().eo_efield(C.byref(g), pd(np.ascontiguousarray(phi, dtype=np.float64)), pd(ef))
+    return ef
+
+
+def species_diag(P, mass):
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    out = np.zeros(5)
+    lib().eo_species_diag(pd(P), P.shape[1], P.shape[1], mass, pd(out))
+    return out
+
+
+def potential_energy(g, ef, vol):
+    return lib().eo_potential_energy(C.byref(g), pd(np.ascontiguousarray(ef)), pd(vol))
+
+
+def update_average(ave, inst, samples):
+    ave = np.ascontiguousarray(ave, dtype=np.float64).copy()
+    lib().eo_update_average(ave.size, pd(ave), pd(np.ascontiguousarray(inst)), samples)
+    return ave
+
+
+# ---------------------------------------------------------------- reference
+def kv_write(path, d):
+    with open(path, "wb") as f:
+        for k, v in d.items():
+            a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+            kb = k.encode()
+            f.write(struct.pack("<i", len(kb)))
+            f.write(kb)
+            f.write(struct.pack("<q", a.size))
+            f.write(a.tobytes())
+
+
+def kv_read(path):
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    off = 0
+    while off < len(data):
+        (ln,) = struct.unpack_from("<i", data, off)
+        off += 4
+        k = data[off:off + ln].decode()
+        off += ln
+        (cnt,) = struct.unpack_from("<q", data, off)
+        off += 8
+        out[k] = np.frombuffer(data, dtype=np.float64, count=cnt, offset=off).copy()
+        off += 8 * cnt
+    return out
+
+
+def run_reference(binary, op, inputs):
+    """Run one reference harness operation; returns its output records."""
+    exe = build_ref.ref_binary(binary)
+    with tempfile.TemporaryDirectory() as td:
+        fi = os.path.join(td, "in.kv")
+        fo = os.path.join(td, "out.kv")
+        kv_write(fi, inputs)
+        subprocess.run([exe, op, fi, fo], check=True, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        return kv_read(fo)

@@ -1,0 +1,54 @@
+/*
+ * ch4_harness.cpp -- drives the reference's ch4 WarmBeamSource (drifting
+ * isotropic thermal injector) through its public API for golden vectors.
+ * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm <in.kv> <out.kv>
+ */
+#include <chrono>
+#include <cmath>
+#include <iostream>
+#include <random>
+#include <string>
+#include <vector>
+#include "harness_io.h"
+#define protected public
+#include "World.h"
+#include "Species.h"
+#include "Source.h"
+#undef protected
+
+int main(int argc, char **argv) {
+    if (argc != 4) { fprintf(stderr, "usage: ref_ch4 op in out\n"); return 1; }
+    std::string op = argv[1];
+    KV in = kv_read(argv[2]), out;
+    const std::vector<double> &gd = kv_get(in, "grid");
+    int ni = (int)gd[0], nj = (int)gd[1], nk = (int)gd[2];
+    const std::vector<double> &x0 = kv_get(in, "x0"), &xm = kv_get(in, "xm");
+    World world(ni, nj, nk);
+    world.setExtents(double3(x0[0], x0[1], x0[2]), double3(xm[0], xm[1], xm[2]));
+    world.setTime(kv_s(in, "dt"), 1);
+    rnd.mt_gen.seed((unsigned)kv_s(in, "seed"));
+    if (kv_has(in, "ef")) field3_in(world.ef, kv_get(in, "ef"), ni, nj, nk);
+    const std::vector<double> &mq = kv_get(in, "sp0_mq");
+    Species sp("sp0", mq[0], mq[1], mq[2], world);
+    if (op != "inject_warm") { fprintf(stderr, "unknown op\n"); return 1; }
+    const std::vector<double> &src = kv_get(in, "source"); /* v_drift den T */
+    WarmBeamSource source(sp, world, src[0], src[1], src[2]);
+    Rnd before = rnd;
+    source.sample();
+    std::vector<double> us;
+    for (long g = 0; g < 200000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+    size_t n = sp.particles.size();
+    std::vector<double> v(7 * n);
+    for (size_t p = 0; p < n; p++) {
+        for (int d = 0; d < 3; d++) {
+            v[d * n + p] = sp.particles[p].pos[d];
+            v[(3 + d) * n + p] = sp.particles[p].vel[d];
+        }
+        v[6 * n + p] = sp.particles[p].mpw;
+    }
+    out["u"] = us;
+    out["sp0_P"] = v;
+    kv_write(argv[3], out);
+    return 0;
+}

@@ -1,0 +1,214 @@
+"""Generate the golden vectors in tests/golden/ by running the reference's own
+CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
+oracle/build_ref.py) on seeded inputs.
+
+Run here, where the reference checkout exists:  python tests/golden/make_golden.py
+The .npz files it writes are committed; the GPU host never needs the
+reference.  Every fixture stores its inputs next to the reference outputs.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import build_ref, pyoracle as po  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+QE, AMU, ME, K = 1.602176565e-19, 1.660538921e-27, 9.10938215e-31, 1.380648e-23
+
+BOX = dict(grid=[21, 21, 21], x0=[-0.1, -0.1, 0.0], xm=[0.1, 0.1, 0.2])
+SPH = dict(grid=[21, 21, 41], x0=[-0.1, -0.1, 0.0], xm=[0.1, 0.1, 0.4])
+SPHERE = [0.0, 0.0, 0.15, 0.05, -100.0]
+
+
+def save(name, **arrays):
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", path, os.path.getsize(path))
+
+
+def rand_particles(rng, geo, n, vscale, wall_frac=0.1, w=1e4):
+    x0, xm = np.array(geo["x0"]), np.array(geo["xm"])
+    pos = x0 + rng.random((n, 3)) * (xm - x0)
+    nw = int(n * wall_frac)
+    # a share of the particles sits within a few steps of a wall
+    axis = rng.integers(0, 3, nw)
+    side = rng.integers(0, 2, nw)
+    eps = rng.random(nw) * 3e-4
+    for m in range(nw):
+        a = axis[m]
+        pos[m, a] = (x0[a] + eps[m]) if side[m] == 0 else (xm[a] - 1e-12 - eps[m])
+    vel = (rng.random((n, 3)) * 2 - 1) * vscale
+    P = np.zeros((7, n))
+    P[0:3] = pos.T
+    P[3:6] = vel.T
+    P[6] = w * (0.5 + rng.random(n))
+    return P
+
+
+def base_inputs(geo, dt=0.0, **kw):
+    d = dict(grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], dt=[dt])
+    d.update(kw)
+    return d
+
+
+def smooth_phi(geo, rng, amp):
+    ni, nj, nk = geo["grid"]
+    k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    phi = amp * (np.sin(np.pi * i / (ni - 1)) * np.sin(np.pi * j / (nj - 1)) *
+                 np.sin(2 * np.pi * k / (nk - 1) + 0.3))
+    phi += amp * 0.01 * rng.standard_normal(phi.shape)
+    return phi.ravel()
+
+
+def box_cases(rng):
+    g = po.grid(BOX["grid"], BOX["x0"], BOX["xm"])
+    vol = po.run_reference("ref_ch2", "node_vol", base_inputs(BOX))["node_vol"]
+    phi = smooth_phi(BOX, rng, 30.0)
+    ef = po.efield(g, phi)
+    dt = 2e-10
+    Pi = rand_particles(rng, BOX, 1200, 2e4, w=1e4)
+    Pe = rand_particles(rng, BOX, 800, 2e6, w=1e4)
+    inp = base_inputs(BOX, dt, ns=[2], sp0_mq=[16 * AMU, QE], sp1_mq=[ME, -QE], sp0_P=Pi,
+                      sp1_P=Pe, ef=ef.ravel())
+    out = po.run_reference("ref_ch2", "push", inp)
+    save("box_push", phi=phi, dt=dt, Pi=Pi, Pe=Pe,
+         Pi_out=out["sp0_P"].reshape(7, -1), Pe_out=out["sp1_P"].reshape(7, -1), node_vol=vol)
+
+    out = po.run_reference("ref_ch2", "deposit", inp)
+    den_i, den_e = out["sp0_den"], out["sp1_den"]
+    save("box_deposit", Pi=Pi, Pe=Pe, den_i=den_i, den_e=den_e, node_vol=vol)
+
+    rinp = base_inputs(BOX, ns=[2], sp0_mq=[16 * AMU, QE], sp1_mq=[ME, -QE], sp0_den=den_i,
+                       sp1_den=den_e)
+    rho = po.run_reference("ref_ch2", "charge", rinp)["rho"]
+    save("box_charge", den_i=den_i, den_e=den_e, rho=rho)
+
+    phi0 = np.zeros(g.nn)
+    sor = {}
+    for tag, tol in (("c1", 1e-4), ("tight", 1e-9)):
+        o = po.run_reference("ref_ch2", "sor", base_inputs(BOX, phi=phi0, rho=rho, max_it=[200000],
+                                                           tol=[tol]))
+        sor["phi_" + tag] = o["phi"]
+        sor["conv_" + tag] = o["conv"]
+    # a warm start: a perturbed phi, few iterations allowed
+    warm = sor["phi_c1"] * 0.9
+    o = po.run_reference("ref_ch2", "sor", base_inputs(BOX, phi=warm, rho=rho, max_it=[30],
+                                                       tol=[1e-30]))
+    save("box_sor", rho=rho, phi_warm=warm, phi_warm30=o["phi"], tol_c1=1e-4, tol_tight=1e-9,
+         **sor)
+
+    o = po.run_reference("ref_ch2", "efield", base_inputs(BOX, phi=phi))
+    save("box_efield", phi=phi, ef=o["ef"].reshape(-1, 3))
+
+    o = po.run_reference("ref_ch2", "diag", inp)
+    save("box_diag", Pi=Pi, Pe=Pe, phi=phi, mi=16 * AMU, me=ME, diag_i=o["sp0_diag"],
+         diag_e=o["sp1_diag"], pe=o["pe"])
+
+    # random and quiet-start loaders (uniforms of the reference's mt19937 recorded)
+    linp = base_inputs(BOX, dt, ns=[1], sp0_mq=[16 * AMU, QE], ef=ef.ravel(), seed=[1234],
+                       x1=BOX["x0"], x2=BOX["xm"], num_den=[1e11], num_mp=[3000])
+    o = po.run_reference("ref_ch2", "load_box", linp)
+    qinp = base_inputs(BOX, dt, ns=[1], sp0_mq=[ME, -QE], ef=ef.ravel(), x1=BOX["x0"],
+                       x2=[0.0, 0.0, 0.1], num_den=[1e11], num_mp=[11, 9, 13])
+    q = po.run_reference("ref_ch2", "load_qs", qinp)
+    save("box_load", phi=phi, dt=dt, u=o["u"], P_box=o["sp0_P"].reshape(7, -1),
+         P_qs=q["sp0_P"].reshape(7, -1), num_mp_box=3000, num_mp_qs=[11, 9, 13],
+         qs_x2=[0.0, 0.0, 0.1])
+
+    # a short run of the ch2 main loop: 80,000/10,000 scaled down to 3,000/600
+    sinp = base_inputs(BOX, dt, ns=[1], sp0_mq=[16 * AMU, QE], seed=[77], x1=BOX["x0"],
+                       x2=BOX["xm"], num_den=[1e11], num_mp=[3000], ef=np.zeros(3 * g.nn))
+    li = po.run_reference("ref_ch2", "load_box", sinp)
+    sinp2 = base_inputs(BOX, dt, ns=[1], sp0_mq=[ME, -QE], seed=[78], x1=BOX["x0"],
+                        x2=[0.0, 0.0, 0.1], num_den=[1e11], num_mp=[600], ef=np.zeros(3 * g.nn))
+    le = po.run_reference("ref_ch2", "load_box", sinp2)
+    Pi0 = li["sp0_P"].reshape(7, -1)
+    Pe0 = le["sp0_P"].reshape(7, -1)
+    st = base_inputs(BOX, dt, steps=[40], ns=[2], sp0_mq=[16 * AMU, QE], sp1_mq=[ME, -QE],
+                     sp0_P=Pi0, sp1_P=Pe0, max_it=[10000], tol=[1e-4], initial_solve=[1])
+    o = po.run_reference("ref_ch2", "steps", st)
+    save("box_steps", Pi0=Pi0, Pe0=Pe0, ui=li["u"], ue=le["u"], dt=dt, steps=40,
+         hist=o["hist"].reshape(41, -1), phi=o["phi"], Pi=o["sp0_P"].reshape(7, -1),
+         Pe=o["sp1_P"].reshape(7, -1))
+
+
+def sphere_cases(rng):
+    g = po.grid(SPH["grid"], SPH["x0"], SPH["xm"])
+    o = po.run_reference("ref_ch3", "objects", base_inputs(SPH, sphere=SPHERE, inlet=[1]))
+    obj, phi_obj = o["object_id"], o["phi"]
+    save("sphere_objects", object_id=obj, phi=phi_obj, sphere=SPHERE)
+
+    dt = 1e-7
+    mi = 16 * AMU
+    phi = smooth_phi(SPH, rng, 20.0)
+    phi[obj > 0] = phi_obj[obj > 0]
+    ef = po.efield(g, phi)
+    # ions: bulk, near walls, near the sphere surface
+    P = rand_particles(rng, SPH, 1500, 4e4, wall_frac=0.15, w=50.0)
+    ns_ = 300
+    d = rng.standard_normal((ns_, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    r = 0.05 + rng.random(ns_) * 4e-3
+    P[0:3, :ns_] = (np.array(SPHERE[:3]) + d * r[:, None]).T
+    P[3:6, :ns_] = (-d * 4e4).T
+    inp = base_inputs(SPH, dt, ns=[1], sp0_mq=[mi, QE, 50.0], sp0_P=P, ef=ef.ravel(),
+                      sphere=SPHERE, inlet=[1])
+    o = po.run_reference("ref_ch3", "push_sphere", inp)
+    save("sphere_push", phi=phi, dt=dt, P=P, P_out=o["sp0_P"].reshape(7, -1))
+
+    o = po.run_reference("ref_ch3", "deposit", inp)
+    vol = po.node_volumes(g)
+    save("sphere_deposit", P=P, den=o["sp0_den"], node_vol=vol)
+    rho = o["sp0_den"] * QE
+
+    ref = [0.0, 3.0, 1e10]
+    gs = {}
+    for tag, tol, mx in (("c2", 1e-4, 20000), ("tight", 1e-9, 400000)):
+        o = po.run_reference("ref_ch3", "gs", base_inputs(SPH, sphere=SPHERE, inlet=[1], rho=rho,
+                                                          ref=ref, max_it=[mx], tol=[tol]))
+        gs["phi_" + tag] = o["phi"]
+        gs["conv_" + tag] = o["conv"]
+    o = po.run_reference("ref_ch3", "qn", base_inputs(SPH, sphere=SPHERE, inlet=[1], rho=rho,
+                                                      ref=ref, max_it=[1], tol=[1.0]))
+    save("sphere_solve", rho=rho, object_id=obj, phi_init=phi_obj, ref=ref, phi_qn=o["phi"], **gs)
+
+    o = po.run_reference("ref_ch3", "efield", base_inputs(SPH, phi=phi))
+    save("sphere_efield", phi=phi, ef=o["ef"].reshape(-1, 3))
+
+    # cold beam injection (ColdBeamSource), uniforms recorded
+    o = po.run_reference("ref_ch3", "inject_cold",
+                         base_inputs(SPH, dt, ns=[1], sp0_mq=[mi, QE, 200.0], ef=ef.ravel(),
+                                     seed=[4321], source=[7000.0, 1e10]))
+    save("inject_cold", phi=phi, dt=dt, mpw0=200.0, v_drift=7000.0, den=1e10, u=o["u"],
+         P=o["sp0_P"].reshape(7, -1))
+    # warm beam injection (ch4 WarmBeamSource), T_i = 0.1 eV
+    T = 0.1 * QE / K
+    o = po.run_reference("ref_ch4", "inject_warm",
+                         base_inputs(SPH, dt, sp0_mq=[mi, QE, 200.0], ef=ef.ravel(), seed=[999],
+                                     source=[7000.0, 1e10, T]))
+    save("inject_warm", phi=phi, dt=dt, mpw0=200.0, v_drift=7000.0, den=1e10, temp=T, u=o["u"],
+         P=o["sp0_P"].reshape(7, -1))
+
+    dens = rng.random((3, g.nn)) * 1e10
+    o = po.run_reference("ref_ch3", "update_average",
+                         base_inputs(SPH, ns=[1], sp0_mq=[mi, QE, 5.0], dens=dens.ravel()))
+    save("update_average", dens=dens, den_ave=o["den_ave"])
+
+    # a short run of the ch3/ver2 main loop (ColdBeamSource, solveGS)
+    st = base_inputs(SPH, dt, steps=[30], ns=[1], sp0_mq=[mi, QE, 5e2], seed=[2024],
+                     sphere=SPHERE, inlet=[1], source=[7000.0, 1e10], ref=[0.0, 1.5, 1e10],
+                     max_it=[20000], tol=[1e-4], initial_solve=[1])
+    o = po.run_reference("ref_ch3", "steps", st)
+    save("sphere_steps", hist=o["hist"].reshape(31, -1), u=o["u"], u_count=o["u_count"],
+         phi=o["phi"], P=o["sp0_P"].reshape(7, -1), den=o["sp0_den"], steps=30, dt=dt,
+         mpw0=5e2)
+
+
+if __name__ == "__main__":
+    build_ref.build_reference()
+    rng = np.random.default_rng(20261203)
+    box_cases(rng)
+    sphere_cases(rng)
