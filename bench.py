@@ -1,0 +1,420 @@
+"""Benchmark of the ES-PIC time step on GB300 (one JSON line on stdout).
+
+Workload (default, the reference's configuration 2): flow past a sphere on a
+64x64x128-node grid over [-0.1,0.1]^2 x [0,0.4] m, sphere r = 0.05 m at
+(0,0,0.15) held at -100 V, z = 0 inlet Dirichlet, other walls Neumann; O+
+warm beam (7 km/s drift, T_i = 0.1 eV, n0 = 1e10 m^-3) with mpw0 = 40 so that
+the steady population is about 4M macroparticles; Boltzmann electrons
+(n0 = 1e10, Te = 3 eV, phi0 = 0); dt = 1e-7 s; Newton-PCG to RMS update
+1e-6 V; counting sort every 20 steps.  The reference has no published
+dataset: the run starts from a synthetic steady-state stand-in, 4M ions
+spread uniformly outside the sphere with the beam's drifting thermal
+velocities (seeded), followed by an initial solve.
+
+A step = inject + push/deposit (+ sort every 20) + charge density + Newton-PCG
++ computeEF.  value = particle-steps/s of the mixed form (int32 cell + f32
+offset + f32 velocity, FP32 PCG under FP64 Newton refinement), timed with
+CUDA events on the library's own stream; the L2 is flushed between timed
+steps (outside the events).  The plain FP64 form runs the same workload.
+e2e = the same step through the C-ABI as a user drives it, with the step's
+injection uniforms copied from pinned host memory and the diagnostics row
+(Output::diagOutput columns) read back every step.
+
+--impl reference times the CPU implementation of the path on this host's
+cores (the C restatement in oracle/: threaded push + deposit as ch9/MT does,
+serial Newton-PCG timed per iteration and scaled to the iteration count the
+GPU needed at this state).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s + Poisson ms/step, mixed vs FP64 on GB300 at phi rel err ≤1e-6"
+QE, AMU, K = 1.602176565e-19, 1.660538921e-27, 1.380648e-23
+
+CONFIGS = {
+    "sphere64": dict(n=(64, 64, 128), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
+                     radius=0.05, phi_s=-100.0, np=4_000_000, mpw0=40.0, dt=1e-7, sort_every=20),
+    "sphere256": dict(n=(256, 256, 512), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
+                      radius=0.04, phi_s=-100.0, np=500_000_000, mpw0=0.32, dt=1e-7, sort_every=20),
+}
+V_DRIFT, N0, TI_EV, TE, PHI0 = 7000.0, 1e10, 0.1, 3.0, 0.0
+NR_TOL, PCG_TOL = 1e-6, 1e-4
+
+
+def espic_module():
+    import importlib
+    return importlib.import_module("plasma-simulations-by-example_gb300")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi clock samples during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 2 + i and s[2 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def synthetic_state(cfg, n, seed):
+    """n ions uniform outside the sphere with drifting thermal velocities."""
+    rng = np.random.default_rng(seed)
+    x0, xm = np.array(cfg["x0"]), np.array(cfg["xm"])
+    c, r = np.array(cfg["center"]), cfg["radius"]
+    m = 16 * AMU
+    vth = np.sqrt(K * TI_EV * QE / K / m)
+    out = np.zeros((7, n))
+    filled = 0
+    while filled < n:
+        b = min(n - filled, 1 << 22)
+        pos = x0 + rng.random((int(b * 1.1) + 16, 3)) * (xm - x0)
+        pos = pos[np.sum((pos - c) ** 2, axis=1) > r * r][:b]
+        k = pos.shape[0]
+        out[0:3, filled:filled + k] = pos.T
+        out[3:6, filled:filled + k] = rng.standard_normal((3, k)) * vth
+        out[5, filled:filled + k] += V_DRIFT
+        filled += k
+    out[6] = cfg["mpw0"]
+    return out
+
+
+def make_world(E, cfg, form, P0, seed=11):
+    ni, nj, nk = cfg["n"]
+    w = E.World(ni, nj, nk, cfg["x0"], cfg["xm"])
+    w.set_seed(seed)
+    w.setTime(cfg["dt"], 1 << 30)
+    w.addSphere(cfg["center"], cfg["radius"], cfg["phi_s"])
+    w.addInlet()
+    cap = int(P0.shape[1] * 1.5) + (1 << 16)
+    s = E.Species(w, "O+", 16 * AMU, QE, mpw0=cfg["mpw0"], capacity=cap, form=form,
+                  walls=E.WALLS_ABSORB)
+    src = E.BeamSource(s, V_DRIFT, N0, TI_EV * QE / K)
+    sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
+    sol.setReferenceValues(PHI0, TE, N0)
+    sol.setNewton(nr_max=20, nr_tol=NR_TOL, pcg_max=20000, pcg_tol=PCG_TOL,
+                  fp32_inner=(form == E.FORM_MIXED))
+    s.set_particles(P0)
+    if form == E.FORM_MIXED:
+        s.sort()
+    s.computeNumberDensity()
+    w.computeChargeDensity()
+    sol.solve()
+    sol.computeEF()
+    return w, s, src, sol
+
+
+def timed_steps(E, torch, w, cfg, steps, warmup, flush):
+    stream = torch.cuda.ExternalStream(w.stream_handle())
+    for _ in range(warmup):
+        w.step(cfg["sort_every"])
+    w.sync()
+    n_before = w.diag_row()[0]
+    l0 = w.launches()
+    s0 = w.solver_totals()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[i][0].record(stream)
+        w.step(cfg["sort_every"])
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    w.sync()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    n_after = w.diag_row()[0]
+    l1 = w.launches()
+    s1 = w.solver_totals()
+    return dict(ms=ms, n=(n_before + n_after) / 2.0, launches=l1 - l0,
+                solves=s1[0] - s0[0], newton=s1[1] - s0[1], inner=s1[2] - s0[2])
+
+
+def profiled_steps(E, w, cfg, steps):
+    w.profile(True)
+    for _ in range(steps):
+        w.step(cfg["sort_every"])
+    ph, _ = w.profile_read()
+    w.profile(False)
+    return {k: v[0] / steps for k, v in ph.items()}, {k: v[1] / steps for k, v in ph.items()}
+
+
+def e2e_steps(E, torch, w, s, src, sol, cfg, steps):
+    """The Main-loop body through the C-ABI: injection uniforms H2D from pinned
+    memory, the phases, the diag row D2H every step."""
+    import ctypes as C
+    lib = E.lib()
+    rng = np.random.default_rng(5)
+    Lx = w.dh[0] * (w.ni - 1)
+    Ly = w.dh[1] * (w.nj - 1)
+    per = N0 * V_DRIFT * Lx * Ly * cfg["dt"] / cfg["mpw0"]
+    nu = 1 + 13 * (int(per) + 2)
+    pinned = torch.empty((steps, nu), dtype=torch.float64, pin_memory=True)
+    pinned.copy_(torch.from_numpy(rng.random((steps, nu))))
+    row = torch.empty(7, dtype=torch.float64, pin_memory=True)
+    used = E.I64()
+    h2d = 0
+    w.sync()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        ptr = C.cast(pinned[i].data_ptr(), E.PD)
+        E.check(lib.espic_source_sample_uniforms(w.h, src.id, ptr, nu, C.byref(used)))
+        h2d += used.value * 8
+        if cfg["sort_every"] and i % cfg["sort_every"] == 0:
+            s.sort()
+        s.advance(deposit=True)
+        w.computeChargeDensity()
+        sol.solve(wait=False)
+        sol.computeEF()
+        E.check(lib.espic_diag_row(w.h, C.cast(row.data_ptr(), E.PD), 7))
+    el = time.perf_counter() - t0
+    return dict(seconds=el, h2d=h2d / steps, d2h=7 * 8, n=float(row[0]))
+
+
+def phi_error(E, w, cfg):
+    """phi of the chosen (FP32-inner) solve against a tight FP64 Newton-PCG
+    on the same charge density."""
+    phi_mixed = w.phi.copy()
+    sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
+    sol.setReferenceValues(PHI0, TE, N0)
+    sol.setNewton(nr_max=50, nr_tol=1e-11, pcg_max=40000, pcg_tol=1e-12, fp32_inner=False)
+    conv, _, _, _ = sol.solve()
+    phi64 = w.phi
+    return float(np.max(np.abs(phi_mixed - phi64)) / np.max(np.abs(phi64))), bool(conv)
+
+
+def cpu_baseline(cfg, P0, inner_per_step, threads, steps=2):
+    """The oracle port on this host: threaded push + compaction + fixed-point
+    deposit on the full particle set (ch9/MT's scheme), and the serial
+    Newton-PCG timed per inner iteration, scaled to the GPU's count."""
+    from oracle import pyoracle as po
+    import ctypes as C
+    g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
+    obj, phi = po.objects(g, cfg["center"], cfg["radius"], cfg["phi_s"])
+    ef = po.efield(g, phi)
+    P = np.ascontiguousarray(P0.copy())
+    n = P.shape[1]
+    sph = np.array(list(cfg["center"]) + [cfg["radius"] ** 2])
+    acc = np.zeros(g.nn, dtype=np.int64)
+    nout = C.c_int64(0)
+    fx = 2.0 ** po.fixed_scale_exponent(cfg["mpw0"], n)
+    t_pd = po.lib().eo_bench_push_deposit(C.byref(g), po.pd(ef), po.pd(sph), QE, 16 * AMU, cfg["dt"], fx,
+                                          po.pd(P), n, n, threads, steps, C.byref(nout), po.pi64(acc))
+    vol = po.node_volumes(g)
+    rho = po.density_from_fixed(acc, fx, vol) * QE
+    it_cap = 8
+    t0 = time.perf_counter()
+    _, _, nr, pcg = po.newton_pcg(g, phi, rho, obj, PHI0, TE, N0, nr_max=1, nr_tol=0.0, pcg_max=it_cap,
+                                  pcg_tol=0.0)
+    t_solve = time.perf_counter() - t0
+    per_iter = t_solve / max(pcg, 1)
+    step_s = t_pd / steps + per_iter * inner_per_step
+    return dict(value=n / step_s, push_deposit_s=t_pd / steps, pcg_iter_s=per_iter,
+                sample="%d steps of threaded push+compaction+deposit over all %d ions (%d threads); "
+                       "serial Newton-PCG timed over %d inner iterations and scaled to %.0f per step"
+                       % (steps, n, threads, pcg, inner_per_step))
+
+
+def run_reference(args):
+    cfg = CONFIGS[args.config]
+    threads = os.cpu_count() or 1
+    P0 = synthetic_state(cfg, cfg["np"] if args.config == "sphere64" else 20_000_000, 1)
+    inner_per_step = float(os.environ.get("ESPIC_REF_INNER_PER_STEP", "800"))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(cfg, P0, inner_per_step, threads, steps=1)
+        if i >= args.warmup:
+            vals.append(b)
+    v = float(np.mean([b["value"] for b in vals]))
+    line = {"metric": METRIC, "value": v, "unit": "particle-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * P0.shape[1] / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.config, "grid": list(cfg["n"]), "particles": P0.shape[1]},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="espic", choices=["espic", "reference"])
+    ap.add_argument("--config", default="sphere64", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain form")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    E = espic_module()
+    if not os.path.exists(E.LIB_PATH):
+        E.build()
+    cfg = CONFIGS[args.config]
+    P0 = synthetic_state(cfg, cfg["np"], 1 + rank)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    # mixed form: the chosen form
+    w, s, src, sol = make_world(E, cfg, E.FORM_MIXED, P0)
+    if dist:
+        dist.barrier()
+    clocks = Clocks()
+    clocks.start()
+    t = timed_steps(E, torch, w, cfg, args.steps, args.warmup, flush)
+    ck = clocks.stop()
+    ms_step = float(np.sum(t["ms"])) / args.steps
+    if dist:
+        tt = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    value = t["n"] * world_size / (ms_step * 1e-3)
+    phases, counts = profiled_steps(E, w, cfg, max(3, min(args.steps, 10)))
+    err, conv64 = phi_error(E, w, cfg)
+    inner_per_step = t["inner"] / max(args.steps, 1)
+    # e2e through the C-ABI (a fresh world, same state)
+    w.close()
+    w, s, src, sol = make_world(E, cfg, E.FORM_MIXED, P0)
+    for _ in range(args.warmup):
+        w.step(cfg["sort_every"])
+    e = e2e_steps(E, torch, w, s, src, sol, cfg, args.steps)
+    w.close()
+
+    # plain FP64 form
+    fp64 = None
+    if not args.no_fp64:
+        w, s, src, sol = make_world(E, cfg, E.FORM_FP64, P0)
+        k64 = max(3, args.steps // 4)
+        t64 = timed_steps(E, torch, w, cfg, k64, 2, flush)
+        ph64, _ = profiled_steps(E, w, cfg, 3)
+        ms64 = float(np.sum(t64["ms"])) / k64
+        fp64 = {"value": t64["n"] / (ms64 * 1e-3), "ms_per_step": ms64, "poisson_ms_per_step": ph64["solve"],
+                "push_ms": ph64["push"], "steps": k64}
+        w.close()
+
+    # roofline of the dominant kernel and of the push
+    hbm, peak_kind = peaks()
+    ni, nj, nk = cfg["n"]
+    n_unknown = (ni - 2) * (nj - 2) * (nk - 2)
+    dom = max(phases, key=lambda k: phases[k])
+    push_bytes = 56.0 * t["n"]
+    push_gbs = push_bytes / (phases["push"] * 1e-3) / 1e9
+    if dom == "solve":
+        alg = 24.0 * n_unknown * inner_per_step
+        achieved = alg / (phases["solve"] * 1e-3) / 1e9
+        kname = "k_newton_pcg<float>"
+    else:
+        alg = push_bytes
+        achieved = push_gbs
+        kname = "k_push_mixed"
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get(args.config, {}).get(kname)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32 particles, f32 PCG under f64 Newton",
+        "data": "synthetic",
+        "config": {"workload": args.config, "grid": list(cfg["n"]), "particles": int(t["n"]),
+                   "mpw0": cfg["mpw0"], "sort_every": cfg["sort_every"], "parallelism": "replicas",
+                   "l2": "flushed between timed steps (256 MB write, outside the events)"},
+        "poisson_ms_per_step": phases["solve"],
+        "phase_ms_per_step": phases,
+        "newton_per_step": t["newton"] / args.steps, "pcg_iterations_per_step": inner_per_step,
+        "phi_rel_err_vs_fp64": err, "fp64_reference_converged": conv64,
+        "fp64": fp64,
+        "speedup_mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        "e2e": {"value": e["n"] * world_size / (e["seconds"] / args.steps), "unit": "particle-steps/s",
+                "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"]},
+        "gpu_launches": t["launches"],
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg},
+        "roofline_push": {"bound": "hbm", "kernel": "k_push_mixed", "achieved": push_gbs, "peak": hbm,
+                          "unit": "GB/s", "frac": push_gbs / hbm, "bytes_per_particle": 56},
+        "clocks": ck,
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        b = cpu_baseline(cfg, P0, inner_per_step, threads)
+        line["cpu_baseline"] = {"value": b["value"], "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                                "sample": b["sample"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

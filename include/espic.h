@@ -1,0 +1,217 @@
+/*
+ * espic.h -- C-ABI of libespic, the GB300-native electrostatic PIC time step
+ * of "Plasma Simulations by Example" (ch2 grounded box, ch3/ver2 flow past a
+ * sphere, ch4 warm-beam injector).
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes and
+ * returns an int status (ESPIC_OK = 0; > 0 not converged; < 0 error).  No
+ * C++ exception crosses this boundary.  Host pointers are ordinary host
+ * memory; the library owns all device memory of a world.  All work of a
+ * world is ordered on one CUDA stream; calls that return values computed on
+ * the device synchronise that stream, the others only enqueue work.
+ *
+ * Each function names the reference interface it replaces (file:line in the
+ * reference tree).
+ */
+#ifndef ESPIC_H
+#define ESPIC_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------- */
+#define ESPIC_OK 0
+#define ESPIC_NOT_CONVERGED 1  /* PotentialSolver::solve returned false */
+#define ESPIC_ERR_ARG (-1)     /* bad argument or handle */
+#define ESPIC_ERR_CUDA (-2)    /* CUDA runtime error (message in espic_last_error) */
+#define ESPIC_ERR_CAPACITY (-3)/* particle buffer full; particles were not added */
+#define ESPIC_ERR_NONFINITE (-4) /* NaN or Inf in the potential solve */
+#define ESPIC_ERR_FIXED (-5)   /* weight outside the fixed-point deposit range */
+#define ESPIC_ERR_STATE (-6)   /* call not valid in this state */
+
+/* particle storage forms */
+#define ESPIC_FORM_FP64 0  /* x, v, mpw in float64 (bit-exact with the reference) */
+#define ESPIC_FORM_MIXED 1 /* int32 cell + float32 in-cell offset + float32 velocity */
+
+/* wall treatment of a species */
+#define ESPIC_WALLS_REFLECT 0 /* ch2/Species.cpp:32-36 one-bounce mirror */
+#define ESPIC_WALLS_ABSORB 1  /* ch3/ver2/Species.cpp:28-32 (also absorbed by the sphere) */
+
+/* potential solvers (ch2/PotentialSolver.h:6-23, ch3/ver2/PotentialSolver.h:40) */
+#define ESPIC_SOLVER_SOR 0        /* linear Poisson, Dirichlet walls, red-black SOR (ch2) */
+#define ESPIC_SOLVER_GS 1         /* Boltzmann electrons, red-black nonlinear SOR (ch3 GS) */
+#define ESPIC_SOLVER_PCG 2        /* Boltzmann electrons, Newton + Jacobi-PCG (ch3 PCG) */
+#define ESPIC_SOLVER_QN 3         /* quasi-neutral log inversion (ch3 QN) */
+
+/* node fields for espic_field_read / espic_field_write */
+#define ESPIC_FIELD_PHI 0
+#define ESPIC_FIELD_RHO 1
+#define ESPIC_FIELD_NODE_VOL 2
+#define ESPIC_FIELD_EF 3      /* 3 values per node, interleaved */
+#define ESPIC_FIELD_DEN 4     /* number density of one species */
+#define ESPIC_FIELD_DEN_AVE 5 /* running average of den */
+#define ESPIC_FIELD_OBJECT_ID 6 /* int32 values travelled as float64 */
+
+typedef struct espic_world espic_world;
+
+/* Copies the last error message of the calling thread into buf. */
+int espic_last_error(char *buf, int len);
+
+/* ---- World --------------------------------------------------------------- */
+/* World::World + World::setExtents, ch2/World.cpp:14-36 (ch3/ver2/World.cpp:14-38).
+ * Node volumes are computed for (ni,nj,nk); dh = (xm-x0)/(n-1). */
+int espic_world_create(int ni, int nj, int nk, const double x0[3], const double xm[3],
+                       espic_world **out);
+int espic_world_destroy(espic_world *w);
+/* World::setTime, ch2/World.h:66 */
+int espic_world_set_time(espic_world *w, double dt, int num_ts);
+/* World::advanceTime, ch2/World.h:69: returns 1 while ts <= num_ts, else 0
+ * (the reference's loop runs num_ts + 1 iterations). */
+int espic_world_advance_time(espic_world *w);
+/* World::getTs / getTime */
+int espic_world_get_time(espic_world *w, int *ts, double *time);
+/* World::addSphere, ch3/ver2/World.cpp:88-106 */
+int espic_world_add_sphere(espic_world *w, const double center[3], double radius, double phi_sphere);
+/* World::addInlet, ch3/ver2/World.cpp:109-116 */
+int espic_world_add_inlet(espic_world *w);
+/* Key of the Philox streams behind every random draw of this world (the
+ * reference seeds a global mt19937 from std::random_device, ch2/World.h:24-33). */
+int espic_world_set_seed(espic_world *w, uint64_t seed);
+/* Waits for the world's stream; returns any error flagged on the device. */
+int espic_world_sync(espic_world *w);
+/* The cudaStream_t (as void*) on which all of the world's work is ordered, so
+ * that a caller can record events on it or order its own work after it.  No
+ * reference counterpart (the reference has no device stream). */
+int espic_world_stream(espic_world *w, void **stream);
+
+/* ---- Species ------------------------------------------------------------- */
+/* Species::Species, ch2/Species.h:25-28 (mpw0 = 0) and ch3/ver2/Species.h:25-29.
+ * capacity = maximum number of macroparticles kept on the device;
+ * weight_bound = largest macroparticle weight the fixed-point deposit must
+ * hold (0: use mpw0, or the weight of the first load). */
+int espic_species_create(espic_world *w, double mass, double charge, double mpw0, int64_t capacity,
+                         int form, int walls, double weight_bound, int *species_id);
+/* Species::getNp, ch2/Species.h:31 */
+int espic_species_count(espic_world *w, int sp, int64_t *np);
+/* Species::addParticle for n particles, ch2/Species.cpp:55-71: particles outside
+ * [x0,xm) are rejected; velocities are rewound by (q/m) E dt/2.  pos3/vel3 are
+ * [n][3], mpw is [n] (NULL: mpw0). */
+int espic_species_add(espic_world *w, int sp, const double *pos3, const double *vel3,
+                      const double *mpw, int64_t n);
+/* Direct state access through the public Species::particles vector
+ * (ch2/Species.h:60): P is [7][stride] = x, y, z, vx, vy, vz, mpw; no rewind.
+ * espic_species_set replaces the particles; espic_species_get copies them out
+ * (the mixed form is converted to float64). */
+int espic_species_set(espic_world *w, int sp, const double *P, int64_t stride, int64_t n);
+int espic_species_get(espic_world *w, int sp, double *P, int64_t stride, int64_t cap, int64_t *n);
+/* Species::loadParticlesBox, ch2/Species.cpp:74-97.  u = 3*num_mp uniforms
+ * (x, y, z per particle) or NULL to draw them from the world's Philox stream. */
+int espic_species_load_box(espic_world *w, int sp, const double x1[3], const double x2[3],
+                           double num_den, int64_t num_mp, const double *u);
+/* Species::loadParticlesBoxQS, ch2/Species.cpp:101-141 */
+int espic_species_load_box_qs(espic_world *w, int sp, const double x1[3], const double x2[3],
+                              double num_den, const int num_mp[3]);
+
+/* ---- the time step ------------------------------------------------------- */
+/* Species::advance, ch2/Species.cpp:7-38 (reflect) or ch3/ver2/Species.cpp:7-48
+ * (absorb + removal).  With deposit != 0 the push also performs
+ * Species::computeNumberDensity (ch2/Species.cpp:41-52) on the moved particles. */
+int espic_push(espic_world *w, int sp, int deposit);
+/* Species::computeNumberDensity, ch2/Species.cpp:41-52 (fixed-point deposit). */
+int espic_deposit(espic_world *w, int sp);
+/* World::computeChargeDensity, ch2/World.cpp:46-54 */
+int espic_charge_density(espic_world *w);
+/* counting sort of a species by cell (mixed form; no-op for float64) */
+int espic_sort(espic_world *w, int sp);
+/* ColdBeamSource (ch3/ver2/Source.h:8-21; temp = 0) and WarmBeamSource
+ * (ch4/Source.h:32-46; temp in K) on the z = x0 face. */
+int espic_source_create(espic_world *w, int sp, double v_drift, double den, double temp,
+                        int *source_id);
+/* ColdBeamSource::sample / WarmBeamSource::sample, ch3/ver2/Source.cpp:4-27,
+ * ch4/Source.cpp:31-55, drawing from the world's Philox stream. */
+int espic_source_sample(espic_world *w, int source);
+/* The same with the uniforms given (the reference's order: the count draw,
+ * then 2 per particle for a cold source, 13 per particle for a warm one);
+ * *used receives the number consumed. */
+int espic_source_sample_uniforms(espic_world *w, int source, const double *u, int64_t nu,
+                                 int64_t *used);
+
+/* PotentialSolver constructor arguments: ch2/PotentialSolver.h:9-10
+ * (max_it, tol) and ch3/ver2/PotentialSolver.h:46-50 (type, max_it, tol). */
+int espic_solver_set(espic_world *w, int kind, int max_it, double tol);
+/* PotentialSolver::setReferenceValues(phi0, Te0, n0), ch3/ver2/PotentialSolver.h:53-57 */
+int espic_solver_set_reference(espic_world *w, double phi0, double te0, double n0);
+/* Newton-PCG controls: at most nr_max Newton steps, stop when RMS(update) <
+ * nr_tol (ch3/ver2/PotentialSolver.cpp:228-229); inner PCG stops at
+ * |r| <= pcg_tol |F|; fp32_inner = 1 runs the PCG in float32 under the
+ * float64 Newton residual (iterative refinement). */
+int espic_solver_set_newton(espic_world *w, int nr_max, double nr_tol, int pcg_max,
+                            double pcg_tol, int fp32_inner);
+/* PotentialSolver::solve, ch2/PotentialSolver.cpp:11-67 and
+ * ch3/ver2/PotentialSolver.h:66-75.  With all out-pointers NULL the solve is
+ * only enqueued; otherwise the call waits and reports iterations and the
+ * final residual.  Returns ESPIC_NOT_CONVERGED when the reference's solve
+ * would return false. */
+int espic_solve(espic_world *w, int *iterations, int *inner_iterations, double *residual);
+/* PotentialSolver::computeEF, ch2/PotentialSolver.cpp:70-110 */
+int espic_efield(espic_world *w);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+/* Species::getRealCount, getMomentum, getKE, ch2/Species.cpp:144-168:
+ * out = {real count, px, py, pz, KE} */
+int espic_species_diag(espic_world *w, int sp, double out[5]);
+/* World::getPE, ch2/World.cpp:72-84 */
+int espic_potential_energy(espic_world *w, double *pe);
+/* The per-step columns of Output::diagOutput, ch3/ver2/Output.cpp:96-132, with
+ * one device round trip: for each species {np, real count, px, py, pz, KE},
+ * then PE.  row must hold 6*ns + 1 values. */
+int espic_diag_row(espic_world *w, double *row, int len);
+/* Species::updateAverages / Field_::updateAverage, ch3/ver2/Field.h:214-220 */
+int espic_update_average(espic_world *w, int sp);
+/* World::steadyState, ch3/ver2/World.cpp:129-158 */
+int espic_steady_state(espic_world *w, int *steady);
+
+/* ---- node fields ------------------------------------------------------------ */
+/* Host mirrors of World::phi/rho/node_vol/ef/object_id and Species::den/den_ave
+ * (the device copy is authoritative, as updateHostPhi in
+ * ch9/CUDA/PotentialSolver.cu:323-328).  n = number of float64 values. */
+int espic_field_read(espic_world *w, int field, int sp, double *host, int64_t n);
+int espic_field_write(espic_world *w, int field, int sp, const double *host, int64_t n);
+
+/* ---- measurement -------------------------------------------------------------- */
+/* phases timed by espic_profile (CUDA events on the world's stream) */
+#define ESPIC_PHASE_INJECT 0  /* source sampling and loads */
+#define ESPIC_PHASE_SORT 1    /* counting sort by cell */
+#define ESPIC_PHASE_PUSH 2    /* the push kernel (with its fused deposit) */
+#define ESPIC_PHASE_COMPACT 3 /* removal of absorbed particles */
+#define ESPIC_PHASE_DENSITY 4 /* accumulator clear, density and charge density */
+#define ESPIC_PHASE_SOLVE 5   /* potential solve */
+#define ESPIC_PHASE_EFIELD 6  /* computeEF */
+#define ESPIC_PHASE_DIAG 7    /* diagnostics reductions */
+#define ESPIC_NPHASES 8
+/* Turns per-phase event timing on (1) or off (0); turning it on clears the
+ * totals.  The reference only records wall time per step
+ * (ch2/World.cpp:39-43, ch2/Output.cpp:99). */
+int espic_profile(espic_world *w, int enable);
+/* Waits for the world's stream and returns, per phase, the summed device
+ * milliseconds and the number of timed ranges; *launches receives the number
+ * of kernels launched on this world so far. */
+int espic_profile_read(espic_world *w, double ms[ESPIC_NPHASES], int64_t count[ESPIC_NPHASES],
+                       int64_t *launches);
+/* Totals over all solves so far: Newton (or SOR) iterations and inner PCG
+ * iterations, summed on the device. */
+int espic_solver_totals(espic_world *w, int64_t *solves, int64_t *outer, int64_t *inner);
+
+/* ---- one whole step --------------------------------------------------------- */
+/* One iteration of the ch3/ver2/Main.cpp:50-72 loop body: sample every
+ * source, push + deposit every species (sorting mixed species every
+ * sort_every steps), charge density, solve, computeEF.  When row != NULL the
+ * diag row of espic_diag_row is also returned (one synchronisation). */
+int espic_step(espic_world *w, int sort_every, double *row, int len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

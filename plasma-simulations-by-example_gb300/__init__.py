@@ -1,0 +1,393 @@
+"""Python view of libespic, the GB300-native electrostatic PIC time step.
+
+The product is the C-ABI shared library built from csrc/ (declared in
+include/espic.h) and the C++ drop-in headers in shim/.  This module is a thin
+ctypes harness over the same C-ABI, used by the tests and the benchmark.  It
+has no compute of its own and no CPU path: if the library is missing or no GPU
+is present, creating a World raises.
+
+Class and method names follow the reference (World, Species, PotentialSolver,
+ColdBeamSource / WarmBeamSource); see include/espic.h for the reference
+interface each call replaces.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libespic.so")
+
+OK, NOT_CONVERGED = 0, 1
+FORM_FP64, FORM_MIXED = 0, 1
+WALLS_REFLECT, WALLS_ABSORB = 0, 1
+SOLVER_SOR, SOLVER_GS, SOLVER_PCG, SOLVER_QN = 0, 1, 2, 3
+FIELD_PHI, FIELD_RHO, FIELD_NODE_VOL, FIELD_EF, FIELD_DEN, FIELD_DEN_AVE, FIELD_OBJECT_ID = range(7)
+
+QE, AMU, ME, K, EPS_0 = 1.602176565e-19, 1.660538921e-27, 9.10938215e-31, 1.380648e-23, 8.85418782e-12
+
+_lib = None
+
+PD = C.POINTER(C.c_double)
+PI = C.POINTER(C.c_int)
+I64 = C.c_int64
+VP = C.c_void_p
+
+
+class EspicError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("espic status %d: %s" % (code, msg))
+        self.code = code
+
+
+def build(force=False):
+    from importlib import util
+    spec = util.spec_from_file_location("_espic_build", os.path.join(PKG_DIR, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """The loaded libespic.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise EspicError(-2, "libespic.so not built (run __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        sigs = {
+            "espic_last_error": [C.c_char_p, C.c_int],
+            "espic_world_create": [C.c_int, C.c_int, C.c_int, PD, PD, C.POINTER(VP)],
+            "espic_world_destroy": [VP],
+            "espic_world_set_time": [VP, C.c_double, C.c_int],
+            "espic_world_advance_time": [VP],
+            "espic_world_get_time": [VP, PI, PD],
+            "espic_world_add_sphere": [VP, PD, C.c_double, C.c_double],
+            "espic_world_add_inlet": [VP],
+            "espic_world_set_seed": [VP, C.c_uint64],
+            "espic_world_sync": [VP],
+            "espic_world_stream": [VP, C.POINTER(VP)],
+            "espic_species_create": [VP, C.c_double, C.c_double, C.c_double, I64, C.c_int, C.c_int,
+                                     C.c_double, PI],
+            "espic_species_count": [VP, C.c_int, C.POINTER(I64)],
+            "espic_species_add": [VP, C.c_int, PD, PD, PD, I64],
+            "espic_species_set": [VP, C.c_int, PD, I64, I64],
+            "espic_species_get": [VP, C.c_int, PD, I64, I64, C.POINTER(I64)],
+            "espic_species_load_box": [VP, C.c_int, PD, PD, C.c_double, I64, PD],
+            "espic_species_load_box_qs": [VP, C.c_int, PD, PD, C.c_double, PI],
+            "espic_push": [VP, C.c_int, C.c_int],
+            "espic_deposit": [VP, C.c_int],
+            "espic_charge_density": [VP],
+            "espic_sort": [VP, C.c_int],
+            "espic_source_create": [VP, C.c_int, C.c_double, C.c_double, C.c_double, PI],
+            "espic_source_sample": [VP, C.c_int],
+            "espic_source_sample_uniforms": [VP, C.c_int, PD, I64, C.POINTER(I64)],
+            "espic_solver_set": [VP, C.c_int, C.c_int, C.c_double],
+            "espic_solver_set_reference": [VP, C.c_double, C.c_double, C.c_double],
+            "espic_solver_set_newton": [VP, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int],
+            "espic_solve": [VP, PI, PI, PD],
+            "espic_efield": [VP],
+            "espic_species_diag": [VP, C.c_int, PD],
+            "espic_potential_energy": [VP, PD],
+            "espic_diag_row": [VP, PD, C.c_int],
+            "espic_update_average": [VP, C.c_int],
+            "espic_steady_state": [VP, PI],
+            "espic_field_read": [VP, C.c_int, C.c_int, PD, I64],
+            "espic_field_write": [VP, C.c_int, C.c_int, PD, I64],
+            "espic_step": [VP, C.c_int, PD, C.c_int],
+            "espic_profile": [VP, C.c_int],
+            "espic_profile_read": [VP, PD, C.POINTER(I64), C.POINTER(I64)],
+            "espic_solver_totals": [VP, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)],
+        }
+        for name, args in sigs.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def last_error():
+    buf = C.create_string_buffer(512)
+    lib().espic_last_error(buf, 512)
+    return buf.value.decode()
+
+
+def check(rc, allow=(OK,)):
+    if rc not in allow:
+        raise EspicError(rc, last_error())
+    return rc
+
+
+def _pd(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(PD)
+
+
+def _d3(v):
+    return (C.c_double * 3)(*[float(x) for x in v])
+
+
+class World:
+    """World (ch2/World.h:38-110, ch3/ver2/World.h:38-147) on the GPU."""
+
+    def __init__(self, ni, nj, nk, x0, xm):
+        h = VP()
+        check(lib().espic_world_create(ni, nj, nk, _d3(x0), _d3(xm), C.byref(h)))
+        self.h = h
+        self.ni, self.nj, self.nk = ni, nj, nk
+        self.nn = ni * nj * nk
+        self.x0 = np.array(x0, dtype=float)
+        self.xm = np.array(xm, dtype=float)
+        self.dh = (self.xm - self.x0) / (np.array([ni, nj, nk]) - 1)
+        self.species = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().espic_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # World API
+    def setTime(self, dt, num_ts):
+        self.dt = dt
+        check(lib().espic_world_set_time(self.h, dt, num_ts))
+
+    def advanceTime(self):
+        return bool(lib().espic_world_advance_time(self.h))
+
+    def addSphere(self, center, radius, phi_sphere):
+        check(lib().espic_world_add_sphere(self.h, _d3(center), radius, phi_sphere))
+
+    def addInlet(self):
+        check(lib().espic_world_add_inlet(self.h))
+
+    def set_seed(self, seed):
+        check(lib().espic_world_set_seed(self.h, seed))
+
+    def sync(self):
+        check(lib().espic_world_sync(self.h))
+
+    def stream_handle(self):
+        """The raw cudaStream_t of this world (for events on its stream)."""
+        v = VP()
+        check(lib().espic_world_stream(self.h, C.byref(v)))
+        return v.value
+
+    def computeChargeDensity(self):
+        check(lib().espic_charge_density(self.h))
+
+    def getPE(self):
+        v = C.c_double()
+        check(lib().espic_potential_energy(self.h, C.byref(v)))
+        return v.value
+
+    def steadyState(self):
+        v = C.c_int()
+        check(lib().espic_steady_state(self.h, C.byref(v)))
+        return bool(v.value)
+
+    def diag_row(self):
+        row = np.zeros(6 * len(self.species) + 1)
+        check(lib().espic_diag_row(self.h, _pd(row), row.size))
+        return row
+
+    def step(self, sort_every=0, row=None):
+        if row is None:
+            check(lib().espic_step(self.h, sort_every, None, 0))
+            return None
+        check(lib().espic_step(self.h, sort_every, _pd(row), row.size))
+        return row
+
+    # measurement
+    PHASES = ("inject", "sort", "push", "compact", "density", "solve", "efield", "diag")
+
+    def profile(self, enable=True):
+        check(lib().espic_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        ms = np.zeros(8)
+        cnt = (I64 * 8)()
+        nl = I64()
+        check(lib().espic_profile_read(self.h, _pd(ms), cnt, C.byref(nl)))
+        return {p: (ms[i], cnt[i]) for i, p in enumerate(self.PHASES)}, nl.value
+
+    def launches(self):
+        nl = I64()
+        check(lib().espic_profile_read(self.h, None, None, C.byref(nl)))
+        return nl.value
+
+    def solver_totals(self):
+        a, b, c = I64(), I64(), I64()
+        check(lib().espic_solver_totals(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    # fields
+    def read(self, field, sp=0):
+        if field == FIELD_EF:
+            out = np.zeros((self.nn, 3))
+        else:
+            out = np.zeros(self.nn)
+        check(lib().espic_field_read(self.h, field, sp, _pd(out), out.size))
+        return out
+
+    def write(self, field, data, sp=0):
+        a = np.ascontiguousarray(data, dtype=np.float64)
+        check(lib().espic_field_write(self.h, field, sp, _pd(a), a.size))
+
+    @property
+    def phi(self):
+        return self.read(FIELD_PHI)
+
+    @property
+    def rho(self):
+        return self.read(FIELD_RHO)
+
+    @property
+    def ef(self):
+        return self.read(FIELD_EF)
+
+    @property
+    def node_vol(self):
+        return self.read(FIELD_NODE_VOL)
+
+    @property
+    def object_id(self):
+        return self.read(FIELD_OBJECT_ID).astype(np.int32)
+
+
+class Species:
+    """Species (ch2/Species.h:22-65, ch3/ver2/Species.h:22-72) on the GPU."""
+
+    def __init__(self, world, name, mass, charge, mpw0=0.0, capacity=1 << 20, form=FORM_FP64,
+                 walls=WALLS_REFLECT, weight_bound=0.0):
+        sid = C.c_int()
+        check(lib().espic_species_create(world.h, mass, charge, mpw0, int(capacity), form, walls,
+                                         weight_bound, C.byref(sid)))
+        self.world, self.name, self.mass, self.charge, self.mpw0 = world, name, mass, charge, mpw0
+        self.id = sid.value
+        self.form = form
+        self.capacity = capacity
+        world.species.append(self)
+
+    def getNp(self):
+        n = I64()
+        check(lib().espic_species_count(self.world.h, self.id, C.byref(n)))
+        return n.value
+
+    def addParticles(self, pos3, vel3, mpw=None):
+        pos3 = np.ascontiguousarray(pos3, dtype=np.float64)
+        vel3 = np.ascontiguousarray(vel3, dtype=np.float64)
+        w = None if mpw is None else np.ascontiguousarray(mpw, dtype=np.float64)
+        check(lib().espic_species_add(self.world.h, self.id, _pd(pos3), _pd(vel3), _pd(w),
+                                      pos3.shape[0]))
+
+    def set_particles(self, P):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        check(lib().espic_species_set(self.world.h, self.id, _pd(P), P.shape[1], P.shape[1]))
+
+    def particles(self):
+        n = self.getNp()
+        P = np.zeros((7, max(n, 1)))
+        m = I64()
+        check(lib().espic_species_get(self.world.h, self.id, _pd(P), P.shape[1], P.shape[1],
+                                      C.byref(m)))
+        return np.ascontiguousarray(P[:, :m.value])
+
+    def loadParticlesBox(self, x1, x2, num_den, num_mp, u=None):
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().espic_species_load_box(self.world.h, self.id, _d3(x1), _d3(x2), num_den,
+                                           int(num_mp), _pd(u)))
+
+    def loadParticlesBoxQS(self, x1, x2, num_den, num_mp):
+        nm = (C.c_int * 3)(*[int(x) for x in num_mp])
+        check(lib().espic_species_load_box_qs(self.world.h, self.id, _d3(x1), _d3(x2), num_den, nm))
+
+    def advance(self, deposit=False):
+        check(lib().espic_push(self.world.h, self.id, 1 if deposit else 0))
+
+    def computeNumberDensity(self):
+        check(lib().espic_deposit(self.world.h, self.id))
+
+    def sort(self):
+        check(lib().espic_sort(self.world.h, self.id))
+
+    def diag(self):
+        out = np.zeros(5)
+        check(lib().espic_species_diag(self.world.h, self.id, _pd(out)))
+        return out
+
+    def updateAverages(self):
+        check(lib().espic_update_average(self.world.h, self.id))
+
+    @property
+    def den(self):
+        return self.world.read(FIELD_DEN, self.id)
+
+    @property
+    def den_ave(self):
+        return self.world.read(FIELD_DEN_AVE, self.id)
+
+
+class BeamSource:
+    """ColdBeamSource (temp = 0, ch3/ver2/Source.h:8-21) and WarmBeamSource
+    (ch4/Source.h:32-46) on the z = x0 face."""
+
+    def __init__(self, species, v_drift, den, temp=0.0):
+        sid = C.c_int()
+        check(lib().espic_source_create(species.world.h, species.id, v_drift, den, temp,
+                                        C.byref(sid)))
+        self.world = species.world
+        self.id = sid.value
+        self.temp = temp
+
+    def sample(self, u=None):
+        if u is None:
+            check(lib().espic_source_sample(self.world.h, self.id))
+            return None
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        used = I64()
+        check(lib().espic_source_sample_uniforms(self.world.h, self.id, _pd(u), u.size,
+                                                 C.byref(used)))
+        return used.value
+
+
+class PotentialSolver:
+    """PotentialSolver (ch2/PotentialSolver.h:6-23, ch3/ver2/PotentialSolver.h:42-104)."""
+
+    def __init__(self, world, kind=SOLVER_SOR, max_it=10000, tol=1e-4):
+        self.world = world
+        check(lib().espic_solver_set(world.h, kind, max_it, tol))
+
+    def setReferenceValues(self, phi0, te0, n0):
+        check(lib().espic_solver_set_reference(self.world.h, phi0, te0, n0))
+
+    def setNewton(self, nr_max=20, nr_tol=1e-3, pcg_max=10000, pcg_tol=1e-6, fp32_inner=False):
+        check(lib().espic_solver_set_newton(self.world.h, nr_max, nr_tol, pcg_max, pcg_tol,
+                                            1 if fp32_inner else 0))
+
+    def solve(self, wait=True):
+        """Returns (converged, iterations, inner_iterations, residual)."""
+        if not wait:
+            check(lib().espic_solve(self.world.h, None, None, None))
+            return None
+        it, inner, res = C.c_int(), C.c_int(), C.c_double()
+        rc = check(lib().espic_solve(self.world.h, C.byref(it), C.byref(inner), C.byref(res)),
+                   allow=(OK, NOT_CONVERGED))
+        return rc == OK, it.value, inner.value, res.value
+
+    def computeEF(self):
+        check(lib().espic_efield(self.world.h))

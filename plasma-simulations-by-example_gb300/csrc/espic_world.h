@@ -1,0 +1,114 @@
+/*
+ * espic_world.h -- host-side records of a World and its Species (device
+ * pointers plus the scalars the launchers need).  Internal to libespic.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <vector>
+
+#include "espic_internal.h"
+
+namespace espic {
+
+struct Species {
+    int id = 0;
+    int form = 0;   /* ESPIC_FORM_* */
+    int walls = 0;  /* ESPIC_WALLS_* */
+    double mass = 0, charge = 0, mpw0 = 0;
+    bool uniform_w = true; /* every particle carries mpw0: the weight row is not read */
+    int64_t cap = 0;
+    /* float64 form: [7][cap] */
+    double *P = nullptr;
+    /* mixed form */
+    int32_t *cell = nullptr, *cell2 = nullptr;
+    float *off = nullptr, *off2 = nullptr; /* [3][cap] */
+    float *vel = nullptr, *vel2 = nullptr; /* [3][cap] */
+    int32_t *sort_count = nullptr;         /* [ncells + 1] */
+    /* compaction */
+    uint32_t *deadmask = nullptr; /* [cap/32 + 1] */
+    int32_t *tiledead = nullptr;  /* [ntiles + 1] */
+    int32_t *tilepre = nullptr;   /* [ntiles + 1] exclusive prefix */
+    int32_t *holes = nullptr;     /* [cap] */
+    int64_t ntiles = 0;
+    int64_t *d_count = nullptr; /* device particle count; [1] = count before compaction */
+    int64_t host_bound = 0;     /* an upper bound of *d_count known without syncing */
+    /* deposit */
+    unsigned long long *acc = nullptr; /* [nn] int64 two's complement */
+    double *den = nullptr, *den_ave = nullptr;
+    int ave_samples = 0;
+    double fx = 1.0;      /* float64 form: quantum 1/fx (fx = 2^S) of real particles */
+    double unit = 1.0;    /* real particles per accumulator count: 1/fx or mpw0*2^-24 */
+    double weight_bound = 0;
+    bool deposit_valid = false;
+};
+
+struct Source {
+    int sp = 0;
+    double v_drift = 0, den = 0, temp = 0;
+    uint64_t calls = 0;
+};
+
+struct World {
+    Geo g{};
+    int64_t nn = 0;
+    double dt = 0, time = 0;
+    int num_ts = 0, ts = -1;
+    cudaStream_t stream = nullptr;
+    int device = 0, sm_count = 0;
+    double *phi = nullptr, *rho = nullptr, *vol = nullptr, *ef = nullptr;
+    float4 *ef4 = nullptr;
+    bool ef4_valid = false;
+    int32_t *obj = nullptr, *target = nullptr;
+    bool targets_valid = false;
+    double sphere[4] = {0, 0, 0, 0}; /* centre, radius^2 */
+    bool has_sphere = false;
+    int *d_err = nullptr;
+    SolveStatus *d_status = nullptr;
+    double *d_partials = nullptr; /* reduction scratch */
+    int partial_slots = 0;
+    double *d_small = nullptr;    /* small results (diag row) */
+    double *h_small = nullptr;    /* pinned mirror */
+    double *d_u = nullptr;        /* staging for host-given uniforms */
+    int64_t d_u_cap = 0;
+    double *d_stage = nullptr;    /* staging for host particles */
+    int32_t *d_blockcnt = nullptr; /* per-block counts of an append */
+    int64_t blockcnt_cap = 0;
+    int64_t d_stage_cap = 0;
+    /* solver */
+    int solver_kind = 0, max_it = 10000;
+    double tol = 1e-4, phi0 = 0, te0 = 1.5, n0 = 1e12;
+    int nr_max = 20, pcg_max = 10000, fp32_inner = 0;
+    double nr_tol = 1e-3, pcg_tol = 1e-6;
+    void *pcg_buf = nullptr;
+    bool pcg_codes_valid = false;
+    size_t pcg_bytes = 0;
+    uint64_t seed = 0x5eed5eed12345ull;
+    uint64_t load_calls = 0;
+    int64_t step_count = 0;
+    int64_t nlaunch = 0; /* kernels launched on this world's stream */
+    /* steady state, ch3/ver2/World.h:137-141 */
+    bool steady = false;
+    double last_mass = 0, last_mom = 0, last_en = 0;
+    std::vector<Species *> species;
+    std::vector<Source> sources;
+    /* per-phase event timing */
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    struct Range {
+        int phase;
+        cudaEvent_t a, b;
+    };
+    std::vector<Range> ranges;
+    double prof_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t prof_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+inline int blocks_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 0x7fffffff) b = 0x7fffffff;
+    return (int)b;
+}
+
+}  // namespace espic

@@ -1,0 +1,1256 @@
+/*
+ * k_fp64.cu -- the float64 plain form of the ES-PIC step, plus the field
+ * kernels shared by both forms.  Compiled with -fmad=false: every product
+ * and sum is rounded separately, in the reference's operand order, so that
+ * positions, velocities, cell indices, absorbed counts and fields reproduce
+ * the reference's g++ results bit for bit.
+ *
+ * Reference correspondence (file:line in the reference tree):
+ *   gather           ch2/Field.h:186-208        k_push_fp64, gather3
+ *   scatter          ch2/Field.h:164-183        deposit8 (fixed point)
+ *   advance (box)    ch2/Species.cpp:7-38       k_push_fp64<REFLECT>
+ *   advance (sphere) ch3/ver2/Species.cpp:7-48  k_push_fp64<ABSORB> + compaction
+ *   addParticle      ch2/Species.cpp:55-71      k_append (all generators)
+ *   computeEF        ch2/PotentialSolver.cpp:70-110   k_efield
+ *   solve (SOR)      ch2/PotentialSolver.cpp:11-67    k_sor_box (red-black)
+ *   solveGS          ch3/ver2/PotentialSolver.cpp:334-430 k_gs_sphere (red-black)
+ *   solveQN          ch3/ver2/PotentialSolver.cpp:204-222 k_qn
+ */
+#include <cooperative_groups.h>
+#include <stdio.h>
+
+#include "espic_world.h"
+
+namespace cg = cooperative_groups;
+
+namespace espic {
+
+#define EPS_0 8.85418782e-12
+#define QE 1.602176565e-19
+#define KB 1.380648e-23
+#define REF_PI 3.141592653
+
+enum { REFLECT = 0, ABSORB = 1 };
+
+__device__ __forceinline__ int clamp_cell(int i, int n) { return i < 0 ? 0 : (i > n - 2 ? n - 2 : i); }
+
+__device__ __forceinline__ int64_t node_of(const Geo &g, int i, int j, int k) {
+    return ((int64_t)k * g.nj + j) * g.ni + i;
+}
+
+/* Field_<double3>::gather with the index clamp: out-of-range truncated
+ * indices (only reachable at x == xm after a one-bounce reflection) are
+ * moved to n-2 keeping di = lc - i, which gives the same weights without
+ * reading node n. */
+__device__ __forceinline__ void gather3(const Geo &g, const double *__restrict__ ef, const double lc[3],
+                                        double e[3]) {
+    int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj), k = clamp_cell((int)lc[2], g.nk);
+    double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+    int64_t n0 = node_of(g, i, j, k);
+    int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    const double *a = ef + 3 * n0;
+    const double *b = ef + 3 * (n0 + 1);
+    const double *c = ef + 3 * (n0 + 1 + sy);
+    const double *d = ef + 3 * (n0 + sy);
+    const double *e4 = ef + 3 * (n0 + sz);
+    const double *f = ef + 3 * (n0 + 1 + sz);
+    const double *h = ef + 3 * (n0 + 1 + sy + sz);
+    const double *m = ef + 3 * (n0 + sy + sz);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        e[q] = a[q] * (1 - di) * (1 - dj) * (1 - dk) + b[q] * (di) * (1 - dj) * (1 - dk) +
+               c[q] * (di) * (dj) * (1 - dk) + d[q] * (1 - di) * (dj) * (1 - dk) +
+               e4[q] * (1 - di) * (1 - dj) * (dk) + f[q] * (di) * (1 - dj) * (dk) +
+               h[q] * (di) * (dj) * (dk) + m[q] * (1 - di) * (dj) * (dk);
+    }
+}
+
+__device__ __forceinline__ void xtol(const Geo &g, const double x[3], double lc[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) lc[d] = (x[d] - g.x0[d]) / g.dh[d];
+}
+
+__device__ __forceinline__ bool in_bounds(const Geo &g, const double x[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        if (x[d] < g.x0[d] || x[d] >= g.xm[d]) return false;
+    return true;
+}
+
+__device__ __forceinline__ bool in_sphere(const double s[4], const double x[3]) {
+    double r0 = x[0] - s[0], r1 = x[1] - s[1], r2 = x[2] - s[2];
+    double rm2 = r0 * r0 + r1 * r1 + r2 * r2;
+    return rm2 <= s[3];
+}
+
+/* Field_::scatter of `value` at x as 64-bit fixed point: each corner weight
+ * value*(1-di)*(1-dj)*(1-dk) (reference order) is rounded once to an integer
+ * count of 1/fx and added exactly. */
+__device__ __forceinline__ void deposit8(const Geo &g, unsigned long long *acc, const double x[3],
+                                         double value, double fx) {
+    double lc[3];
+    xtol(g, x, lc);
+    int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj), k = clamp_cell((int)lc[2], g.nk);
+    double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+    int64_t n0 = node_of(g, i, j, k);
+    int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    double w[8];
+    w[0] = value * (1 - di) * (1 - dj) * (1 - dk);
+    w[1] = value * (di) * (1 - dj) * (1 - dk);
+    w[2] = value * (di) * (dj) * (1 - dk);
+    w[3] = value * (1 - di) * (dj) * (1 - dk);
+    w[4] = value * (1 - di) * (1 - dj) * (dk);
+    w[5] = value * (di) * (1 - dj) * (dk);
+    w[6] = value * (di) * (dj) * (dk);
+    w[7] = value * (1 - di) * (dj) * (dk);
+    int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        long long q = __double2ll_rn(w[m] * fx);
+        if (q != 0) atomicAdd(acc + idx[m], (unsigned long long)q);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Species::advance, fused with Species::computeNumberDensity of the moved
+ * particles.  One thread per particle; a warp writes one word of the dead
+ * mask and adds its dead count to the particle tile's counter. */
+template <int WALLS, bool DEPOSIT, bool UNIFORM>
+__global__ void __launch_bounds__(256) k_push_fp64(Geo g, const double *__restrict__ ef, double s,
+                                                   double dt, double *P, int64_t stride,
+                                                   const int64_t *__restrict__ d_count, double4 sph,
+                                                   uint32_t *deadmask, int32_t *tiledead,
+                                                   unsigned long long *acc, double fx, double w0,
+                                                   int *err) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t n = d_count[0];
+    bool dead = false;
+    if (p < n) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        double lc[3], e[3];
+        xtol(g, x, lc);
+        gather3(g, ef, lc, e);
+#pragma unroll
+        for (int d = 0; d < 3; d++) v[d] += e[d] * s;
+#pragma unroll
+        for (int d = 0; d < 3; d++) x[d] += v[d] * dt;
+        if (WALLS == REFLECT) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                if (x[d] < g.x0[d]) {
+                    x[d] = 2 * g.x0[d] - x[d];
+                    v[d] *= -1.0;
+                } else if (x[d] >= g.xm[d]) {
+                    x[d] = 2 * g.xm[d] - x[d];
+                    v[d] *= -1.0;
+                }
+            }
+        } else {
+            double sp[4] = {sph.x, sph.y, sph.z, sph.w};
+            dead = in_sphere(sp, x) || !in_bounds(g, x);
+        }
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+            atomicOr(err, DERR_NONFINITE);
+            dead = true;
+        }
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + p] = x[d];
+            P[(3 + d) * stride + p] = v[d];
+        }
+        if (DEPOSIT && !dead) {
+            double w = UNIFORM ? w0 : P[6 * stride + p];
+            deposit8(g, acc, x, w, fx);
+        }
+    }
+    if (WALLS == ABSORB) {
+        unsigned m = __ballot_sync(0xffffffffu, dead);
+        if ((threadIdx.x & 31) == 0 && p < n) {
+            deadmask[p >> 5] = m;
+            if (m) atomicAdd(tiledead + (p / TILE_PARTICLES), __popc(m));
+        }
+    }
+}
+
+template <bool UNIFORM>
+__global__ void __launch_bounds__(256) k_deposit_fp64(Geo g, const double *__restrict__ P, int64_t stride,
+                                                      const int64_t *__restrict__ d_count,
+                                                      unsigned long long *acc, double fx, double w0) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+    double w = UNIFORM ? w0 : P[6 * stride + p];
+    deposit8(g, acc, x, w, fx);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Deterministic in-place compaction (both forms).  With D dead among n, the
+ * r-th dead slot below n-D receives the r-th live particle at or above n-D.
+ * 1) tile scan: exclusive prefix of dead counts per 32768-particle tile;
+ * 2) holes: dead slots below n-D are listed by rank;
+ * 3) movers: live particles at or above n-D copy into the hole of their rank. */
+__global__ void __launch_bounds__(1024) k_tile_scan(int64_t *d_count, int32_t *tiledead, int32_t *tilepre) {
+    __shared__ int32_t warp_sums[32];
+    int64_t n = d_count[0];
+    int64_t ntiles = (n + TILE_PARTICLES - 1) / TILE_PARTICLES;
+    int t = threadIdx.x;
+    int64_t per = (ntiles + blockDim.x - 1) / blockDim.x;
+    int64_t a = t * per, b = a + per;
+    if (b > ntiles) b = ntiles;
+    int32_t sum = 0;
+    for (int64_t i = a; i < b; i++) sum += tiledead[i];
+    /* block exclusive scan of sum */
+    int lane = t & 31, wid = t >> 5;
+    int32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t ws = warp_sums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        warp_sums[lane] = ws;
+    }
+    __syncthreads();
+    int32_t run = (wid ? warp_sums[wid - 1] : 0) + incl - sum;
+    for (int64_t i = a; i < b; i++) {
+        tilepre[i] = run;
+        run += tiledead[i];
+        tiledead[i] = 0; /* ready for the next push */
+    }
+    __syncthreads();
+    if (t == blockDim.x - 1) {
+        int64_t D = run;
+        tilepre[ntiles] = (int32_t)D;
+        d_count[1] = n;     /* count before compaction */
+        d_count[2] = D;     /* dead */
+        d_count[0] = n - D; /* count after */
+    }
+}
+
+/* block-wide exclusive scan helper for 1024 threads */
+__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *sh, int32_t *total) {
+    int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    int32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) sh[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t ws = sh[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        sh[lane] = ws;
+    }
+    __syncthreads();
+    int32_t r = (wid ? sh[wid - 1] : 0) + incl - v;
+    if (total) *total = sh[31];
+    __syncthreads();
+    return r;
+}
+
+/* one block per tile, one thread per 32-particle mask word */
+__global__ void __launch_bounds__(1024) k_holes(const int64_t *__restrict__ d_count,
+                                                const uint32_t *__restrict__ deadmask,
+                                                const int32_t *__restrict__ tilepre, int32_t *holes) {
+    __shared__ int32_t sh[32];
+    int64_t n_old = d_count[1], n_new = d_count[0];
+    int64_t ntiles = (n_old + TILE_PARTICLES - 1) / TILE_PARTICLES;
+    for (int64_t T = blockIdx.x; T < ntiles; T += gridDim.x) {
+        if (tilepre[T + 1] == tilepre[T]) continue;        /* no dead in tile */
+        if ((int64_t)T * TILE_PARTICLES >= n_new) continue; /* tile entirely above n_new */
+        int64_t word = T * (TILE_PARTICLES / 32) + threadIdx.x;
+        uint32_t m = (word * 32 < n_old) ? deadmask[word] : 0u;
+        int32_t pre = block_excl_scan(__popc(m), sh, nullptr);
+        int32_t base = tilepre[T] + pre;
+        while (m) {
+            int b = __ffs(m) - 1;
+            m &= m - 1;
+            int64_t idx = word * 32 + b;
+            if (idx < n_new) holes[base] = (int32_t)idx;
+            base++;
+        }
+    }
+}
+
+/* number of dead particles with index < x (x <= n_old) */
+__device__ int64_t dead_before(int64_t x, const uint32_t *deadmask, const int32_t *tilepre, int32_t *sh) {
+    int64_t T = x / TILE_PARTICLES;
+    int64_t w0 = T * (TILE_PARTICLES / 32);
+    int64_t wx = x >> 5;
+    int64_t word = w0 + threadIdx.x;
+    int32_t c = 0;
+    if (word < wx) c = __popc(deadmask[word]);
+    else if (word == wx && (x & 31)) c = __popc(deadmask[word] & ((1u << (x & 31)) - 1u));
+    int32_t tot;
+    block_excl_scan(c, sh, &tot);
+    return (int64_t)tilepre[T] + tot;
+}
+
+template <int FORM>
+__device__ __forceinline__ void move_particle(int64_t dst, int64_t src, double *P, int32_t *cell, float *off,
+                                              float *vel, int64_t stride, int rows) {
+    if (FORM == 0) {
+        for (int c = 0; c < rows; c++) P[c * stride + dst] = P[c * stride + src];
+    } else {
+        cell[dst] = cell[src];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            off[c * stride + dst] = off[c * stride + src];
+            vel[c * stride + dst] = vel[c * stride + src];
+        }
+    }
+}
+
+template <int FORM>
+__global__ void __launch_bounds__(1024) k_movers(const int64_t *__restrict__ d_count,
+                                                 const uint32_t *__restrict__ deadmask,
+                                                 const int32_t *__restrict__ tilepre,
+                                                 const int32_t *__restrict__ holes, double *P, int32_t *cell,
+                                                 float *off, float *vel, int64_t stride, int rows) {
+    __shared__ int32_t sh[32];
+    int64_t n_old = d_count[1], n_new = d_count[0];
+    if (n_old == n_new) return;
+    int64_t T0 = n_new / TILE_PARTICLES, T1 = (n_old - 1) / TILE_PARTICLES;
+    int64_t dead_at_new = -1;
+    for (int64_t T = T0 + blockIdx.x; T <= T1; T += gridDim.x) {
+        if (dead_at_new < 0) dead_at_new = dead_before(n_new, deadmask, tilepre, sh);
+        int64_t word = T * (TILE_PARTICLES / 32) + threadIdx.x;
+        uint32_t m = (word * 32 < n_old) ? deadmask[word] : 0xffffffffu;
+        int32_t pre = block_excl_scan(__popc(m), sh, nullptr);
+        int64_t dead_before_word = tilepre[T] + pre;
+        for (int b = 0; b < 32; b++) {
+            int64_t q = word * 32 + b;
+            if (q < n_new || q >= n_old) continue;
+            if ((m >> b) & 1u) continue;
+            int64_t db = dead_before_word + __popc(m & ((1u << b) - 1u));
+            int64_t rank = (q - n_new) - (db - dead_at_new);
+            move_particle<FORM>(holes[rank], q, P, cell, off, vel, stride, rows);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Candidate generators for appended particles.  Each produces the position,
+ * velocity and weight of candidate i exactly as the reference's loader or
+ * source computes them before calling addParticle. */
+struct GenHost { /* Species::addParticle from a host list */
+    const double *pos3, *vel3, *w;
+    double w0;
+    __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
+        for (int d = 0; d < 3; d++) {
+            x[d] = pos3[3 * i + d];
+            v[d] = vel3[3 * i + d];
+        }
+        w_ = w ? w[i] : w0;
+    }
+    __device__ void pos(int64_t i, double x[3]) const {
+        for (int d = 0; d < 3; d++) x[d] = pos3[3 * i + d];
+    }
+};
+
+struct GenBox { /* Species::loadParticlesBox, ch2/Species.cpp:74-97 */
+    double x1[3], x2[3], mpw;
+    const double *u; /* 3 per particle or null -> Philox */
+    uint64_t seed, stream;
+    __device__ double U(int64_t k) const { return u ? u[k] : philox_uniform(seed, stream, (uint64_t)k); }
+    __device__ void pos(int64_t i, double x[3]) const {
+        for (int d = 0; d < 3; d++) x[d] = x1[d] + U(3 * i + d) * (x2[d] - x1[d]);
+    }
+    __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
+        pos(i, x);
+        v[0] = v[1] = v[2] = 0;
+        w_ = mpw;
+    }
+};
+
+struct GenQS { /* Species::loadParticlesBoxQS, ch2/Species.cpp:101-141 */
+    double x1[3], x2[3], mpw, di, dj, dk;
+    int n0, n1, n2;
+    __device__ void idx(int64_t t, int &i, int &j, int &k) const {
+        k = (int)(t % n2);
+        int64_t r = t / n2;
+        j = (int)(r % n1);
+        i = (int)(r / n1);
+    }
+    __device__ void pos(int64_t t, double x[3]) const {
+        int i, j, k;
+        idx(t, i, j, k);
+        x[0] = x1[0] + i * di;
+        x[1] = x1[1] + j * dj;
+        x[2] = x1[2] + k * dk;
+        if (x[0] == x2[0]) x[0] -= 1e-4 * di;
+        if (x[1] == x2[1]) x[1] -= 1e-4 * dj;
+        if (x[2] == x2[2]) x[2] -= 1e-4 * dk;
+    }
+    __device__ void make(int64_t t, double x[3], double v[3], double &w_) const {
+        pos(t, x);
+        int i, j, k;
+        idx(t, i, j, k);
+        double w = 1;
+        if (i == 0 || i == n0 - 1) w *= 0.5;
+        if (j == 0 || j == n1 - 1) w *= 0.5;
+        if (k == 0 || k == n2 - 1) w *= 0.5;
+        v[0] = v[1] = v[2] = 0;
+        w_ = mpw * w;
+    }
+};
+
+struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27) and
+                    WarmBeamSource::sample (ch4/Source.cpp:31-55) */
+    double x0[3], Lx, Ly, v_drift, mpw0, v_th;
+    int warm;
+    const double *u; /* count draw at 0, then 2 or 13 per particle */
+    uint64_t seed, stream;
+    __device__ double U(int64_t k) const { return u ? u[k] : philox_uniform(seed, stream, (uint64_t)k); }
+    __device__ int64_t base(int64_t i) const { return 1 + (warm ? 13 : 2) * i; }
+    __device__ void pos(int64_t i, double x[3]) const {
+        int64_t b = base(i);
+        x[0] = x0[0] + U(b) * Lx;
+        x[1] = x0[1] + U(b + 1) * Ly;
+        x[2] = x0[2];
+    }
+    __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
+        pos(i, x);
+        w_ = mpw0;
+        if (!warm) {
+            v[0] = 0;
+            v[1] = 0;
+            v[2] = v_drift;
+            return;
+        }
+        /* Species::sampleIsotropicVel and sampleVth, ch4/Species.cpp:149-175 */
+        int64_t b = base(i) + 2;
+        double theta = 2 * REF_PI * U(b);
+        double r = -1.0 + 2 * U(b + 1);
+        double a = sqrt(1 - r * r);
+        double d[3] = {r, cos(theta) * a, sin(theta) * a};
+        double v1 = v_th * (U(b + 2) + U(b + 3) + U(b + 4) - 1.5);
+        double v2 = v_th * (U(b + 5) + U(b + 6) + U(b + 7) - 1.5);
+        double v3 = v_th * (U(b + 8) + U(b + 9) + U(b + 10) - 1.5);
+        double speed = 3 / sqrt(6.0) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+        for (int c = 0; c < 3; c++) v[c] = d[c] * speed;
+        v[2] += v_drift;
+    }
+};
+
+/* Pass 1: accepted candidates per block (addParticle rejects x outside
+ * [x0,xm)). */
+template <class Gen>
+__global__ void __launch_bounds__(256) k_append_count(Geo g, Gen gen, int64_t ncand, int32_t *blockcnt) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = false;
+    if (i < ncand) {
+        double x[3];
+        gen.pos(i, x);
+        ok = in_bounds(g, x);
+    }
+    int c = __syncthreads_count(ok);
+    if (threadIdx.x == 0) blockcnt[blockIdx.x] = c;
+}
+
+/* Pass 2 (one block): exclusive prefix of the block counts in place; the
+ * particle count before the append goes to d_count[1], the new count (at
+ * most the capacity) to d_count[0]. */
+__global__ void __launch_bounds__(1024) k_append_scan(int32_t *blockcnt, int64_t nblocks, int64_t *d_count,
+                                                      int64_t cap, int *err) {
+    __shared__ int32_t sh[32];
+    int t = threadIdx.x;
+    int64_t per = (nblocks + blockDim.x - 1) / blockDim.x;
+    int64_t a = t * per, b = a + per;
+    if (b > nblocks) b = nblocks;
+    int64_t sum = 0;
+    for (int64_t i = a; i < b; i++) sum += blockcnt[i];
+    int32_t total;
+    int32_t run = block_excl_scan((int32_t)sum, sh, &total);
+    for (int64_t i = a; i < b; i++) {
+        int32_t c = blockcnt[i];
+        blockcnt[i] = run;
+        run += c;
+    }
+    if (t == 0) {
+        int64_t n_old = d_count[0];
+        int64_t n_new = n_old + total;
+        if (n_new > cap) {
+            atomicOr(err, DERR_CAPACITY);
+            n_new = cap;
+        }
+        d_count[1] = n_old;
+        d_count[0] = n_new;
+    }
+}
+
+/* Pass 3: each accepted candidate is rewound by (q/m)E dt/2 and written at
+ * n_old + (number of accepted candidates before it), so the order is the
+ * candidates' order, as the reference's emplace_back. */
+template <class Gen, int FORM>
+__global__ void __launch_bounds__(256) k_append_write(Geo g, Gen gen, int64_t ncand,
+                                                      const int32_t *__restrict__ blockpre,
+                                                      const int64_t *__restrict__ d_count,
+                                                      const double *__restrict__ ef, double qm, double dt,
+                                                      double *P, int32_t *cell, float *off, float *vel,
+                                                      int64_t stride, int64_t cap, int write_w) {
+    __shared__ int32_t sh[8];
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t s_base = d_count[1] + blockpre[blockIdx.x];
+    double x[3], v[3], w = 0;
+    bool ok = false;
+    if (i < ncand) {
+        gen.make(i, x, v, w);
+        ok = in_bounds(g, x);
+    }
+    /* block exclusive rank of ok (256 threads = 8 warps) */
+    unsigned bal = __ballot_sync(0xffffffffu, ok);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = __popc(bal);
+    __syncthreads();
+    int32_t pre = 0;
+    for (int k = 0; k < wid; k++) pre += sh[k];
+    pre += __popc(bal & ((1u << lane) - 1u));
+    if (ok) {
+        int64_t dst = s_base + pre;
+        if (dst < cap) {
+            double lc[3], e[3];
+            xtol(g, x, lc);
+            gather3(g, ef, lc, e);
+            for (int d = 0; d < 3; d++) v[d] = v[d] - e[d] * qm * (0.5 * dt);
+            if (FORM == 0) {
+                for (int d = 0; d < 3; d++) {
+                    P[d * stride + dst] = x[d];
+                    P[(3 + d) * stride + dst] = v[d];
+                }
+                if (write_w) P[6 * stride + dst] = w;
+            } else {
+                int ci = clamp_cell((int)lc[0], g.ni), cj = clamp_cell((int)lc[1], g.nj),
+                    ck = clamp_cell((int)lc[2], g.nk);
+                cell[dst] = ci | (cj << 10) | (ck << 20);
+                off[dst] = (float)(lc[0] - ci);
+                off[stride + dst] = (float)(lc[1] - cj);
+                off[2 * stride + dst] = (float)(lc[2] - ck);
+                for (int d = 0; d < 3; d++) vel[d * stride + dst] = (float)v[d];
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
+ * central inside.  Also writes the float32 copy used by the mixed push. */
+__global__ void __launch_bounds__(256) k_efield(Geo g, const double *__restrict__ phi, double *ef, float4 *ef4) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    if (u >= nn) return;
+    int i = (int)(u % g.ni);
+    int j = (int)((u / g.ni) % g.nj);
+    int k = (int)(u / ((int64_t)g.ni * g.nj));
+    int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    double dx = g.dh[0], dy = g.dh[1], dz = g.dh[2];
+    double e0, e1, e2;
+    if (i == 0)
+        e0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]) / (2 * dx);
+    else if (i == g.ni - 1)
+        e0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]) / (2 * dx);
+    else
+        e0 = -(phi[u + 1] - phi[u - 1]) / (2 * dx);
+    if (j == 0)
+        e1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]) / (2 * dy);
+    else if (j == g.nj - 1)
+        e1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]) / (2 * dy);
+    else
+        e1 = -(phi[u + sy] - phi[u - sy]) / (2 * dy);
+    if (k == 0)
+        e2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]) / (2 * dz);
+    else if (k == g.nk - 1)
+        e2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]) / (2 * dz);
+    else
+        e2 = -(phi[u + sz] - phi[u - sz]) / (2 * dz);
+    ef[3 * u] = e0;
+    ef[3 * u + 1] = e1;
+    ef[3 * u + 2] = e2;
+    if (ef4) ef4[u] = make_float4((float)e0, (float)e1, (float)e2, 0.f);
+}
+
+/* ------------------------------------------------------------------------ */
+/* World::addSphere: node position x0 + dh*(i,j,k), inside or on the sphere */
+__global__ void k_objects_sphere(Geo g, double4 sph, double phi_s, int32_t *obj, double *phi) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    if (u >= nn) return;
+    double l[3] = {(double)(u % g.ni), (double)((u / g.ni) % g.nj), (double)(u / ((int64_t)g.ni * g.nj))};
+    double x[3];
+    for (int d = 0; d < 3; d++) x[d] = g.x0[d] + g.dh[d] * l[d];
+    double s[4] = {sph.x, sph.y, sph.z, sph.w};
+    if (in_sphere(s, x)) {
+        obj[u] = 1;
+        phi[u] = phi_s;
+    }
+}
+
+/* World::addInlet: the k = 0 plane is Dirichlet 0 V */
+__global__ void k_objects_inlet(Geo g, int32_t *obj, double *phi) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= (int64_t)g.ni * g.nj) return;
+    obj[u] = 2;
+    phi[u] = 0;
+}
+
+/* immediate Neumann neighbour in the precedence of solveGS,
+ * ch3/ver2/PotentialSolver.cpp:359-370; -1 for interior nodes */
+__device__ __forceinline__ int64_t neumann_next(const Geo &g, int i, int j, int k) {
+    if (i == 0) return node_of(g, i + 1, j, k);
+    if (i == g.ni - 1) return node_of(g, i - 1, j, k);
+    if (j == 0) return node_of(g, i, j + 1, k);
+    if (j == g.nj - 1) return node_of(g, i, j - 1, k);
+    if (k == 0) return node_of(g, i, j, k + 1);
+    if (k == g.nk - 1) return node_of(g, i, j, k - 1);
+    return -1;
+}
+
+/* end of each boundary node's chain of Neumann copies (-1 elsewhere) */
+__global__ void k_targets(Geo g, const int32_t *__restrict__ obj, int32_t *target) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    if (u >= nn) return;
+    target[u] = -1;
+    if (obj[u] > 0) return;
+    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
+    int64_t t = neumann_next(g, i, j, k);
+    if (t < 0) return;
+    for (int guard = 0; guard < 8; guard++) {
+        if (obj[t] > 0) break;
+        int ti = (int)(t % g.ni), tj = (int)((t / g.ni) % g.nj), tk = (int)(t / ((int64_t)g.ni * g.nj));
+        int64_t n2 = neumann_next(g, ti, tj, tk);
+        if (n2 < 0) break;
+        t = n2;
+    }
+    target[u] = (int32_t)t;
+}
+
+/* ------------------------------------------------------------------------ */
+/* den = acc * unit / node_vol (0 where the volume is 0): the fixed-point sum
+ * followed by Field_::operator/=, ch2/Field.h:125-134 */
+__global__ void k_density(int64_t nn, const unsigned long long *__restrict__ acc, double unit,
+                          const double *__restrict__ vol, double *den) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    double d = __ll2double_rn((long long)acc[u]) * unit;
+    double v = vol[u];
+    den[u] = (v != 0) ? d / v : 0.0;
+}
+
+struct ChargeArgs {
+    int ns;
+    const double *den[8];
+    double q[8];
+};
+
+/* World::computeChargeDensity: rho = 0; rho += den_s * q_s (charged species) */
+__global__ void k_charge(int64_t nn, ChargeArgs a, double *rho) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    double r = 0;
+    for (int s = 0; s < a.ns; s++) r += a.den[s][u] * a.q[s];
+    rho[u] = r;
+}
+
+/* Field_::updateAverage */
+__global__ void k_update_average(int64_t nn, const double *__restrict__ den, double *ave, int samples) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    ave[u] = (den[u] + samples * ave[u]) / (samples + 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Deterministic reductions: a fixed grid of blocks, fixed per-thread order,
+ * fixed tree within the block, partials summed in block order. */
+constexpr int RED_BLOCKS = 592, RED_THREADS = 256;
+
+template <int NV>
+__device__ __forceinline__ void block_sum_store(double (&v)[NV], double *out) {
+    __shared__ double sh[NV][RED_THREADS / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[q][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0;
+        for (int k = 0; k < RED_THREADS / 32; k++) s += sh[threadIdx.x][k];
+        out[threadIdx.x] = s;
+    }
+}
+
+/* per block: {count, mx, my, mz, 2KE/m} of Species::getRealCount/getMomentum/getKE */
+template <int FORM>
+__global__ void __launch_bounds__(RED_THREADS) k_diag_partials(const double *__restrict__ P,
+                                                               const float *__restrict__ vel, int64_t stride,
+                                                               const int64_t *__restrict__ d_count, int uniform,
+                                                               double w0, double *partials) {
+    int64_t n = d_count[0];
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int64_t p = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; p < n; p += (int64_t)RED_BLOCKS * RED_THREADS) {
+        double w, v0, v1, v2;
+        if (FORM == 0) {
+            w = uniform ? w0 : P[6 * stride + p];
+            v0 = P[3 * stride + p];
+            v1 = P[4 * stride + p];
+            v2 = P[5 * stride + p];
+        } else {
+            w = w0;
+            v0 = vel[p];
+            v1 = vel[stride + p];
+            v2 = vel[2 * stride + p];
+        }
+        acc[0] += w;
+        acc[1] += v0 * w;
+        acc[2] += v1 * w;
+        acc[3] += v2 * w;
+        double vv = v0 * v0 + v1 * v1 + v2 * v2;
+        acc[4] += w * vv;
+    }
+    block_sum_store<5>(acc, partials + 5 * blockIdx.x);
+}
+
+__global__ void k_diag_final(const double *__restrict__ partials, double mass, double *out) {
+    if (threadIdx.x != 0) return;
+    double s[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < RED_BLOCKS; b++)
+        for (int q = 0; q < 5; q++) s[q] += partials[5 * b + q];
+    out[0] = s[0];
+    out[1] = s[1] * mass;
+    out[2] = s[2] * mass;
+    out[3] = s[3] * mass;
+    out[4] = 0.5 * mass * s[4];
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_pe_partials(int64_t nn, const double *__restrict__ ef,
+                                                             const double *__restrict__ vol, double *partials) {
+    double acc[1] = {0};
+    for (int64_t u = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; u < nn; u += (int64_t)RED_BLOCKS * RED_THREADS) {
+        double e0 = ef[3 * u], e1 = ef[3 * u + 1], e2 = ef[3 * u + 2];
+        double ef2 = e0 * e0 + e1 * e1 + e2 * e2;
+        acc[0] += ef2 * vol[u];
+    }
+    block_sum_store<1>(acc, partials + blockIdx.x);
+}
+
+__global__ void k_pe_final(const double *__restrict__ partials, double *out) {
+    if (threadIdx.x != 0) return;
+    double s = 0;
+    for (int b = 0; b < RED_BLOCKS; b++) s += partials[b];
+    out[0] = 0.5 * EPS_0 * s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Red-black SOR (omega = 1.4) of PotentialSolver::solve over interior nodes,
+ * as one cooperative launch: colour c = (i+j+k)&1 holds the nodes updated in
+ * half-sweep c; the residual of ch2/PotentialSolver.cpp:44-61 is evaluated
+ * every 25 iterations, reduced deterministically and tested by every block. */
+__device__ __forceinline__ double grid_sum(cg::grid_group &grid, double v, double *partials, int &round) {
+    __shared__ double sh[32];
+    __shared__ double total;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double *slot = partials + (round & 1) * gridDim.x;
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k];
+        slot[blockIdx.x] = s;
+    }
+    round++;
+    grid.sync();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (unsigned b = 0; b < gridDim.x; b++) s += slot[b];
+        total = s;
+    }
+    __syncthreads();
+    return total;
+}
+
+struct ColourRange {
+    int hx; /* colour nodes per interior row, rounded up */
+    int64_t count;
+};
+
+__device__ __forceinline__ bool colour_node(const Geo &g, const ColourRange &cr, int64_t t, int c, int &i, int &j,
+                                            int &k) {
+    int i2 = (int)(t % cr.hx);
+    int64_t r = t / cr.hx;
+    j = 1 + (int)(r % (g.nj - 2));
+    k = 1 + (int)(r / (g.nj - 2));
+    i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
+    return i <= g.ni - 2;
+}
+
+__global__ void __launch_bounds__(256) k_sor_box(Geo g, double *phi, const double *__restrict__ rho, int max_it,
+                                                 double tol, double *partials, SolveStatus *st, int *err) {
+    cg::grid_group grid = cg::this_grid();
+    const double idx2 = 1.0 / (g.dh[0] * g.dh[0]);
+    const double idy2 = 1.0 / (g.dh[1] * g.dh[1]);
+    const double idz2 = 1.0 / (g.dh[2] * g.dh[2]);
+    const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    ColourRange cr;
+    cr.hx = (g.ni - 2 + 1) / 2;
+    cr.count = (int64_t)cr.hx * (g.nj - 2) * (g.nk - 2);
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t gsize = (int64_t)gridDim.x * blockDim.x;
+    const int64_t interior = (int64_t)(g.ni - 2) * (g.nj - 2) * (g.nk - 2);
+    double L2 = 0;
+    int conv = 0, it, round = 0;
+    for (it = 0; it < max_it; it++) {
+        for (int c = 0; c < 2; c++) {
+            for (int64_t t = gtid; t < cr.count; t += gsize) {
+                int i, j, k;
+                if (!colour_node(g, cr, t, c, i, j, k)) continue;
+                int64_t u = node_of(g, i, j, k);
+                double phi_new = (rho[u] / EPS_0 + idx2 * (phi[u - 1] + phi[u + 1]) +
+                                  idy2 * (phi[u - sy] + phi[u + sy]) + idz2 * (phi[u - sz] + phi[u + sz])) /
+                                 (2 * idx2 + 2 * idy2 + 2 * idz2);
+                phi[u] = phi[u] + 1.4 * (phi_new - phi[u]);
+            }
+            grid.sync();
+        }
+        if (it % 25 == 0) {
+            double sum = 0;
+            for (int64_t t = gtid; t < interior; t += gsize) {
+                int i = 1 + (int)(t % (g.ni - 2));
+                int64_t r = t / (g.ni - 2);
+                int j = 1 + (int)(r % (g.nj - 2));
+                int k = 1 + (int)(r / (g.nj - 2));
+                int64_t u = node_of(g, i, j, k);
+                double R = -phi[u] * (2 * idx2 + 2 * idy2 + 2 * idz2) + rho[u] / EPS_0 +
+                           idx2 * (phi[u - 1] + phi[u + 1]) + idy2 * (phi[u - sy] + phi[u + sy]) +
+                           idz2 * (phi[u - sz] + phi[u + sz]);
+                sum += R * R;
+            }
+            double tot = grid_sum(grid, sum, partials, round);
+            L2 = sqrt(tot / ((double)g.ni * g.nj * g.nk));
+            if (!isfinite(L2)) {
+                if (gtid == 0) atomicOr(err, DERR_NONFINITE);
+                break;
+            }
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (gtid == 0) {
+        st->converged = conv;
+        st->iterations = conv ? it + 1 : it;
+        st->inner_iterations = 0;
+        st->residual = L2;
+        st->solves += 1;
+        st->outer_total += st->iterations;
+    }
+}
+
+/* Red-black form of solveGS: red then black interior non-Dirichlet nodes with
+ * the Boltzmann term, then every Neumann node copies the end of its chain. */
+__global__ void __launch_bounds__(256) k_gs_sphere(Geo g, double *phi, const double *__restrict__ rho,
+                                                   const int32_t *__restrict__ obj,
+                                                   const int32_t *__restrict__ target, double phi0, double te0,
+                                                   double n0, int max_it, double tol, double *partials,
+                                                   SolveStatus *st, int *err) {
+    cg::grid_group grid = cg::this_grid();
+    const double idx2 = 1.0 / (g.dh[0] * g.dh[0]);
+    const double idy2 = 1.0 / (g.dh[1] * g.dh[1]);
+    const double idz2 = 1.0 / (g.dh[2] * g.dh[2]);
+    const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    ColourRange cr;
+    cr.hx = (g.ni - 2 + 1) / 2;
+    cr.count = (int64_t)cr.hx * (g.nj - 2) * (g.nk - 2);
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t gsize = (int64_t)gridDim.x * blockDim.x;
+    double L2 = 0;
+    int conv = 0, it, round = 0;
+    for (it = 0; it < max_it; it++) {
+        for (int c = 0; c < 2; c++) {
+            for (int64_t t = gtid; t < cr.count; t += gsize) {
+                int i, j, k;
+                if (!colour_node(g, cr, t, c, i, j, k)) continue;
+                int64_t u = node_of(g, i, j, k);
+                if (obj[u] > 0) continue;
+                double ne = n0 * exp((phi[u] - phi0) / te0);
+                double phi_new = ((rho[u] - QE * ne) / EPS_0 + idx2 * (phi[u - 1] + phi[u + 1]) +
+                                  idy2 * (phi[u - sy] + phi[u + sy]) + idz2 * (phi[u - sz] + phi[u + sz])) /
+                                 (2 * idx2 + 2 * idy2 + 2 * idz2);
+                phi[u] = phi[u] + 1.4 * (phi_new - phi[u]);
+            }
+            grid.sync();
+        }
+        for (int64_t u = gtid; u < nn; u += gsize) {
+            int32_t t = target[u];
+            if (t >= 0) phi[u] = phi[t];
+        }
+        grid.sync();
+        if (it % 25 == 0) {
+            double sum = 0;
+            for (int64_t u = gtid; u < nn; u += gsize) {
+                if (obj[u] > 0) continue;
+                int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / sz);
+                int64_t nb = neumann_next(g, i, j, k);
+                double R;
+                if (nb >= 0)
+                    R = phi[u] - phi[nb];
+                else {
+                    double ne = n0 * exp((phi[u] - phi0) / te0);
+                    R = -phi[u] * (2 * idx2 + 2 * idy2 + 2 * idz2) + (rho[u] - QE * ne) / EPS_0 +
+                        idx2 * (phi[u - 1] + phi[u + 1]) + idy2 * (phi[u - sy] + phi[u + sy]) +
+                        idz2 * (phi[u - sz] + phi[u + sz]);
+                }
+                sum += R * R;
+            }
+            double tot = grid_sum(grid, sum, partials, round);
+            L2 = sqrt(tot / ((double)g.ni * g.nj * g.nk));
+            if (!isfinite(L2)) {
+                if (gtid == 0) atomicOr(err, DERR_NONFINITE);
+                break;
+            }
+            if (L2 < tol) {
+                conv = 1;
+                break;
+            }
+        }
+    }
+    if (gtid == 0) {
+        st->converged = conv;
+        st->iterations = conv ? it + 1 : it;
+        st->inner_iterations = 0;
+        st->residual = L2;
+        st->solves += 1;
+        st->outer_total += st->iterations;
+    }
+}
+
+/* solveQN: phi = phi0 + Te0 ln(max(rho/rho0, 1e-6)) off the Dirichlet nodes */
+__global__ void k_qn(int64_t nn, double *phi, const double *__restrict__ rho, const int32_t *__restrict__ obj,
+                     double phi0, double te0, double n0) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn || obj[u] > 0) return;
+    double rho0 = n0 * QE;
+    double ratio = rho[u] / rho0;
+    if (ratio < 1e-6) ratio = 1e-6;
+    phi[u] = phi0 + te0 * log(ratio);
+}
+
+/* World::computeNodeVolumes, ch2/World.cpp:58-69 */
+__global__ void k_node_vol(Geo g, double *vol) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    if (u >= nn) return;
+    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
+    double V = g.dh[0] * g.dh[1] * g.dh[2];
+    if (i == 0 || i == g.ni - 1) V *= 0.5;
+    if (j == 0 || j == g.nj - 1) V *= 0.5;
+    if (k == 0 || k == g.nk - 1) V *= 0.5;
+    vol[u] = V;
+}
+
+__global__ void k_ef_to_ef4(int64_t nn, const double *__restrict__ ef, float4 *ef4) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    ef4[u] = make_float4((float)ef[3 * u], (float)ef[3 * u + 1], (float)ef[3 * u + 2], 0.f);
+}
+
+/* weight row of a float64 species that switches from uniform to per-particle weights */
+__global__ void k_fill(double *x, int64_t n, double v) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < n) x[u] = v;
+}
+
+/* ======================================================================== */
+/* launchers; each adds the number of kernels it launched to w.nlaunch        */
+void launch_objects_sphere(World &w, const double c[3], double radius, double phi_s) {
+    double4 s = make_double4(c[0], c[1], c[2], radius * radius);
+    k_objects_sphere<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, s, phi_s, w.obj, w.phi);
+    w.nlaunch++;
+}
+
+void launch_objects_inlet(World &w) {
+    k_objects_inlet<<<blocks_for((int64_t)w.g.ni * w.g.nj, 256), 256, 0, w.stream>>>(w.g, w.obj, w.phi);
+    w.nlaunch++;
+}
+
+void launch_targets(World &w) {
+    k_targets<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.obj, w.target);
+    w.nlaunch++;
+}
+
+void launch_efield(World &w) {
+    bool mixed = false;
+    for (Species *s : w.species) mixed |= (s->form == 1);
+    k_efield<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.phi, w.ef, mixed ? w.ef4 : nullptr);
+    w.nlaunch++;
+    if (mixed) w.ef4_valid = true;
+    else w.ef4_valid = false;
+}
+
+template <int WALLS, bool DEP, bool UNI>
+static void push_fp64_as(World &w, Species &s, int blocks) {
+    double sc = w.dt * s.charge / s.mass;
+    double4 sph = make_double4(w.sphere[0], w.sphere[1], w.sphere[2], w.has_sphere ? w.sphere[3] : -1.0);
+    k_push_fp64<WALLS, DEP, UNI><<<blocks, 256, 0, w.stream>>>(w.g, w.ef, sc, w.dt, s.P, s.cap, s.d_count, sph,
+                                                              s.deadmask, s.tiledead, s.acc, s.fx, s.mpw0, w.d_err);
+    w.nlaunch++;
+}
+
+void launch_push_fp64(World &w, Species &s, bool deposit) {
+    int64_t n = s.host_bound;
+    if (n <= 0) return;
+    int blocks = blocks_for(n, 256);
+    if (s.walls == 0) {
+        if (!deposit)
+            push_fp64_as<REFLECT, false, true>(w, s, blocks);
+        else if (s.uniform_w)
+            push_fp64_as<REFLECT, true, true>(w, s, blocks);
+        else
+            push_fp64_as<REFLECT, true, false>(w, s, blocks);
+    } else {
+        if (!deposit)
+            push_fp64_as<ABSORB, false, true>(w, s, blocks);
+        else if (s.uniform_w)
+            push_fp64_as<ABSORB, true, true>(w, s, blocks);
+        else
+            push_fp64_as<ABSORB, true, false>(w, s, blocks);
+    }
+}
+
+void launch_deposit_fp64(World &w, Species &s) {
+    int64_t n = s.host_bound;
+    if (n <= 0) return;
+    if (s.uniform_w)
+        k_deposit_fp64<true><<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, s.acc, s.fx,
+                                                                       s.mpw0);
+    else
+        k_deposit_fp64<false><<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, s.acc, s.fx,
+                                                                        s.mpw0);
+    w.nlaunch++;
+}
+
+void launch_compact(World &w, Species &s) {
+    if (s.host_bound <= 0) return;
+    int64_t ntiles = (s.host_bound + TILE_PARTICLES - 1) / TILE_PARTICLES;
+    k_tile_scan<<<1, 1024, 0, w.stream>>>(s.d_count, s.tiledead, s.tilepre);
+    int g1 = (int)(ntiles < 2 * (int64_t)w.sm_count ? ntiles : 2 * (int64_t)w.sm_count);
+    k_holes<<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes);
+    int rows = s.uniform_w ? 6 : 7;
+    if (s.form == 0)
+        k_movers<0><<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, s.P, nullptr, nullptr,
+                                                nullptr, s.cap, rows);
+    else
+        k_movers<1><<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, nullptr, s.cell, s.off,
+                                                s.vel, s.cap, rows);
+    w.nlaunch += 3;
+}
+
+void launch_density(World &w, Species &s) {
+    k_density<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, s.acc, s.unit, w.vol, s.den);
+    w.nlaunch++;
+}
+
+void launch_charge(World &w) {
+    ChargeArgs a;
+    a.ns = 0;
+    for (Species *s : w.species) {
+        if (s->charge == 0) continue;
+        if (a.ns == 8) break;
+        a.den[a.ns] = s->den;
+        a.q[a.ns] = s->charge;
+        a.ns++;
+    }
+    k_charge<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, a, w.rho);
+    w.nlaunch++;
+}
+
+void launch_update_average(World &w, Species &s) {
+    k_update_average<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, s.den, s.den_ave, s.ave_samples);
+    w.nlaunch++;
+    s.ave_samples++;
+}
+
+template <class Gen>
+static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int write_w) {
+    if (ncand <= 0) return;
+    int64_t blocks = (ncand + 255) / 256;
+    if (blocks > w.blockcnt_cap) {
+        if (w.d_blockcnt) {
+            cudaStreamSynchronize(w.stream);
+            cudaFree(w.d_blockcnt);
+        }
+        w.blockcnt_cap = blocks + 1024;
+        if (cudaMalloc(&w.d_blockcnt, w.blockcnt_cap * sizeof(int32_t)) != cudaSuccess) {
+            w.d_blockcnt = nullptr;
+            w.blockcnt_cap = 0;
+            return;
+        }
+    }
+    double qm = s.charge / s.mass;
+    k_append_count<Gen><<<(unsigned)blocks, 256, 0, w.stream>>>(w.g, gen, ncand, w.d_blockcnt);
+    k_append_scan<<<1, 1024, 0, w.stream>>>(w.d_blockcnt, blocks, s.d_count, s.cap, w.d_err);
+    if (s.form == 0)
+        k_append_write<Gen, 0><<<(unsigned)blocks, 256, 0, w.stream>>>(
+            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, s.P, nullptr, nullptr, nullptr, s.cap, s.cap,
+            write_w);
+    else
+        k_append_write<Gen, 1><<<(unsigned)blocks, 256, 0, w.stream>>>(
+            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, nullptr, s.cell, s.off, s.vel, s.cap, s.cap,
+            0);
+    w.nlaunch += 3;
+    s.host_bound += ncand;
+    if (s.host_bound > s.cap) s.host_bound = s.cap;
+}
+
+void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3, const double *d_w,
+                     int64_t n, int rewind) {
+    (void)rewind;
+    GenHost gh{d_pos3, d_vel3, d_w, s.mpw0};
+    append(w, s, gh, n, s.uniform_w ? 0 : 1);
+}
+
+void launch_load_box(World &w, Species &s, const double x1[3], const double x2[3], double mpw, int64_t num_mp,
+                     const double *d_u, uint64_t stream_id) {
+    GenBox gb;
+    for (int d = 0; d < 3; d++) {
+        gb.x1[d] = x1[d];
+        gb.x2[d] = x2[d];
+    }
+    gb.mpw = mpw;
+    gb.u = d_u;
+    gb.seed = w.seed;
+    gb.stream = stream_id;
+    append(w, s, gb, num_mp, s.uniform_w ? 0 : 1);
+}
+
+void launch_load_qs(World &w, Species &s, const double x1[3], const double x2[3], double mpw,
+                    const int num_mp[3]) {
+    GenQS q;
+    for (int d = 0; d < 3; d++) {
+        q.x1[d] = x1[d];
+        q.x2[d] = x2[d];
+    }
+    q.mpw = mpw;
+    q.di = (x2[0] - x1[0]) / (num_mp[0] - 1);
+    q.dj = (x2[1] - x1[1]) / (num_mp[1] - 1);
+    q.dk = (x2[2] - x1[2]) / (num_mp[2] - 1);
+    q.n0 = num_mp[0];
+    q.n1 = num_mp[1];
+    q.n2 = num_mp[2];
+    append(w, s, q, (int64_t)num_mp[0] * num_mp[1] * num_mp[2], s.uniform_w ? 0 : 1);
+}
+
+void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp, const double *d_u,
+                   uint64_t stream_id) {
+    GenBeam b;
+    for (int d = 0; d < 3; d++) b.x0[d] = w.g.x0[d];
+    b.Lx = w.g.dh[0] * (w.g.ni - 1);
+    b.Ly = w.g.dh[1] * (w.g.nj - 1);
+    b.v_drift = v_drift;
+    b.mpw0 = s.mpw0;
+    b.warm = temp > 0;
+    b.v_th = b.warm ? sqrt(2 * KB * temp / s.mass) : 0;
+    b.u = d_u;
+    b.seed = w.seed;
+    b.stream = stream_id;
+    append(w, s, b, num_sim, s.uniform_w ? 0 : 1);
+}
+
+void launch_diag(World &w, Species &s, double *d_out5) {
+    if (s.form != 0) {
+        launch_diag_mixed(w, s, d_out5);
+        return;
+    }
+    k_diag_partials<0><<<RED_BLOCKS, RED_THREADS, 0, w.stream>>>(s.P, nullptr, s.cap, s.d_count, s.uniform_w,
+                                                                 s.mpw0, w.d_partials);
+    k_diag_final<<<1, 32, 0, w.stream>>>(w.d_partials, s.mass, d_out5);
+    w.nlaunch += 2;
+}
+
+void launch_pe(World &w, double *d_out1) {
+    k_pe_partials<<<RED_BLOCKS, RED_THREADS, 0, w.stream>>>(w.nn, w.ef, w.vol, w.d_partials);
+    k_pe_final<<<1, 32, 0, w.stream>>>(w.d_partials, d_out1);
+    w.nlaunch += 2;
+}
+
+static int coop_grid(World &w, const void *fn, int threads, int64_t work) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    if (per_sm < 1) per_sm = 1;
+    int64_t maxb = (int64_t)per_sm * w.sm_count;
+    int64_t need = (work + threads - 1) / threads;
+    if (need < 1) need = 1;
+    int g = (int)(need < maxb ? need : maxb);
+    if (g > w.partial_slots / 2) g = w.partial_slots / 2;
+    return g;
+}
+
+int launch_sor_box(World &w, int max_it, double tol) {
+    int64_t work = (int64_t)((w.g.ni - 1) / 2) * (w.g.nj - 2) * (w.g.nk - 2);
+    int grid = coop_grid(w, (const void *)k_sor_box, 256, work);
+    Geo g = w.g;
+    double *phi = w.phi;
+    const double *rho = w.rho;
+    double *part = w.d_partials;
+    SolveStatus *st = w.d_status;
+    int *err = w.d_err;
+    void *args[] = {&g, &phi, &rho, &max_it, &tol, &part, &st, &err};
+    w.nlaunch++;
+    return (int)cudaLaunchCooperativeKernel((const void *)k_sor_box, grid, 256, args, 0, w.stream);
+}
+
+int launch_gs_sphere(World &w, int max_it, double tol) {
+    int64_t work = (int64_t)((w.g.ni - 1) / 2) * (w.g.nj - 2) * (w.g.nk - 2);
+    int grid = coop_grid(w, (const void *)k_gs_sphere, 256, work);
+    Geo g = w.g;
+    double *phi = w.phi;
+    const double *rho = w.rho;
+    const int32_t *obj = w.obj, *tg = w.target;
+    double phi0 = w.phi0, te0 = w.te0, n0 = w.n0;
+    double *part = w.d_partials;
+    SolveStatus *st = w.d_status;
+    int *err = w.d_err;
+    void *args[] = {&g, &phi, &rho, &obj, &tg, &phi0, &te0, &n0, &max_it, &tol, &part, &st, &err};
+    w.nlaunch++;
+    return (int)cudaLaunchCooperativeKernel((const void *)k_gs_sphere, grid, 256, args, 0, w.stream);
+}
+
+void launch_node_vol(World &w) {
+    k_node_vol<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.vol);
+    w.nlaunch++;
+}
+
+void launch_ef4(World &w) {
+    k_ef_to_ef4<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.ef, w.ef4);
+    w.nlaunch++;
+    w.ef4_valid = true;
+}
+
+void launch_fill(World &w, double *x, int64_t n, double v) {
+    if (n <= 0) return;
+    k_fill<<<blocks_for(n, 256), 256, 0, w.stream>>>(x, n, v);
+    w.nlaunch++;
+}
+
+void launch_qn(World &w) {
+    k_qn<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.phi, w.rho, w.obj, w.phi0, w.te0, w.n0);
+    w.nlaunch++;
+}
+
+}  // namespace espic

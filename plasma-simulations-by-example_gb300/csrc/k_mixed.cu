@@ -1,0 +1,500 @@
+/*
+ * k_mixed.cu -- the mixed-precision form of the particle step: a particle is
+ * an int32 cell key (i | j<<10 | k<<20), an f32 in-cell offset and an f32
+ * velocity (28 bytes), with the species weight mpw0.  The push gathers E from
+ * the f32 copy ef4 (one 16-byte load per corner), moves the particle in cell
+ * units, applies the walls / sphere, and deposits its CIC weights as 24-bit
+ * fixed-point fractions of mpw0 with warp-aggregated 64-bit atomics (lanes of
+ * a warp that share a cell are summed with one redux, then one atomic per
+ * corner).  Integer sums make the density independent of particle order.
+ *
+ * Reference behaviour restated: Species::advance (ch3/ver2/Species.cpp:7-48,
+ * ch2/Species.cpp:7-38), Field_::gather/scatter (ch2/Field.h:164-208),
+ * Species::computeNumberDensity (ch2/Species.cpp:41-52).  The counting sort
+ * by cell has no reference counterpart (the reference never reorders
+ * particles except by its removal step).
+ */
+#include "espic_world.h"
+
+namespace espic {
+
+enum { M_REFLECT = 0, M_ABSORB = 1 };
+
+struct MixArgs {
+    int ni, nj, nk;
+    float qmdt;        /* q/m dt */
+    float dtdh[3];     /* dt/dh per axis: m/s -> cells per step */
+    float dh[3];
+    float sx[3];       /* x0 - sphere centre */
+    float r2;          /* sphere radius^2, < 0 when there is no sphere */
+};
+
+__device__ __forceinline__ void unpack(int32_t key, int &i, int &j, int &k) {
+    i = key & 1023;
+    j = (key >> 10) & 1023;
+    k = key >> 20;
+}
+
+__device__ __forceinline__ void cic_w(float fx, float fy, float fz, float w[8]) {
+    float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
+    w[0] = gx * gy * gz;
+    w[1] = fx * gy * gz;
+    w[2] = fx * fy * gz;
+    w[3] = gx * fy * gz;
+    w[4] = gx * gy * fz;
+    w[5] = fx * gy * fz;
+    w[6] = fx * fy * fz;
+    w[7] = gx * fy * fz;
+}
+
+/* move a coordinate in cell units: returns the new cell index */
+__device__ __forceinline__ int advance_axis(int i, float &f, float dv) {
+    f += dv;
+    float fl = floorf(f);
+    i += (int)fl;
+    f -= fl;
+    if (f >= 1.f) {
+        f -= 1.f;
+        i += 1;
+    }
+    return i;
+}
+
+__device__ __forceinline__ void reflect_axis(int &i, float &f, float &v, int n) {
+    float p = (float)i + f;
+    float top = (float)(n - 1);
+    if (p < 0.f) {
+        p = -p;
+        v = -v;
+    } else if (p >= top) {
+        p = 2.f * top - p;
+        v = -v;
+    }
+    int ii = (int)p;
+    if (ii > n - 2) ii = n - 2;
+    if (ii < 0) ii = 0;
+    i = ii;
+    f = p - (float)ii;
+}
+
+/* warp-aggregated fixed-point CIC deposit of the lanes in `active` */
+__device__ __forceinline__ void deposit_warp(unsigned active, bool me, int32_t key, int ni, int nj,
+                                             float fx, float fy, float fz, unsigned long long *acc) {
+    if (!me) return;
+    unsigned peers = __match_any_sync(active, key);
+    int leader = __ffs(peers) - 1;
+    float w[8];
+    cic_w(fx, fy, fz, w);
+    unsigned q[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) q[c] = __reduce_add_sync(peers, __float2uint_rn(w[c] * 16777216.f));
+    if ((int)(threadIdx.x & 31) == leader) {
+        int i, j, k;
+        unpack(key, i, j, k);
+        int64_t sy = ni, sz = (int64_t)ni * nj;
+        int64_t n0 = ((int64_t)k * nj + j) * ni + i;
+        int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            if (q[c]) atomicAdd(acc + idx[c], (unsigned long long)q[c]);
+    }
+}
+
+template <int WALLS, bool DEPOSIT>
+__global__ void __launch_bounds__(256) k_push_mixed(MixArgs a, const float4 *__restrict__ ef4, int32_t *cell,
+                                                    float *off, float *vel, int64_t stride,
+                                                    const int64_t *__restrict__ d_count, uint32_t *deadmask,
+                                                    int32_t *tiledead, unsigned long long *acc, int *err) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t n = d_count[0];
+    bool live = p < n;
+    bool dead = false;
+    int32_t key = -1;
+    float fx = 0, fy = 0, fz = 0;
+    if (live) {
+        int i, j, k;
+        unpack(cell[p], i, j, k);
+        fx = off[p];
+        fy = off[stride + p];
+        fz = off[2 * stride + p];
+        float vx = vel[p], vy = vel[stride + p], vz = vel[2 * stride + p];
+        int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+        int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+        float w[8];
+        cic_w(fx, fy, fz, w);
+        float4 e0 = __ldg(ef4 + n0), e1 = __ldg(ef4 + n0 + 1), e2 = __ldg(ef4 + n0 + 1 + sy),
+               e3 = __ldg(ef4 + n0 + sy), e4 = __ldg(ef4 + n0 + sz), e5 = __ldg(ef4 + n0 + 1 + sz),
+               e6 = __ldg(ef4 + n0 + 1 + sy + sz), e7 = __ldg(ef4 + n0 + sy + sz);
+        float ex = w[0] * e0.x + w[1] * e1.x + w[2] * e2.x + w[3] * e3.x + w[4] * e4.x + w[5] * e5.x +
+                   w[6] * e6.x + w[7] * e7.x;
+        float ey = w[0] * e0.y + w[1] * e1.y + w[2] * e2.y + w[3] * e3.y + w[4] * e4.y + w[5] * e5.y +
+                   w[6] * e6.y + w[7] * e7.y;
+        float ez = w[0] * e0.z + w[1] * e1.z + w[2] * e2.z + w[3] * e3.z + w[4] * e4.z + w[5] * e5.z +
+                   w[6] * e6.z + w[7] * e7.z;
+        vx += ex * a.qmdt;
+        vy += ey * a.qmdt;
+        vz += ez * a.qmdt;
+        i = advance_axis(i, fx, vx * a.dtdh[0]);
+        j = advance_axis(j, fy, vy * a.dtdh[1]);
+        k = advance_axis(k, fz, vz * a.dtdh[2]);
+        if (WALLS == M_REFLECT) {
+            reflect_axis(i, fx, vx, a.ni);
+            reflect_axis(j, fy, vy, a.nj);
+            reflect_axis(k, fz, vz, a.nk);
+        } else {
+            dead = i < 0 || i > a.ni - 2 || j < 0 || j > a.nj - 2 || k < 0 || k > a.nk - 2;
+            if (!dead && a.r2 >= 0.f) {
+                float rx = ((float)i + fx) * a.dh[0] + a.sx[0];
+                float ry = ((float)j + fy) * a.dh[1] + a.sx[1];
+                float rz = ((float)k + fz) * a.dh[2] + a.sx[2];
+                dead = rx * rx + ry * ry + rz * rz <= a.r2;
+            }
+        }
+        if (!(isfinite(fx) && isfinite(fy) && isfinite(fz) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
+            atomicOr(err, DERR_NONFINITE);
+            dead = true;
+            i = j = k = 0;
+            fx = fy = fz = 0.f;
+        }
+        key = (i & 1023) | ((j & 1023) << 10) | (k << 20);
+        cell[p] = key;
+        off[p] = fx;
+        off[stride + p] = fy;
+        off[2 * stride + p] = fz;
+        vel[p] = vx;
+        vel[stride + p] = vy;
+        vel[2 * stride + p] = vz;
+    }
+    if (DEPOSIT) {
+        bool me = live && !dead;
+        unsigned active = __ballot_sync(0xffffffffu, me);
+        deposit_warp(active, me, key, a.ni, a.nj, fx, fy, fz, acc);
+    }
+    if (WALLS == M_ABSORB) {
+        unsigned m = __ballot_sync(0xffffffffu, dead);
+        if ((threadIdx.x & 31) == 0 && live) {
+            deadmask[p >> 5] = m;
+            if (m) atomicAdd(tiledead + (p / TILE_PARTICLES), __popc(m));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_deposit_mixed(MixArgs a, const int32_t *__restrict__ cell,
+                                                       const float *__restrict__ off, int64_t stride,
+                                                       const int64_t *__restrict__ d_count,
+                                                       unsigned long long *acc) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool me = p < d_count[0];
+    int32_t key = -1;
+    float fx = 0, fy = 0, fz = 0;
+    if (me) {
+        key = cell[p];
+        fx = off[p];
+        fy = off[stride + p];
+        fz = off[2 * stride + p];
+    }
+    unsigned active = __ballot_sync(0xffffffffu, me);
+    deposit_warp(active, me, key, a.ni, a.nj, fx, fy, fz, acc);
+}
+
+/* float64 block -> mixed form (World::XtoL in float64, then split) */
+__global__ void k_to_mixed(Geo g, const double *__restrict__ P, int64_t pstride, int64_t n, int64_t first,
+                           int32_t *cell, float *off, float *vel, int64_t stride) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int64_t dst = first + t;
+    int c[3];
+    int nmax[3] = {g.ni, g.nj, g.nk};
+    for (int d = 0; d < 3; d++) {
+        double lc = (P[d * pstride + t] - g.x0[d]) / g.dh[d];
+        int i = (int)lc;
+        if (i < 0) i = 0;
+        if (i > nmax[d] - 2) i = nmax[d] - 2;
+        c[d] = i;
+        off[d * stride + dst] = (float)(lc - i);
+        vel[d * stride + dst] = (float)P[(3 + d) * pstride + t];
+    }
+    cell[dst] = c[0] | (c[1] << 10) | (c[2] << 20);
+}
+
+/* mixed form -> float64 block (x = x0 + (i + f) dh) */
+__global__ void k_from_mixed(Geo g, const int32_t *__restrict__ cell, const float *__restrict__ off,
+                             const float *__restrict__ vel, int64_t stride, const int64_t *__restrict__ d_count,
+                             double w0, double *P, int64_t pstride) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    int i[3];
+    unpack(cell[p], i[0], i[1], i[2]);
+    for (int d = 0; d < 3; d++) {
+        P[d * pstride + p] = g.x0[d] + ((double)i[d] + (double)off[d * stride + p]) * g.dh[d];
+        P[(3 + d) * pstride + p] = (double)vel[d * stride + p];
+    }
+    P[6 * pstride + p] = w0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* counting sort by cell: histogram, exclusive scan, scatter               */
+__device__ __forceinline__ int32_t linear_cell(int32_t key, int ni, int nj) {
+    int i, j, k;
+    unpack(key, i, j, k);
+    return (k * (nj - 1) + j) * (ni - 1) + i;
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(const int32_t *__restrict__ cell,
+                                                   const int64_t *__restrict__ d_count, int ni, int nj,
+                                                   int32_t *counts) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool me = p < d_count[0];
+    int32_t lc = me ? linear_cell(cell[p], ni, nj) : -1;
+    unsigned active = __ballot_sync(0xffffffffu, me);
+    if (!me) return;
+    unsigned peers = __match_any_sync(active, lc);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counts + lc, __popc(peers));
+}
+
+constexpr int SCAN_PER_BLOCK = 8192; /* 1024 threads x 8 */
+
+__device__ __forceinline__ int32_t scan_block(int32_t v, int32_t *sh, int32_t *total) {
+    int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    int32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) sh[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t ws = sh[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        sh[lane] = ws;
+    }
+    __syncthreads();
+    int32_t r = (wid ? sh[wid - 1] : 0) + incl - v;
+    if (total) *total = sh[31];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_reduce(const int32_t *__restrict__ x, int64_t n, int32_t *bsum) {
+    __shared__ int32_t sh[32];
+    int64_t base = (int64_t)blockIdx.x * SCAN_PER_BLOCK + threadIdx.x * 8;
+    int32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (base + q < n) s += x[base + q];
+    int32_t tot;
+    scan_block(s, sh, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_bsum(int32_t *bsum, int64_t nb) {
+    __shared__ int32_t sh[32];
+    int64_t per = (nb + 1023) / 1024;
+    int64_t a = threadIdx.x * per, b = a + per;
+    if (b > nb) b = nb;
+    int32_t s = 0;
+    for (int64_t i = a; i < b; i++) s += bsum[i];
+    int32_t run = scan_block(s, sh, nullptr);
+    for (int64_t i = a; i < b; i++) {
+        int32_t c = bsum[i];
+        bsum[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_down(int32_t *x, int64_t n, const int32_t *__restrict__ bsum) {
+    __shared__ int32_t sh[32];
+    int64_t base = (int64_t)blockIdx.x * SCAN_PER_BLOCK + threadIdx.x * 8;
+    int32_t v[8], s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        v[q] = (base + q < n) ? x[base + q] : 0;
+        s += v[q];
+    }
+    int32_t run = scan_block(s, sh, nullptr) + bsum[blockIdx.x];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        if (base + q < n) x[base + q] = run;
+        run += v[q];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict__ cell,
+                                                      const float *__restrict__ off,
+                                                      const float *__restrict__ vel, int64_t stride,
+                                                      const int64_t *__restrict__ d_count, int ni, int nj,
+                                                      int32_t *cursor, int32_t *cell2, float *off2, float *vel2) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool me = p < d_count[0];
+    int32_t key = me ? cell[p] : -1;
+    int32_t lc = me ? linear_cell(key, ni, nj) : -1;
+    unsigned active = __ballot_sync(0xffffffffu, me);
+    if (!me) return;
+    unsigned peers = __match_any_sync(active, lc);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor + lc, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    int64_t dst = base + __popc(peers & ((1u << lane) - 1u));
+    cell2[dst] = key;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        off2[d * stride + dst] = off[d * stride + p];
+        vel2[d * stride + dst] = vel[d * stride + p];
+    }
+}
+
+/* per block: {count, mx, my, mz, sum w v^2} for the mixed form: float sums
+ * over runs of 32 particles folded into float64 */
+__global__ void __launch_bounds__(256) k_diag_mixed(const float *__restrict__ vel, int64_t stride,
+                                                    const int64_t *__restrict__ d_count, double *partials,
+                                                    int nblocks) {
+    int64_t n = d_count[0];
+    double acc[5] = {0, 0, 0, 0, 0};
+    float f[5] = {0, 0, 0, 0, 0};
+    int run = 0;
+    for (int64_t p = (int64_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (int64_t)nblocks * 256) {
+        float v0 = vel[p], v1 = vel[stride + p], v2 = vel[2 * stride + p];
+        f[0] += 1.f;
+        f[1] += v0;
+        f[2] += v1;
+        f[3] += v2;
+        f[4] += v0 * v0 + v1 * v1 + v2 * v2;
+        if (++run == 32) {
+            for (int q = 0; q < 5; q++) {
+                acc[q] += (double)f[q];
+                f[q] = 0.f;
+            }
+            run = 0;
+        }
+    }
+    for (int q = 0; q < 5; q++) acc[q] += (double)f[q];
+    __shared__ double sh[5][8];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int q = 0; q < 5; q++) {
+        double x = acc[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[q][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double s = 0;
+        for (int k = 0; k < 8; k++) s += sh[threadIdx.x][k];
+        partials[5 * blockIdx.x + threadIdx.x] = s;
+    }
+}
+
+__global__ void k_diag_mixed_final(const double *__restrict__ partials, int nblocks, double mass, double w0,
+                                   double *out) {
+    if (threadIdx.x != 0) return;
+    double s[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < nblocks; b++)
+        for (int q = 0; q < 5; q++) s[q] += partials[5 * b + q];
+    out[0] = s[0] * w0;
+    out[1] = s[1] * w0 * mass;
+    out[2] = s[2] * w0 * mass;
+    out[3] = s[3] * w0 * mass;
+    out[4] = 0.5 * mass * (w0 * s[4]);
+}
+
+/* ======================================================================== */
+static MixArgs mix_args(World &w, Species &s) {
+    MixArgs a;
+    a.ni = w.g.ni;
+    a.nj = w.g.nj;
+    a.nk = w.g.nk;
+    a.qmdt = (float)(s.charge / s.mass * w.dt);
+    for (int d = 0; d < 3; d++) {
+        a.dtdh[d] = (float)(w.dt / w.g.dh[d]);
+        a.dh[d] = (float)w.g.dh[d];
+        a.sx[d] = (float)(w.g.x0[d] - w.sphere[d]);
+    }
+    a.r2 = w.has_sphere ? (float)w.sphere[3] : -1.f;
+    return a;
+}
+
+template <int WALLS, bool DEP>
+static void push_mixed_as(World &w, Species &s, int blocks) {
+    MixArgs a = mix_args(w, s);
+    k_push_mixed<WALLS, DEP><<<blocks, 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.cap, s.d_count,
+                                                           s.deadmask, s.tiledead, s.acc, w.d_err);
+    w.nlaunch++;
+}
+
+void launch_push_mixed(World &w, Species &s, bool deposit) {
+    int64_t n = s.host_bound;
+    if (n <= 0) return;
+    int blocks = blocks_for(n, 256);
+    if (s.walls == 0) {
+        if (deposit)
+            push_mixed_as<M_REFLECT, true>(w, s, blocks);
+        else
+            push_mixed_as<M_REFLECT, false>(w, s, blocks);
+    } else {
+        if (deposit)
+            push_mixed_as<M_ABSORB, true>(w, s, blocks);
+        else
+            push_mixed_as<M_ABSORB, false>(w, s, blocks);
+    }
+}
+
+void launch_deposit_mixed(World &w, Species &s) {
+    int64_t n = s.host_bound;
+    if (n <= 0) return;
+    MixArgs a = mix_args(w, s);
+    k_deposit_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(a, s.cell, s.off, s.cap, s.d_count, s.acc);
+    w.nlaunch++;
+}
+
+void launch_to_mixed(World &w, Species &s, const double *P, int64_t stride, int64_t first, int64_t n) {
+    if (n <= 0) return;
+    k_to_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, P, stride, n, first, s.cell, s.off, s.vel,
+                                                          s.cap);
+    w.nlaunch++;
+}
+
+void launch_from_mixed(World &w, Species &s, double *P, int64_t stride, int64_t n) {
+    if (n <= 0) return;
+    k_from_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.cell, s.off, s.vel, s.cap, s.d_count, s.mpw0, P,
+                                                           stride);
+    w.nlaunch++;
+}
+
+void launch_sort_mixed(World &w, Species &s) {
+    int64_t n = s.host_bound;
+    if (n <= 0) return;
+    int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    int32_t *counts = s.sort_count;
+    int32_t *bsum = counts + ncells + 1;
+    int64_t nb = (ncells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+    cudaMemsetAsync(counts, 0, (ncells + 1) * sizeof(int32_t), w.stream);
+    k_sort_hist<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, w.g.ni, w.g.nj, counts);
+    k_scan_reduce<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
+    k_scan_bsum<<<1, 1024, 0, w.stream>>>(bsum, nb);
+    k_scan_down<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
+    k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.off, s.vel, s.cap, s.d_count, w.g.ni,
+                                                             w.g.nj, counts, s.cell2, s.off2, s.vel2);
+    w.nlaunch += 5;
+    int32_t *tc = s.cell;
+    s.cell = s.cell2;
+    s.cell2 = tc;
+    float *to = s.off;
+    s.off = s.off2;
+    s.off2 = to;
+    float *tv = s.vel;
+    s.vel = s.vel2;
+    s.vel2 = tv;
+}
+
+void launch_diag_mixed(World &w, Species &s, double *d_out5) {
+    const int nb = 592;
+    k_diag_mixed<<<nb, 256, 0, w.stream>>>(s.vel, s.cap, s.d_count, w.d_partials, nb);
+    k_diag_mixed_final<<<1, 32, 0, w.stream>>>(w.d_partials, nb, s.mass, s.mpw0, d_out5);
+    w.nlaunch += 2;
+}
+
+}  // namespace espic

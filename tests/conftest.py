@@ -23,3 +23,19 @@ def po():
     from oracle import pyoracle
     pyoracle.lib()
     return pyoracle
+
+
+def _espic_module():
+    import importlib
+    return importlib.import_module("plasma-simulations-by-example_gb300")
+
+
+@pytest.fixture(scope="session")
+def espic():
+    """The ctypes view of libespic on a GPU (built on first use)."""
+    mod = _espic_module()
+    import os as _os
+    if not _os.path.exists(mod.LIB_PATH):
+        mod.build()
+    mod.lib()
+    return mod
