@@ -149,6 +149,16 @@ int espic_solver_set_reference(espic_world *w, double phi0, double te0, double n
  * float64 Newton residual (iterative refinement). */
 int espic_solver_set_newton(espic_world *w, int nr_max, double nr_tol, int pcg_max,
                             double pcg_tol, int fp32_inner);
+/* Preconditioner of the Newton-PCG inner solve: levels = number of
+ * aggregation-multigrid levels below the node grid (0: Jacobi, as the
+ * reference's solvePCGLinear, ch3/ver2/PotentialSolver.cpp:299-331; the
+ * default 12 means as many as the grid allows), scale = coarse-correction
+ * scale (default 1.6). */
+int espic_solver_set_multigrid(espic_world *w, int levels, double scale);
+/* Upper bound on the thread blocks of the cooperative solver launches
+ * (0: one per SM).  A tuning knob with no reference counterpart: small grids
+ * are bound by grid-barrier latency, which falls with fewer blocks. */
+int espic_solver_set_launch(espic_world *w, int max_blocks);
 /* PotentialSolver::solve, ch2/PotentialSolver.cpp:11-67 and
  * ch3/ver2/PotentialSolver.h:66-75.  With all out-pointers NULL the solve is
  * only enqueued; otherwise the call waits and reports iterations and the

@@ -85,6 +85,8 @@ def lib():
             "espic_solver_set": [VP, C.c_int, C.c_int, C.c_double],
             "espic_solver_set_reference": [VP, C.c_double, C.c_double, C.c_double],
             "espic_solver_set_newton": [VP, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int],
+            "espic_solver_set_multigrid": [VP, C.c_int, C.c_double],
+            "espic_solver_set_launch": [VP, C.c_int],
             "espic_solve": [VP, PI, PI, PD],
             "espic_efield": [VP],
             "espic_species_diag": [VP, C.c_int, PD],
@@ -378,6 +380,13 @@ class PotentialSolver:
     def setNewton(self, nr_max=20, nr_tol=1e-3, pcg_max=10000, pcg_tol=1e-6, fp32_inner=False):
         check(lib().espic_solver_set_newton(self.world.h, nr_max, nr_tol, pcg_max, pcg_tol,
                                             1 if fp32_inner else 0))
+
+    def setMultigrid(self, levels=12, scale=1.6):
+        """levels = 0 selects the Jacobi preconditioner."""
+        check(lib().espic_solver_set_multigrid(self.world.h, levels, scale))
+
+    def setLaunch(self, max_blocks=0):
+        check(lib().espic_solver_set_launch(self.world.h, max_blocks))
 
     def solve(self, wait=True):
         """Returns (converged, iterations, inner_iterations, residual)."""

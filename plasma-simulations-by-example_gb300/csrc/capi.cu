@@ -754,6 +754,21 @@ extern "C" int espic_solver_set_newton(espic_world *h, int nr_max, double nr_tol
     return ESPIC_OK;
 }
 
+extern "C" int espic_solver_set_multigrid(espic_world *h, int levels, double scale) {
+    WORLD(h);
+    if (levels < 0 || levels > 12 || !(scale > 0 && scale < 2)) return fail(ESPIC_ERR_ARG, "bad multigrid controls");
+    w.mg_levels_max = levels;
+    w.mg_scale = scale;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_solver_set_launch(espic_world *h, int max_blocks) {
+    WORLD(h);
+    if (max_blocks < 0) return fail(ESPIC_ERR_ARG, "bad block count");
+    w.solver_blocks = max_blocks;
+    return ESPIC_OK;
+}
+
 static int enqueue_solve(World &w) {
     PhaseScope ph(w, ESPIC_PHASE_SOLVE);
     int e = 0;

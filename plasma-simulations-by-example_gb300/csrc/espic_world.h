@@ -82,6 +82,10 @@ struct World {
     double nr_tol = 1e-3, pcg_tol = 1e-6;
     void *pcg_buf = nullptr;
     bool pcg_codes_valid = false;
+    int pcg_elem = 0;       /* element size the PCG buffers were laid out for */
+    int mg_levels_max = 12; /* multigrid levels of the PCG preconditioner (0: Jacobi) */
+    double mg_scale = 1.6;  /* coarse-correction scale */
+    int solver_blocks = 0;  /* cap on cooperative solver blocks (0: occupancy limit) */
     size_t pcg_bytes = 0;
     uint64_t seed = 0x5eed5eed12345ull;
     uint64_t load_calls = 0;

@@ -774,10 +774,12 @@ __device__ __forceinline__ double grid_sum(cg::grid_group &grid, double v, doubl
     }
     round++;
     grid.sync();
-    if (threadIdx.x == 0) {
+    /* every block sums the partials identically: lane l takes l, l+32, ... */
+    if (wid == 0) {
         double s = 0;
-        for (unsigned b = 0; b < gridDim.x; b++) s += slot[b];
-        total = s;
+        for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) total = s;
     }
     __syncthreads();
     return total;
@@ -1198,6 +1200,7 @@ static int coop_grid(World &w, const void *fn, int threads, int64_t work) {
     if (need < 1) need = 1;
     int g = (int)(need < maxb ? need : maxb);
     if (g > w.partial_slots / 2) g = w.partial_slots / 2;
+    if (w.solver_blocks > 0 && g > w.solver_blocks) g = w.solver_blocks;
     return g;
 }
 

@@ -19,6 +19,17 @@
  * inner solve of an iterative refinement whose outer residual is float64.
  * Dot products are reduced per block and summed by every block in block
  * order, so every block takes the same branch.
+ *
+ * Preconditioner: an aggregation multigrid V-cycle.  Level l+1 groups the
+ * level-l unknowns in 2x2x2 blocks of the structured index space; its
+ * operator is the Galerkin product P^T A_l P with piecewise-constant P
+ * (a 7-point stencil again, with per-node weights), built once per geometry
+ * by a deterministic gather.  Smoothing is red-black Gauss-Seidel (red then
+ * black before the coarse correction, black then red after), restriction is
+ * P^T, prolongation P scaled by a constant, and the coarsest level gets
+ * symmetric sweeps, so the preconditioner is symmetric as CG requires.
+ * Levels with fewer than 32768 nodes run on block 0 alone between two grid
+ * barriers.  Without levels, the preconditioner is Jacobi.
  */
 #include <cooperative_groups.h>
 
@@ -61,6 +72,10 @@ __global__ void k_pcg_codes(Geo g, const int32_t *__restrict__ obj, uint16_t *co
     code[u] = c;
 }
 
+/* Grid-wide sums of NV values: block partials, one grid barrier, then every
+ * block sums the partials with its first warp (lane l takes partials l,
+ * l+32, ... in order; a fixed shuffle tree combines the lanes).  Every block
+ * computes bit-identical totals, so all blocks take the same branches. */
 template <int NV>
 __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV], double *partials, int &round) {
     __shared__ double sh[NV][32];
@@ -81,23 +96,353 @@ __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV]
     }
     round++;
     grid.sync();
-    if (threadIdx.x < NV) {
-        double s = 0;
-        for (unsigned b = 0; b < gridDim.x; b++) s += slot[(size_t)b * NV + threadIdx.x];
-        tot[threadIdx.x] = s;
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double s = 0;
+            for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + (size_t)b * NV + q);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) tot[q] = s;
+        }
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < NV; q++) v[q] = tot[q];
 }
 
+
+constexpr int MG_MAX = 12;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_newton_pcg(Geo g, double *phi, const double *__restrict__ rho,
-                                                    const uint16_t *__restrict__ code,
-                                                    const int32_t *__restrict__ target, double phi0, double te0,
-                                                    double n0, int nr_max, double nr_tol, int pcg_max,
-                                                    double pcg_tol, T *y, T *r, T *z, T *p, T *q, T *dg,
-                                                    double *partials, SolveStatus *st, int *err) {
+struct MgLevel {
+    int nx, ny, nz, pad;
+    int64_t n;
+    T *diag, *w, *b, *e; /* w: 6 weights per node, [m][n] */
+};
+
+template <typename T>
+struct MgArgs {
+    int nlev;        /* coarse levels (0: Jacobi preconditioner) */
+    int grid_levels; /* coarse levels 1..grid_levels-1 run on the whole grid */
+    int nu_coarse;   /* sweeps each way on the coarsest level */
+    T scale;         /* coarse-correction scale */
+    MgLevel<T> L[MG_MAX];
+};
+
+/* everything the level-0 (node grid) operations need */
+template <typename T>
+struct Fine {
+    Geo g;
+    const uint16_t *code;
+    T ct[3];
+    int64_t off[6];
+    T *dg, *r, *z;
+};
+
+__device__ __forceinline__ void span(bool whole, int64_t &t0, int64_t &ts) {
+    if (whole) {
+        t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        ts = (int64_t)gridDim.x * blockDim.x;
+    } else {
+        t0 = threadIdx.x;
+        ts = blockDim.x;
+    }
+}
+
+/* red-black half sweep on the node grid: z = (r + sum c z_nb) / dg */
+/* Red-black Gauss-Seidel pieces.  A Gauss-Seidel update never reads the
+ * node's own old value, which allows three fusions: the first red half
+ * sweep from a zero guess is pointwise (e = b / diag) and is done by whoever
+ * produces b; the prolongation of the coarse correction is applied on the
+ * fly to the red neighbours read by the following black half sweep (the red
+ * nodes are overwritten next anyway); and the dot product r.z of CG is
+ * accumulated by the last two half sweeps, which produce the final z. */
+template <typename T>
+__device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &C, int64_t u) {
+    const Geo &g = F.g;
+    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
+    return ((int64_t)(k >> 1) * C.ny + (j >> 1)) * C.nx + (i >> 1);
+}
+
+/* node-grid half sweep of colour c over the unknowns; with C != null the
+ * neighbours are read with the coarse correction added (post-smoothing);
+ * returns the local sum of r*z of the nodes it updated */
+template <typename T>
+__device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
+    const Geo &g = F.g;
+    int hx = (g.ni - 1) / 2;
+    int64_t count = (int64_t)hx * (g.nj - 2) * (g.nk - 2);
+    int64_t t0, ts;
+    span(true, t0, ts);
+    T rz = 0;
+    for (int64_t t = t0; t < count; t += ts) {
+        int i2 = (int)(t % hx);
+        int64_t rr = t / hx;
+        int j = 1 + (int)(rr % (g.nj - 2));
+        int k = 1 + (int)(rr / (g.nj - 2));
+        int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
+        if (i > g.ni - 2) continue;
+        int64_t u = ((int64_t)k * g.nj + j) * g.ni + i;
+        /* interior node: all six neighbours are in bounds, so their loads
+         * are issued before the code word arrives; the code only selects */
+        uint16_t cc = F.code[u];
+        T ru = F.r[u];
+        T dgu = F.dg[u];
+        T zn[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
+        if (C) {
+            const MgLevel<T> &Cc = *C;
+            int64_t I0 = ((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1);
+            int64_t Ix[2] = {((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ((i - 1) >> 1),
+                             ((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ((i + 1) >> 1)};
+            int64_t Iy[2] = {((int64_t)(k >> 1) * Cc.ny + ((j - 1) >> 1)) * Cc.nx + (i >> 1),
+                             ((int64_t)(k >> 1) * Cc.ny + ((j + 1) >> 1)) * Cc.nx + (i >> 1)};
+            int64_t Iz[2] = {((int64_t)((k - 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1),
+                             ((int64_t)((k + 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1)};
+            (void)I0;
+            zn[0] += scale * Cc.e[Ix[0]];
+            zn[1] += scale * Cc.e[Ix[1]];
+            zn[2] += scale * Cc.e[Iy[0]];
+            zn[3] += scale * Cc.e[Iy[1]];
+            zn[4] += scale * Cc.e[Iz[0]];
+            zn[5] += scale * Cc.e[Iz[1]];
+        }
+        if (!(cc & SELF)) continue;
+        T s = ru;
+#pragma unroll
+        for (int m = 0; m < 6; m++) s += (cc & (1u << m)) ? F.ct[m >> 1] * zn[m] : (T)0;
+        T zu = s / dgu;
+        F.z[u] = zu;
+        rz += ru * zu;
+    }
+    return rz;
+}
+
+template <typename T>
+__device__ __forceinline__ int64_t coarse_agg(const MgLevel<T> &L, const MgLevel<T> &C, int64_t u) {
+    int i = (int)(u % L.nx), j = (int)((u / L.nx) % L.ny), k = (int)(u / ((int64_t)L.nx * L.ny));
+    return ((int64_t)(k >> 1) * C.ny + (j >> 1)) * C.nx + (i >> 1);
+}
+
+template <typename T>
+__device__ void coarse_half(const MgLevel<T> &L, int c, bool whole, const MgLevel<T> *C, T scale) {
+    int hx = (L.nx + 1) / 2;
+    int64_t count = (int64_t)hx * L.ny * L.nz;
+    int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
+    int64_t t0, ts;
+    span(whole, t0, ts);
+    for (int64_t t = t0; t < count; t += ts) {
+        int i2 = (int)(t % hx);
+        int64_t rr = t / hx;
+        int j = (int)(rr % L.ny);
+        int k = (int)(rr / L.ny);
+        int i = 2 * i2 + ((j + k + c) & 1);
+        if (i >= L.nx) continue;
+        int64_t I = ((int64_t)k * L.ny + j) * L.nx + i;
+        /* all loads first (neighbour indices clamped into the level; a zero
+         * weight deselects them), then the arithmetic */
+        T d = L.diag[I];
+        T s = L.b[I];
+        T wm[6], en[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            int64_t nb = I + offs[m];
+            nb = nb < 0 ? 0 : (nb >= L.n ? L.n - 1 : nb);
+            wm[m] = L.w[m * L.n + I];
+            en[m] = L.e[nb];
+            if (C) en[m] += scale * C->e[coarse_agg(L, *C, nb)];
+        }
+        if (d == (T)0) continue;
+#pragma unroll
+        for (int m = 0; m < 6; m++) s += (wm[m] != (T)0) ? wm[m] * en[m] : (T)0;
+        L.e[I] = s / d;
+    }
+}
+
+/* b of level l+1 = sum of the children's residuals (b - A e); the first red
+ * half sweep of level l+1 (e = b / diag) is fused in */
+template <typename T>
+__device__ void restrict_fine(const Fine<T> &F, const MgLevel<T> &C) {
+    const Geo &g = F.g;
+    int64_t t0, ts;
+    span(true, t0, ts);
+    for (int64_t I = t0; I < C.n; I += ts) {
+        int ci = (int)(I % C.nx);
+        int cj = (int)((I / C.nx) % C.ny);
+        int ck = (int)(I / ((int64_t)C.nx * C.ny));
+        T sum = 0;
+        /* the four red children (black residuals are zero after the black
+         * sweep); a child off the grid or not an unknown contributes 0 */
+        int64_t uu[4];
+        uint16_t cc[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int d = (q << 1) | (((q & 1) + (q >> 1)) & 1); /* dx makes dx+dy+dz even: a red child */
+            int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+            bool in = i < g.ni && j < g.nj && k < g.nk;
+            uu[q] = in ? ((int64_t)k * g.nj + j) * g.ni + i : 0;
+            cc[q] = in ? F.code[uu[q]] : (uint16_t)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (!(cc[q] & SELF)) continue;
+            int64_t u = uu[q];
+            T zn[6];
+#pragma unroll
+            for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
+            T res = F.r[u] - F.dg[u] * F.z[u];
+#pragma unroll
+            for (int m = 0; m < 6; m++) res += (cc[q] & (1u << m)) ? F.ct[m >> 1] * zn[m] : (T)0;
+            sum += res;
+        }
+        C.b[I] = sum;
+        if (((ci + cj + ck) & 1) == 0) {
+            T d = C.diag[I];
+            if (d != (T)0) C.e[I] = sum / d;
+        }
+    }
+}
+
+template <typename T>
+__device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool whole) {
+    int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
+    int64_t t0, ts;
+    span(whole, t0, ts);
+    for (int64_t I = t0; I < C.n; I += ts) {
+        int ci = (int)(I % C.nx);
+        int cj = (int)((I / C.nx) % C.ny);
+        int ck = (int)(I / ((int64_t)C.nx * C.ny));
+        T sum = 0;
+        for (int d = 0; d < 8; d++) {
+            int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+            if (i >= L.nx || j >= L.ny || k >= L.nz) continue;
+            if (((i + j + k) & 1) == 1) continue;
+            int64_t u = ((int64_t)k * L.ny + j) * L.nx + i;
+            T dd = L.diag[u];
+            if (dd == (T)0) continue;
+            T res = L.b[u] - dd * L.e[u];
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                T wm = L.w[m * L.n + u];
+                if (wm != (T)0) res += wm * L.e[u + offs[m]];
+            }
+            sum += res;
+        }
+        C.b[I] = sum;
+        if (((ci + cj + ck) & 1) == 0) {
+            T d = C.diag[I];
+            if (d != (T)0) C.e[I] = sum / d;
+        }
+    }
+}
+
+/* The V-cycle z = M r after its first red half sweep on the node grid
+ * (done by the caller, fused with the CG update of r).  Every block executes
+ * the same grid barriers; returns the grid-wide r.z of the final z (the
+ * last barrier is the one of that reduction). */
+template <typename T>
+__device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgArgs<T> &A, double *partials,
+                              int &round) {
+    const int NL = A.nlev;
+    if (NL == 0) { /* Jacobi: the caller computed z on every node */
+        T rz = 0;
+        int64_t nn = (int64_t)F.g.ni * F.g.nj * F.g.nk;
+        int64_t t0, ts;
+        span(true, t0, ts);
+        for (int64_t u = t0; u < nn; u += ts)
+            if (F.code[u] & SELF) rz += F.r[u] * F.z[u];
+        double v[1] = {(double)rz};
+        grid_sum_n<1>(grid, v, partials, round);
+        return v[0];
+    }
+    const int GL = A.grid_levels;
+    const T sc = A.scale;
+    fine_half(F, 1, (const MgLevel<T> *)nullptr, sc);
+    grid.sync();
+    restrict_fine(F, A.L[0]);
+    grid.sync();
+    int l = 1; /* level l lives in A.L[l-1] and its red half was fused */
+    for (; l < GL && l < NL; l++) {
+        coarse_half(A.L[l - 1], 1, true, (const MgLevel<T> *)nullptr, sc);
+        grid.sync();
+        restrict_coarse(A.L[l - 1], A.L[l], true);
+        grid.sync();
+    }
+    const int lblock = l;
+    const bool coarsest_whole = NL < GL;
+    const int nuc = A.nu_coarse;
+    if (!coarsest_whole) {
+        if (blockIdx.x == 0) {
+            for (int b = lblock; b < NL; b++) {
+                coarse_half(A.L[b - 1], 1, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+                restrict_coarse(A.L[b - 1], A.L[b], false);
+                __syncthreads();
+            }
+            const MgLevel<T> &Lc = A.L[NL - 1];
+            for (int s = 0; s < nuc; s++) {
+                if (s) {
+                    coarse_half(Lc, 0, false, (const MgLevel<T> *)nullptr, sc);
+                    __syncthreads();
+                }
+                coarse_half(Lc, 1, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+            }
+            for (int s = 0; s < nuc; s++) {
+                coarse_half(Lc, 1, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+                coarse_half(Lc, 0, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+            }
+            for (int b = NL - 1; b >= lblock; b--) {
+                coarse_half(A.L[b - 1], 1, false, &A.L[b], sc);
+                __syncthreads();
+                coarse_half(A.L[b - 1], 0, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+            }
+        }
+        grid.sync();
+    } else {
+        const MgLevel<T> &Lc = A.L[NL - 1];
+        for (int s = 0; s < nuc; s++) {
+            if (s) {
+                coarse_half(Lc, 0, true, (const MgLevel<T> *)nullptr, sc);
+                grid.sync();
+            }
+            coarse_half(Lc, 1, true, (const MgLevel<T> *)nullptr, sc);
+            grid.sync();
+        }
+        for (int s = 0; s < nuc; s++) {
+            coarse_half(Lc, 1, true, (const MgLevel<T> *)nullptr, sc);
+            grid.sync();
+            coarse_half(Lc, 0, true, (const MgLevel<T> *)nullptr, sc);
+            grid.sync();
+        }
+    }
+    const int top = coarsest_whole ? NL - 1 : lblock - 1;
+    for (int b = top; b >= 1; b--) {
+        coarse_half(A.L[b - 1], 1, true, &A.L[b], sc);
+        grid.sync();
+        coarse_half(A.L[b - 1], 0, true, (const MgLevel<T> *)nullptr, sc);
+        grid.sync();
+    }
+    T rz = fine_half(F, 1, &A.L[0], sc);
+    grid.sync();
+    rz += fine_half(F, 0, (const MgLevel<T> *)nullptr, sc);
+    double v[1] = {(double)rz};
+    grid_sum_n<1>(grid, v, partials, round);
+    return v[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, const double *__restrict__ rho,
+                                                        const uint16_t *__restrict__ code,
+                                                        const int32_t *__restrict__ target, double phi0,
+                                                        double te0, double n0, int nr_max, double nr_tol,
+                                                        int pcg_max, double pcg_tol, T *y, T *r, T *z, T *p0,
+                                                        T *p1, T *q, T *dg, MgArgs<T> mg, double *partials,
+                                                        SolveStatus *st, int *err) {
     cg::grid_group grid = cg::this_grid();
     const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
@@ -107,96 +452,116 @@ __global__ void __launch_bounds__(256) k_newton_pcg(Geo g, double *phi, const do
     const double A0 = PCG_QE * n0 / PCG_EPS_0;
     const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t gsize = (int64_t)gridDim.x * blockDim.x;
+    const bool jacobi = mg.nlev == 0;
+    Fine<T> F;
+    F.g = g;
+    F.code = code;
+    for (int m = 0; m < 3; m++) F.ct[m] = ct[m];
+    for (int m = 0; m < 6; m++) F.off[m] = off[m];
+    F.dg = dg;
+    F.r = r;
+    F.z = z;
     int round = 0, nr, conv = 0, inner = 0;
     double norm = 0;
     for (nr = 0; nr < nr_max; nr++) {
-        /* Newton residual and Jacobian diagonal (float64) */
-        T ff = 0, rz = 0;
+        /* Newton residual and Jacobian diagonal (float64); the first red
+         * smoothing half sweep (or Jacobi) of the preconditioner rides along */
+        double ff = 0;
         for (int64_t u = gtid; u < nn; u += gsize) {
             uint16_t c = code[u];
             if (!(c & SELF)) continue;
-            double ph = phi[u], L = 0, dL = 0;
+            double ph = phi[u], L = 0, dL = 0, pn[6];
+#pragma unroll
+            for (int m = 0; m < 6; m++) pn[m] = phi[u + off[m]];
 #pragma unroll
             for (int m = 0; m < 6; m++) {
-                if (c & ((1u << m) | (1u << (6 + m)))) {
-                    L += cd[m >> 1] * (ph - phi[u + off[m]]);
-                    dL += cd[m >> 1];
-                }
+                bool on = c & ((1u << m) | (1u << (6 + m)));
+                L += on ? cd[m >> 1] * (ph - pn[m]) : 0.0;
+                dL += on ? cd[m >> 1] : 0.0;
             }
             double e = exp((ph - phi0) / te0);
-            double F = L + A0 * e - rho[u] / PCG_EPS_0;
+            double Fv = L + A0 * e - rho[u] / PCG_EPS_0;
             T d = (T)(dL + A0 / te0 * e);
-            T rr = (T)F;
-            T zz = rr / d;
+            T rv = (T)Fv;
             dg[u] = d;
-            r[u] = rr;
-            z[u] = zz;
-            p[u] = zz;
+            r[u] = rv;
             y[u] = 0;
-            ff += (T)(F * F);
-            rz += rr * zz;
+            int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / sz);
+            if (jacobi || ((i + j + k) & 1) == 0) z[u] = rv / d;
+            ff += Fv * Fv;
         }
-        double s2[2] = {(double)ff, (double)rz};
-        grid_sum_n<2>(grid, s2, partials, round);
-        double FF = s2[0], RZ = s2[1];
+        double s1[1] = {ff};
+        grid_sum_n<1>(grid, s1, partials, round);
+        double FF = s1[0];
         if (!isfinite(FF)) {
             if (gtid == 0) atomicOr(err, DERR_NONFINITE);
             break;
         }
         if (FF > 0) {
             const double stop2 = pcg_tol * pcg_tol * FF;
+            double RZ = vcycle_rest(grid, F, mg, partials, round);
+            T beta = 0;
+            T *pold = p0, *pnew = p1;
             for (int it = 0; it < pcg_max; it++) {
+                /* p = z + beta p (on the fly at the node and its neighbours),
+                 * q = J p */
                 T pq = 0;
                 for (int64_t u = gtid; u < nn; u += gsize) {
                     uint16_t c = code[u];
                     if (!(c & SELF)) continue;
-                    T pu = p[u];
-                    T s = dg[u] * pu;
+                    /* an unknown is interior: neighbour loads need no code bit */
+                    T zc = z[u], pc = it ? pold[u] : (T)0, d = dg[u];
+                    T zn[6], pn[6];
 #pragma unroll
-                    for (int m = 0; m < 6; m++)
-                        if (c & (1u << m)) s -= ct[m >> 1] * p[u + off[m]];
+                    for (int m = 0; m < 6; m++) {
+                        zn[m] = z[u + off[m]];
+                        pn[m] = it ? pold[u + off[m]] : (T)0;
+                    }
+                    T pu = zc + beta * pc;
+                    T s = d * pu;
+#pragma unroll
+                    for (int m = 0; m < 6; m++) s -= (c & (1u << m)) ? ct[m >> 1] * (zn[m] + beta * pn[m]) : (T)0;
+                    pnew[u] = pu;
                     q[u] = s;
                     pq += pu * s;
                 }
-                double s1[1] = {(double)pq};
-                grid_sum_n<1>(grid, s1, partials, round);
-                const T alpha = (T)(RZ / s1[0]);
-                T rr = 0, rzn = 0;
+                double s3[1] = {(double)pq};
+                grid_sum_n<1>(grid, s3, partials, round);
+                const T alpha = (T)(RZ / s3[0]);
+                /* y += alpha p, r -= alpha q, and the first red half sweep */
+                T rr = 0;
                 for (int64_t u = gtid; u < nn; u += gsize) {
                     if (!(code[u] & SELF)) continue;
-                    T yy = y[u] + alpha * p[u];
+                    y[u] += alpha * pnew[u];
                     T ru = r[u] - alpha * q[u];
-                    T zu = ru / dg[u];
-                    y[u] = yy;
                     r[u] = ru;
-                    z[u] = zu;
                     rr += ru * ru;
-                    rzn += ru * zu;
+                    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / sz);
+                    if (jacobi || ((i + j + k) & 1) == 0) z[u] = ru / dg[u];
                 }
-                double s3[2] = {(double)rr, (double)rzn};
-                grid_sum_n<2>(grid, s3, partials, round);
+                double s4[1] = {(double)rr};
+                grid_sum_n<1>(grid, s4, partials, round);
                 inner++;
-                if (!(s3[0] > stop2)) break; /* also leaves on NaN */
-                const T beta = (T)(s3[1] / RZ);
-                RZ = s3[1];
-                for (int64_t u = gtid; u < nn; u += gsize) {
-                    if (!(code[u] & SELF)) continue;
-                    p[u] = z[u] + beta * p[u];
-                }
-                grid.sync();
+                if (!(s4[0] > stop2)) break; /* also leaves on NaN */
+                double RZn = vcycle_rest(grid, F, mg, partials, round);
+                beta = (T)(RZn / RZ);
+                RZ = RZn;
+                T *tp = pold;
+                pold = pnew;
+                pnew = tp;
             }
         }
         /* Newton update */
-        T yy = 0;
+        double yy = 0;
         for (int64_t u = gtid; u < nn; u += gsize) {
             if (!(code[u] & SELF)) continue;
-            T yu = y[u];
-            phi[u] -= (double)yu;
+            double yu = (double)y[u];
+            phi[u] -= yu;
             yy += yu * yu;
         }
-        double s4[1] = {(double)yy};
-        grid_sum_n<1>(grid, s4, partials, round);
-        norm = sqrt(s4[0] / (double)nn);
+        double s6[1] = {yy};
+        grid_sum_n<1>(grid, s6, partials, round);
+        norm = sqrt(s6[0] / (double)nn);
         if (!isfinite(norm)) {
             if (gtid == 0) atomicOr(err, DERR_NONFINITE);
             break;
@@ -223,46 +588,139 @@ __global__ void __launch_bounds__(256) k_newton_pcg(Geo g, double *phi, const do
     }
 }
 
-/* ======================================================================== */
-struct PcgBufs {
-    uint16_t *code;
-    void *v[6];
-};
-
-static bool pcg_alloc(World &w, bool fp32) {
-    size_t es = fp32 ? sizeof(float) : sizeof(double);
-    size_t vec = ((w.nn * es + 255) / 256) * 256;
-    size_t need = 6 * vec + ((w.nn * sizeof(uint16_t) + 255) / 256) * 256;
-    if (w.pcg_bytes < need) {
-        if (w.pcg_buf) cudaFree(w.pcg_buf);
-        w.pcg_buf = nullptr;
-        w.pcg_bytes = 0;
-        if (cudaMalloc(&w.pcg_buf, need) != cudaSuccess) return false;
-        w.pcg_bytes = need;
-        w.pcg_codes_valid = false;
+/* Galerkin coarse operator of level l+1 from level l (deterministic gather:
+ * one thread per coarse node, children and their links in a fixed order).
+ * Level 0 is the node grid with the operator L (Dirichlet links kept on the
+ * diagonal); the Boltzmann diagonal term is left to the fine smoother. */
+template <typename T>
+__global__ void k_mg_setup(Geo g, const uint16_t *__restrict__ code, MgLevel<T> Lf, MgLevel<T> C, int from_fine) {
+    int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= C.n) return;
+    int ci = (int)(I % C.nx);
+    int cj = (int)((I / C.nx) % C.ny);
+    int ck = (int)(I / ((int64_t)C.nx * C.ny));
+    const double cd[3] = {1.0 / (g.dh[0] * g.dh[0]), 1.0 / (g.dh[1] * g.dh[1]), 1.0 / (g.dh[2] * g.dh[2])};
+    double diag = 0, w[6] = {0, 0, 0, 0, 0, 0};
+    int nx = from_fine ? g.ni : Lf.nx, ny = from_fine ? g.nj : Lf.ny, nz = from_fine ? g.nk : Lf.nz;
+    int64_t offs[6] = {-1, 1, -(int64_t)nx, nx, -(int64_t)nx * ny, (int64_t)nx * ny};
+    const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
+    for (int d = 0; d < 8; d++) {
+        int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+        if (i >= nx || j >= ny || k >= nz) continue;
+        int64_t u = ((int64_t)k * ny + j) * nx + i;
+        if (from_fine) {
+            uint16_t c = code[u];
+            if (!(c & SELF)) continue;
+            for (int m = 0; m < 6; m++)
+                if (c & ((1u << m) | (1u << (6 + m)))) diag += cd[m >> 1];
+            for (int m = 0; m < 6; m++) {
+                if (!(c & (1u << m))) continue;
+                bool inside = ((i + di[m]) >> 1) == ci && ((j + dj[m]) >> 1) == cj && ((k + dk[m]) >> 1) == ck;
+                if (inside)
+                    diag -= cd[m >> 1];
+                else
+                    w[m] += cd[m >> 1];
+            }
+        } else {
+            double dd = (double)Lf.diag[u];
+            if (dd == 0) continue;
+            diag += dd;
+            for (int m = 0; m < 6; m++) {
+                double wm = (double)Lf.w[m * Lf.n + u];
+                if (wm == 0) continue;
+                bool inside = ((i + di[m]) >> 1) == ci && ((j + dj[m]) >> 1) == cj && ((k + dk[m]) >> 1) == ck;
+                if (inside)
+                    diag -= wm;
+                else
+                    w[m] += wm;
+            }
+        }
+        (void)offs;
     }
-    return true;
+    C.diag[I] = (T)diag;
+    for (int m = 0; m < 6; m++) C.w[m * C.n + I] = (T)w[m];
 }
 
-int launch_newton_pcg(World &w, bool fp32) {
-    if (!pcg_alloc(w, fp32)) return (int)cudaErrorMemoryAllocation;
-    size_t es = fp32 ? sizeof(float) : sizeof(double);
+/* ======================================================================== */
+template <typename T>
+static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
+    size_t off = 0;
+    int nx = (w.g.ni + 1) / 2, ny = (w.g.nj + 1) / 2, nz = (w.g.nk + 1) / 2;
+    int nlev = 0, grid_levels = 1;
+    while (nlev < MG_MAX) {
+        MgLevel<T> &L = A.L[nlev];
+        L.nx = nx;
+        L.ny = ny;
+        L.nz = nz;
+        L.pad = 0;
+        L.n = (int64_t)nx * ny * nz;
+        size_t bytes = ((L.n * sizeof(T) + 255) / 256) * 256;
+        L.diag = (T *)(base ? base + off : nullptr);
+        off += bytes;
+        L.w = (T *)(base ? base + off : nullptr);
+        off += 6 * bytes;
+        L.b = (T *)(base ? base + off : nullptr);
+        off += bytes;
+        L.e = (T *)(base ? base + off : nullptr);
+        off += bytes;
+        nlev++;
+        if (L.n >= 32768) grid_levels = nlev + 1;
+        if (L.n <= 64 || (nx <= 2 && ny <= 2 && nz <= 2)) break;
+        nx = (nx + 1) / 2;
+        ny = (ny + 1) / 2;
+        nz = (nz + 1) / 2;
+    }
+    A.nlev = w.mg_levels_max < nlev ? w.mg_levels_max : nlev;
+    A.grid_levels = grid_levels;
+    A.nu_coarse = 2;
+    A.scale = (T)w.mg_scale;
+    return off;
+}
+
+template <typename T>
+static int run_pcg(World &w) {
+    size_t es = sizeof(T);
     size_t vec = ((w.nn * es + 255) / 256) * 256;
+    size_t codeb = ((w.nn * sizeof(uint16_t) + 255) / 256) * 256;
+    MgArgs<T> A;
+    size_t mgb = mg_layout<T>(w, A, nullptr);
+    size_t need = 7 * vec + codeb + mgb;
+    if (w.pcg_bytes < need || w.pcg_elem != (int)es) {
+        if (w.pcg_buf) {
+            cudaStreamSynchronize(w.stream);
+            cudaFree(w.pcg_buf);
+        }
+        w.pcg_buf = nullptr;
+        w.pcg_bytes = 0;
+        if (cudaMalloc(&w.pcg_buf, need) != cudaSuccess) return (int)cudaErrorMemoryAllocation;
+        cudaMemsetAsync(w.pcg_buf, 0, need, w.stream);
+        w.pcg_bytes = need;
+        w.pcg_elem = (int)es;
+        w.pcg_codes_valid = false;
+    }
     char *base = (char *)w.pcg_buf;
-    uint16_t *code = (uint16_t *)(base + 6 * vec);
+    uint16_t *code = (uint16_t *)(base + 7 * vec);
+    mg_layout<T>(w, A, base + 7 * vec + codeb);
     if (!w.pcg_codes_valid) {
         k_pcg_codes<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.obj, code);
         w.nlaunch++;
+        for (int l = 0; l < A.nlev; l++) {
+            MgLevel<T> prev = l ? A.L[l - 1] : A.L[0];
+            k_mg_setup<T><<<blocks_for(A.L[l].n, 256), 256, 0, w.stream>>>(w.g, code, prev, A.L[l], l == 0);
+            w.nlaunch++;
+        }
         w.pcg_codes_valid = true;
     }
-    const void *fn = fp32 ? (const void *)k_newton_pcg<float> : (const void *)k_newton_pcg<double>;
+    const void *fn = (const void *)k_newton_pcg<T>;
+    const int threads = 1024;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
     if (per_sm < 1) per_sm = 1;
     int64_t maxb = (int64_t)per_sm * w.sm_count;
-    int64_t need = (w.nn + 255) / 256;
-    int grid = (int)(need < maxb ? need : maxb);
+    int64_t needb = (w.nn + threads - 1) / threads;
+    int grid = (int)(needb < maxb ? needb : maxb);
     if (grid > w.partial_slots / 4) grid = w.partial_slots / 4;
+    if (w.solver_blocks > 0 && grid > w.solver_blocks) grid = w.solver_blocks;
     Geo g = w.g;
     double *phi = w.phi;
     const double *rho = w.rho;
@@ -270,15 +728,17 @@ int launch_newton_pcg(World &w, bool fp32) {
     const uint16_t *cc = code;
     double phi0 = w.phi0, te0 = w.te0, n0 = w.n0, nr_tol = w.nr_tol, pcg_tol = w.pcg_tol;
     int nr_max = w.nr_max, pcg_max = w.pcg_max;
-    void *v[6];
-    for (int i = 0; i < 6; i++) v[i] = base + i * vec;
+    T *v[7];
+    for (int i = 0; i < 7; i++) v[i] = (T *)(base + i * vec);
     double *part = w.d_partials;
     SolveStatus *st = w.d_status;
     int *err = w.d_err;
-    void *args[] = {&g,      &phi,     &rho,  &cc,   &tg,   &phi0, &te0,  &n0,   &nr_max, &nr_tol, &pcg_max,
-                    &pcg_tol, &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &part, &st,    &err};
+    void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,   &nr_max, &nr_tol, &pcg_max, &pcg_tol,
+                    &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,   &part, &st,     &err};
     w.nlaunch++;
-    return (int)cudaLaunchCooperativeKernel(fn, grid, 256, args, 0, w.stream);
+    return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, 0, w.stream);
 }
+
+int launch_newton_pcg(World &w, bool fp32) { return fp32 ? run_pcg<float>(w) : run_pcg<double>(w); }
 
 }  // namespace espic

@@ -181,7 +181,7 @@ def test_sphere_push_absorb_and_compaction(espic, po):
             w.write(espic.FIELD_PHI, f["phi"])
             espic.PotentialSolver(w).computeEF()
             s = espic.Species(w, "O+", 16 * AMU, QE, mpw0=50.0, capacity=4096, form=form,
-                              walls=espic.WALLS_ABSORB)
+                              walls=espic.WALLS_ABSORB, weight_bound=100.0)
             s.set_particles(f["P"])
             s.advance()
             P = s.particles()
@@ -262,7 +262,9 @@ def test_nonlinear_gs_redblack(espic, po):
 
 
 @pytest.mark.parametrize("fp32", [False, True])
-def test_newton_pcg(espic, po, fp32):
+@pytest.mark.parametrize("levels", [0, 12])
+def test_newton_pcg(espic, po, fp32, levels):
+    """Newton-PCG with the Jacobi (levels=0) or multigrid preconditioner."""
     f = golden("sphere_solve")
     phi0, te0, n0 = f["ref"]
     with world(espic, SPH) as w:
@@ -271,10 +273,13 @@ def test_newton_pcg(espic, po, fp32):
         sol.setReferenceValues(phi0, te0, n0)
         sol.setNewton(nr_max=50, nr_tol=1e-10, pcg_max=20000, pcg_tol=1e-5 if fp32 else 1e-12,
                       fp32_inner=fp32)
+        sol.setMultigrid(levels)
         conv, nr, inner, norm = sol.solve()
         assert conv, (nr, inner, norm)
         # phi relative error against the reference's converged solveGS
         assert rel(w.phi, f["phi_tight"]) <= (1e-6 if fp32 else 1e-8)
+        if levels:
+            assert inner < 40 * nr, (nr, inner)
 
 
 def test_qn(espic, po):
