@@ -24,6 +24,7 @@ UNITS = {
     "k_fp64.cu": ["-fmad=false"],
     "k_mixed.cu": [],
     "k_pcg.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

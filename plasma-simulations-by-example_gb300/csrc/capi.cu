@@ -56,6 +56,10 @@ static int fail(int code, const char *fmt, ...) {
         return fail(ESPIC_ERR_ARG, "species id %d out of range", (int)(sp));         \
     Species &s = *w.species[(sp)]
 
+/* lets other translation units of the library report errors through
+ * espic_last_error */
+int espic_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
 extern "C" int espic_last_error(char *buf, int len) {
     if (!buf || len <= 0) return ESPIC_ERR_ARG;
     snprintf(buf, (size_t)len, "%s", g_last_error.c_str());
