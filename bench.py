@@ -290,6 +290,34 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def ncu_case(args):
+    """The workload's state, then exactly one k_push_mixed (push + deposit)
+    and one k_newton_pcg<float> launch: the case profiled with
+    ncu -k regex:"k_push_mixed|k_newton_pcg" -c 2."""
+    E = espic_module()
+    if not os.path.exists(E.LIB_PATH):
+        E.build()
+    cfg = CONFIGS[args.config]
+    P0 = synthetic_state(cfg, cfg["np"], 1)
+    ni, nj, nk = cfg["n"]
+    w = E.World(ni, nj, nk, cfg["x0"], cfg["xm"])
+    w.setTime(cfg["dt"], 100)
+    w.addSphere(cfg["center"], cfg["radius"], cfg["phi_s"])
+    w.addInlet()
+    s = E.Species(w, "O+", 16 * AMU, QE, mpw0=cfg["mpw0"], capacity=int(P0.shape[1] * 1.5),
+                  form=E.FORM_MIXED, walls=E.WALLS_ABSORB)
+    sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
+    sol.setReferenceValues(PHI0, TE, N0)
+    sol.setNewton(nr_max=20, nr_tol=NR_TOL, pcg_max=20000, pcg_tol=PCG_TOL, fp32_inner=True)
+    s.set_particles(P0)
+    s.sort()
+    sol.computeEF()
+    s.advance(deposit=True)
+    w.computeChargeDensity()
+    print(json.dumps({"ncu_case": args.config, "solve": sol.solve(), "particles": s.getNp()}))
+    w.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -299,6 +327,8 @@ def main():
     ap.add_argument("--config", default="sphere64", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain form")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="one push + one solve of the workload (mixed form), for an ncu capture")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -306,6 +336,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
+        return
+    if args.ncu_case:
+        ncu_case(args)
         return
 
     import torch

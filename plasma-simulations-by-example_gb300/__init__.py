@@ -48,6 +48,23 @@ def build(force=False):
     return mod.build(force=force)
 
 
+def _build_module():
+    from importlib import util
+    spec = util.spec_from_file_location("_espic_build", os.path.join(PKG_DIR, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def build_shim(force=False):
+    """libespic_shim.a: the drop-in World/Species/PotentialSolver classes."""
+    return _build_module().build_shim(force=force)
+
+
+def compile_drop_in(main_source, out, stdin_source=False):
+    return _build_module().compile_drop_in(main_source, out, stdin_source)
+
+
 def lib():
     """The loaded libespic.so (raises if it has not been built)."""
     global _lib

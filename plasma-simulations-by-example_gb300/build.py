@@ -86,5 +86,45 @@ def build(force=False, verbose=False, extra=()):
     return LIB
 
 
+SHIM = os.path.join(PKG, "shim")
+SHIM_LIB = os.path.join(OUT, "libespic_shim.a")
+
+
+def build_shim(force=False):
+    """The drop-in C++ classes (shim/espic_shim.cpp) as a static archive:
+    link a reference Main.cpp with -lespic_shim -lespic."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(SHIM, "espic_shim.cpp")
+    obj = os.path.join(OUT, "espic_shim.o")
+    deps = [src, __file__, os.path.join(ROOT, "include", "espic.h")] + [
+        os.path.join(SHIM, f) for f in os.listdir(SHIM) if f.endswith(".h")]
+    if force or _stale(SHIM_LIB, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", src, "-o", obj, "-I", SHIM,
+               "-I", os.path.join(ROOT, "include")]
+        subprocess.check_call(cmd)
+        if os.path.exists(SHIM_LIB):
+            os.remove(SHIM_LIB)
+        subprocess.check_call(["ar", "rcs", SHIM_LIB, obj])
+    return SHIM_LIB
+
+
+def compile_drop_in(main_source, out, stdin_source=False):
+    """Compile a program written against the reference's headers (World.h,
+    Species.h, ...) with the drop-in headers and link libespic.  With
+    stdin_source the file is fed on stdin from an empty directory, so that
+    its own directory's headers are not found first."""
+    build(False)
+    build_shim(False)
+    cmd = ["g++", "-O2", "-std=c++17", "-x", "c++", "-I", SHIM, "-I", os.path.join(ROOT, "include")]
+    cmd += ["-"] if stdin_source else [main_source]
+    cmd += ["-x", "none", SHIM_LIB, "-L", OUT, "-lespic", "-Wl,-rpath," + OUT, "-o", out]
+    if stdin_source:
+        import tempfile
+        with tempfile.TemporaryDirectory() as td, open(main_source) as f:
+            return subprocess.run(cmd, stdin=f, cwd=td, capture_output=True, text=True)
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_shim(force="--force" in sys.argv))

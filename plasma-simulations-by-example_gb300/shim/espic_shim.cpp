@@ -1,0 +1,544 @@
+/*
+ * espic_shim.cpp -- the drop-in World / Species / PotentialSolver / sources /
+ * Output classes, implemented on the libespic C-ABI (include/espic.h).
+ * Compile the reference's unchanged Main.cpp against the headers of this
+ * directory, add this file, and link -lespic.
+ *
+ * Environment knobs (no reference counterpart): ESPIC_CAPACITY (particles
+ * per species kept on the GPU, default 16M), ESPIC_FORM=mixed (store
+ * species with a default weight in the mixed form), ESPIC_SEED (Philox key).
+ */
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+
+#include "Output.h"
+#include "PotentialSolver.h"
+#include "Source.h"
+#include "Species.h"
+#include "World.h"
+#include "espic.h"
+
+Rnd rnd;
+
+static void ck(int rc, const char *what) {
+    if (rc >= 0) return;
+    char msg[512];
+    espic_last_error(msg, sizeof msg);
+    throw std::runtime_error(std::string(what) + ": " + msg);
+}
+
+static int64_t env_int(const char *name, int64_t def) {
+    const char *v = getenv(name);
+    return v && *v ? atoll(v) : def;
+}
+
+/* ------------------------------------------------------------------ World */
+World::World(int ni, int nj, int nk)
+    : ni{ni}, nj{nj}, nk{nk}, nn{ni, nj, nk}, phi(ni, nj, nk), rho(ni, nj, nk), node_vol(ni, nj, nk),
+      ef(ni, nj, nk), object_id(ni, nj, nk) {
+    time_start = std::chrono::high_resolution_clock::now();
+}
+
+World::~World() {
+    if (h) espic_world_destroy(h);
+}
+
+void World::setExtents(const double3 _x0, const double3 _xm) {
+    x0 = _x0;
+    xm = _xm;
+    for (int i = 0; i < 3; i++) dh[i] = (xm(i) - x0(i)) / (nn(i) - 1);
+    xc = 0.5 * (x0 + xm);
+    if (h) {
+        espic_world_destroy(h);
+        h = nullptr;
+    }
+    double a[3] = {x0(0), x0(1), x0(2)}, b[3] = {xm(0), xm(1), xm(2)};
+    ck(espic_world_create(ni, nj, nk, a, b, &h), "espic_world_create");
+    int64_t seed = env_int("ESPIC_SEED", 0);
+    if (seed) espic_world_set_seed(h, (uint64_t)seed);
+    if (dt > 0) espic_world_set_time(h, dt, num_ts);
+    bind_fields();
+    fields_written(1 | 2 | 4 | 8 | 16);
+}
+
+void World::bind_fields() {
+    espic_world *hh = h;
+    int64_t n = (int64_t)ni * nj * nk;
+    auto bind_d = [hh, n](Field &f, int id) {
+        f.bind([hh, n, id](void *dst) { ck(espic_field_read(hh, id, 0, (double *)dst, n), "espic_field_read"); },
+               [hh, n, id](const void *src) {
+                   ck(espic_field_write(hh, id, 0, (const double *)src, n), "espic_field_write");
+               });
+    };
+    bind_d(phi, ESPIC_FIELD_PHI);
+    bind_d(rho, ESPIC_FIELD_RHO);
+    bind_d(node_vol, ESPIC_FIELD_NODE_VOL);
+    ef.bind([hh, n](void *dst) { ck(espic_field_read(hh, ESPIC_FIELD_EF, 0, (double *)dst, 3 * n), "read ef"); },
+            [hh, n](const void *src) {
+                ck(espic_field_write(hh, ESPIC_FIELD_EF, 0, (const double *)src, 3 * n), "write ef");
+            });
+    object_id.bind(
+        [hh, n](void *dst) {
+            std::vector<double> tmp(n);
+            ck(espic_field_read(hh, ESPIC_FIELD_OBJECT_ID, 0, tmp.data(), n), "read object_id");
+            int *o = (int *)dst;
+            for (int64_t u = 0; u < n; u++) o[u] = (int)tmp[u];
+        },
+        [hh, n](const void *src) {
+            std::vector<double> tmp(n);
+            const int *o = (const int *)src;
+            for (int64_t u = 0; u < n; u++) tmp[u] = o[u];
+            ck(espic_field_write(hh, ESPIC_FIELD_OBJECT_ID, 0, tmp.data(), n), "write object_id");
+        });
+}
+
+void World::push_host_edits() {
+    phi.push();
+    rho.push();
+    node_vol.push();
+    ef.push();
+    object_id.push();
+}
+
+void World::fields_written(int mask) {
+    if (mask & 1) phi.device_written();
+    if (mask & 2) rho.device_written();
+    if (mask & 4) ef.device_written();
+    if (mask & 8) object_id.device_written();
+    if (mask & 16) node_vol.device_written();
+}
+
+double World::getWallTime() {
+    auto now = std::chrono::high_resolution_clock::now();
+    std::chrono::duration<double> d = now - time_start;
+    return d.count();
+}
+
+void World::setTime(double dt_, int num_ts_) {
+    dt = dt_;
+    num_ts = num_ts_;
+    if (h) ck(espic_world_set_time(h, dt, num_ts), "espic_world_set_time");
+}
+
+bool World::advanceTime() {
+    time += dt;
+    ts++;
+    if (h) espic_world_advance_time(h);
+    return ts <= num_ts;
+}
+
+void World::computeChargeDensity(std::vector<Species> &species) {
+    for (Species &sp : species) {
+        sp.settle();
+        sp.den.push();
+    }
+    push_host_edits();
+    ck(espic_charge_density(h), "espic_charge_density");
+    fields_written(2);
+}
+
+double World::getPE() {
+    push_host_edits();
+    double pe = 0;
+    ck(espic_potential_energy(h, &pe), "espic_potential_energy");
+    return pe;
+}
+
+void World::addSphere(double3 c, double radius, double phi_sphere) {
+    sphere_x0 = c;
+    sphere_rad2 = radius * radius;
+    push_host_edits();
+    double cc[3] = {c(0), c(1), c(2)};
+    ck(espic_world_add_sphere(h, cc, radius, phi_sphere), "espic_world_add_sphere");
+    fields_written(1 | 8);
+}
+
+bool World::inSphere(double3 x) {
+    double3 r = x - sphere_x0;
+    double r_mag2 = (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    return r_mag2 <= sphere_rad2;
+}
+
+void World::addInlet() {
+    push_host_edits();
+    ck(espic_world_add_inlet(h), "espic_world_add_inlet");
+    fields_written(1 | 8);
+}
+
+/* World::steadyState, ch3/ver2/World.cpp:129-158 */
+bool World::steadyState(std::vector<Species> &species) {
+    if (steady_state) return true;
+    double tot_mass = 0, tot_mom = 0, tot_en = getPE();
+    for (Species &sp : species) {
+        tot_mass += sp.getRealCount();
+        double3 mom = sp.getMomentum();
+        tot_mom += std::abs(mom[2]);
+        tot_en += sp.getKE();
+    }
+    const double tol = 1e-3;
+    if (std::abs((tot_mass - last_mass) / tot_mass) < tol && std::abs((tot_mom - last_mom) / tot_mom) < tol &&
+        std::abs((tot_en - last_en) / tot_en) < tol) {
+        steady_state = true;
+        std::cout << "Steady state reached at time step " << ts << std::endl;
+    }
+    last_mass = tot_mass;
+    last_mom = tot_mom;
+    last_en = tot_en;
+    return steady_state;
+}
+
+/* ---------------------------------------------------------------- Species */
+std::vector<Particle> &ParticleVector::host() {
+    if (!host_valid) {
+        owner->pull_particles(v);
+        host_valid = true;
+        host_dirty = false;
+    }
+    return v;
+}
+
+Species::Species(std::string name, double mass, double charge, World &world)
+    : name(name), mass(mass), charge(charge), mpw0(0), den(world.ni, world.nj, world.nk),
+      den_ave(world.ni, world.nj, world.nk), world(world) {
+    create(ESPIC_WALLS_REFLECT);
+}
+
+Species::Species(std::string name, double mass, double charge, double mpw0, World &world)
+    : name(name), mass(mass), charge(charge), mpw0(mpw0), den(world.ni, world.nj, world.nk),
+      den_ave(world.ni, world.nj, world.nk), world(world) {
+    create(ESPIC_WALLS_ABSORB);
+}
+
+Species::Species(Species &&o) noexcept
+    : name(o.name), mass(o.mass), charge(o.charge), mpw0(o.mpw0), particles(std::move(o.particles)),
+      den(std::move(o.den)), den_ave(std::move(o.den_ave)), world(o.world), sid(o.sid),
+      push_pending(o.push_pending), diag_valid(o.diag_valid) {
+    particles.owner = this;
+    memcpy(diag, o.diag, sizeof diag);
+    o.sid = -1;
+}
+
+void Species::create(int walls) {
+    if (!world.handle()) throw std::runtime_error("Species: call World::setExtents first");
+    int64_t cap = env_int("ESPIC_CAPACITY", 16 << 20);
+    const char *f = getenv("ESPIC_FORM");
+    int form = (f && !strcmp(f, "mixed") && mpw0 > 0) ? ESPIC_FORM_MIXED : ESPIC_FORM_FP64;
+    ck(espic_species_create(world.handle(), mass, charge, mpw0, cap, form, walls, 0.0, &sid),
+       "espic_species_create");
+    particles.owner = this;
+    particles.host_valid = true;
+    bind_fields();
+}
+
+void Species::bind_fields() {
+    espic_world *hh = world.handle();
+    int64_t n = (int64_t)world.ni * world.nj * world.nk;
+    int s = sid;
+    den.bind([hh, n, s](void *d) { ck(espic_field_read(hh, ESPIC_FIELD_DEN, s, (double *)d, n), "read den"); },
+             [hh, n, s](const void *d) {
+                 ck(espic_field_write(hh, ESPIC_FIELD_DEN, s, (const double *)d, n), "write den");
+             });
+    den_ave.bind(
+        [hh, n, s](void *d) { ck(espic_field_read(hh, ESPIC_FIELD_DEN_AVE, s, (double *)d, n), "read den_ave"); },
+        [hh, n, s](const void *d) {
+            ck(espic_field_write(hh, ESPIC_FIELD_DEN_AVE, s, (const double *)d, n), "write den_ave");
+        });
+}
+
+/* run a pending push and send host edits of the particle mirror */
+void Species::settle() {
+    espic_world *hh = world.handle();
+    if (push_pending) {
+        world.push_host_edits();
+        ck(espic_push(hh, sid, 0), "espic_push");
+        push_pending = false;
+        particles.host_valid = false;
+        diag_valid = false;
+    }
+    if (particles.host_dirty) {
+        std::vector<Particle> &v = particles.v;
+        int64_t n = (int64_t)v.size();
+        std::vector<double> P(7 * (n > 0 ? n : 1));
+        for (int64_t p = 0; p < n; p++) {
+            for (int d = 0; d < 3; d++) {
+                P[d * n + p] = v[p].pos[d];
+                P[(3 + d) * n + p] = v[p].vel[d];
+            }
+            P[6 * n + p] = v[p].mpw;
+        }
+        ck(espic_species_set(hh, sid, P.data(), n, n), "espic_species_set");
+        particles.host_dirty = false;
+        diag_valid = false;
+    }
+}
+
+void Species::pull_particles(std::vector<Particle> &out) {
+    if (push_pending) settle();
+    int64_t n = 0;
+    ck(espic_species_count(world.handle(), sid, &n), "espic_species_count");
+    std::vector<double> P(7 * (n > 0 ? n : 1));
+    ck(espic_species_get(world.handle(), sid, P.data(), n, n, &n), "espic_species_get");
+    out.clear();
+    out.reserve(n);
+    for (int64_t p = 0; p < n; p++)
+        out.emplace_back(double3(P[p], P[n + p], P[2 * n + p]), double3(P[3 * n + p], P[4 * n + p], P[5 * n + p]),
+                         P[6 * n + p]);
+}
+
+size_t Species::getNp() {
+    settle();
+    int64_t n = 0;
+    ck(espic_species_count(world.handle(), sid, &n), "espic_species_count");
+    return (size_t)n;
+}
+
+void Species::refresh_diag() {
+    settle();
+    if (!diag_valid) {
+        ck(espic_species_diag(world.handle(), sid, diag), "espic_species_diag");
+        diag_valid = true;
+    }
+}
+
+double Species::getRealCount() {
+    refresh_diag();
+    return diag[0];
+}
+
+double3 Species::getMomentum() {
+    refresh_diag();
+    return double3(diag[1], diag[2], diag[3]);
+}
+
+double Species::getKE() {
+    refresh_diag();
+    return diag[4];
+}
+
+void Species::advance() {
+    settle();
+    push_pending = true; /* fused with the next computeNumberDensity */
+    particles.host_valid = false;
+    diag_valid = false;
+}
+
+void Species::computeNumberDensity() {
+    espic_world *hh = world.handle();
+    den.push();
+    if (push_pending) {
+        world.push_host_edits();
+        ck(espic_push(hh, sid, 1), "espic_push");
+        push_pending = false;
+    } else {
+        settle();
+        ck(espic_deposit(hh, sid), "espic_deposit");
+    }
+    den.device_written();
+}
+
+void Species::addParticle(double3 pos, double3 vel, double mpwt) {
+    settle();
+    world.push_host_edits();
+    double p[3] = {pos[0], pos[1], pos[2]}, v[3] = {vel[0], vel[1], vel[2]};
+    ck(espic_species_add(world.handle(), sid, p, v, &mpwt, 1), "espic_species_add");
+    particles.host_valid = false;
+    diag_valid = false;
+}
+
+void Species::loadParticlesBox(double3 x1, double3 x2, double num_den, int num_mp) {
+    settle();
+    world.push_host_edits();
+    double a[3] = {x1[0], x1[1], x1[2]}, b[3] = {x2[0], x2[1], x2[2]};
+    ck(espic_species_load_box(world.handle(), sid, a, b, num_den, num_mp, nullptr), "espic_species_load_box");
+    particles.host_valid = false;
+    diag_valid = false;
+}
+
+void Species::loadParticlesBoxQS(double3 x1, double3 x2, double num_den, int3 num_mp) {
+    settle();
+    world.push_host_edits();
+    double a[3] = {x1[0], x1[1], x1[2]}, b[3] = {x2[0], x2[1], x2[2]};
+    int nm[3] = {num_mp[0], num_mp[1], num_mp[2]};
+    ck(espic_species_load_box_qs(world.handle(), sid, a, b, num_den, nm), "espic_species_load_box_qs");
+    particles.host_valid = false;
+    diag_valid = false;
+}
+
+void Species::updateAverages() {
+    den.push();
+    den_ave.push();
+    ck(espic_update_average(world.handle(), sid), "espic_update_average");
+    den_ave.device_written();
+}
+
+/* Species::sampleVth / sampleIsotropicVel, ch4/Species.cpp:149-175 (host) */
+double Species::sampleVth(double T) {
+    double v_th = sqrt(2 * Const::K * T / mass);
+    double v1 = v_th * (rnd() + rnd() + rnd() - 1.5);
+    double v2 = v_th * (rnd() + rnd() + rnd() - 1.5);
+    double v3 = v_th * (rnd() + rnd() + rnd() - 1.5);
+    return 3 / sqrt(2 + 2 + 2) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+}
+
+double3 Species::sampleIsotropicVel(double T) {
+    double theta = 2 * Const::PI * rnd();
+    double r = -1.0 + 2 * rnd();
+    double a = sqrt(1 - r * r);
+    double3 d;
+    d[0] = r;
+    d[1] = cos(theta) * a;
+    d[2] = sin(theta) * a;
+    double v_th = sampleVth(T);
+    return v_th * d;
+}
+
+/* ---------------------------------------------------------- PotentialSolver */
+PotentialSolver::PotentialSolver(World &world, int max_it, double tol)
+    : world(world), kind(ESPIC_SOLVER_SOR), max_solver_it(max_it), tolerance(tol) {}
+
+PotentialSolver::PotentialSolver(World &world, SolverType type, int max_it, double tol)
+    : world(world), kind(ESPIC_SOLVER_GS), max_solver_it(max_it), tolerance(tol) {
+    switch (type) {
+        case GS:
+        case GSCUDA: kind = ESPIC_SOLVER_GS; break;
+        case PCG: kind = ESPIC_SOLVER_PCG; break;
+        case QN: kind = ESPIC_SOLVER_QN; break;
+    }
+    buildMatrix();
+}
+
+void PotentialSolver::configure() {
+    espic_world *h = world.handle();
+    ck(espic_solver_set(h, kind, (int)max_solver_it, tolerance), "espic_solver_set");
+    ck(espic_solver_set_reference(h, phi0, Te0, n0), "espic_solver_set_reference");
+    if (kind == ESPIC_SOLVER_PCG)
+        ck(espic_solver_set_newton(h, 20, 1e-3, (int)max_solver_it, 1e-6, 0), "espic_solver_set_newton");
+}
+
+/* the matrix is applied matrix-free on the GPU; like the reference's
+ * buildMatrix (ch3/ver2/PotentialSolver.cpp:146-201) this ends in solveQN */
+void PotentialSolver::buildMatrix() {
+    int keep = kind;
+    kind = ESPIC_SOLVER_QN;
+    solve();
+    kind = keep;
+}
+
+bool PotentialSolver::solve() {
+    world.push_host_edits();
+    configure();
+    int it = 0, inner = 0;
+    double res = 0;
+    int rc = espic_solve(world.handle(), &it, &inner, &res);
+    ck(rc, "espic_solve");
+    world.fields_written(1);
+    if (rc == ESPIC_NOT_CONVERGED) {
+        if (kind == ESPIC_SOLVER_PCG)
+            std::cout << "NR+PCG failed to converge, norm = " << res << std::endl;
+        else
+            std::cerr << "GS failed to converge, L2=" << res << std::endl;
+    }
+    return rc == ESPIC_OK;
+}
+
+void PotentialSolver::computeEF() {
+    world.push_host_edits();
+    ck(espic_efield(world.handle()), "espic_efield");
+    world.fields_written(4);
+}
+
+/* ------------------------------------------------------------------ sources */
+static void sample_source(World &world, Species &sp, int &src, double v_drift, double den, double T) {
+    if (src < 0) ck(espic_source_create(world.handle(), sp.id(), v_drift, den, T, &src), "espic_source_create");
+    sp.settle();
+    world.push_host_edits();
+    ck(espic_source_sample(world.handle(), src), "espic_source_sample");
+    sp.particles.host_valid = false;
+    sp.particles.host_dirty = false;
+}
+
+void ColdBeamSource::sample() { sample_source(world, sp, src, v_drift, den, 0.0); }
+
+void WarmBeamSource::sample() { sample_source(world, sp, src, v_drift, den, T); }
+
+/* ------------------------------------------------------------------ Output */
+namespace Output {
+std::ofstream f_diag;
+}
+
+/* Output::fields, ch3/ver2/Output.cpp:12-79: VTK ImageData, ASCII */
+void Output::fields(World &world, std::vector<Species> &species) {
+    std::stringstream name;
+    name << "results/fields_" << std::setfill('0') << std::setw(5) << world.getTs() << ".vti";
+    std::ofstream out(name.str());
+    if (!out.is_open()) {
+        std::cerr << "Could not open " << name.str() << std::endl;
+        return;
+    }
+    double3 x0 = world.getX0(), dh = world.getDh();
+    out << "<VTKFile type=\"ImageData\">\n";
+    out << "<ImageData Origin=\"" << x0[0] << " " << x0[1] << " " << x0[2] << "\" ";
+    out << "Spacing=\"" << dh[0] << " " << dh[1] << " " << dh[2] << "\" ";
+    out << "WholeExtent=\"0 " << world.ni - 1 << " 0 " << world.nj - 1 << " 0 " << world.nk - 1 << "\">\n";
+    out << "<PointData>\n";
+    auto array = [&out](const std::string &nm, int comps, const char *type) {
+        out << "<DataArray Name=\"" << nm << "\" NumberOfComponents=\"" << comps << "\" format=\"ascii\" type=\""
+            << type << "\">\n";
+    };
+    array("object_id", 1, "Int32");
+    out << world.object_id << "</DataArray>\n";
+    array("NodeVol", 1, "Float64");
+    out << world.node_vol << "</DataArray>\n";
+    array("phi", 1, "Float64");
+    out << world.phi << "</DataArray>\n";
+    array("rho", 1, "Float64");
+    out << world.rho << "</DataArray>\n";
+    for (Species &sp : species) {
+        array("nd." + sp.name, 1, "Float64");
+        out << sp.den << "</DataArray>\n";
+    }
+    for (Species &sp : species) {
+        array("nd-ave." + sp.name, 1, "Float64");
+        out << sp.den_ave << "</DataArray>\n";
+    }
+    array("ef", 3, "Float64");
+    out << world.ef << "</DataArray>\n";
+    out << "</PointData>\n</ImageData>\n</VTKFile>\n";
+}
+
+void Output::screenOutput(World &world, std::vector<Species> &species) {
+    std::cout << "ts: " << world.getTs();
+    for (Species &sp : species) std::cout << std::setprecision(3) << "\t " << sp.name << ":" << sp.getNp();
+    std::cout << std::endl;
+}
+
+/* Output::diagOutput, ch3/ver2/Output.cpp:96-132: runtime_diags.csv */
+void Output::diagOutput(World &world, std::vector<Species> &species) {
+    if (!f_diag.is_open()) {
+        f_diag.open("runtime_diags.csv");
+        f_diag << "ts,time,wall_time";
+        for (Species &sp : species)
+            f_diag << ",mp_count." << sp.name << ",real_count." << sp.name << ",px." << sp.name << ",py." << sp.name
+                   << ",pz." << sp.name << ",KE." << sp.name;
+        f_diag << ",PE,E_total" << std::endl;
+    }
+    f_diag << world.getTs() << "," << world.getTime() << "," << world.getWallTime();
+    double tot_KE = 0;
+    for (Species &sp : species) {
+        double KE = sp.getKE();
+        tot_KE += KE;
+        double3 mom = sp.getMomentum();
+        f_diag << "," << sp.getNp() << "," << sp.getRealCount() << "," << mom[0] << "," << mom[1] << "," << mom[2]
+               << "," << KE;
+    }
+    double PE = world.getPE();
+    f_diag << "," << PE << "," << (tot_KE + PE) << "\n";
+    if (world.getTs() % 25 == 0) f_diag.flush();
+}

@@ -1,0 +1,43 @@
+// A flow-past-a-sphere run written against the reference's class API
+// (World with addSphere/addInlet, Species with mpw0, ColdBeamSource,
+// PotentialSolver GS, steadyState, averages) built with the drop-in headers.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+#include "World.h"
+#include "Species.h"
+#include "PotentialSolver.h"
+#include "Source.h"
+
+int main(int argc, char **argv) {
+    int steps = argc > 1 ? atoi(argv[1]) : 10;
+    World world(21, 21, 41);
+    world.setExtents({-0.1, -0.1, 0}, {0.1, 0.1, 0.4});
+    world.setTime(1e-7, steps);
+    world.addSphere({0, 0, 0.15}, 0.05, -100);
+    world.addInlet();
+    std::vector<Species> species;
+    species.push_back(Species("O+", 16 * Const::AMU, Const::QE, 5e2, world));
+    std::vector<ColdBeamSource> sources;
+    sources.push_back(ColdBeamSource(species[0], world, 7000, 1e10));
+    PotentialSolver solver(world, SolverType::GS, 20000, 1e-4);
+    solver.setReferenceValues(0, 1.5, 1e10);
+    solver.solve();
+    solver.computeEF();
+    while (world.advanceTime()) {
+        for (ColdBeamSource &s : sources) s.sample();
+        for (Species &sp : species) {
+            sp.advance();
+            sp.computeNumberDensity();
+        }
+        world.computeChargeDensity(species);
+        solver.solve();
+        solver.computeEF();
+        if (world.steadyState(species))
+            for (Species &sp : species) sp.updateAverages();
+        printf("%d %zu %.17g %.17g %.17g\n", world.getTs(), species[0].getNp(), species[0].getRealCount(),
+               species[0].getKE(), world.getPE());
+    }
+    printf("obj %d phi %.17g\n", world.object_id(10, 10, 15), world.phi(10, 10, 15));
+    return 0;
+}
