@@ -312,6 +312,8 @@ __device__ __forceinline__ void move_particle(int64_t dst, int64_t src, double *
     }
 }
 
+/* one block per 1024-particle chunk of the tail [n_new, n_old), one thread
+ * per particle (warp w holds mask word w of the chunk) */
 template <int FORM>
 __global__ void __launch_bounds__(1024) k_movers(const int64_t *__restrict__ d_count,
                                                  const uint32_t *__restrict__ deadmask,
@@ -319,24 +321,36 @@ __global__ void __launch_bounds__(1024) k_movers(const int64_t *__restrict__ d_c
                                                  const int32_t *__restrict__ holes, double *P, int32_t *cell,
                                                  float *off, float *vel, int64_t stride, int rows) {
     __shared__ int32_t sh[32];
+    __shared__ int32_t wsum[32];
     int64_t n_old = d_count[1], n_new = d_count[0];
     if (n_old == n_new) return;
-    int64_t T0 = n_new / TILE_PARTICLES, T1 = (n_old - 1) / TILE_PARTICLES;
-    int64_t dead_at_new = -1;
-    for (int64_t T = T0 + blockIdx.x; T <= T1; T += gridDim.x) {
-        if (dead_at_new < 0) dead_at_new = dead_before(n_new, deadmask, tilepre, sh);
-        int64_t word = T * (TILE_PARTICLES / 32) + threadIdx.x;
+    const int64_t c0 = n_new >> 10, c1 = (n_old - 1) >> 10;
+    if (c0 + (int64_t)blockIdx.x > c1) return;
+    const int64_t dead_at_new = dead_before(n_new, deadmask, tilepre, sh);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t c = c0 + blockIdx.x; c <= c1; c += gridDim.x) {
+        /* dead particles in the chunk's tile before the chunk */
+        int64_t T = (c << 10) / TILE_PARTICLES;
+        int64_t wt0 = T * (TILE_PARTICLES / 32), wc0 = c * 32;
+        int64_t word_t = wt0 + threadIdx.x;
+        int32_t cnt = (word_t < wc0) ? __popc(deadmask[word_t]) : 0;
+        int32_t tot;
+        block_excl_scan(cnt, sh, &tot);
+        const int64_t dead_before_chunk = (int64_t)tilepre[T] + tot;
+        /* the chunk's words */
+        int64_t word = wc0 + warp;
         uint32_t m = (word * 32 < n_old) ? deadmask[word] : 0xffffffffu;
-        int32_t pre = block_excl_scan(__popc(m), sh, nullptr);
-        int64_t dead_before_word = tilepre[T] + pre;
-        for (int b = 0; b < 32; b++) {
-            int64_t q = word * 32 + b;
-            if (q < n_new || q >= n_old) continue;
-            if ((m >> b) & 1u) continue;
-            int64_t db = dead_before_word + __popc(m & ((1u << b) - 1u));
+        if (lane == 0) wsum[warp] = __popc(m);
+        __syncthreads();
+        int32_t wpre = 0;
+        for (int k = 0; k < warp; k++) wpre += wsum[k];
+        int64_t q = word * 32 + lane;
+        if (q >= n_new && q < n_old && !((m >> lane) & 1u)) {
+            int64_t db = dead_before_chunk + wpre + __popc(m & ((1u << lane) - 1u));
             int64_t rank = (q - n_new) - (db - dead_at_new);
             move_particle<FORM>(holes[rank], q, P, cell, off, vel, stride, rows);
         }
+        __syncthreads();
     }
 }
 
@@ -724,16 +738,22 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag_partials(const double *__r
     block_sum_store<5>(acc, partials + 5 * blockIdx.x);
 }
 
+/* final sums by one warp: lane l adds partials l, l+32, ... in order, then a
+ * fixed butterfly; the same bits on every run */
 __global__ void k_diag_final(const double *__restrict__ partials, double mass, double *out) {
-    if (threadIdx.x != 0) return;
+    int lane = threadIdx.x & 31;
     double s[5] = {0, 0, 0, 0, 0};
-    for (int b = 0; b < RED_BLOCKS; b++)
+    for (int b = lane; b < RED_BLOCKS; b += 32)
         for (int q = 0; q < 5; q++) s[q] += partials[5 * b + q];
-    out[0] = s[0];
-    out[1] = s[1] * mass;
-    out[2] = s[2] * mass;
-    out[3] = s[3] * mass;
-    out[4] = 0.5 * mass * s[4];
+    for (int q = 0; q < 5; q++)
+        for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+    if (threadIdx.x == 0) {
+        out[0] = s[0];
+        out[1] = s[1] * mass;
+        out[2] = s[2] * mass;
+        out[3] = s[3] * mass;
+        out[4] = 0.5 * mass * s[4];
+    }
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_pe_partials(int64_t nn, const double *__restrict__ ef,
@@ -748,10 +768,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_pe_partials(int64_t nn, const d
 }
 
 __global__ void k_pe_final(const double *__restrict__ partials, double *out) {
-    if (threadIdx.x != 0) return;
+    int lane = threadIdx.x & 31;
     double s = 0;
-    for (int b = 0; b < RED_BLOCKS; b++) s += partials[b];
-    out[0] = 0.5 * EPS_0 * s;
+    for (int b = lane; b < RED_BLOCKS; b += 32) s += partials[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[0] = 0.5 * EPS_0 * s;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1055,10 +1076,10 @@ void launch_compact(World &w, Species &s) {
     k_holes<<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes);
     int rows = s.uniform_w ? 6 : 7;
     if (s.form == 0)
-        k_movers<0><<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, s.P, nullptr, nullptr,
+        k_movers<0><<<g1 * 4, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, s.P, nullptr, nullptr,
                                                 nullptr, s.cap, rows);
     else
-        k_movers<1><<<g1, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, nullptr, s.cell, s.off,
+        k_movers<1><<<g1 * 4, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, nullptr, s.cell, s.off,
                                                 s.vel, s.cap, rows);
     w.nlaunch += 3;
 }

@@ -390,15 +390,19 @@ __global__ void __launch_bounds__(256) k_diag_mixed(const float *__restrict__ ve
 
 __global__ void k_diag_mixed_final(const double *__restrict__ partials, int nblocks, double mass, double w0,
                                    double *out) {
-    if (threadIdx.x != 0) return;
+    int lane = threadIdx.x & 31;
     double s[5] = {0, 0, 0, 0, 0};
-    for (int b = 0; b < nblocks; b++)
+    for (int b = lane; b < nblocks; b += 32)
         for (int q = 0; q < 5; q++) s[q] += partials[5 * b + q];
-    out[0] = s[0] * w0;
-    out[1] = s[1] * w0 * mass;
-    out[2] = s[2] * w0 * mass;
-    out[3] = s[3] * w0 * mass;
-    out[4] = 0.5 * mass * (w0 * s[4]);
+    for (int q = 0; q < 5; q++)
+        for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+    if (threadIdx.x == 0) {
+        out[0] = s[0] * w0;
+        out[1] = s[1] * w0 * mass;
+        out[2] = s[2] * w0 * mass;
+        out[3] = s[3] * w0 * mass;
+        out[4] = 0.5 * mass * (w0 * s[4]);
+    }
 }
 
 /* ======================================================================== */

@@ -42,7 +42,7 @@ namespace espic {
 #define PCG_EPS_0 8.85418782e-12
 #define PCG_QE 1.602176565e-19
 
-enum : uint16_t { SELF = 1u << 12 };
+enum : uint16_t { SELF = 1u << 12, BLACK = 1u << 13 };
 
 /* neighbour m: 0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z.  bit m: unknown; bit 6+m:
  * Dirichlet; SELF: the node is an unknown. */
@@ -55,6 +55,7 @@ __global__ void k_pcg_codes(Geo g, const int32_t *__restrict__ obj, uint16_t *co
     bool interior = i > 0 && j > 0 && k > 0 && i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1;
     if (interior && obj[u] == 0) {
         c |= SELF;
+        if ((i + j + k) & 1) c |= BLACK;
         int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
         int64_t nb[6] = {u - 1, u + 1, u - sy, u + sy, u - sz, u + sz};
         int ii[6] = {i - 1, i + 1, i, i, i, i}, jj[6] = {j, j, j - 1, j + 1, j, j},
@@ -137,7 +138,31 @@ struct Fine {
     T ct[3];
     int64_t off[6];
     T *dg, *r, *z;
+    const int32_t *list[2]; /* interior nodes of each colour (-1: padding) */
+    const int32_t *pk[2];   /* their coordinates, i | j<<10 | k<<20 */
+    int32_t nlist;          /* entries per list */
 };
+
+/* the interior nodes of colour c in a fixed order, with packed coordinates
+ * (built once per geometry so that the sweeps need no division) */
+__global__ void k_pcg_lists(Geo g, int c, int32_t *list, int32_t *pk) {
+    int hx = (g.ni - 1) / 2;
+    int64_t count = (int64_t)hx * (g.nj - 2) * (g.nk - 2);
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    int i2 = (int)(t % hx);
+    int64_t rr = t / hx;
+    int j = 1 + (int)(rr % (g.nj - 2));
+    int k = 1 + (int)(rr / (g.nj - 2));
+    int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
+    if (i > g.ni - 2) {
+        list[t] = -1;
+        pk[t] = 0;
+        return;
+    }
+    list[t] = (int32_t)(((int64_t)k * g.nj + j) * g.ni + i);
+    pk[t] = i | (j << 10) | (k << 20);
+}
 
 __device__ __forceinline__ void span(bool whole, int64_t &t0, int64_t &ts) {
     if (whole) {
@@ -169,20 +194,14 @@ __device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &
  * returns the local sum of r*z of the nodes it updated */
 template <typename T>
 __device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
-    const Geo &g = F.g;
-    int hx = (g.ni - 1) / 2;
-    int64_t count = (int64_t)hx * (g.nj - 2) * (g.nk - 2);
     int64_t t0, ts;
     span(true, t0, ts);
     T rz = 0;
-    for (int64_t t = t0; t < count; t += ts) {
-        int i2 = (int)(t % hx);
-        int64_t rr = t / hx;
-        int j = 1 + (int)(rr % (g.nj - 2));
-        int k = 1 + (int)(rr / (g.nj - 2));
-        int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
-        if (i > g.ni - 2) continue;
-        int64_t u = ((int64_t)k * g.nj + j) * g.ni + i;
+    const int32_t *list = F.list[c], *pk = F.pk[c];
+    for (int64_t t = t0; t < F.nlist; t += ts) {
+        int32_t uu = list[t];
+        if (uu < 0) continue;
+        int64_t u = uu;
         /* interior node: all six neighbours are in bounds, so their loads
          * are issued before the code word arrives; the code only selects */
         uint16_t cc = F.code[u];
@@ -193,20 +212,21 @@ __device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
         for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
         if (C) {
             const MgLevel<T> &Cc = *C;
-            int64_t I0 = ((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1);
-            int64_t Ix[2] = {((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ((i - 1) >> 1),
-                             ((int64_t)(k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ((i + 1) >> 1)};
-            int64_t Iy[2] = {((int64_t)(k >> 1) * Cc.ny + ((j - 1) >> 1)) * Cc.nx + (i >> 1),
-                             ((int64_t)(k >> 1) * Cc.ny + ((j + 1) >> 1)) * Cc.nx + (i >> 1)};
-            int64_t Iz[2] = {((int64_t)((k - 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1),
-                             ((int64_t)((k + 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1)};
-            (void)I0;
-            zn[0] += scale * Cc.e[Ix[0]];
-            zn[1] += scale * Cc.e[Ix[1]];
-            zn[2] += scale * Cc.e[Iy[0]];
-            zn[3] += scale * Cc.e[Iy[1]];
-            zn[4] += scale * Cc.e[Iz[0]];
-            zn[5] += scale * Cc.e[Iz[1]];
+            int32_t p = pk[t];
+            int i = p & 1023, j = (p >> 10) & 1023, k = p >> 20;
+            int32_t row = ((k >> 1) * Cc.ny + (j >> 1)) * Cc.nx;
+            int32_t ci = i >> 1;
+            int32_t Ix0 = row + ((i - 1) >> 1), Ix1 = row + ((i + 1) >> 1);
+            int32_t Iy0 = ((k >> 1) * Cc.ny + ((j - 1) >> 1)) * Cc.nx + ci;
+            int32_t Iy1 = ((k >> 1) * Cc.ny + ((j + 1) >> 1)) * Cc.nx + ci;
+            int32_t Iz0 = (((k - 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ci;
+            int32_t Iz1 = (((k + 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ci;
+            zn[0] += scale * Cc.e[Ix0];
+            zn[1] += scale * Cc.e[Ix1];
+            zn[2] += scale * Cc.e[Iy0];
+            zn[3] += scale * Cc.e[Iy1];
+            zn[4] += scale * Cc.e[Iz0];
+            zn[5] += scale * Cc.e[Iz1];
         }
         if (!(cc & SELF)) continue;
         T s = ru;
@@ -220,9 +240,10 @@ __device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
 }
 
 template <typename T>
-__device__ __forceinline__ int64_t coarse_agg(const MgLevel<T> &L, const MgLevel<T> &C, int64_t u) {
-    int i = (int)(u % L.nx), j = (int)((u / L.nx) % L.ny), k = (int)(u / ((int64_t)L.nx * L.ny));
-    return ((int64_t)(k >> 1) * C.ny + (j >> 1)) * C.nx + (i >> 1);
+__device__ __forceinline__ int32_t coarse_agg(const MgLevel<T> &L, const MgLevel<T> &C, int64_t u) {
+    uint32_t uu = (uint32_t)u, nx = (uint32_t)L.nx, ny = (uint32_t)L.ny;
+    uint32_t i = uu % nx, r = uu / nx, j = r % ny, k = r / ny;
+    return (int32_t)(((k >> 1) * (uint32_t)C.ny + (j >> 1)) * (uint32_t)C.nx + (i >> 1));
 }
 
 template <typename T>
@@ -233,11 +254,11 @@ __device__ void coarse_half(const MgLevel<T> &L, int c, bool whole, const MgLeve
     int64_t t0, ts;
     span(whole, t0, ts);
     for (int64_t t = t0; t < count; t += ts) {
-        int i2 = (int)(t % hx);
-        int64_t rr = t / hx;
-        int j = (int)(rr % L.ny);
-        int k = (int)(rr / L.ny);
-        int i = 2 * i2 + ((j + k + c) & 1);
+        uint32_t tt = (uint32_t)t;
+        uint32_t i2 = tt % (uint32_t)hx, rr = tt / (uint32_t)hx;
+        int j = (int)(rr % (uint32_t)L.ny);
+        int k = (int)(rr / (uint32_t)L.ny);
+        int i = 2 * (int)i2 + ((j + k + c) & 1);
         if (i >= L.nx) continue;
         int64_t I = ((int64_t)k * L.ny + j) * L.nx + i;
         /* all loads first (neighbour indices clamped into the level; a zero
@@ -268,9 +289,10 @@ __device__ void restrict_fine(const Fine<T> &F, const MgLevel<T> &C) {
     int64_t t0, ts;
     span(true, t0, ts);
     for (int64_t I = t0; I < C.n; I += ts) {
-        int ci = (int)(I % C.nx);
-        int cj = (int)((I / C.nx) % C.ny);
-        int ck = (int)(I / ((int64_t)C.nx * C.ny));
+        uint32_t I32 = (uint32_t)I, cr = I32 / (uint32_t)C.nx;
+        int ci = (int)(I32 % (uint32_t)C.nx);
+        int cj = (int)(cr % (uint32_t)C.ny);
+        int ck = (int)(cr / (uint32_t)C.ny);
         T sum = 0;
         /* the four red children (black residuals are zero after the black
          * sweep); a child off the grid or not an unknown contributes 0 */
@@ -310,9 +332,10 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
     int64_t t0, ts;
     span(whole, t0, ts);
     for (int64_t I = t0; I < C.n; I += ts) {
-        int ci = (int)(I % C.nx);
-        int cj = (int)((I / C.nx) % C.ny);
-        int ck = (int)(I / ((int64_t)C.nx * C.ny));
+        uint32_t I32 = (uint32_t)I, cr = I32 / (uint32_t)C.nx;
+        int ci = (int)(I32 % (uint32_t)C.nx);
+        int cj = (int)(cr % (uint32_t)C.ny);
+        int ck = (int)(cr / (uint32_t)C.ny);
         T sum = 0;
         for (int d = 0; d < 8; d++) {
             int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
@@ -441,8 +464,8 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         const int32_t *__restrict__ target, double phi0,
                                                         double te0, double n0, int nr_max, double nr_tol,
                                                         int pcg_max, double pcg_tol, T *y, T *r, T *z, T *p0,
-                                                        T *p1, T *q, T *dg, MgArgs<T> mg, double *partials,
-                                                        SolveStatus *st, int *err) {
+                                                        T *p1, T *q, T *dg, MgArgs<T> mg, const int32_t *lists,
+                                                        double *partials, SolveStatus *st, int *err) {
     cg::grid_group grid = cg::this_grid();
     const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
@@ -461,6 +484,11 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     F.dg = dg;
     F.r = r;
     F.z = z;
+    F.nlist = (int32_t)((int64_t)((g.ni - 1) / 2) * (g.nj - 2) * (g.nk - 2));
+    F.list[0] = lists;
+    F.pk[0] = lists + F.nlist;
+    F.list[1] = lists + 2 * (int64_t)F.nlist;
+    F.pk[1] = lists + 3 * (int64_t)F.nlist;
     int round = 0, nr, conv = 0, inner = 0;
     double norm = 0;
     for (nr = 0; nr < nr_max; nr++) {
@@ -486,8 +514,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             dg[u] = d;
             r[u] = rv;
             y[u] = 0;
-            int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / sz);
-            if (jacobi || ((i + j + k) & 1) == 0) z[u] = rv / d;
+            if (jacobi || !(c & BLACK)) z[u] = rv / d;
             ff += Fv * Fv;
         }
         double s1[1] = {ff};
@@ -531,13 +558,13 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 /* y += alpha p, r -= alpha q, and the first red half sweep */
                 T rr = 0;
                 for (int64_t u = gtid; u < nn; u += gsize) {
-                    if (!(code[u] & SELF)) continue;
+                    uint16_t c = code[u];
+                    if (!(c & SELF)) continue;
                     y[u] += alpha * pnew[u];
                     T ru = r[u] - alpha * q[u];
                     r[u] = ru;
                     rr += ru * ru;
-                    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / sz);
-                    if (jacobi || ((i + j + k) & 1) == 0) z[u] = ru / dg[u];
+                    if (jacobi || !(c & BLACK)) z[u] = ru / dg[u];
                 }
                 double s4[1] = {(double)rr};
                 grid_sum_n<1>(grid, s4, partials, round);
@@ -679,12 +706,16 @@ static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
 
 template <typename T>
 static int run_pcg(World &w) {
+    /* the colour lists pack coordinates in 10 + 10 + 11 bits */
+    if (w.g.ni > 1024 || w.g.nj > 1024 || w.g.nk > 2048) return (int)cudaErrorInvalidValue;
     size_t es = sizeof(T);
     size_t vec = ((w.nn * es + 255) / 256) * 256;
     size_t codeb = ((w.nn * sizeof(uint16_t) + 255) / 256) * 256;
     MgArgs<T> A;
     size_t mgb = mg_layout<T>(w, A, nullptr);
-    size_t need = 7 * vec + codeb + mgb;
+    int64_t nlist = (int64_t)((w.g.ni - 1) / 2) * (w.g.nj - 2) * (w.g.nk - 2);
+    size_t listb = ((4 * nlist * sizeof(int32_t) + 255) / 256) * 256;
+    size_t need = 7 * vec + codeb + mgb + listb;
     if (w.pcg_bytes < need || w.pcg_elem != (int)es) {
         if (w.pcg_buf) {
             cudaStreamSynchronize(w.stream);
@@ -700,10 +731,16 @@ static int run_pcg(World &w) {
     }
     char *base = (char *)w.pcg_buf;
     uint16_t *code = (uint16_t *)(base + 7 * vec);
+    int32_t *lists = (int32_t *)(base + 7 * vec + codeb + mgb);
     mg_layout<T>(w, A, base + 7 * vec + codeb);
     if (!w.pcg_codes_valid) {
         k_pcg_codes<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.obj, code);
         w.nlaunch++;
+        for (int c = 0; c < 2; c++) {
+            k_pcg_lists<<<blocks_for(nlist, 256), 256, 0, w.stream>>>(w.g, c, lists + 2 * c * nlist,
+                                                                      lists + (2 * c + 1) * nlist);
+            w.nlaunch++;
+        }
         for (int l = 0; l < A.nlev; l++) {
             MgLevel<T> prev = l ? A.L[l - 1] : A.L[0];
             k_mg_setup<T><<<blocks_for(A.L[l].n, 256), 256, 0, w.stream>>>(w.g, code, prev, A.L[l], l == 0);
@@ -733,8 +770,9 @@ static int run_pcg(World &w) {
     double *part = w.d_partials;
     SolveStatus *st = w.d_status;
     int *err = w.d_err;
-    void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,   &nr_max, &nr_tol, &pcg_max, &pcg_tol,
-                    &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,   &part, &st,     &err};
+    const int32_t *lst = lists;
+    void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
+                    &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, 0, w.stream);
 }
