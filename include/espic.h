@@ -110,6 +110,16 @@ int espic_species_get(espic_world *w, int sp, double *P, int64_t stride, int64_t
  * (x, y, z per particle) or NULL to draw them from the world's Philox stream. */
 int espic_species_load_box(espic_world *w, int sp, const double x1[3], const double x2[3],
                            double num_den, int64_t num_mp, const double *u);
+/* loadParticlesBox with velocities: num_mp particles of weight mpw (0: the
+ * species' mpw0), uniform in the box, velocities a drifting Maxwellian of
+ * temperature temp (K) about v_drift, sampled by Box-Muller; rewound by half
+ * a step like addParticle.  No single reference counterpart (closest:
+ * Species::sampleIsotropicVel, ch4/Species.cpp:161-175).  u = 7 uniforms per
+ * particle (x, y, z, then 4 for the normals) or NULL for the world's Philox
+ * stream.  Used to set up steady-state-like initial states. */
+int espic_species_load_box_thermal(espic_world *w, int sp, const double x1[3], const double x2[3],
+                                   double mpw, int64_t num_mp, const double v_drift[3], double temp,
+                                   const double *u);
 /* Species::loadParticlesBoxQS, ch2/Species.cpp:101-141 */
 int espic_species_load_box_qs(espic_world *w, int sp, const double x1[3], const double x2[3],
                               double num_den, const int num_mp[3]);

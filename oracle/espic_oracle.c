@@ -317,6 +317,30 @@ int64_t eo_load_box_qs(const eo_grid *g, const double *ef, double charge, double
     return np;
 }
 
+/* The CUDA path's thermal box loader (an extension with no reference
+ * counterpart): positions as loadParticlesBox, velocities vd + sigma * N(0,1)
+ * by Box-Muller with sigma = sqrt(K T / m); 7 uniforms per particle. */
+int64_t eo_load_box_thermal(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                            const double x1[3], const double x2[3], double mpw, int64_t num_mp,
+                            const double vd[3], double temp, const double *u, double *P, int64_t stride,
+                            int64_t np0, int64_t cap) {
+    double sigma = sqrt(EO_K * temp / mass);
+    int64_t np = np0;
+    for (int64_t p = 0; p < num_mp; p++) {
+        const double *up = u + 7 * p;
+        double pos[3], vel[3];
+        for (int d = 0; d < 3; d++) pos[d] = x1[d] + up[d] * (x2[d] - x1[d]);
+        double r1 = sqrt(-2.0 * log(1.0 - up[3])), a1 = 2 * EO_PI * up[4];
+        double r2 = sqrt(-2.0 * log(1.0 - up[5])), a2 = 2 * EO_PI * up[6];
+        vel[0] = vd[0] + sigma * (r1 * cos(a1));
+        vel[1] = vd[1] + sigma * (r1 * sin(a1));
+        vel[2] = vd[2] + sigma * (r2 * cos(a2));
+        np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &mpw, 1, P, stride, np, cap);
+        if (np < 0) return -1;
+    }
+    return np;
+}
+
 /* Number of macroparticles a beam source creates this step,
  * ch3/ver2/Source.cpp:7-18: (int)(n*v*A*dt/mpw0 + U). */
 int eo_inject_count(const eo_grid *g, double dt, double mpw0, double v_drift, double den,

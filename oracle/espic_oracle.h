@@ -70,6 +70,10 @@ int64_t eo_load_box(const eo_grid *g, const double *ef, double charge, double ma
 int64_t eo_load_box_qs(const eo_grid *g, const double *ef, double charge, double mass, double dt,
                        const double x1[3], const double x2[3], double num_den, const int num_mp[3],
                        double *P, int64_t stride, int64_t np0, int64_t cap);
+int64_t eo_load_box_thermal(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                            const double x1[3], const double x2[3], double mpw, int64_t num_mp,
+                            const double vd[3], double temp, const double *u, double *P, int64_t stride,
+                            int64_t np0, int64_t cap);
 int64_t eo_inject_cold(const eo_grid *g, const double *ef, double charge, double mass, double dt,
                        double mpw0, double v_drift, double den, const double *u, int64_t *u_used,
                        double *P, int64_t stride, int64_t np0, int64_t cap);

@@ -61,6 +61,9 @@ def _sig(L):
     L.eo_load_box.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, D, I64, PD, PD, I64, I64, I64]
     L.eo_load_box_qs.restype = I64
     L.eo_load_box_qs.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, D, PI, PD, I64, I64, I64]
+    L.eo_load_box_thermal.restype = I64
+    L.eo_load_box_thermal.argtypes = [C.POINTER(Grid), PD, D, D, D, PD, PD, D, I64, PD, D, PD, PD, I64, I64,
+                                      I64]
     L.eo_inject_count.restype = C.c_int
     L.eo_inject_count.argtypes = [C.POINTER(Grid), D, D, D, D, D]
     L.eo_inject_cold.restype = I64
@@ -190,6 +193,14 @@ def load_box_qs(g, ef, charge, mass, dt, x1, x2, num_den, num_mp):
     nm = np.asarray(num_mp, dtype=np.int32)
     m = lib().eo_load_box_qs(C.byref(g), pd(ef), charge, mass, dt, arr3(x1), arr3(x2), num_den,
                              pi(nm), pd(B), cap, 0, cap)
+    return np.ascontiguousarray(B[:, :m])
+
+
+def load_box_thermal(g, ef, charge, mass, dt, x1, x2, mpw, num_mp, vd, temp, u):
+    B = np.zeros((7, num_mp))
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    m = lib().eo_load_box_thermal(C.byref(g), pd(ef), charge, mass, dt, arr3(x1), arr3(x2), mpw, num_mp,
+                                  arr3(vd), temp, pd(u), pd(B), num_mp, 0, num_mp)
     return np.ascontiguousarray(B[:, :m])
 
 

@@ -92,6 +92,7 @@ def lib():
             "espic_species_get": [VP, C.c_int, PD, I64, I64, C.POINTER(I64)],
             "espic_species_load_box": [VP, C.c_int, PD, PD, C.c_double, I64, PD],
             "espic_species_load_box_qs": [VP, C.c_int, PD, PD, C.c_double, PI],
+            "espic_species_load_box_thermal": [VP, C.c_int, PD, PD, C.c_double, I64, PD, C.c_double, PD],
             "espic_push": [VP, C.c_int, C.c_int],
             "espic_deposit": [VP, C.c_int],
             "espic_charge_density": [VP],
@@ -330,6 +331,12 @@ class Species:
         u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
         check(lib().espic_species_load_box(self.world.h, self.id, _d3(x1), _d3(x2), num_den,
                                            int(num_mp), _pd(u)))
+
+    def loadParticlesBoxThermal(self, x1, x2, mpw, num_mp, v_drift, temp, u=None):
+        """num_mp particles of weight mpw (0: mpw0) with a drifting Maxwellian."""
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().espic_species_load_box_thermal(self.world.h, self.id, _d3(x1), _d3(x2), mpw,
+                                                   int(num_mp), _d3(v_drift), temp, _pd(u)))
 
     def loadParticlesBoxQS(self, x1, x2, num_den, num_mp):
         nm = (C.c_int * 3)(*[int(x) for x in num_mp])

@@ -386,7 +386,7 @@ extern "C" int espic_species_create(espic_world *h, double mass, double charge, 
     cudaMemsetAsync(s->den, 0, w.nn * sizeof(double), w.stream);
     cudaMemsetAsync(s->den_ave, 0, w.nn * sizeof(double), w.stream);
     if (form == ESPIC_FORM_MIXED) {
-        s->unit = mpw0 / 16777216.0;
+        s->unit = mpw0 / 8388608.0; /* counts of mpw0 * 2^-23 */
         s->weight_bound = mpw0;
         if (!w.ef4_valid) launch_ef4(w);
     } else {
@@ -564,6 +564,31 @@ extern "C" int espic_species_load_box(espic_world *h, int sp, const double x1[3]
     }
     uint64_t stream_id = ((uint64_t)(0x10000u + w.load_calls++) << 32);
     launch_load_box(w, s, x1, x2, mpw, num_mp, du, stream_id);
+    CHECK_LAUNCH();
+    CK(cudaStreamSynchronize(w.stream));
+    return take_device_errors(w);
+}
+
+extern "C" int espic_species_load_box_thermal(espic_world *h, int sp, const double x1[3], const double x2[3],
+                                              double mpw, int64_t num_mp, const double v_drift[3], double temp,
+                                              const double *u) {
+    WORLD(h);
+    SPECIES(sp);
+    if (!x1 || !x2 || !v_drift || num_mp < 0 || temp < 0 || mpw < 0) return fail(ESPIC_ERR_ARG, "bad thermal load");
+    if (num_mp == 0) return ESPIC_OK;
+    if (mpw == 0) mpw = s.mpw0;
+    if (!(mpw > 0)) return fail(ESPIC_ERR_ARG, "no weight: give mpw or a species mpw0");
+    int rc = prepare_weights(w, s, nullptr, 1, mpw);
+    if (rc != ESPIC_OK) return rc;
+    const double *du = nullptr;
+    if (u) {
+        if ((rc = ensure_u(w, 7 * num_mp)) != ESPIC_OK) return rc;
+        CK(cudaMemcpyAsync(w.d_u, u, 7 * num_mp * sizeof(double), cudaMemcpyHostToDevice, w.stream));
+        du = w.d_u;
+    }
+    uint64_t stream_id = ((uint64_t)(0x20000u + w.load_calls++) << 32);
+    PhaseScope ph(w, ESPIC_PHASE_INJECT);
+    launch_load_thermal(w, s, x1, x2, mpw, num_mp, v_drift, temp, du, stream_id);
     CHECK_LAUNCH();
     CK(cudaStreamSynchronize(w.stream));
     return take_device_errors(w);

@@ -99,6 +99,8 @@ void launch_load_box(World &w, Species &s, const double x1[3], const double x2[3
                      int64_t num_mp, const double *d_u, uint64_t stream_id);
 void launch_load_qs(World &w, Species &s, const double x1[3], const double x2[3], double mpw,
                     const int num_mp[3]);
+void launch_load_thermal(World &w, Species &s, const double x1[3], const double x2[3], double mpw,
+                         int64_t num_mp, const double vd[3], double temp, const double *d_u, uint64_t stream_id);
 void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp,
                    const double *d_u, uint64_t stream_id);
 void launch_diag(World &w, Species &s, double *d_out5);

@@ -458,6 +458,26 @@ struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27) and
     }
 };
 
+struct GenThermal { /* uniform box with a drifting Maxwellian (no reference counterpart) */
+    double x1[3], x2[3], mpw, sigma, vd[3];
+    const double *u; /* 7 per particle or null -> Philox */
+    uint64_t seed, stream;
+    __device__ double U(int64_t k) const { return u ? u[k] : philox_uniform(seed, stream, (uint64_t)k); }
+    __device__ void pos(int64_t i, double x[3]) const {
+        for (int d = 0; d < 3; d++) x[d] = x1[d] + U(7 * i + d) * (x2[d] - x1[d]);
+    }
+    __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
+        pos(i, x);
+        /* Box-Muller: 1-u keeps the logarithm finite */
+        double r1 = sqrt(-2.0 * log(1.0 - U(7 * i + 3))), a1 = 2 * REF_PI * U(7 * i + 4);
+        double r2 = sqrt(-2.0 * log(1.0 - U(7 * i + 5))), a2 = 2 * REF_PI * U(7 * i + 6);
+        v[0] = vd[0] + sigma * (r1 * cos(a1));
+        v[1] = vd[1] + sigma * (r1 * sin(a1));
+        v[2] = vd[2] + sigma * (r2 * cos(a2));
+        w_ = mpw;
+    }
+};
+
 /* Pass 1: accepted candidates per block (addParticle rejects x outside
  * [x0,xm)). */
 template <class Gen>
@@ -1177,6 +1197,22 @@ void launch_load_qs(World &w, Species &s, const double x1[3], const double x2[3]
     q.n1 = num_mp[1];
     q.n2 = num_mp[2];
     append(w, s, q, (int64_t)num_mp[0] * num_mp[1] * num_mp[2], s.uniform_w ? 0 : 1);
+}
+
+void launch_load_thermal(World &w, Species &s, const double x1[3], const double x2[3], double mpw,
+                         int64_t num_mp, const double vd[3], double temp, const double *d_u, uint64_t stream_id) {
+    GenThermal g;
+    for (int d = 0; d < 3; d++) {
+        g.x1[d] = x1[d];
+        g.x2[d] = x2[d];
+        g.vd[d] = vd[d];
+    }
+    g.mpw = mpw;
+    g.sigma = sqrt(KB * temp / s.mass);
+    g.u = d_u;
+    g.seed = w.seed;
+    g.stream = stream_id;
+    append(w, s, g, num_mp, s.uniform_w ? 0 : 1);
 }
 
 void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp, const double *d_u,

@@ -3,10 +3,14 @@
  * an int32 cell key (i | j<<10 | k<<20), an f32 in-cell offset and an f32
  * velocity (28 bytes), with the species weight mpw0.  The push gathers E from
  * the f32 copy ef4 (one 16-byte load per corner), moves the particle in cell
- * units, applies the walls / sphere, and deposits its CIC weights as 24-bit
- * fixed-point fractions of mpw0 with warp-aggregated 64-bit atomics (lanes of
- * a warp that share a cell are summed with one redux, then one atomic per
- * corner).  Integer sums make the density independent of particle order.
+ * units, applies the walls / sphere, and deposits its CIC weights as 23-bit
+ * fixed-point fractions of mpw0.  The push kernel accumulates a thread
+ * block's deposits in a shared-memory box spanning the block's cells (the
+ * particles of a block are neighbours after the counting sort, and the common
+ * drift keeps them together between sorts) with 32-bit shared atomics, then
+ * adds the box to the int64 grid with one global atomic per touched node;
+ * blocks whose cells span too large a box use global atomics directly.
+ * Integer sums make the density independent of particle order.
  *
  * Reference behaviour restated: Species::advance (ch3/ver2/Species.cpp:7-48,
  * ch2/Species.cpp:7-38), Field_::gather/scatter (ch2/Field.h:164-208),
@@ -19,6 +23,11 @@
 namespace espic {
 
 enum { M_REFLECT = 0, M_ABSORB = 1 };
+
+/* a corner weight in [0,1] becomes round(w * 2^23) counts of mpw0 * 2^-23;
+ * 256 particles of a block cannot overflow a 32-bit shared counter */
+#define MIX_Q 8388608.f
+constexpr int BOX_CAP = 4096; /* nodes of the shared deposit box (16 KB) */
 
 struct MixArgs {
     int ni, nj, nk;
@@ -77,26 +86,71 @@ __device__ __forceinline__ void reflect_axis(int &i, float &f, float &v, int n) 
     f = p - (float)ii;
 }
 
-/* warp-aggregated fixed-point CIC deposit of the lanes in `active` */
-__device__ __forceinline__ void deposit_warp(unsigned active, bool me, int32_t key, int ni, int nj,
-                                             float fx, float fy, float fz, unsigned long long *acc) {
-    if (!me) return;
-    unsigned peers = __match_any_sync(active, key);
-    int leader = __ffs(peers) - 1;
+/* Block-wide deposit through a shared-memory box (called by every thread of
+ * the block; `me` marks the threads with a particle to deposit). */
+__device__ __forceinline__ void deposit_block(bool me, int32_t key, int ni, int nj, float fx, float fy, float fz,
+                                              unsigned long long *acc) {
+    __shared__ unsigned int sbox[BOX_CAP];
+    __shared__ int s_lo[3], s_hi[3];
+    int i = 0, j = 0, k = 0;
+    if (me) unpack(key, i, j, k);
+    if (threadIdx.x < 3) {
+        s_lo[threadIdx.x] = 0x7fffffff;
+        s_hi[threadIdx.x] = -1;
+    }
+    __syncthreads();
+    int mi = __reduce_min_sync(0xffffffffu, me ? i : 0x7fffffff);
+    int mj = __reduce_min_sync(0xffffffffu, me ? j : 0x7fffffff);
+    int mk = __reduce_min_sync(0xffffffffu, me ? k : 0x7fffffff);
+    int xi = __reduce_max_sync(0xffffffffu, me ? i : -1);
+    int xj = __reduce_max_sync(0xffffffffu, me ? j : -1);
+    int xk = __reduce_max_sync(0xffffffffu, me ? k : -1);
+    if ((threadIdx.x & 31) == 0 && xi >= 0) {
+        atomicMin(&s_lo[0], mi);
+        atomicMin(&s_lo[1], mj);
+        atomicMin(&s_lo[2], mk);
+        atomicMax(&s_hi[0], xi);
+        atomicMax(&s_hi[1], xj);
+        atomicMax(&s_hi[2], xk);
+    }
+    __syncthreads();
+    const int li = s_lo[0], lj = s_lo[1], lk = s_lo[2];
+    if (s_hi[0] < 0) return; /* nothing to deposit in this block (uniform) */
+    const int bi = s_hi[0] - li + 2, bj = s_hi[1] - lj + 2, bk = s_hi[2] - lk + 2;
+    const int64_t vol = (int64_t)bi * bj * bk;
     float w[8];
     cic_w(fx, fy, fz, w);
-    unsigned q[8];
+    if (vol <= BOX_CAP) {
+        for (int t = threadIdx.x; t < (int)vol; t += blockDim.x) sbox[t] = 0u;
+        __syncthreads();
+        if (me) {
+            int L = ((k - lk) * bj + (j - lj)) * bi + (i - li);
+            int idx[8] = {L, L + 1, L + 1 + bi, L + bi, L + bi * bj, L + 1 + bi * bj, L + 1 + bi + bi * bj,
+                          L + bi + bi * bj};
 #pragma unroll
-    for (int c = 0; c < 8; c++) q[c] = __reduce_add_sync(peers, __float2uint_rn(w[c] * 16777216.f));
-    if ((int)(threadIdx.x & 31) == leader) {
-        int i, j, k;
-        unpack(key, i, j, k);
-        int64_t sy = ni, sz = (int64_t)ni * nj;
-        int64_t n0 = ((int64_t)k * nj + j) * ni + i;
+            for (int c = 0; c < 8; c++) {
+                unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                if (q) atomicAdd(&sbox[idx[c]], q);
+            }
+        }
+        __syncthreads();
+        const int64_t sy = ni, sz = (int64_t)ni * nj;
+        for (int t = threadIdx.x; t < (int)vol; t += blockDim.x) {
+            unsigned v = sbox[t];
+            if (!v) continue;
+            int ti = t % bi, r = t / bi, tj = r % bj, tk = r / bj;
+            int64_t n = (int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + (li + ti);
+            atomicAdd(acc + n, (unsigned long long)v);
+        }
+    } else if (me) {
+        const int64_t sy = ni, sz = (int64_t)ni * nj;
+        int64_t n0 = (int64_t)k * sz + (int64_t)j * sy + i;
         int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
 #pragma unroll
-        for (int c = 0; c < 8; c++)
-            if (q[c]) atomicAdd(acc + idx[c], (unsigned long long)q[c]);
+        for (int c = 0; c < 8; c++) {
+            unsigned q = __float2uint_rn(w[c] * MIX_Q);
+            if (q) atomicAdd(acc + idx[c], (unsigned long long)q);
+        }
     }
 }
 
@@ -165,11 +219,7 @@ __global__ void __launch_bounds__(256) k_push_mixed(MixArgs a, const float4 *__r
         vel[stride + p] = vy;
         vel[2 * stride + p] = vz;
     }
-    if (DEPOSIT) {
-        bool me = live && !dead;
-        unsigned active = __ballot_sync(0xffffffffu, me);
-        deposit_warp(active, me, key, a.ni, a.nj, fx, fy, fz, acc);
-    }
+    if (DEPOSIT) deposit_block(live && !dead, key, a.ni, a.nj, fx, fy, fz, acc);
     if (WALLS == M_ABSORB) {
         unsigned m = __ballot_sync(0xffffffffu, dead);
         if ((threadIdx.x & 31) == 0 && live) {
@@ -193,8 +243,7 @@ __global__ void __launch_bounds__(256) k_deposit_mixed(MixArgs a, const int32_t 
         fy = off[stride + p];
         fz = off[2 * stride + p];
     }
-    unsigned active = __ballot_sync(0xffffffffu, me);
-    deposit_warp(active, me, key, a.ni, a.nj, fx, fy, fz, acc);
+    deposit_block(me, key, a.ni, a.nj, fx, fy, fz, acc);
 }
 
 /* float64 block -> mixed form (World::XtoL in float64, then split) */

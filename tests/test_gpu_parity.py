@@ -411,3 +411,31 @@ def test_deposit_is_deterministic_across_orders(espic, po):
         a.computeNumberDensity()
         b.computeNumberDensity()
         assert np.array_equal(a.den, b.den)
+
+
+def test_thermal_loader(espic, po):
+    """The drifting-Maxwellian loader: positions bit-exact with the oracle,
+    velocities within 1e-13 (log/cos/sin), moments within sampling error."""
+    g = po.grid(*SPH)
+    ef = po.efield(g, golden("sphere_efield")["phi"])
+    T = 0.1 * QE / K
+    vd = [0.0, 0.0, 7000.0]
+    u = np.random.default_rng(3).random(7 * 5000)
+    with world(espic, SPH) as w:
+        w.setTime(1e-7, 1)
+        w.write(espic.FIELD_PHI, golden("sphere_efield")["phi"])
+        espic.PotentialSolver(w).computeEF()
+        s = espic.Species(w, "O+", 16 * AMU, QE, mpw0=40.0, capacity=1 << 20, walls=espic.WALLS_ABSORB)
+        s.loadParticlesBoxThermal(SPH[1], SPH[2], 0.0, 5000, vd, T, u=u)
+        P = s.particles()
+        want = po.load_box_thermal(g, ef, QE, 16 * AMU, 1e-7, SPH[1], SPH[2], 40.0, 5000, vd, T, u)
+        assert np.array_equal(P[0:3], want[0:3]) and np.array_equal(P[6], want[6])
+        assert rel(P[3:6], want[3:6]) <= 1e-13
+        big = espic.Species(w, "O+", 16 * AMU, QE, mpw0=40.0, capacity=1 << 20, walls=espic.WALLS_ABSORB)
+        w.write(espic.FIELD_PHI, np.zeros(g.nn))
+        espic.PotentialSolver(w).computeEF()
+        big.loadParticlesBoxThermal(SPH[1], SPH[2], 0.0, 400000, vd, T)
+        V = big.particles()[3:6]
+        sigma = np.sqrt(K * T / (16 * AMU))
+        assert abs(V[2].mean() - 7000.0) < 5 * sigma / np.sqrt(4e5)
+        assert abs(V[0].std() / sigma - 1) < 0.01
