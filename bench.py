@@ -46,6 +46,9 @@ CONFIGS = {
                      radius=0.05, phi_s=-100.0, np=4_000_000, mpw0=40.0, dt=1e-7, sort_every=20),
     "sphere256": dict(n=(256, 256, 512), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
                       radius=0.04, phi_s=-100.0, np=500_000_000, mpw0=0.32, dt=1e-7, sort_every=20),
+    # the reference's configuration 1: ch2 grounded box, FP64 plain form
+    "box21": dict(n=(21, 21, 21), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.2), np=90_000, dt=2e-10,
+                  sort_every=0),
 }
 V_DRIFT, N0, TI_EV, TE, PHI0 = 7000.0, 1e10, 0.1, 3.0, 0.0
 NR_TOL, PCG_TOL = 1e-6, 1e-4
@@ -304,24 +307,97 @@ def ncu_case(args):
     if not os.path.exists(E.LIB_PATH):
         E.build()
     cfg = CONFIGS[args.config]
-    P0 = synthetic_state(cfg, cfg["np"], 1)
+    npart = args.ncu_particles or cfg["np"]
     ni, nj, nk = cfg["n"]
     w = E.World(ni, nj, nk, cfg["x0"], cfg["xm"])
     w.setTime(cfg["dt"], 100)
     w.addSphere(cfg["center"], cfg["radius"], cfg["phi_s"])
     w.addInlet()
-    s = E.Species(w, "O+", 16 * AMU, QE, mpw0=cfg["mpw0"], capacity=int(P0.shape[1] * 1.5),
+    s = E.Species(w, "O+", 16 * AMU, QE, mpw0=cfg["mpw0"] * cfg["np"] / npart, capacity=int(npart * 1.5),
                   form=E.FORM_MIXED, walls=E.WALLS_ABSORB)
     sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
     sol.setReferenceValues(PHI0, TE, N0)
     sol.setNewton(nr_max=20, nr_tol=NR_TOL, pcg_max=20000, pcg_tol=PCG_TOL, fp32_inner=True)
-    s.set_particles(P0)
+    s.loadParticlesBoxThermal(cfg["x0"], cfg["xm"], 0.0, npart, (0.0, 0.0, V_DRIFT), TI_EV * QE / K)
     s.sort()
     sol.computeEF()
     s.advance(deposit=True)
     w.computeChargeDensity()
     print(json.dumps({"ncu_case": args.config, "solve": sol.solve(), "particles": s.getNp()}))
     w.close()
+
+
+def aggregate(ms_step, n_local, dist, device):
+    """Max step time over ranks and the whole-job throughput (units all ranks
+    processed / that time), as the replica runs of --gpus N report it."""
+    import torch
+    world_size = dist.get_world_size() if dist else 1
+    if dist:
+        t = torch.tensor([ms_step, n_local], dtype=torch.float64, device=device)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tsum = t.clone()
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        return float(tmax[0]), float(tsum[1]) / (float(tmax[0]) * 1e-3), world_size
+    return ms_step, n_local / (ms_step * 1e-3), 1
+
+
+def run_box(args, E, torch, dist, rank, world_size):
+    """Configuration 1: the ch2 grounded box, 80,000 O+ uniform at n = 1e11
+    and 10,000 electrons in the octant [-0.1,0]^2 x [0,0.1], zero velocity,
+    dt = 2e-10, red-black SOR (omega 1.4) to L2 residual 1e-4; FP64 plain
+    form (bit-exact with the reference's arithmetic)."""
+    cfg = CONFIGS["box21"]
+    QE_, AMU_, ME_ = E.QE, E.AMU, E.ME
+
+    def world():
+        w = E.World(*cfg["n"], cfg["x0"], cfg["xm"])
+        w.set_seed(1 + rank)
+        w.setTime(cfg["dt"], 1 << 30)
+        si = E.Species(w, "O+", 16 * AMU_, QE_, capacity=1 << 17)
+        se = E.Species(w, "e-", ME_, -QE_, capacity=1 << 15)
+        si.loadParticlesBox(cfg["x0"], cfg["xm"], 1e11, 80000)
+        se.loadParticlesBox(cfg["x0"], (0.0, 0.0, 0.1), 1e11, 10000)
+        sol = E.PotentialSolver(w, E.SOLVER_SOR, 10000, 1e-4)
+        sol.solve()
+        sol.computeEF()
+        return w
+    w = world()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    if dist:
+        dist.barrier()
+    clocks = Clocks()
+    clocks.start()
+    t = timed_steps(E, torch, w, cfg, args.steps, args.warmup, flush)
+    ck = clocks.stop()
+    ms = float(np.sum(t["ms"])) / args.steps
+    ms_max, value, ws = aggregate(ms, 90000.0, dist, "cuda")
+    phases, _ = profiled_steps(E, w, cfg, max(3, min(args.steps, 10)))
+    w.close()
+    # e2e: the ch2 loop body through the C-ABI, diag row read back each step
+    w = world()
+    for _ in range(args.warmup):
+        w.step(0)
+    row = np.zeros(13)
+    w.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.step(0, row)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    w.close()
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "box21", "grid": list(cfg["n"]), "particles": 90000, "form": "fp64 plain",
+                       "solver": "red-black SOR, omega 1.4, tol 1e-4",
+                       "l2": "flushed between timed steps (256 MB write, outside the events)"},
+            "poisson_ms_per_step": phases["solve"], "phase_ms_per_step": phases,
+            "sor_iterations_per_step": t["newton"] / args.steps,
+            "e2e": {"value": 90000.0 * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 13 * 8},
+            "gpu_launches": t["launches"], "clocks": ck}
+    if rank == 0:
+        print(json.dumps(line))
 
 
 def main():
@@ -335,6 +411,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain form")
     ap.add_argument("--ncu-case", action="store_true",
                     help="one push + one solve of the workload (mixed form), for an ncu capture")
+    ap.add_argument("--ncu-particles", type=int, default=0,
+                    help="ions of the --ncu-case state (default: the workload's); keeps captures small")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -356,6 +434,11 @@ def main():
     E = espic_module()
     if not os.path.exists(E.LIB_PATH):
         E.build()
+    if args.config == "box21":
+        run_box(args, E, torch, dist, rank, world_size)
+        if dist:
+            dist.destroy_process_group()
+        return
     cfg = CONFIGS[args.config]
     big = cfg["np"] > 50_000_000
     # large cases are loaded on the GPU; the CPU baseline then uses a sample
@@ -370,12 +453,7 @@ def main():
     clocks.start()
     t = timed_steps(E, torch, w, cfg, args.steps, args.warmup, flush)
     ck = clocks.stop()
-    ms_step = float(np.sum(t["ms"])) / args.steps
-    if dist:
-        tt = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_step = float(tt.item())
-    value = t["n"] * world_size / (ms_step * 1e-3)
+    ms_step, value, _ = aggregate(float(np.sum(t["ms"])) / args.steps, t["n"], dist, "cuda")
     phases, counts = profiled_steps(E, w, cfg, max(3, min(args.steps, 10)))
     err, conv64 = phi_error(E, w, cfg)
     inner_per_step = t["inner"] / max(args.steps, 1)

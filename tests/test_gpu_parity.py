@@ -117,6 +117,47 @@ def test_sor_box_redblack_bitexact(espic, po):
         assert np.array_equal(w.phi, want)
 
 
+@pytest.mark.parametrize("n", [[21, 21, 21], [45, 41, 43]])
+def test_sor_box_grid_sizes(espic, po, n):
+    """Red-black SOR on a small and a larger, non-cubic grid: bit-exact with
+    the oracle, same iteration count."""
+    geo = (n, [-0.1, -0.1, 0.0], [0.1, 0.1, 0.2])
+    g = po.grid(*geo)
+    rng = np.random.default_rng(7)
+    x = np.linspace(0, 1, g.nn)
+    rho = 1e-9 * (np.sin(40 * x) + 0.3 * rng.standard_normal(g.nn))
+    with world(espic, geo) as w:
+        w.write(espic.FIELD_PHI, np.zeros(g.nn))
+        w.write(espic.FIELD_RHO, rho)
+        conv, it, _, l2 = espic.PotentialSolver(w, espic.SOLVER_SOR, 5000, 1e-3).solve()
+        want, conv_o, l2_o, it_o = po.sor_box(g, np.zeros(g.nn), rho, 5000, 1e-3, "rb")
+        assert conv == conv_o and it == it_o
+        assert np.array_equal(w.phi, want)
+        assert abs(l2 - l2_o) <= 1e-12 * l2_o
+
+
+@pytest.mark.parametrize("n", [[21, 21, 41], [33, 33, 65]])
+def test_gs_sphere_grid_sizes(espic, po, n):
+    geo = (n, [-0.1, -0.1, 0.0], [0.1, 0.1, 0.4])
+    g = po.grid(*geo)
+    phi0, te0, n0 = 0.0, 1.5, 1e12
+    with world(espic, geo) as w:
+        w.addSphere(*SPHERE)
+        w.addInlet()
+        obj = w.read(espic.FIELD_OBJECT_ID).astype(np.int32)
+        phi_init = w.phi
+        z = np.repeat(np.linspace(0, 1, n[2]), n[0] * n[1])
+        rho = QE * n0 * (1.0 + 0.2 * np.cos(6 * z))
+        w.write(espic.FIELD_RHO, rho)
+        sol = espic.PotentialSolver(w, espic.SOLVER_GS, 3000, 1e-3)
+        sol.setReferenceValues(phi0, te0, n0)
+        conv, it, _, _ = sol.solve()
+        want, conv_o, _, it_o = po.gs_sphere(g, phi_init, rho, obj, phi0, te0, n0, 3000, 1e-3, "rb")
+        assert conv == conv_o and abs(it - it_o) <= 25
+        if it == it_o:
+            assert rel(w.phi, want) <= 1e-10
+
+
 def test_diagnostics(espic, po):
     f = golden("box_diag")
     g = po.grid(*BOX)
