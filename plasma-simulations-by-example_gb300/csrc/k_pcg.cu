@@ -18,7 +18,11 @@
  * float64.  The inner PCG runs in T = double or float: with float it is the
  * inner solve of an iterative refinement whose outer residual is float64.
  * Dot products are reduced per block and summed by every block in block
- * order, so every block takes the same branch.
+ * order, so every block takes the same branch.  The inner PCG stops when
+ * |r| <= pcg_tol |F|, or earlier once the RMS of the preconditioned residual
+ * z = M r (an estimate of the error left in the Newton update y) is below
+ * nr_tol / 10: the Newton test RMS(y) < nr_tol cannot then depend on more
+ * inner accuracy, and the last Newton step stops needing a full solve.
  *
  * Preconditioner: an aggregation multigrid V-cycle.  Level l+1 groups the
  * level-l unknowns in 2x2x2 blocks of the structured index space; its
@@ -137,7 +141,7 @@ struct Fine {
     const uint16_t *code;
     T ct[3];
     int64_t off[6];
-    T *dg, *r, *z;
+    T *dg, *r, *z; /* dg: the Boltzmann part of the Jacobian diagonal */
     const int32_t *list[2]; /* interior nodes of each colour (-1: padding) */
     const int32_t *pk[2];   /* their coordinates, i | j<<10 | k<<20 */
     int32_t nlist;          /* entries per list */
@@ -174,13 +178,36 @@ __device__ __forceinline__ void span(bool whole, int64_t &t0, int64_t &ts) {
     }
 }
 
-/* red-black half sweep on the node grid: z = (r + sum c z_nb) / dg */
+/* Full Jacobian diagonal of an unknown: its Boltzmann part plus c per
+ * unknown or Dirichlet neighbour. */
+template <typename T>
+__device__ __forceinline__ T full_diag(uint16_t cc, T dB, const T ct[3]) {
+    T d = dB;
+#pragma unroll
+    for (int m = 0; m < 6; m++) d += (cc & ((1u << m) | (1u << (6 + m)))) ? ct[m >> 1] : (T)0;
+    return d;
+}
+
+/* J x at an unknown in difference form, dB x_u + sum_unknown c (x_u - x_nb)
+ * + sum_Dirichlet c x_u: no term is the difference of two large products,
+ * so float keeps full relative accuracy on the smooth modes, where the
+ * equivalent diag x_u - sum c x_nb loses most of its digits at fine spacing */
+template <typename T>
+__device__ __forceinline__ T jacobian_apply(uint16_t cc, T dB, const T ct[3], T xu, const T xn[6]) {
+    T s = dB * xu;
+#pragma unroll
+    for (int m = 0; m < 6; m++)
+        s += (cc & (1u << m)) ? ct[m >> 1] * (xu - xn[m]) : ((cc & (1u << (6 + m))) ? ct[m >> 1] * xu : (T)0);
+    return s;
+}
+
+/* red-black half sweep on the node grid: z = (r + sum c z_nb) / diag */
 /* Red-black Gauss-Seidel pieces.  A Gauss-Seidel update never reads the
  * node's own old value, which allows three fusions: the first red half
  * sweep from a zero guess is pointwise (e = b / diag) and is done by whoever
  * produces b; the prolongation of the coarse correction is applied on the
  * fly to the red neighbours read by the following black half sweep (the red
- * nodes are overwritten next anyway); and the dot product r.z of CG is
+ * nodes are overwritten next anyway); and the dot products r.z and z.z are
  * accumulated by the last two half sweeps, which produce the final z. */
 template <typename T>
 __device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &C, int64_t u) {
@@ -191,12 +218,11 @@ __device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &
 
 /* node-grid half sweep of colour c over the unknowns; with C != null the
  * neighbours are read with the coarse correction added (post-smoothing);
- * returns the local sum of r*z of the nodes it updated */
+ * adds r*z and z*z of the nodes it updated to rz and zz */
 template <typename T>
-__device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
+__device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale, T &rz, T &zz) {
     int64_t t0, ts;
     span(true, t0, ts);
-    T rz = 0;
     const int32_t *list = F.list[c], *pk = F.pk[c];
     for (int64_t t = t0; t < F.nlist; t += ts) {
         int32_t uu = list[t];
@@ -206,7 +232,7 @@ __device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
          * are issued before the code word arrives; the code only selects */
         uint16_t cc = F.code[u];
         T ru = F.r[u];
-        T dgu = F.dg[u];
+        T dBu = F.dg[u];
         T zn[6];
 #pragma unroll
         for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
@@ -232,11 +258,11 @@ __device__ T fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale) {
         T s = ru;
 #pragma unroll
         for (int m = 0; m < 6; m++) s += (cc & (1u << m)) ? F.ct[m >> 1] * zn[m] : (T)0;
-        T zu = s / dgu;
+        T zu = s / full_diag(cc, dBu, F.ct);
         F.z[u] = zu;
         rz += ru * zu;
+        zz += zu * zu;
     }
-    return rz;
 }
 
 template <typename T>
@@ -313,9 +339,7 @@ __device__ void restrict_fine(const Fine<T> &F, const MgLevel<T> &C) {
             T zn[6];
 #pragma unroll
             for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
-            T res = F.r[u] - F.dg[u] * F.z[u];
-#pragma unroll
-            for (int m = 0; m < 6; m++) res += (cc[q] & (1u << m)) ? F.ct[m >> 1] * zn[m] : (T)0;
+            T res = F.r[u] - jacobian_apply(cc[q], F.dg[u], F.ct, F.z[u], zn);
             sum += res;
         }
         C.b[I] = sum;
@@ -362,26 +386,32 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
 
 /* The V-cycle z = M r after its first red half sweep on the node grid
  * (done by the caller, fused with the CG update of r).  Every block executes
- * the same grid barriers; returns the grid-wide r.z of the final z (the
- * last barrier is the one of that reduction). */
+ * the same grid barriers; returns the grid-wide r.z of the final z and puts
+ * z.z in zz (the last barrier is the one of that reduction). */
 template <typename T>
 __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgArgs<T> &A, double *partials,
-                              int &round) {
+                              int &round, double &zz) {
     const int NL = A.nlev;
     if (NL == 0) { /* Jacobi: the caller computed z on every node */
-        T rz = 0;
+        T rz = 0, z2 = 0;
         int64_t nn = (int64_t)F.g.ni * F.g.nj * F.g.nk;
         int64_t t0, ts;
         span(true, t0, ts);
         for (int64_t u = t0; u < nn; u += ts)
-            if (F.code[u] & SELF) rz += F.r[u] * F.z[u];
-        double v[1] = {(double)rz};
-        grid_sum_n<1>(grid, v, partials, round);
+            if (F.code[u] & SELF) {
+                T zu = F.z[u];
+                rz += F.r[u] * zu;
+                z2 += zu * zu;
+            }
+        double v[2] = {(double)rz, (double)z2};
+        grid_sum_n<2>(grid, v, partials, round);
+        zz = v[1];
         return v[0];
     }
     const int GL = A.grid_levels;
     const T sc = A.scale;
-    fine_half(F, 1, (const MgLevel<T> *)nullptr, sc);
+    T rz = 0, z2 = 0, rz_unused = 0, z2_unused = 0;
+    fine_half(F, 1, (const MgLevel<T> *)nullptr, sc, rz_unused, z2_unused);
     grid.sync();
     restrict_fine(F, A.L[0]);
     grid.sync();
@@ -450,11 +480,12 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
         coarse_half(A.L[b - 1], 0, true, (const MgLevel<T> *)nullptr, sc);
         grid.sync();
     }
-    T rz = fine_half(F, 1, &A.L[0], sc);
+    fine_half(F, 1, &A.L[0], sc, rz, z2);
     grid.sync();
-    rz += fine_half(F, 0, (const MgLevel<T> *)nullptr, sc);
-    double v[1] = {(double)rz};
-    grid_sum_n<1>(grid, v, partials, round);
+    fine_half(F, 0, (const MgLevel<T> *)nullptr, sc, rz, z2);
+    double v[2] = {(double)rz, (double)z2};
+    grid_sum_n<2>(grid, v, partials, round);
+    zz = v[1];
     return v[0];
 }
 
@@ -473,6 +504,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     const double cd[3] = {1.0 / (g.dh[0] * g.dh[0]), 1.0 / (g.dh[1] * g.dh[1]), 1.0 / (g.dh[2] * g.dh[2])};
     const T ct[3] = {(T)cd[0], (T)cd[1], (T)cd[2]};
     const double A0 = PCG_QE * n0 / PCG_EPS_0;
+    const double inv_te0 = 1.0 / te0, A0_te0 = A0 / te0, inv_eps0 = 1.0 / PCG_EPS_0;
     const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t gsize = (int64_t)gridDim.x * blockDim.x;
     const bool jacobi = mg.nlev == 0;
@@ -491,9 +523,11 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     F.pk[1] = lists + 3 * (int64_t)F.nlist;
     int round = 0, nr, conv = 0, inner = 0;
     double norm = 0;
+    const double zz_stop = 0.01 * nr_tol * nr_tol * (double)nn;
     for (nr = 0; nr < nr_max; nr++) {
-        /* Newton residual and Jacobian diagonal (float64); the first red
-         * smoothing half sweep (or Jacobi) of the preconditioner rides along */
+        /* Newton residual (float64) and the Boltzmann part of the Jacobian
+         * diagonal; the first red smoothing half sweep (or Jacobi) of the
+         * preconditioner rides along */
         double ff = 0;
         for (int64_t u = gtid; u < nn; u += gsize) {
             uint16_t c = code[u];
@@ -507,14 +541,14 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 L += on ? cd[m >> 1] * (ph - pn[m]) : 0.0;
                 dL += on ? cd[m >> 1] : 0.0;
             }
-            double e = exp((ph - phi0) / te0);
-            double Fv = L + A0 * e - rho[u] / PCG_EPS_0;
-            T d = (T)(dL + A0 / te0 * e);
+            double e = exp((ph - phi0) * inv_te0);
+            double Fv = L + A0 * e - rho[u] * inv_eps0;
+            double dB = A0_te0 * e;
             T rv = (T)Fv;
-            dg[u] = d;
+            dg[u] = (T)dB;
             r[u] = rv;
             y[u] = 0;
-            if (jacobi || !(c & BLACK)) z[u] = rv / d;
+            if (jacobi || !(c & BLACK)) z[u] = rv / (T)(dL + dB);
             ff += Fv * Fv;
         }
         double s1[1] = {ff};
@@ -526,7 +560,8 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         }
         if (FF > 0) {
             const double stop2 = pcg_tol * pcg_tol * FF;
-            double RZ = vcycle_rest(grid, F, mg, partials, round);
+            double ZZ;
+            double RZ = vcycle_rest(grid, F, mg, partials, round, ZZ);
             T beta = 0;
             T *pold = p0, *pnew = p1;
             for (int it = 0; it < pcg_max; it++) {
@@ -537,7 +572,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                     uint16_t c = code[u];
                     if (!(c & SELF)) continue;
                     /* an unknown is interior: neighbour loads need no code bit */
-                    T zc = z[u], pc = it ? pold[u] : (T)0, d = dg[u];
+                    T zc = z[u], pc = it ? pold[u] : (T)0, dB = dg[u];
                     T zn[6], pn[6];
 #pragma unroll
                     for (int m = 0; m < 6; m++) {
@@ -545,9 +580,9 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                         pn[m] = it ? pold[u + off[m]] : (T)0;
                     }
                     T pu = zc + beta * pc;
-                    T s = d * pu;
 #pragma unroll
-                    for (int m = 0; m < 6; m++) s -= (c & (1u << m)) ? ct[m >> 1] * (zn[m] + beta * pn[m]) : (T)0;
+                    for (int m = 0; m < 6; m++) pn[m] = zn[m] + beta * pn[m];
+                    T s = jacobian_apply(c, dB, ct, pu, pn);
                     pnew[u] = pu;
                     q[u] = s;
                     pq += pu * s;
@@ -564,13 +599,17 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                     T ru = r[u] - alpha * q[u];
                     r[u] = ru;
                     rr += ru * ru;
-                    if (jacobi || !(c & BLACK)) z[u] = ru / dg[u];
+                    if (jacobi || !(c & BLACK)) z[u] = ru / full_diag(c, dg[u], ct);
                 }
                 double s4[1] = {(double)rr};
                 grid_sum_n<1>(grid, s4, partials, round);
                 inner++;
                 if (!(s4[0] > stop2)) break; /* also leaves on NaN */
-                double RZn = vcycle_rest(grid, F, mg, partials, round);
+                double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ);
+                /* z = M r estimates the remaining error of y: once its RMS is
+                 * below a tenth of the Newton tolerance, further inner
+                 * iterations cannot change the outcome of the Newton test */
+                if (ZZ < zz_stop) break;
                 beta = (T)(RZn / RZ);
                 RZ = RZn;
                 T *tp = pold;

@@ -323,6 +323,39 @@ def test_newton_pcg(espic, po, fp32, levels):
             assert inner < 40 * nr, (nr, inner)
 
 
+def test_newton_pcg_fp32_inner_accuracy(espic, po):
+    """One Newton step from a perturbed solution on a fine grid: the FP32 inner
+    solve reaches the same accuracy as the FP64 one.  (A float Jacobian
+    written as diag*x - sum c*x_nb loses ~4 digits on the smooth modes here
+    and would leave ~1e-3 of the perturbation behind.)"""
+    geo = ([129, 129, 257], [-0.1, -0.1, 0.0], [0.1, 0.1, 0.4])
+    phi0, te0, n0 = 0.0, 3.0, 1e10
+    with world(espic, geo) as w:
+        w.addSphere(*SPHERE)
+        w.addInlet()
+        ni, nj, nk = geo[0]
+        z = np.repeat(np.linspace(0, 1, nk), ni * nj)
+        w.write(espic.FIELD_RHO, QE * n0 * (1.0 + 0.3 * np.cos(5 * z)))
+        sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 100, 1e-4)
+        sol.setReferenceValues(phi0, te0, n0)
+        sol.setNewton(nr_max=50, nr_tol=1e-11, pcg_max=5000, pcg_tol=1e-12, fp32_inner=False)
+        assert sol.solve()[0]
+        tight = w.phi
+        obj = w.object_id
+        k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+        pert = 1e-3 * (np.sin(np.pi * i / (ni - 1)) * np.sin(np.pi * j / (nj - 1)) *
+                       np.sin(np.pi * k / (nk - 1))).ravel()
+        pert[obj > 0] = 0.0
+        err = {}
+        for fp32 in (False, True):
+            w.write(espic.FIELD_PHI, tight + pert)
+            sol.setNewton(nr_max=1, nr_tol=1e-12, pcg_max=5000, pcg_tol=1e-4, fp32_inner=fp32)
+            sol.solve()
+            err[fp32] = np.max(np.abs(w.phi - tight))
+        assert err[False] < 1e-3 * 1e-2
+        assert err[True] <= 2 * err[False] + 1e-9, err
+
+
 def test_qn(espic, po):
     f = golden("sphere_solve")
     phi0, te0, n0 = f["ref"]
