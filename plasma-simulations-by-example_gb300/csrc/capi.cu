@@ -87,6 +87,7 @@ static int take_device_errors(World &w) {
     if (bits & DERR_CAPACITY) return fail(ESPIC_ERR_CAPACITY, "particle capacity exceeded; particles not added");
     if (bits & DERR_NONFINITE) return fail(ESPIC_ERR_NONFINITE, "non-finite value in the step");
     if (bits & DERR_FIXED_RANGE) return fail(ESPIC_ERR_FIXED, "weight outside the fixed-point range");
+    if (bits & DERR_TIMEOUT) return fail(ESPIC_ERR_CUDA, "a bounded wait on a bulk copy timed out");
     return ESPIC_OK;
 }
 
@@ -351,6 +352,7 @@ extern "C" int espic_species_create(espic_world *h, double mass, double charge, 
     s->charge = charge;
     s->mpw0 = mpw0;
     s->cap = capacity;
+    s->ms = (capacity + 63) / 64 * 64;
     int64_t words = capacity / 32 + 2;
     s->ntiles = capacity / TILE_PARTICLES + 2;
     int rc = ESPIC_OK;
@@ -363,12 +365,12 @@ extern "C" int espic_species_create(espic_world *h, double mass, double charge, 
         TRY(dalloc(&s->P, 7 * (size_t)capacity));
     } else {
         int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
-        TRY(dalloc(&s->cell, capacity));
-        TRY(dalloc(&s->cell2, capacity));
-        TRY(dalloc(&s->off, 3 * (size_t)capacity));
-        TRY(dalloc(&s->off2, 3 * (size_t)capacity));
-        TRY(dalloc(&s->vel, 3 * (size_t)capacity));
-        TRY(dalloc(&s->vel2, 3 * (size_t)capacity));
+        TRY(dalloc(&s->cell, s->ms));
+        TRY(dalloc(&s->cell2, s->ms));
+        TRY(dalloc(&s->off, 3 * (size_t)s->ms));
+        TRY(dalloc(&s->off2, 3 * (size_t)s->ms));
+        TRY(dalloc(&s->vel, 3 * (size_t)s->ms));
+        TRY(dalloc(&s->vel2, 3 * (size_t)s->ms));
         TRY(dalloc(&s->sort_count, ncells + 2 + ncells / 8192 + 2));
     }
     TRY(dalloc(&s->deadmask, words));

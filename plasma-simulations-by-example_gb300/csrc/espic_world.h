@@ -18,12 +18,14 @@ struct Species {
     double mass = 0, charge = 0, mpw0 = 0;
     bool uniform_w = true; /* every particle carries mpw0: the weight row is not read */
     int64_t cap = 0;
+    int64_t ms = 0; /* mixed form: row stride of cell/off/vel, cap rounded up to 64, so every row
+                       starts 256-byte aligned for bulk copies */
     /* float64 form: [7][cap] */
     double *P = nullptr;
     /* mixed form */
     int32_t *cell = nullptr, *cell2 = nullptr;
-    float *off = nullptr, *off2 = nullptr; /* [3][cap] */
-    float *vel = nullptr, *vel2 = nullptr; /* [3][cap] */
+    float *off = nullptr, *off2 = nullptr; /* [3][ms] */
+    float *vel = nullptr, *vel2 = nullptr; /* [3][ms] */
     int32_t *sort_count = nullptr;         /* [ncells + 1] */
     /* compaction */
     uint32_t *deadmask = nullptr; /* [cap/32 + 1] */

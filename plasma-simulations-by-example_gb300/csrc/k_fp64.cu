@@ -1100,7 +1100,7 @@ void launch_compact(World &w, Species &s) {
                                                 nullptr, s.cap, rows);
     else
         k_movers<1><<<g1 * 4, 1024, 0, w.stream>>>(s.d_count, s.deadmask, s.tilepre, s.holes, nullptr, s.cell, s.off,
-                                                s.vel, s.cap, rows);
+                                                s.vel, s.ms, rows);
     w.nlaunch += 3;
 }
 
@@ -1154,7 +1154,7 @@ static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int writ
             write_w);
     else
         k_append_write<Gen, 1><<<(unsigned)blocks, 256, 0, w.stream>>>(
-            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, nullptr, s.cell, s.off, s.vel, s.cap, s.cap,
+            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, nullptr, s.cell, s.off, s.vel, s.ms, s.cap,
             0);
     w.nlaunch += 3;
     s.host_bound += ncand;

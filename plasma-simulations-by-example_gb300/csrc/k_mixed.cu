@@ -154,8 +154,62 @@ __device__ __forceinline__ void deposit_block(bool me, int32_t key, int ni, int 
     }
 }
 
+/* One particle of Species::advance in the mixed form: gather E at the cell
+ * corners from ef4 (one 16-byte load per corner), v += (q/m) E dt, move in
+ * cell units, then the walls (REFLECT: one mirror bounce per axis; ABSORB:
+ * out of the domain or inside the sphere).  A non-finite state is flagged and
+ * the particle killed.  Returns true when the particle is dead. */
+template <int WALLS>
+__device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const float4 *__restrict__ ef4, int32_t &key,
+                                                    float &fx, float &fy, float &fz, float &vx, float &vy,
+                                                    float &vz, int *err) {
+    int i, j, k;
+    unpack(key, i, j, k);
+    int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+    float w[8];
+    cic_w(fx, fy, fz, w);
+    float4 e0 = __ldg(ef4 + n0), e1 = __ldg(ef4 + n0 + 1), e2 = __ldg(ef4 + n0 + 1 + sy), e3 = __ldg(ef4 + n0 + sy),
+           e4 = __ldg(ef4 + n0 + sz), e5 = __ldg(ef4 + n0 + 1 + sz), e6 = __ldg(ef4 + n0 + 1 + sy + sz),
+           e7 = __ldg(ef4 + n0 + sy + sz);
+    float ex = w[0] * e0.x + w[1] * e1.x + w[2] * e2.x + w[3] * e3.x + w[4] * e4.x + w[5] * e5.x + w[6] * e6.x +
+               w[7] * e7.x;
+    float ey = w[0] * e0.y + w[1] * e1.y + w[2] * e2.y + w[3] * e3.y + w[4] * e4.y + w[5] * e5.y + w[6] * e6.y +
+               w[7] * e7.y;
+    float ez = w[0] * e0.z + w[1] * e1.z + w[2] * e2.z + w[3] * e3.z + w[4] * e4.z + w[5] * e5.z + w[6] * e6.z +
+               w[7] * e7.z;
+    vx += ex * a.qmdt;
+    vy += ey * a.qmdt;
+    vz += ez * a.qmdt;
+    i = advance_axis(i, fx, vx * a.dtdh[0]);
+    j = advance_axis(j, fy, vy * a.dtdh[1]);
+    k = advance_axis(k, fz, vz * a.dtdh[2]);
+    bool dead = false;
+    if (WALLS == M_REFLECT) {
+        reflect_axis(i, fx, vx, a.ni);
+        reflect_axis(j, fy, vy, a.nj);
+        reflect_axis(k, fz, vz, a.nk);
+    } else {
+        dead = i < 0 || i > a.ni - 2 || j < 0 || j > a.nj - 2 || k < 0 || k > a.nk - 2;
+        if (!dead && a.r2 >= 0.f) {
+            float rx = ((float)i + fx) * a.dh[0] + a.sx[0];
+            float ry = ((float)j + fy) * a.dh[1] + a.sx[1];
+            float rz = ((float)k + fz) * a.dh[2] + a.sx[2];
+            dead = rx * rx + ry * ry + rz * rz <= a.r2;
+        }
+    }
+    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
+        atomicOr(err, DERR_NONFINITE);
+        dead = true;
+        i = j = k = 0;
+        fx = fy = fz = 0.f;
+    }
+    key = (i & 1023) | ((j & 1023) << 10) | (k << 20);
+    return dead;
+}
+
 template <int WALLS, bool DEPOSIT>
-__global__ void __launch_bounds__(256) k_push_mixed(MixArgs a, const float4 *__restrict__ ef4, int32_t *cell,
+__global__ void __launch_bounds__(256, 5) k_push_mixed(MixArgs a, const float4 *__restrict__ ef4, int32_t *cell,
                                                     float *off, float *vel, int64_t stride,
                                                     const int64_t *__restrict__ d_count, uint32_t *deadmask,
                                                     int32_t *tiledead, unsigned long long *acc, int *err) {
@@ -166,51 +220,12 @@ __global__ void __launch_bounds__(256) k_push_mixed(MixArgs a, const float4 *__r
     int32_t key = -1;
     float fx = 0, fy = 0, fz = 0;
     if (live) {
-        int i, j, k;
-        unpack(cell[p], i, j, k);
+        key = cell[p];
         fx = off[p];
         fy = off[stride + p];
         fz = off[2 * stride + p];
         float vx = vel[p], vy = vel[stride + p], vz = vel[2 * stride + p];
-        int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
-        int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
-        float w[8];
-        cic_w(fx, fy, fz, w);
-        float4 e0 = __ldg(ef4 + n0), e1 = __ldg(ef4 + n0 + 1), e2 = __ldg(ef4 + n0 + 1 + sy),
-               e3 = __ldg(ef4 + n0 + sy), e4 = __ldg(ef4 + n0 + sz), e5 = __ldg(ef4 + n0 + 1 + sz),
-               e6 = __ldg(ef4 + n0 + 1 + sy + sz), e7 = __ldg(ef4 + n0 + sy + sz);
-        float ex = w[0] * e0.x + w[1] * e1.x + w[2] * e2.x + w[3] * e3.x + w[4] * e4.x + w[5] * e5.x +
-                   w[6] * e6.x + w[7] * e7.x;
-        float ey = w[0] * e0.y + w[1] * e1.y + w[2] * e2.y + w[3] * e3.y + w[4] * e4.y + w[5] * e5.y +
-                   w[6] * e6.y + w[7] * e7.y;
-        float ez = w[0] * e0.z + w[1] * e1.z + w[2] * e2.z + w[3] * e3.z + w[4] * e4.z + w[5] * e5.z +
-                   w[6] * e6.z + w[7] * e7.z;
-        vx += ex * a.qmdt;
-        vy += ey * a.qmdt;
-        vz += ez * a.qmdt;
-        i = advance_axis(i, fx, vx * a.dtdh[0]);
-        j = advance_axis(j, fy, vy * a.dtdh[1]);
-        k = advance_axis(k, fz, vz * a.dtdh[2]);
-        if (WALLS == M_REFLECT) {
-            reflect_axis(i, fx, vx, a.ni);
-            reflect_axis(j, fy, vy, a.nj);
-            reflect_axis(k, fz, vz, a.nk);
-        } else {
-            dead = i < 0 || i > a.ni - 2 || j < 0 || j > a.nj - 2 || k < 0 || k > a.nk - 2;
-            if (!dead && a.r2 >= 0.f) {
-                float rx = ((float)i + fx) * a.dh[0] + a.sx[0];
-                float ry = ((float)j + fy) * a.dh[1] + a.sx[1];
-                float rz = ((float)k + fz) * a.dh[2] + a.sx[2];
-                dead = rx * rx + ry * ry + rz * rz <= a.r2;
-            }
-        }
-        if (!(isfinite(fx) && isfinite(fy) && isfinite(fz) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
-            atomicOr(err, DERR_NONFINITE);
-            dead = true;
-            i = j = k = 0;
-            fx = fy = fz = 0.f;
-        }
-        key = (i & 1023) | ((j & 1023) << 10) | (k << 20);
+        dead = push_particle_mixed<WALLS>(a, ef4, key, fx, fy, fz, vx, vy, vz, err);
         cell[p] = key;
         off[p] = fx;
         off[stride + p] = fy;
@@ -471,27 +486,27 @@ static MixArgs mix_args(World &w, Species &s) {
 }
 
 template <int WALLS, bool DEP>
-static void push_mixed_as(World &w, Species &s, int blocks) {
+static void push_mixed_as(World &w, Species &s, int64_t n) {
     MixArgs a = mix_args(w, s);
-    k_push_mixed<WALLS, DEP><<<blocks, 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.cap, s.d_count,
-                                                           s.deadmask, s.tiledead, s.acc, w.d_err);
+    k_push_mixed<WALLS, DEP><<<blocks_for(n, 256), 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
+                                                                      s.d_count, s.deadmask, s.tiledead, s.acc,
+                                                                      w.d_err);
     w.nlaunch++;
 }
 
 void launch_push_mixed(World &w, Species &s, bool deposit) {
     int64_t n = s.host_bound;
     if (n <= 0) return;
-    int blocks = blocks_for(n, 256);
     if (s.walls == 0) {
         if (deposit)
-            push_mixed_as<M_REFLECT, true>(w, s, blocks);
+            push_mixed_as<M_REFLECT, true>(w, s, n);
         else
-            push_mixed_as<M_REFLECT, false>(w, s, blocks);
+            push_mixed_as<M_REFLECT, false>(w, s, n);
     } else {
         if (deposit)
-            push_mixed_as<M_ABSORB, true>(w, s, blocks);
+            push_mixed_as<M_ABSORB, true>(w, s, n);
         else
-            push_mixed_as<M_ABSORB, false>(w, s, blocks);
+            push_mixed_as<M_ABSORB, false>(w, s, n);
     }
 }
 
@@ -499,20 +514,20 @@ void launch_deposit_mixed(World &w, Species &s) {
     int64_t n = s.host_bound;
     if (n <= 0) return;
     MixArgs a = mix_args(w, s);
-    k_deposit_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(a, s.cell, s.off, s.cap, s.d_count, s.acc);
+    k_deposit_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(a, s.cell, s.off, s.ms, s.d_count, s.acc);
     w.nlaunch++;
 }
 
 void launch_to_mixed(World &w, Species &s, const double *P, int64_t stride, int64_t first, int64_t n) {
     if (n <= 0) return;
     k_to_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, P, stride, n, first, s.cell, s.off, s.vel,
-                                                          s.cap);
+                                                          s.ms);
     w.nlaunch++;
 }
 
 void launch_from_mixed(World &w, Species &s, double *P, int64_t stride, int64_t n) {
     if (n <= 0) return;
-    k_from_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.cell, s.off, s.vel, s.cap, s.d_count, s.mpw0, P,
+    k_from_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.cell, s.off, s.vel, s.ms, s.d_count, s.mpw0, P,
                                                            stride);
     w.nlaunch++;
 }
@@ -529,7 +544,7 @@ void launch_sort_mixed(World &w, Species &s) {
     k_scan_reduce<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
     k_scan_bsum<<<1, 1024, 0, w.stream>>>(bsum, nb);
     k_scan_down<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
-    k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.off, s.vel, s.cap, s.d_count, w.g.ni,
+    k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.off, s.vel, s.ms, s.d_count, w.g.ni,
                                                              w.g.nj, counts, s.cell2, s.off2, s.vel2);
     w.nlaunch += 5;
     int32_t *tc = s.cell;
@@ -545,7 +560,7 @@ void launch_sort_mixed(World &w, Species &s) {
 
 void launch_diag_mixed(World &w, Species &s, double *d_out5) {
     const int nb = 592;
-    k_diag_mixed<<<nb, 256, 0, w.stream>>>(s.vel, s.cap, s.d_count, w.d_partials, nb);
+    k_diag_mixed<<<nb, 256, 0, w.stream>>>(s.vel, s.ms, s.d_count, w.d_partials, nb);
     k_diag_mixed_final<<<1, 32, 0, w.stream>>>(w.d_partials, nb, s.mass, s.mpw0, d_out5);
     w.nlaunch += 2;
 }
