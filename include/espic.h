@@ -258,6 +258,65 @@ int espic_deposit_noalloc(const double *d_P, int64_t stride, int64_t n, int ni, 
  * diag row of espic_diag_row is also returned (one synchronisation). */
 int espic_step(espic_world *w, int sort_every, double *row, int len);
 
+/* ---- batched ensemble of independent boxes ------------------------------ */
+/* No single reference interface: an ensemble is many ch2 grounded boxes
+ * (ch2/Main.cpp:14-75: World, two Species with reflecting walls, the SOR
+ * PotentialSolver) stepped together.  Every box has its own node counts and
+ * extents; every (box, species) its own weight mpw0 and capacity.  Particles
+ * are in the mixed form.  A step runs push + deposit of all boxes in one
+ * launch over a flattened work list, then one launch in which blocks claim
+ * boxes and compute charge density, red-black SOR (float32 sweeps under a
+ * float64 residual, ch2/PotentialSolver.cpp:11-67 convergence test) and E;
+ * espic_ensemble_step replays the step as a captured CUDA graph. */
+typedef struct espic_ensemble espic_ensemble;
+/* nodes[3*b..], x0[3*b..], xm[3*b..] per box; mass[s], charge[s] per species;
+ * mpw0[b*nspecies + s] and capacity[b*nspecies + s] per box and species */
+int espic_ensemble_create(int nbox, const int32_t *nodes, const double *x0, const double *xm, int nspecies,
+                          const double *mass, const double *charge, const double *mpw0, const int64_t *capacity,
+                          double dt, espic_ensemble **out);
+void espic_ensemble_destroy(espic_ensemble *e);
+int espic_ensemble_set_seed(espic_ensemble *e, uint64_t seed);
+/* particles of (box, species) from a host [7][stride] float64 block (replaces
+ * the segment); the weight row is ignored (the segment's mpw0 is used) */
+int espic_ensemble_set_particles(espic_ensemble *e, int box, int sp, const double *P, int64_t stride, int64_t n);
+/* P = NULL returns the count only */
+int espic_ensemble_get_particles(espic_ensemble *e, int box, int sp, double *P, int64_t stride, int64_t cap,
+                                 int64_t *n);
+/* Species::loadParticlesBox (ch2/Species.cpp:74-97) on the GPU: num_mp
+ * particles uniform in [x1, x2) from the ensemble's Philox stream, v = 0 */
+int espic_ensemble_load_box(espic_ensemble *e, int box, int sp, const double x1[3], const double x2[3],
+                            int64_t num_mp);
+/* SOR controls shared by every box; omega = 0 selects each box's optimal
+ * red-black factor (Young), omega in (0, 2) is used as given (the reference
+ * hard-codes 1.4) */
+int espic_ensemble_set_solver(espic_ensemble *e, int max_it, double tol, double omega);
+/* launch shape: particles per work item (>= 256), push block (128/256/512),
+ * solve block (256/512/1024); results do not depend on it */
+int espic_ensemble_set_launch(espic_ensemble *e, int chunk, int push_threads, int solve_threads);
+int espic_ensemble_get_launch(espic_ensemble *e, int *chunk, int *push_threads, int *solve_threads);
+/* times every launch shape on real steps and keeps the fastest (consumes 18
+ * steps of the run; results do not depend on the shape) */
+int espic_ensemble_autotune(espic_ensemble *e, int *chunk, int *push_threads, int *solve_threads, double *push_ms,
+                            double *solve_ms);
+/* deposit, charge density, solve and E: the state before the first step */
+int espic_ensemble_prepare(espic_ensemble *e);
+/* nsteps steps through the captured step graph (asynchronous) */
+int espic_ensemble_step(espic_ensemble *e, int nsteps);
+/* the same steps as direct launches */
+int espic_ensemble_step_direct(espic_ensemble *e, int nsteps);
+int espic_ensemble_sync(espic_ensemble *e);
+void *espic_ensemble_stream(espic_ensemble *e);
+int espic_ensemble_launches(espic_ensemble *e, int64_t *n);
+int espic_ensemble_steps_taken(espic_ensemble *e, int64_t *steps);
+/* per box: sweeps and convergence of the last solve, its float64 residual */
+int espic_ensemble_status(espic_ensemble *e, int32_t *sweeps, int32_t *converged, double *residual);
+/* ESPIC_FIELD_PHI, _RHO, _EF ([nn][3]) or _DEN (of species sp) of one box */
+int espic_ensemble_read(espic_ensemble *e, int box, int field, int sp, double *out);
+/* out[b*(nspecies+1) + s]: kinetic energy of species s, out[b*(nspecies+1) +
+ * nspecies]: field energy (getKE, ch2/Species.cpp:144-168; getPE,
+ * ch2/World.cpp:72-84) */
+int espic_ensemble_diag(espic_ensemble *e, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -118,11 +118,34 @@ def lib():
             "espic_profile": [VP, C.c_int],
             "espic_profile_read": [VP, PD, C.POINTER(I64), C.POINTER(I64)],
             "espic_solver_totals": [VP, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)],
+            "espic_ensemble_create": [C.c_int, PI, PD, PD, C.c_int, PD, PD, PD, C.POINTER(I64), C.c_double,
+                                      C.POINTER(VP)],
+            "espic_ensemble_set_seed": [VP, C.c_uint64],
+            "espic_ensemble_set_particles": [VP, C.c_int, C.c_int, PD, I64, I64],
+            "espic_ensemble_get_particles": [VP, C.c_int, C.c_int, PD, I64, I64, C.POINTER(I64)],
+            "espic_ensemble_load_box": [VP, C.c_int, C.c_int, PD, PD, I64],
+            "espic_ensemble_set_solver": [VP, C.c_int, C.c_double, C.c_double],
+            "espic_ensemble_set_launch": [VP, C.c_int, C.c_int, C.c_int],
+            "espic_ensemble_get_launch": [VP, PI, PI, PI],
+            "espic_ensemble_autotune": [VP, PI, PI, PI, PD, PD],
+            "espic_ensemble_prepare": [VP],
+            "espic_ensemble_step": [VP, C.c_int],
+            "espic_ensemble_step_direct": [VP, C.c_int],
+            "espic_ensemble_sync": [VP],
+            "espic_ensemble_launches": [VP, C.POINTER(I64)],
+            "espic_ensemble_steps_taken": [VP, C.POINTER(I64)],
+            "espic_ensemble_status": [VP, PI, PI, PD],
+            "espic_ensemble_read": [VP, C.c_int, C.c_int, C.c_int, PD],
+            "espic_ensemble_diag": [VP, PD],
         }
         for name, args in sigs.items():
             f = getattr(L, name)
             f.argtypes = args
             f.restype = C.c_int
+        L.espic_ensemble_destroy.argtypes = [VP]
+        L.espic_ensemble_destroy.restype = None
+        L.espic_ensemble_stream.argtypes = [VP]
+        L.espic_ensemble_stream.restype = VP
         _lib = L
     return _lib
 
@@ -424,3 +447,119 @@ class PotentialSolver:
 
     def computeEF(self):
         check(lib().espic_efield(self.world.h))
+
+
+class Ensemble:
+    """A batched ensemble of independent ch2 grounded boxes (ch2/Main.cpp:14-75
+    per member): per-box node counts and extents, per (box, species) weights
+    and capacities, stepped together on one GPU (see espic_ensemble_* in
+    include/espic.h)."""
+
+    def __init__(self, nodes, x0, xm, mass, charge, mpw0, capacity, dt):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32).reshape(-1, 3)
+        nbox = nodes.shape[0]
+        x0 = np.ascontiguousarray(np.broadcast_to(np.asarray(x0, dtype=np.float64), (nbox, 3)))
+        xm = np.ascontiguousarray(np.broadcast_to(np.asarray(xm, dtype=np.float64), (nbox, 3)))
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        charge = np.ascontiguousarray(charge, dtype=np.float64)
+        nsp = mass.size
+        mpw0 = np.ascontiguousarray(np.broadcast_to(np.asarray(mpw0, dtype=np.float64), (nbox, nsp)))
+        capacity = np.ascontiguousarray(np.broadcast_to(np.asarray(capacity, dtype=np.int64), (nbox, nsp)))
+        h = VP()
+        check(lib().espic_ensemble_create(nbox, nodes.ctypes.data_as(PI), _pd(x0), _pd(xm), nsp, _pd(mass),
+                                          _pd(charge), _pd(mpw0), capacity.ctypes.data_as(C.POINTER(I64)), dt,
+                                          C.byref(h)))
+        self.h = h
+        self.nodes, self.x0, self.xm = nodes, x0, xm
+        self.nbox, self.nsp = nbox, nsp
+        self.mass, self.charge, self.mpw0 = mass, charge, mpw0
+
+    def close(self):
+        if self.h:
+            lib().espic_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_seed(self, seed):
+        check(lib().espic_ensemble_set_seed(self.h, seed))
+
+    def set_particles(self, box, sp, P):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        check(lib().espic_ensemble_set_particles(self.h, box, sp, _pd(P), P.shape[1], P.shape[1]))
+
+    def particles(self, box, sp, cap=None):
+        n = I64()
+        check(lib().espic_ensemble_get_particles(self.h, box, sp, None, 0, 0, C.byref(n)))
+        P = np.zeros((7, max(n.value, 1)))
+        check(lib().espic_ensemble_get_particles(self.h, box, sp, _pd(P), P.shape[1], P.shape[1],
+                                                 C.byref(n)))
+        return np.ascontiguousarray(P[:, :n.value])
+
+    def load_box(self, box, sp, x1, x2, num_mp):
+        check(lib().espic_ensemble_load_box(self.h, box, sp, _d3(x1), _d3(x2), int(num_mp)))
+
+    def set_solver(self, max_it=10000, tol=1e-4, omega=0.0):
+        check(lib().espic_ensemble_set_solver(self.h, max_it, tol, omega))
+
+    def set_launch(self, chunk, push_threads, solve_threads):
+        check(lib().espic_ensemble_set_launch(self.h, chunk, push_threads, solve_threads))
+
+    def get_launch(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().espic_ensemble_get_launch(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def autotune(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        pm, sm = C.c_double(), C.c_double()
+        check(lib().espic_ensemble_autotune(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(pm),
+                                            C.byref(sm)))
+        return dict(chunk=a.value, push_threads=b.value, solve_threads=c.value, push_ms=pm.value,
+                    solve_ms=sm.value)
+
+    def prepare(self):
+        check(lib().espic_ensemble_prepare(self.h))
+
+    def step(self, nsteps=1, graph=True):
+        f = lib().espic_ensemble_step if graph else lib().espic_ensemble_step_direct
+        check(f(self.h, nsteps))
+
+    def sync(self):
+        check(lib().espic_ensemble_sync(self.h))
+
+    def stream_handle(self):
+        return lib().espic_ensemble_stream(self.h)
+
+    def launches(self):
+        n = I64()
+        check(lib().espic_ensemble_launches(self.h, C.byref(n)))
+        return n.value
+
+    def status(self):
+        it = np.zeros(self.nbox, dtype=np.int32)
+        cv = np.zeros(self.nbox, dtype=np.int32)
+        res = np.zeros(self.nbox)
+        check(lib().espic_ensemble_status(self.h, it.ctypes.data_as(PI), cv.ctypes.data_as(PI), _pd(res)))
+        return it, cv.astype(bool), res
+
+    def read(self, box, field, sp=0):
+        nn = int(np.prod(self.nodes[box]))
+        out = np.zeros(nn * (3 if field == FIELD_EF else 1))
+        check(lib().espic_ensemble_read(self.h, box, field, sp, _pd(out)))
+        return out.reshape(nn, 3) if field == FIELD_EF else out
+
+    def diag(self):
+        out = np.zeros((self.nbox, self.nsp + 1))
+        check(lib().espic_ensemble_diag(self.h, _pd(out)))
+        return out

@@ -25,6 +25,7 @@ UNITS = {
     "k_mixed.cu": [],
     "k_pcg.cu": [],
     "noalloc.cu": ["-fmad=false"],
+    "k_ensemble.cu": ["-fmad=false"],
 }
 
 

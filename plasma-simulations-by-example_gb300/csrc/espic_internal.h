@@ -80,6 +80,34 @@ __host__ __device__ inline double philox_uniform(uint64_t seed, uint64_t stream,
     return (index & 1) ? u53(c[2], c[3]) : u53(c[0], c[1]);
 }
 
+/* ---------------- batched ensemble of independent boxes ---------------- */
+/* One box: its geometry and where its nodes sit in the concatenated node
+ * fields of the ensemble. */
+struct EnsBox {
+    Geo g;
+    int64_t node0; /* first node of the box in the concatenated node fields */
+    int64_t nn;
+    double omega;  /* red-black SOR relaxation factor */
+    float dtdh[3]; /* dt / dh per axis */
+    int pad;
+};
+
+/* The particles of one species in one box: rows [p0, p0 + n) of the
+ * concatenated mixed-form particle rows. */
+struct EnsSeg {
+    int box, sp;
+    int64_t p0, n, cap;
+    double unit; /* real particles per deposit count: mpw0 * 2^-23 */
+    double q;    /* charge */
+    float qmdt;  /* q / m dt */
+    int pad;
+};
+
+struct EnsStat {
+    int sweeps, converged;
+    double residual;
+};
+
 /* ---------------- launchers (stream-ordered, asynchronous) ------------- */
 struct Species;
 struct World;
@@ -122,6 +150,13 @@ void launch_to_mixed(World &w, Species &s, const double *P, int64_t stride, int6
 void launch_from_mixed(World &w, Species &s, double *P, int64_t stride, int64_t n);
 void launch_sort_mixed(World &w, Species &s);
 void launch_diag_mixed(World &w, Species &s, double *d_out5);
+void launch_ens_push(cudaStream_t st, bool push, int blocks, int threads, const EnsBox *boxes, const EnsSeg *segs,
+                     const int4 *work, int nwork, const float4 *ef4, int32_t *cell, float *off, float *vel,
+                     int64_t stride, unsigned long long *acc, int64_t total_nodes, int *err);
+void launch_to_mixed_raw(cudaStream_t st, const Geo &g, const double *P, int64_t pstride, int64_t n, int64_t first,
+                         int32_t *cell, float *off, float *vel, int64_t stride);
+void launch_from_mixed_raw(cudaStream_t st, const Geo &g, const int32_t *cell, const float *off, const float *vel,
+                           int64_t stride, int64_t first, int64_t n, double w0, double *P, int64_t pstride);
 
 /* k_pcg.cu */
 int launch_newton_pcg(World &w, bool fp32_inner);

@@ -261,6 +261,99 @@ __global__ void __launch_bounds__(256) k_deposit_mixed(MixArgs a, const int32_t 
     deposit_block(me, key, a.ni, a.nj, fx, fy, fz, acc);
 }
 
+/* ---------------------------------------------------------------------- */
+/* Batched ensemble: push (reflecting walls, the ch2 box) and CIC deposit of
+ * every box and species in one launch over a flattened work list.  Work item
+ * w = (segment, first particle, count) lies inside one species of one box;
+ * blocks take items w = blockIdx.x, + gridDim.x, ...  The particle arithmetic
+ * is push_particle_mixed, the deposit the same 2^-23 fixed-point counts as
+ * deposit_block, so a box of the ensemble evolves bit for bit like the same
+ * box run as a World.  With PUSH false the items are only deposited. */
+template <bool PUSH>
+__global__ void __launch_bounds__(512) k_ens_push(const EnsBox *__restrict__ boxes, const EnsSeg *__restrict__ segs,
+                                                  const int4 *__restrict__ work, int nwork,
+                                                  const float4 *__restrict__ ef4, int32_t *cell, float *off,
+                                                  float *vel, int64_t stride, unsigned long long *acc,
+                                                  int64_t total_nodes, int *err) {
+    for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
+        const int4 W = work[wi];
+        const EnsSeg sg = segs[W.x];
+        const EnsBox B = boxes[sg.box];
+        MixArgs a;
+        a.ni = B.g.ni;
+        a.nj = B.g.nj;
+        a.nk = B.g.nk;
+        a.qmdt = sg.qmdt;
+        for (int d = 0; d < 3; d++) {
+            a.dtdh[d] = B.dtdh[d];
+            a.dh[d] = (float)B.g.dh[d];
+            a.sx[d] = 0.f;
+        }
+        a.r2 = -1.f;
+        const float4 *E = ef4 + B.node0;
+        unsigned long long *A = acc + (int64_t)sg.sp * total_nodes + B.node0;
+        const int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+        for (int q = threadIdx.x; q < W.z; q += blockDim.x) {
+            const int64_t p = sg.p0 + W.y + q;
+            int32_t key = cell[p];
+            float fx = off[p], fy = off[stride + p], fz = off[2 * stride + p];
+            bool dead = false;
+            if (PUSH) {
+                float vx = vel[p], vy = vel[stride + p], vz = vel[2 * stride + p];
+                dead = push_particle_mixed<M_REFLECT>(a, E, key, fx, fy, fz, vx, vy, vz, err);
+                cell[p] = key;
+                off[p] = fx;
+                off[stride + p] = fy;
+                off[2 * stride + p] = fz;
+                vel[p] = vx;
+                vel[stride + p] = vy;
+                vel[2 * stride + p] = vz;
+            }
+            if (dead) continue;
+            int i, j, k;
+            unpack(key, i, j, k);
+            const int64_t n0 = (int64_t)k * sz + (int64_t)j * sy + i;
+            const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                    n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+            float w[8];
+            cic_w(fx, fy, fz, w);
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                unsigned qc = __float2uint_rn(w[c] * MIX_Q);
+                if (qc) atomicAdd(A + idx[c], (unsigned long long)qc);
+            }
+        }
+    }
+}
+
+void launch_ens_push(cudaStream_t st, bool push, int blocks, int threads, const EnsBox *boxes, const EnsSeg *segs,
+                     const int4 *work, int nwork, const float4 *ef4, int32_t *cell, float *off, float *vel,
+                     int64_t stride, unsigned long long *acc, int64_t total_nodes, int *err) {
+    if (nwork <= 0) return;
+    if (push)
+        k_ens_push<true><<<blocks, threads, 0, st>>>(boxes, segs, work, nwork, ef4, cell, off, vel, stride, acc,
+                                                     total_nodes, err);
+    else
+        k_ens_push<false><<<blocks, threads, 0, st>>>(boxes, segs, work, nwork, ef4, cell, off, vel, stride, acc,
+                                                      total_nodes, err);
+}
+
+/* mixed form -> float64 block for n particles from row `first` */
+__global__ void k_from_mixed_n(Geo g, const int32_t *__restrict__ cell, const float *__restrict__ off,
+                               const float *__restrict__ vel, int64_t stride, int64_t first, int64_t n, double w0,
+                               double *P, int64_t pstride) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int64_t p = first + t;
+    int i[3];
+    unpack(cell[p], i[0], i[1], i[2]);
+    for (int d = 0; d < 3; d++) {
+        P[d * pstride + t] = g.x0[d] + ((double)i[d] + (double)off[d * stride + p]) * g.dh[d];
+        P[(3 + d) * pstride + t] = (double)vel[d * stride + p];
+    }
+    P[6 * pstride + t] = w0;
+}
+
 /* float64 block -> mixed form (World::XtoL in float64, then split) */
 __global__ void k_to_mixed(Geo g, const double *__restrict__ P, int64_t pstride, int64_t n, int64_t first,
                            int32_t *cell, float *off, float *vel, int64_t stride) {
@@ -523,6 +616,18 @@ void launch_to_mixed(World &w, Species &s, const double *P, int64_t stride, int6
     k_to_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, P, stride, n, first, s.cell, s.off, s.vel,
                                                           s.ms);
     w.nlaunch++;
+}
+
+void launch_to_mixed_raw(cudaStream_t st, const Geo &g, const double *P, int64_t pstride, int64_t n, int64_t first,
+                         int32_t *cell, float *off, float *vel, int64_t stride) {
+    if (n <= 0) return;
+    k_to_mixed<<<blocks_for(n, 256), 256, 0, st>>>(g, P, pstride, n, first, cell, off, vel, stride);
+}
+
+void launch_from_mixed_raw(cudaStream_t st, const Geo &g, const int32_t *cell, const float *off, const float *vel,
+                           int64_t stride, int64_t first, int64_t n, double w0, double *P, int64_t pstride) {
+    if (n <= 0) return;
+    k_from_mixed_n<<<blocks_for(n, 256), 256, 0, st>>>(g, cell, off, vel, stride, first, n, w0, P, pstride);
 }
 
 void launch_from_mixed(World &w, Species &s, double *P, int64_t stride, int64_t n) {
