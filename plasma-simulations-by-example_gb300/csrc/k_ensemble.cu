@@ -50,6 +50,19 @@ namespace espic {
 constexpr int ENS_VW = 1024;      /* virtual width of the deterministic reductions */
 constexpr int ENS_SWEEPS = 25;    /* float32 sweeps between float64 residual checks */
 
+/* a / b correctly rounded, given y = RN(1/b) for b > 0: q = a y, the exact
+ * remainder r = a - b q (one FMA) and q + r y rounded, Markstein's
+ * correction (P. Markstein, IBM J. Res. Develop. 34(1), 1990), which yields
+ * the correctly rounded quotient for normal operands; a = +-0 returns a y,
+ * the zero of the right sign.  Three float64 operations instead of a
+ * division, whose cost the GB300's float64 rate makes dominant. */
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+    const double q = a * y;
+    const double r = __fma_rn(-q, b, a);
+    const double q2 = __fma_rn(r, y, q);
+    return a == 0.0 ? q : q2;
+}
+
 /* sum of part[0..ENS_VW) in a fixed tree; every thread gets the total */
 __device__ double ens_tree_sum(double *part) {
     __syncthreads();
@@ -70,29 +83,58 @@ __device__ __forceinline__ double ens_node_volume(const Geo &g, int i, int j, in
     return V;
 }
 
-/* E at node u = (i, j, k) of a box, the differences of k_efield */
-__device__ __forceinline__ void ens_efield(const Geo &g, const double *phi, int64_t u, int i, int j, int k,
-                                           double &e0, double &e1, double &e2) {
+/* d / node_vol: node_vol = V0 2^-h (h boundary halvings), so the quotient is
+ * the correctly rounded d / V0 scaled by 2^h, exactly */
+__device__ __forceinline__ double ens_per_volume(const Geo &g, int i, int j, int k, double d, double V0,
+                                                 double yV0) {
+    double scale = 1.0;
+    if (i == 0 || i == g.ni - 1) scale *= 2.0;
+    if (j == 0 || j == g.nj - 1) scale *= 2.0;
+    if (k == 0 || k == g.nk - 1) scale *= 2.0;
+    return div_rcp(d, V0, yV0) * scale;
+}
+
+/* reciprocals of 2 dh per axis: the divisors of the E differences */
+struct EfRcp {
+    double d2[3], y2[3];
+};
+
+__device__ __forceinline__ EfRcp ef_rcp(const Geo &g) {
+    EfRcp r;
+    for (int d = 0; d < 3; d++) {
+        r.d2[d] = 2 * g.dh[d];
+        r.y2[d] = 1.0 / r.d2[d];
+    }
+    return r;
+}
+
+/* E at node u = (i, j, k) of a box, the differences of k_efield (the same
+ * numerators; the division by 2 dh correctly rounded through div_rcp) */
+__device__ __forceinline__ void ens_efield(const Geo &g, const EfRcp &rc, const double *phi, int64_t u, int i, int j,
+                                           int k, double &e0, double &e1, double &e2) {
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
-    const double dx = g.dh[0], dy = g.dh[1], dz = g.dh[2];
+    double n0, n1, n2;
     if (i == 0)
-        e0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]) / (2 * dx);
+        n0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]);
     else if (i == g.ni - 1)
-        e0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]) / (2 * dx);
+        n0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]);
     else
-        e0 = -(phi[u + 1] - phi[u - 1]) / (2 * dx);
+        n0 = -(phi[u + 1] - phi[u - 1]);
     if (j == 0)
-        e1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]) / (2 * dy);
+        n1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]);
     else if (j == g.nj - 1)
-        e1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]) / (2 * dy);
+        n1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]);
     else
-        e1 = -(phi[u + sy] - phi[u - sy]) / (2 * dy);
+        n1 = -(phi[u + sy] - phi[u - sy]);
     if (k == 0)
-        e2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]) / (2 * dz);
+        n2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]);
     else if (k == g.nk - 1)
-        e2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]) / (2 * dz);
+        n2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]);
     else
-        e2 = -(phi[u + sz] - phi[u - sz]) / (2 * dz);
+        n2 = -(phi[u + sz] - phi[u - sz]);
+    e0 = div_rcp(n0, rc.d2[0], rc.y2[0]);
+    e1 = div_rcp(n1, rc.d2[1], rc.y2[1]);
+    e2 = div_rcp(n2, rc.d2[2], rc.y2[2]);
 }
 
 __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ boxes, const EnsSeg *__restrict__ segs,
@@ -120,15 +162,16 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
         float *R = res + B.node0;
         /* 1. rho = sum_s q_s den_s, den_s = counts * unit_s / node_vol; the
          *    accumulators are cleared for the next deposit */
+        const double V0 = g.dh[0] * g.dh[1] * g.dh[2];
+        const double yV0 = 1.0 / V0;
         for (int64_t u = tid; u < nn; u += nt) {
             const int i = (int)(u % ni), j = (int)((u / ni) % nj), k = (int)(u / ((int64_t)ni * nj));
-            const double V = ens_node_volume(g, i, j, k);
             double r = 0;
             for (int s = 0; s < nsp; s++) {
                 const EnsSeg &sg = segs[bid * nsp + s];
                 unsigned long long *A = acc + (int64_t)s * total_nodes + B.node0;
                 const double d = __ll2double_rn((long long)A[u]) * sg.unit;
-                const double den = (V != 0) ? d / V : 0.0;
+                const double den = ens_per_volume(g, i, j, k, d, V0, yV0);
                 A[u] = 0ull;
                 if (sg.q != 0) r += den * sg.q;
             }
@@ -142,7 +185,8 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
         const double idy2 = 1.0 / (g.dh[1] * g.dh[1]);
         const double idz2 = 1.0 / (g.dh[2] * g.dh[2]);
         const double D = 2 * idx2 + 2 * idy2 + 2 * idz2;
-        const float fcx = (float)idx2, fcy = (float)idy2, fcz = (float)idz2, fD = (float)D;
+        const float fcx = (float)idx2, fcy = (float)idy2, fcz = (float)idz2, fiD = (float)(1.0 / D);
+        const double yeps = 1.0 / ENS_EPS_0;
         const float fw = (float)B.omega;
         const int sy = ni, sz = ni * nj;
         const int hx = (ni - 2 + 1) / 2;
@@ -159,7 +203,7 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
                     const int j = 1 + r % (nj - 2);
                     const int k = 1 + r / (nj - 2);
                     const int u = (k * nj + j) * ni + i;
-                    const double Ru = -ph[u] * D + rh[u] / ENS_EPS_0 + idx2 * (ph[u - 1] + ph[u + 1]) +
+                    const double Ru = -ph[u] * D + div_rcp(rh[u], ENS_EPS_0, yeps) + idx2 * (ph[u - 1] + ph[u + 1]) +
                                       idy2 * (ph[u - sy] + ph[u + sy]) + idz2 * (ph[u - sz] + ph[u + sz]);
                     R[u] = (float)Ru;
                     e[u] = 0.f;
@@ -178,26 +222,48 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
                 break;
             }
             if (sweeps >= max_it) break;
-            const int ns = max_it - sweeps < ENS_SWEEPS ? max_it - sweeps : ENS_SWEEPS;
-            for (int s = 0; s < ns; s++) {
-                for (int c = 0; c < 2; c++) {
-                    for (int t = tid; t < count; t += nt) {
-                        const int i2 = t % hx;
-                        const int r = t / hx;
-                        const int j = 1 + r % (nj - 2);
-                        const int k = 1 + r / (nj - 2);
-                        const int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
-                        if (i > ni - 2) continue;
-                        const int u = (k * nj + j) * ni + i;
-                        const float en = (R[u] + fcx * (e[u - 1] + e[u + 1]) + fcy * (e[u - sy] + e[u + sy]) +
-                                          fcz * (e[u - sz] + e[u + sz])) /
-                                         fD;
-                        e[u] = e[u] + fw * (en - e[u]);
+            /* ENS_SWEEPS float32 sweeps of L e = -R, then phi += e and the
+             * float64 residual decides again */
+            {
+                const int ns = max_it - sweeps < ENS_SWEEPS ? max_it - sweeps : ENS_SWEEPS;
+                for (int s = 0; s < ns; s++) {
+                    for (int c = 0; c < 2; c++) {
+                        /* four independent nodes of colour c per thread: all
+                         * loads before any store */
+                        for (int tb = tid; tb < count; tb += 4 * nt) {
+                            int uq[4];
+                            float eo[4], sum[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                const int t = tb + q * nt;
+                                uq[q] = -1;
+                                eo[q] = 0.f;
+                                sum[q] = 0.f;
+                                if (t >= count) continue;
+                                const int i2 = t % hx;
+                                const int r = t / hx;
+                                const int j = 1 + r % (nj - 2);
+                                const int k = 1 + r / (nj - 2);
+                                const int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
+                                if (i > ni - 2) continue;
+                                const int u = (k * nj + j) * ni + i;
+                                uq[q] = u;
+                                eo[q] = e[u];
+                                sum[q] = R[u] + fcx * (e[u - 1] + e[u + 1]) + fcy * (e[u - sy] + e[u + sy]) +
+                                         fcz * (e[u - sz] + e[u + sz]);
+                            }
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                if (uq[q] < 0) continue;
+                                const float en = sum[q] * fiD;
+                                e[uq[q]] = eo[q] + fw * (en - eo[q]);
+                            }
+                        }
+                        __syncthreads();
                     }
-                    __syncthreads();
                 }
+                sweeps += ns;
             }
-            sweeps += ns;
             for (int t = tid; t < interior; t += nt) {
                 const int i = 1 + t % (ni - 2);
                 const int r = t / (ni - 2);
@@ -209,10 +275,11 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
             __syncthreads();
         }
         /* 3. E = -grad phi, float32 copy for the push */
+        const EfRcp rc = ef_rcp(g);
         for (int64_t u = tid; u < nn; u += nt) {
             const int i = (int)(u % ni), j = (int)((u / ni) % nj), k = (int)(u / ((int64_t)ni * nj));
             double e0, e1, e2;
-            ens_efield(g, ph, u, i, j, k, e0, e1, e2);
+            ens_efield(g, rc, ph, u, i, j, k, e0, e1, e2);
             ef4[B.node0 + u] = make_float4((float)e0, (float)e1, (float)e2, 0.f);
         }
         if (tid == 0) {
@@ -231,7 +298,7 @@ __global__ void k_ens_efield64(Geo g, const double *__restrict__ phi, double *ef
     if (u >= nn) return;
     const int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
     double e0, e1, e2;
-    ens_efield(g, phi, u, i, j, k, e0, e1, e2);
+    ens_efield(g, ef_rcp(g), phi, u, i, j, k, e0, e1, e2);
     ef[3 * u] = e0;
     ef[3 * u + 1] = e1;
     ef[3 * u + 2] = e2;
@@ -243,9 +310,9 @@ __global__ void k_ens_density(Geo g, const unsigned long long *__restrict__ acc,
     int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     if (u >= nn) return;
     const int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
-    const double V = ens_node_volume(g, i, j, k);
+    const double V0 = g.dh[0] * g.dh[1] * g.dh[2];
     const double d = __ll2double_rn((long long)acc[u]) * unit;
-    den[u] = (V != 0) ? d / V : 0.0;
+    den[u] = ens_per_volume(g, i, j, k, d, V0, 1.0 / V0);
 }
 
 /* loadParticlesBox (ch2/Species.cpp:74-97) into a segment: x = x1 + U (x2 -
@@ -298,12 +365,13 @@ __global__ void __launch_bounds__(256) k_ens_diag(const EnsBox *__restrict__ box
         if (threadIdx.x == 0) out[bid * ncol + s] = 0.5 * mass[s] * mpw[bid * nsp + s] * t;
     }
     const double *ph = phi + B.node0;
+    const EfRcp rc = ef_rcp(g);
     for (int v = threadIdx.x; v < ENS_VW; v += blockDim.x) {
         double a = 0;
         for (int64_t u = v; u < B.nn; u += ENS_VW) {
             const int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
             double e0, e1, e2;
-            ens_efield(g, ph, u, i, j, k, e0, e1, e2);
+            ens_efield(g, rc, ph, u, i, j, k, e0, e1, e2);
             a += (e0 * e0 + e1 * e1 + e2 * e2) * ens_node_volume(g, i, j, k);
         }
         part[v] = a;

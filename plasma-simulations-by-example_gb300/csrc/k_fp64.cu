@@ -578,9 +578,24 @@ __global__ void __launch_bounds__(256) k_append_write(Geo g, Gen gen, int64_t nc
 }
 
 /* ------------------------------------------------------------------------ */
+/* a / b correctly rounded, given y = RN(1/b) for b > 0: q = a y, the exact
+ * remainder r = a - b q (one FMA), then q + r y rounded -- Markstein's
+ * correction (P. Markstein, IBM J. Res. Develop. 34(1), 1990), which yields
+ * the correctly rounded quotient for normal operands, so results equal the
+ * division's bit for bit; a = +-0 returns a y, the zero of the right sign.
+ * Three float64 operations instead of a division: the GB300's float64 rate
+ * makes the division dominate the kernels below. */
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+    const double q = a * y;
+    const double r = __fma_rn(-q, b, a);
+    const double q2 = __fma_rn(r, y, q);
+    return a == 0.0 ? q : q2;
+}
+
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
  * central inside.  Also writes the float32 copy used by the mixed push. */
-__global__ void __launch_bounds__(256) k_efield(Geo g, const double *__restrict__ phi, double *ef, float4 *ef4) {
+__global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double *__restrict__ phi, double *ef,
+                                                float4 *ef4) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     if (u >= nn) return;
@@ -588,26 +603,29 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, const double *__restrict_
     int j = (int)((u / g.ni) % g.nj);
     int k = (int)(u / ((int64_t)g.ni * g.nj));
     int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
-    double dx = g.dh[0], dy = g.dh[1], dz = g.dh[2];
-    double e0, e1, e2;
+    const double d2x = 2 * g.dh[0], d2y = 2 * g.dh[1], d2z = 2 * g.dh[2];
+    double n0, n1, n2;
     if (i == 0)
-        e0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]) / (2 * dx);
+        n0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]);
     else if (i == g.ni - 1)
-        e0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]) / (2 * dx);
+        n0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]);
     else
-        e0 = -(phi[u + 1] - phi[u - 1]) / (2 * dx);
+        n0 = -(phi[u + 1] - phi[u - 1]);
     if (j == 0)
-        e1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]) / (2 * dy);
+        n1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]);
     else if (j == g.nj - 1)
-        e1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]) / (2 * dy);
+        n1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]);
     else
-        e1 = -(phi[u + sy] - phi[u - sy]) / (2 * dy);
+        n1 = -(phi[u + sy] - phi[u - sy]);
     if (k == 0)
-        e2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]) / (2 * dz);
+        n2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]);
     else if (k == g.nk - 1)
-        e2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]) / (2 * dz);
+        n2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]);
     else
-        e2 = -(phi[u + sz] - phi[u - sz]) / (2 * dz);
+        n2 = -(phi[u + sz] - phi[u - sz]);
+    const double e0 = div_rcp(n0, d2x, y2.x);
+    const double e1 = div_rcp(n1, d2y, y2.y);
+    const double e2 = div_rcp(n2, d2z, y2.z);
     ef[3 * u] = e0;
     ef[3 * u + 1] = e1;
     ef[3 * u + 2] = e2;
@@ -1040,7 +1058,9 @@ void launch_targets(World &w) {
 void launch_efield(World &w) {
     bool mixed = false;
     for (Species *s : w.species) mixed |= (s->form == 1);
-    k_efield<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.phi, w.ef, mixed ? w.ef4 : nullptr);
+    /* RN(1 / (2 dh)) per axis, for div_rcp */
+    double3 y2 = make_double3(1.0 / (2 * w.g.dh[0]), 1.0 / (2 * w.g.dh[1]), 1.0 / (2 * w.g.dh[2]));
+    k_efield<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, mixed ? w.ef4 : nullptr);
     w.nlaunch++;
     if (mixed) w.ef4_valid = true;
     else w.ef4_valid = false;
