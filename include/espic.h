@@ -317,6 +317,33 @@ int espic_ensemble_read(espic_ensemble *e, int box, int field, int sp, double *o
  * ch2/World.cpp:72-84) */
 int espic_ensemble_diag(espic_ensemble *e, double *out);
 
+/* ---- differentiable sphere run --------------------------------------------- */
+/* No reference counterpart.  One ion species in a World that has its sphere
+ * and inlet and Boltzmann reference values set (the Newton-PCG controls of
+ * espic_solver_set_newton apply), stepped without injection.  Absorption is
+ * the C1 factor of an absorbing layer of thickness delta just inside the
+ * sphere and every face (delta -> 0 is the reference's removal,
+ * ch3/ver2/Species.cpp:26-33).  Loss = alpha * field energy of the final
+ * potential (World::getPE, ch2/World.cpp:72-84) + beta * ions in the wake
+ * box (nodes with z in [wake_z0, wake_z1], CIC weights).  Gradients come from
+ * hand-written adjoint kernels of push, gather, deposit, E stencil and solve
+ * (the adjoint solve is the Newton-PCG kernel in linear mode), with
+ * checkpoints every checkpoint_every steps and recompute.  precision 0:
+ * float64 particles and adjoints, 1: float32 (solves keep float64 outer
+ * iterations). */
+typedef struct espic_diff espic_diff;
+int espic_diff_create(espic_world *w, int precision, double mass, double charge, double mpw0, int64_t n,
+                      double delta, double wake_z0, double wake_z1, double alpha, double beta,
+                      int checkpoint_every, espic_diff **out);
+void espic_diff_destroy(espic_diff *d);
+/* initial positions x[3][n] and velocities v[3][n] */
+int espic_diff_set_state(espic_diff *d, const double *x, const double *v);
+/* nsteps steps with the sphere at phi_sphere; *loss receives the loss */
+int espic_diff_forward(espic_diff *d, double phi_sphere, int nsteps, double *loss);
+/* gradients of the last forward's loss with respect to phi_sphere, x[3][n]
+ * and v[3][n] (NULL to skip one) */
+int espic_diff_backward(espic_diff *d, double *dloss_dphi_sphere, double *dloss_dx, double *dloss_dv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -137,6 +137,11 @@ def lib():
             "espic_ensemble_status": [VP, PI, PI, PD],
             "espic_ensemble_read": [VP, C.c_int, C.c_int, C.c_int, PD],
             "espic_ensemble_diag": [VP, PD],
+            "espic_diff_create": [VP, C.c_int, C.c_double, C.c_double, C.c_double, I64, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, C.c_int, C.POINTER(VP)],
+            "espic_diff_set_state": [VP, PD, PD],
+            "espic_diff_forward": [VP, C.c_double, C.c_int, PD],
+            "espic_diff_backward": [VP, PD, PD, PD],
         }
         for name, args in sigs.items():
             f = getattr(L, name)
@@ -146,6 +151,8 @@ def lib():
         L.espic_ensemble_destroy.restype = None
         L.espic_ensemble_stream.argtypes = [VP]
         L.espic_ensemble_stream.restype = VP
+        L.espic_diff_destroy.argtypes = [VP]
+        L.espic_diff_destroy.restype = None
         _lib = L
     return _lib
 
@@ -563,3 +570,76 @@ class Ensemble:
         out = np.zeros((self.nbox, self.nsp + 1))
         check(lib().espic_ensemble_diag(self.h, _pd(out)))
         return out
+
+
+class DiffRun:
+    """Differentiable sphere run (espic_diff_* in include/espic.h): one ion
+    species in `world` (sphere, inlet, reference values and Newton controls
+    set on the world), no injection, C1 absorption over a layer of thickness
+    delta.  Loss = alpha * final field energy + beta * ions in the wake box
+    (nodes with z in wake_z).  precision: "fp64" or "fp32"."""
+
+    def __init__(self, world, n, mass, charge, mpw0, delta, wake_z, alpha=1.0, beta=1.0, checkpoint_every=20,
+                 precision="fp64"):
+        h = VP()
+        check(lib().espic_diff_create(world.h, 0 if precision == "fp64" else 1, mass, charge, mpw0, int(n), delta,
+                                      wake_z[0], wake_z[1], alpha, beta, checkpoint_every, C.byref(h)))
+        self.h, self.world, self.n = h, world, int(n)
+
+    def close(self):
+        if self.h:
+            lib().espic_diff_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, x, v):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(3, self.n)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(3, self.n)
+        check(lib().espic_diff_set_state(self.h, _pd(x), _pd(v)))
+
+    def forward(self, phi_sphere, nsteps):
+        loss = C.c_double()
+        check(lib().espic_diff_forward(self.h, phi_sphere, int(nsteps), C.byref(loss)))
+        return loss.value
+
+    def backward(self):
+        """(d loss / d phi_sphere, d loss / d x [3][n], d loss / d v [3][n])"""
+        dps = C.c_double()
+        dx = np.zeros((3, self.n))
+        dv = np.zeros((3, self.n))
+        check(lib().espic_diff_backward(self.h, C.byref(dps), _pd(dx), _pd(dv)))
+        return dps.value, dx, dv
+
+
+def sphere_run_loss(run, phi_sphere, x0, v0, nsteps):
+    """The loss of a DiffRun as a differentiable torch function of the sphere
+    potential (0-d tensor), the initial positions and velocities ([3, n]
+    float64 tensors); backward() calls the adjoint kernels."""
+    import torch
+
+    class _SphereRun(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, ps, x, v):
+            run.set_state(x.detach().cpu().numpy(), v.detach().cpu().numpy())
+            loss = run.forward(float(ps), nsteps)
+            ctx.dev = x.device
+            return torch.tensor(loss, dtype=torch.float64, device=x.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            dps, dx, dv = run.backward()
+            t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=ctx.dev)
+            return g * t(dps), g * t(dx), g * t(dv)
+
+    return _SphereRun.apply(phi_sphere, x0, v0)

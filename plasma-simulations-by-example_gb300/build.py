@@ -26,6 +26,7 @@ UNITS = {
     "k_pcg.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "k_ensemble.cu": ["-fmad=false"],
+    "adjoint.cu": [],
 }
 
 

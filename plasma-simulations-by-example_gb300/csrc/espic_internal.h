@@ -160,5 +160,6 @@ void launch_from_mixed_raw(cudaStream_t st, const Geo &g, const int32_t *cell, c
 
 /* k_pcg.cu */
 int launch_newton_pcg(World &w, bool fp32_inner);
+int launch_pcg_linear(World &w, bool fp32, const double *b, double *y, double rel_tol, int max_outer);
 
 }  // namespace espic

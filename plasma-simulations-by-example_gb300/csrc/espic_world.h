@@ -88,6 +88,8 @@ struct World {
     int mg_levels_max = 12; /* multigrid levels of the PCG preconditioner (0: Jacobi) */
     double mg_scale = 1.6;  /* coarse-correction scale */
     int solver_blocks = 0;  /* cap on cooperative solver blocks (0: occupancy limit) */
+    double *lin_y = nullptr;       /* linear (adjoint) mode of the Newton-PCG kernel: solution */
+    const double *lin_b = nullptr; /* and right-hand side; null for the Newton solve */
     size_t pcg_bytes = 0;
     uint64_t seed = 0x5eed5eed12345ull;
     uint64_t load_calls = 0;

@@ -496,7 +496,8 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         double te0, double n0, int nr_max, double nr_tol,
                                                         int pcg_max, double pcg_tol, T *y, T *r, T *z, T *p0,
                                                         T *p1, T *q, T *dg, MgArgs<T> mg, const int32_t *lists,
-                                                        double *partials, SolveStatus *st, int *err) {
+                                                        double *partials, SolveStatus *st, int *err,
+                                                        double *lin_y, const double *__restrict__ lin_b) {
     cg::grid_group grid = cg::this_grid();
     const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
@@ -523,7 +524,11 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     F.pk[1] = lists + 3 * (int64_t)F.nlist;
     int round = 0, nr, conv = 0, inner = 0;
     double norm = 0;
-    const double zz_stop = 0.01 * nr_tol * nr_tol * (double)nn;
+    /* linear mode (lin_y != null): Newton on F(y) = J y - b with J frozen at
+     * phi solves J y = b; the stopping test is relative to the first update */
+    const bool linear = lin_y != nullptr;
+    double nr_scale = linear ? 0.0 : 1.0;
+    double zz_stop = 0.01 * nr_tol * nr_tol * (double)nn * nr_scale;
     for (nr = 0; nr < nr_max; nr++) {
         /* Newton residual (float64) and the Boltzmann part of the Jacobian
          * diagonal; the first red smoothing half sweep (or Jacobi) of the
@@ -532,18 +537,19 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         for (int64_t u = gtid; u < nn; u += gsize) {
             uint16_t c = code[u];
             if (!(c & SELF)) continue;
-            double ph = phi[u], L = 0, dL = 0, pn[6];
+            const double *X = linear ? lin_y : phi;
+            double xu = X[u], L = 0, dL = 0, pn[6];
 #pragma unroll
-            for (int m = 0; m < 6; m++) pn[m] = phi[u + off[m]];
+            for (int m = 0; m < 6; m++) pn[m] = X[u + off[m]];
 #pragma unroll
             for (int m = 0; m < 6; m++) {
                 bool on = c & ((1u << m) | (1u << (6 + m)));
-                L += on ? cd[m >> 1] * (ph - pn[m]) : 0.0;
+                L += on ? cd[m >> 1] * (xu - pn[m]) : 0.0;
                 dL += on ? cd[m >> 1] : 0.0;
             }
-            double e = exp((ph - phi0) * inv_te0);
-            double Fv = L + A0 * e - rho[u] * inv_eps0;
+            double e = exp((phi[u] - phi0) * inv_te0);
             double dB = A0_te0 * e;
+            double Fv = linear ? L + dB * xu - lin_b[u] : L + A0 * e - rho[u] * inv_eps0;
             T rv = (T)Fv;
             dg[u] = (T)dB;
             r[u] = rv;
@@ -619,10 +625,11 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         }
         /* Newton update */
         double yy = 0;
+        double *X = linear ? lin_y : phi;
         for (int64_t u = gtid; u < nn; u += gsize) {
             if (!(code[u] & SELF)) continue;
             double yu = (double)y[u];
-            phi[u] -= yu;
+            X[u] -= yu;
             yy += yu * yu;
         }
         double s6[1] = {yy};
@@ -632,14 +639,18 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             if (gtid == 0) atomicOr(err, DERR_NONFINITE);
             break;
         }
-        if (norm < nr_tol) {
+        if (linear && nr == 0) {
+            nr_scale = norm;
+            zz_stop = 0.01 * nr_tol * nr_tol * norm * norm * (double)nn;
+        }
+        if (norm < nr_tol * nr_scale || (linear && norm == 0.0)) {
             conv = 1;
             nr++;
             break;
         }
     }
     /* Neumann boundary nodes take the value at the end of their chain */
-    for (int64_t u = gtid; u < nn; u += gsize) {
+    for (int64_t u = gtid; u < nn && !linear; u += gsize) {
         int32_t t = target[u];
         if (t >= 0) phi[u] = phi[t];
     }
@@ -810,12 +821,34 @@ static int run_pcg(World &w) {
     SolveStatus *st = w.d_status;
     int *err = w.d_err;
     const int32_t *lst = lists;
+    double *ly = w.lin_y;
+    const double *lb = w.lin_b;
     void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
-                    &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err};
+                    &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
+                    &ly,   &lb};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, 0, w.stream);
 }
 
 int launch_newton_pcg(World &w, bool fp32) { return fp32 ? run_pcg<float>(w) : run_pcg<double>(w); }
+
+/* y = J^-1 b on the unknowns, J the Jacobian of the Boltzmann problem at the
+ * current phi (the adjoint solve: J is symmetric); y must be zero off the
+ * unknowns.  Outer iterations until the update's RMS is below rel_tol times
+ * the first one's. */
+int launch_pcg_linear(World &w, bool fp32, const double *b, double *y, double rel_tol, int max_outer) {
+    double keep_tol = w.nr_tol;
+    int keep_max = w.nr_max;
+    w.lin_b = b;
+    w.lin_y = y;
+    w.nr_tol = rel_tol;
+    w.nr_max = max_outer;
+    int rc = fp32 ? run_pcg<float>(w) : run_pcg<double>(w);
+    w.lin_b = nullptr;
+    w.lin_y = nullptr;
+    w.nr_tol = keep_tol;
+    w.nr_max = keep_max;
+    return rc;
+}
 
 }  // namespace espic
