@@ -152,3 +152,45 @@ def test_torch_autograd_function(espic, setup):
     assert rel(ps.grad.item(), dps) <= 1e-12
     assert rel(vd.grad.item(), dv[2].sum()) <= 1e-12
     assert np.allclose(x.grad.numpy(), dx, rtol=0, atol=1e-12 * np.max(np.abs(dx)))
+
+
+def test_full_scale_gradients_converge(espic):
+    """The 32x32x64 box, 500k ions, 400 steps, checkpoints every 20: over this
+    horizon the loss is linear only at small relative scales (perturbations
+    grow through the dynamics), so the central difference uses h = 1e-7."""
+    n, steps = 500_000, 400
+    rng = np.random.default_rng(11)
+    lo, hi, c = np.array(X0), np.array(XM), np.array([0.0, 0.0, 0.15])
+    pos = lo + rng.random((3 * n, 3)) * (hi - lo)
+    pos = pos[np.sum((pos - c) ** 2, axis=1) > 0.055 ** 2][:n]
+    x = np.ascontiguousarray(pos.T)
+    vth = rng.normal(0, 775.0, (3, n))
+    geo = (32, 32, 64)
+    dh = min(0.2 / 31, 0.3 / 63)
+
+    def mk():
+        w = espic.World(*geo, X0, XM)
+        w.setTime(1e-7, 10 ** 6)
+        w.addSphere((0.0, 0.0, 0.15), 0.05, PHI_S)
+        w.addInlet()
+        sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 100, 1e-4)
+        sol.setReferenceValues(0.0, 3.0, 1e10)
+        sol.setNewton(nr_max=60, nr_tol=1e-12, pcg_max=5000, pcg_tol=1e-10, fp32_inner=False)
+        return w
+
+    kw = dict(n=n, mass=16 * AMU, charge=QE, mpw0=1e10 * 0.0115 / n, delta=0.5 * dh, wake_z=(0.2, 0.3),
+              checkpoint_every=20)
+    w = mk()
+    with espic.DiffRun(w, alpha=1e8, beta=1e-7, **kw) as r:
+        def loss(ps=PHI_S, v=None):
+            r.set_state(x, with_drift(vth, VD) if v is None else v)
+            return r.forward(ps, steps)
+
+        loss()
+        dps, _, dv = r.backward()
+        h = 1e-7
+        fd = (loss(ps=PHI_S * (1 + h)) - loss(ps=PHI_S * (1 - h))) / (2 * PHI_S * h)
+        assert rel(fd, dps) <= 1e-4, (fd, dps)
+        fd = (loss(v=with_drift(vth, VD * (1 + h))) - loss(v=with_drift(vth, VD * (1 - h)))) / (2 * VD * h)
+        assert rel(fd, dv[2].sum()) <= 1e-4, (fd, dv[2].sum())
+    w.close()
