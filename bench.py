@@ -64,6 +64,20 @@ def espic_module():
     return importlib.import_module("plasma-simulations-by-example_gb300")
 
 
+def measured_traffic(workload, kernel, units):
+    """DRAM bytes of one launch of `kernel` processing `units` (PCG iterations
+    or particles), scaled from the ncu capture recorded in
+    profiles/traffic.txt; None when there is none."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = line.split()
+        if len(f) >= 4 and not f[0].startswith("#") and f[0] == workload and f[1] == kernel:
+            return float(f[2]) / float(f[3]) * float(units)
+    return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -729,13 +743,8 @@ def main():
         alg = push_bytes
         achieved = push_gbs
         kname = "k_push_mixed"
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get(args.config, {}).get(kname)
-        except Exception:
-            traffic = None
+    traffic = measured_traffic(args.config, kname, inner_per_step if dom == "solve" else t["n"])
+    push_traffic = measured_traffic(args.config, "k_push_mixed", t["n"])
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -758,7 +767,8 @@ def main():
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg},
         "roofline_push": {"bound": "hbm", "kernel": "k_push_mixed", "achieved": push_gbs, "peak": hbm,
-                          "unit": "GB/s", "frac": push_gbs / hbm, "bytes_per_particle": 56},
+                          "unit": "GB/s", "frac": push_gbs / hbm, "bytes_per_particle": 56,
+                          "traffic": push_traffic},
         "clocks": ck,
     }
     if rank == 0 and not args.no_cpu:
