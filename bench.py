@@ -329,6 +329,17 @@ def ncu_case(args):
     E = espic_module()
     if not os.path.exists(E.LIB_PATH):
         E.build()
+    if args.config == "ensemble512":
+        cfg = dict(CONFIGS["ensemble512"])
+        cfg["nbox"] = args.ncu_boxes or cfg["nbox"]
+        ens, npart, _ = make_ensemble(E, cfg)
+        ens.set_launch(4096, 512, 1024)
+        ens.step(1, graph=False)
+        sweeps, conv, _ = ens.status()
+        print(json.dumps({"ncu_case": "ensemble", "boxes": cfg["nbox"], "particles": npart,
+                          "sweeps_mean": float(sweeps.mean()), "converged": int(conv.sum())}))
+        ens.close()
+        return
     cfg = CONFIGS[args.config]
     npart = args.ncu_particles or cfg["np"]
     ni, nj, nk = cfg["n"]
@@ -655,6 +666,8 @@ def main():
                     help="one push + one solve of the workload (mixed form), for an ncu capture")
     ap.add_argument("--ncu-particles", type=int, default=0,
                     help="ions of the --ncu-case state (default: the workload's); keeps captures small")
+    ap.add_argument("--ncu-boxes", type=int, default=0,
+                    help="boxes of the ensemble --ncu-case (default: the workload's)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
