@@ -169,6 +169,16 @@ int espic_solver_set_multigrid(espic_world *w, int levels, double scale);
  * (0: one per SM).  A tuning knob with no reference counterpart: small grids
  * are bound by grid-barrier latency, which falls with fewer blocks. */
 int espic_solver_set_launch(espic_world *w, int max_blocks);
+/* Newton predictor (default on): when exactly one charge density was
+ * computed since the last solve (consecutive steps), the Newton-PCG solve
+ * starts from 2 phi^n - phi^(n-1) on the unknowns instead of phi^n; the
+ * converged solution and its test are unchanged.  No reference counterpart
+ * (the reference starts from phi^n). */
+int espic_solver_set_predictor(espic_world *w, int enable);
+/* Multigrid levels with fewer than block_nodes nodes run on one thread block
+ * between two grid barriers (default 4096); larger levels run on the whole
+ * grid.  A tuning knob with no reference counterpart. */
+int espic_solver_set_coarse(espic_world *w, int64_t block_nodes);
 /* PotentialSolver::solve, ch2/PotentialSolver.cpp:11-67 and
  * ch3/ver2/PotentialSolver.h:66-75.  With all out-pointers NULL the solve is
  * only enqueued; otherwise the call waits and reports iterations and the

@@ -105,6 +105,8 @@ def lib():
             "espic_solver_set_newton": [VP, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int],
             "espic_solver_set_multigrid": [VP, C.c_int, C.c_double],
             "espic_solver_set_launch": [VP, C.c_int],
+            "espic_solver_set_coarse": [VP, I64],
+            "espic_solver_set_predictor": [VP, C.c_int],
             "espic_solve": [VP, PI, PI, PD],
             "espic_efield": [VP],
             "espic_species_diag": [VP, C.c_int, PD],
@@ -441,6 +443,14 @@ class PotentialSolver:
 
     def setLaunch(self, max_blocks=0):
         check(lib().espic_solver_set_launch(self.world.h, max_blocks))
+
+    def setPredictor(self, enable=True):
+        """Start Newton solves of consecutive steps from 2 phi^n - phi^(n-1)."""
+        check(lib().espic_solver_set_predictor(self.world.h, 1 if enable else 0))
+
+    def setCoarse(self, block_nodes):
+        """Multigrid levels with fewer nodes than this run on one block."""
+        check(lib().espic_solver_set_coarse(self.world.h, int(block_nodes)))
 
     def solve(self, wait=True):
         """Returns (converged, iterations, inner_iterations, residual)."""

@@ -153,7 +153,7 @@ static void free_world(World &w) {
     for (Species *s : w.species) free_species(s);
     w.species.clear();
     void *ptrs[] = {w.phi, w.rho, w.vol, w.ef, w.ef4, w.obj, w.target, w.d_err, w.d_status, w.d_partials,
-                    w.d_small, w.d_u, w.d_stage, w.d_blockcnt, w.pcg_buf};
+                    w.d_small, w.d_u, w.d_stage, w.d_blockcnt, w.pcg_buf, w.phi_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (w.h_small) cudaFreeHost(w.h_small);
@@ -279,6 +279,7 @@ extern "C" int espic_world_add_sphere(espic_world *h, const double c[3], double 
     CHECK_LAUNCH();
     w.targets_valid = false;
     w.pcg_codes_valid = false;
+    w.phi_prev_valid = false;
     return ESPIC_OK;
 }
 
@@ -288,6 +289,7 @@ extern "C" int espic_world_add_inlet(espic_world *h) {
     CHECK_LAUNCH();
     w.targets_valid = false;
     w.pcg_codes_valid = false;
+    w.phi_prev_valid = false;
     return ESPIC_OK;
 }
 
@@ -674,6 +676,7 @@ extern "C" int espic_charge_density(espic_world *h) {
     WORLD(h);
     PhaseScope ph(w, ESPIC_PHASE_DENSITY);
     launch_charge(w);
+    w.rho_version++;
     CHECK_LAUNCH();
     return ESPIC_OK;
 }
@@ -793,6 +796,20 @@ extern "C" int espic_solver_set_multigrid(espic_world *h, int levels, double sca
     return ESPIC_OK;
 }
 
+extern "C" int espic_solver_set_coarse(espic_world *h, int64_t block_nodes) {
+    WORLD(h);
+    if (block_nodes < 0) return fail(ESPIC_ERR_ARG, "bad coarse-level size");
+    w.mg_block_nodes = block_nodes;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_solver_set_predictor(espic_world *h, int enable) {
+    WORLD(h);
+    w.predictor = enable != 0;
+    w.phi_prev_valid = false;
+    return ESPIC_OK;
+}
+
 extern "C" int espic_solver_set_launch(espic_world *h, int max_blocks) {
     WORLD(h);
     if (max_blocks < 0) return fail(ESPIC_ERR_ARG, "bad block count");
@@ -812,6 +829,21 @@ static int enqueue_solve(World &w) {
             if (!w.targets_valid) {
                 launch_targets(w);
                 w.targets_valid = true;
+            }
+            if (w.solver_kind == ESPIC_SOLVER_PCG && w.predictor) {
+                /* predictor: between consecutive steps (one new charge
+                 * density since the last solve) the Newton solve starts
+                 * from 2 phi^n - phi^(n-1); otherwise from phi^n */
+                if (!w.phi_prev && cudaMalloc(&w.phi_prev, w.nn * sizeof(double)) != cudaSuccess) {
+                    w.phi_prev = nullptr;
+                    w.predictor = false;
+                }
+                if (w.phi_prev) {
+                    bool extrapolate = w.phi_prev_valid && w.rho_version == w.solve_rho_version + 1;
+                    launch_predict(w, extrapolate);
+                    w.phi_prev_valid = true;
+                    w.solve_rho_version = w.rho_version;
+                }
             }
             e = w.solver_kind == ESPIC_SOLVER_GS ? launch_gs_sphere(w, w.max_it, w.tol)
                                                  : launch_newton_pcg(w, w.fp32_inner != 0);
@@ -1009,6 +1041,7 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
         CK(cudaStreamSynchronize(w.stream));
         w.targets_valid = false;
         w.pcg_codes_valid = false;
+        w.phi_prev_valid = false;
         return ESPIC_OK;
     }
     double *p;
@@ -1018,6 +1051,8 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
     if (n < cnt) return fail(ESPIC_ERR_ARG, "buffer holds %lld of %lld values", (long long)n, (long long)cnt);
     CK(cudaMemcpyAsync(p, host, cnt * sizeof(double), cudaMemcpyHostToDevice, w.stream));
     if (field == ESPIC_FIELD_EF) launch_ef4(w);
+    if (field == ESPIC_FIELD_PHI) w.phi_prev_valid = false;
+    if (field == ESPIC_FIELD_RHO) w.rho_version++;
     CHECK_LAUNCH();
     CK(cudaStreamSynchronize(w.stream));
     return ESPIC_OK;
@@ -1043,6 +1078,7 @@ extern "C" int espic_step(espic_world *h, int sort_every, double *row, int len) 
     {
         PhaseScope ph(w, ESPIC_PHASE_DENSITY);
         launch_charge(w);
+        w.rho_version++;
     }
     CHECK_LAUNCH();
     if ((rc = enqueue_solve(w)) != ESPIC_OK) return rc;

@@ -141,6 +141,7 @@ void launch_qn(World &w);
 void launch_node_vol(World &w);
 void launch_ef4(World &w);
 void launch_fill(World &w, double *x, int64_t n, double v);
+void launch_predict(World &w, bool extrapolate);
 
 /* k_mixed.cu */
 void launch_push_mixed(World &w, Species &s, bool deposit);

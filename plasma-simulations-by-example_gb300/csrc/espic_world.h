@@ -87,7 +87,13 @@ struct World {
     int pcg_elem = 0;       /* element size the PCG buffers were laid out for */
     int mg_levels_max = 12; /* multigrid levels of the PCG preconditioner (0: Jacobi) */
     double mg_scale = 1.6;  /* coarse-correction scale */
+    int64_t mg_block_nodes = 4096; /* multigrid levels smaller than this run on one block */
     int solver_blocks = 0;  /* cap on cooperative solver blocks (0: occupancy limit) */
+    double *phi_prev = nullptr;    /* the potential before the last Newton solve (predictor) */
+    bool phi_prev_valid = false;
+    bool predictor = true;         /* start the Newton solve from 2 phi^n - phi^(n-1) */
+    int64_t rho_version = 0;       /* charge densities computed so far */
+    int64_t solve_rho_version = -1;
     double *lin_y = nullptr;       /* linear (adjoint) mode of the Newton-PCG kernel: solution */
     const double *lin_b = nullptr; /* and right-hand side; null for the Newton solve */
     size_t pcg_bytes = 0;

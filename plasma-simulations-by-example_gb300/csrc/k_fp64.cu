@@ -1031,6 +1031,25 @@ __global__ void k_ef_to_ef4(int64_t nn, const double *__restrict__ ef, float4 *e
     ef4[u] = make_float4((float)ef[3 * u], (float)ef[3 * u + 1], (float)ef[3 * u + 2], 0.f);
 }
 
+/* Newton predictor: on the unknowns phi <- 2 phi - phi_prev and phi_prev <-
+ * the old phi (extrapolate), or only phi_prev <- phi */
+__global__ void k_predict(Geo g, const int32_t *__restrict__ obj, double *phi, double *phi_prev, int extrapolate) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    if (u >= nn) return;
+    const double cur = phi[u];
+    if (extrapolate && obj[u] == 0) {
+        const int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
+        if (i > 0 && j > 0 && k > 0 && i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1) phi[u] = 2.0 * cur - phi_prev[u];
+    }
+    phi_prev[u] = cur;
+}
+
+void launch_predict(World &w, bool extrapolate) {
+    k_predict<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.obj, w.phi, w.phi_prev, extrapolate ? 1 : 0);
+    w.nlaunch++;
+}
+
 /* weight row of a float64 species that switches from uniform to per-particle weights */
 __global__ void k_fill(double *x, int64_t n, double v) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -22,7 +22,8 @@
  * |r| <= pcg_tol |F|, or earlier once the RMS of the preconditioned residual
  * z = M r (an estimate of the error left in the Newton update y) is below
  * nr_tol / 10: the Newton test RMS(y) < nr_tol cannot then depend on more
- * inner accuracy, and the last Newton step stops needing a full solve.
+ * inner accuracy, and the last Newton step stops needing a full solve; when
+ * the first V-cycle's z is already that small, z itself is the update.
  *
  * Preconditioner: an aggregation multigrid V-cycle.  Level l+1 groups the
  * level-l unknowns in 2x2x2 blocks of the structured index space; its
@@ -32,8 +33,9 @@
  * black before the coarse correction, black then red after), restriction is
  * P^T, prolongation P scaled by a constant, and the coarsest level gets
  * symmetric sweeps, so the preconditioner is symmetric as CG requires.
- * Levels with fewer than 32768 nodes run on block 0 alone between two grid
- * barriers.  Without levels, the preconditioner is Jacobi.
+ * Levels with fewer than World::mg_block_nodes nodes (default 4096) run on
+ * block 0 alone between two grid barriers.  Without levels, the
+ * preconditioner is Jacobi.
  */
 #include <cooperative_groups.h>
 
@@ -117,6 +119,7 @@ __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV]
 
 
 constexpr int MG_MAX = 12;
+constexpr size_t PCG_SMEM_MAX = 160 * 1024; /* shared memory for block 0's coarse levels */
 
 template <typename T>
 struct MgLevel {
@@ -131,8 +134,41 @@ struct MgArgs {
     int grid_levels; /* coarse levels 1..grid_levels-1 run on the whole grid */
     int nu_coarse;   /* sweeps each way on the coarsest level */
     T scale;         /* coarse-correction scale */
+    int smem_from;   /* block 0 keeps levels L[smem_from..] in shared memory (-1: none) */
     MgLevel<T> L[MG_MAX];
 };
+
+/* bytes of one level's arrays (diag, 6 weights, b, e) in shared memory */
+template <typename T>
+__host__ __device__ inline size_t level_smem_bytes(int64_t n) {
+    return ((size_t)n * sizeof(T) + 15) / 16 * 16 * 9;
+}
+
+/* block 0's view of the levels it works alone: shared-memory copies of
+ * L[smem_from..] (diag and weights copied once per launch) */
+template <typename T>
+__device__ void smem_levels_init(const MgArgs<T> &A, MgArgs<T> &S, unsigned char *base) {
+    if (threadIdx.x == 0) {
+        S = A;
+        size_t off = 0;
+        for (int i = A.smem_from; i < A.nlev; i++) {
+            const int64_t n = A.L[i].n;
+            const size_t a = ((size_t)n * sizeof(T) + 15) / 16 * 16;
+            S.L[i].diag = (T *)(base + off);
+            S.L[i].w = (T *)(base + off + a);
+            S.L[i].b = (T *)(base + off + 7 * a);
+            S.L[i].e = (T *)(base + off + 8 * a);
+            off += 9 * a;
+        }
+    }
+    __syncthreads();
+    for (int i = A.smem_from; i < A.nlev; i++) {
+        const int64_t n = A.L[i].n;
+        for (int64_t t = threadIdx.x; t < n; t += blockDim.x) S.L[i].diag[t] = A.L[i].diag[t];
+        for (int64_t t = threadIdx.x; t < 6 * n; t += blockDim.x) S.L[i].w[t] = A.L[i].w[t];
+    }
+    __syncthreads();
+}
 
 /* everything the level-0 (node grid) operations need */
 template <typename T>
@@ -390,7 +426,7 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
  * z.z in zz (the last barrier is the one of that reduction). */
 template <typename T>
 __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgArgs<T> &A, double *partials,
-                              int &round, double &zz) {
+                              int &round, double &zz, const MgArgs<T> *SB) {
     const int NL = A.nlev;
     if (NL == 0) { /* Jacobi: the caller computed z on every node */
         T rz = 0, z2 = 0;
@@ -427,13 +463,24 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
     const int nuc = A.nu_coarse;
     if (!coarsest_whole) {
         if (blockIdx.x == 0) {
-            for (int b = lblock; b < NL; b++) {
-                coarse_half(A.L[b - 1], 1, false, (const MgLevel<T> *)nullptr, sc);
-                __syncthreads();
-                restrict_coarse(A.L[b - 1], A.L[b], false);
+            /* with shared-memory levels, stage b and e of the first one */
+            const bool staged = SB && SB->smem_from == lblock - 1;
+            const MgArgs<T> &B = staged ? *SB : A;
+            if (staged) {
+                const MgLevel<T> &G0 = A.L[lblock - 1], &S0 = SB->L[lblock - 1];
+                for (int64_t t = threadIdx.x; t < G0.n; t += blockDim.x) {
+                    S0.b[t] = G0.b[t];
+                    S0.e[t] = G0.e[t];
+                }
                 __syncthreads();
             }
-            const MgLevel<T> &Lc = A.L[NL - 1];
+            for (int b = lblock; b < NL; b++) {
+                coarse_half(B.L[b - 1], 1, false, (const MgLevel<T> *)nullptr, sc);
+                __syncthreads();
+                restrict_coarse(B.L[b - 1], B.L[b], false);
+                __syncthreads();
+            }
+            const MgLevel<T> &Lc = B.L[NL - 1];
             for (int s = 0; s < nuc; s++) {
                 if (s) {
                     coarse_half(Lc, 0, false, (const MgLevel<T> *)nullptr, sc);
@@ -449,10 +496,14 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
                 __syncthreads();
             }
             for (int b = NL - 1; b >= lblock; b--) {
-                coarse_half(A.L[b - 1], 1, false, &A.L[b], sc);
+                coarse_half(B.L[b - 1], 1, false, &B.L[b], sc);
                 __syncthreads();
-                coarse_half(A.L[b - 1], 0, false, (const MgLevel<T> *)nullptr, sc);
+                coarse_half(B.L[b - 1], 0, false, (const MgLevel<T> *)nullptr, sc);
                 __syncthreads();
+            }
+            if (staged) {
+                const MgLevel<T> &G0 = A.L[lblock - 1], &S0 = SB->L[lblock - 1];
+                for (int64_t t = threadIdx.x; t < G0.n; t += blockDim.x) G0.e[t] = S0.e[t];
             }
         }
         grid.sync();
@@ -499,6 +550,13 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         double *partials, SolveStatus *st, int *err,
                                                         double *lin_y, const double *__restrict__ lin_b) {
     cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char pcg_smem[];
+    __shared__ MgArgs<T> smem_args;
+    const MgArgs<T> *SB = nullptr;
+    if (mg.smem_from >= 0 && mg.nlev > 0 && blockIdx.x == 0) {
+        smem_levels_init(mg, smem_args, pcg_smem);
+        SB = &smem_args;
+    }
     const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
     const int64_t off[6] = {-1, 1, -sy, sy, -sz, sz};
@@ -564,13 +622,17 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             if (gtid == 0) atomicOr(err, DERR_NONFINITE);
             break;
         }
+        bool take_z = false;
         if (FF > 0) {
             const double stop2 = pcg_tol * pcg_tol * FF;
             double ZZ;
-            double RZ = vcycle_rest(grid, F, mg, partials, round, ZZ);
+            double RZ = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
+            /* the first preconditioned residual already estimates an update
+             * below a tenth of the Newton tolerance: it is the update */
+            take_z = ZZ < zz_stop;
             T beta = 0;
             T *pold = p0, *pnew = p1;
-            for (int it = 0; it < pcg_max; it++) {
+            for (int it = 0; it < pcg_max && !take_z; it++) {
                 /* p = z + beta p (on the fly at the node and its neighbours),
                  * q = J p */
                 T pq = 0;
@@ -611,7 +673,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 grid_sum_n<1>(grid, s4, partials, round);
                 inner++;
                 if (!(s4[0] > stop2)) break; /* also leaves on NaN */
-                double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ);
+                double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
                 /* z = M r estimates the remaining error of y: once its RMS is
                  * below a tenth of the Newton tolerance, further inner
                  * iterations cannot change the outcome of the Newton test */
@@ -628,7 +690,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         double *X = linear ? lin_y : phi;
         for (int64_t u = gtid; u < nn; u += gsize) {
             if (!(code[u] & SELF)) continue;
-            double yu = (double)y[u];
+            double yu = take_z ? (double)z[u] : (double)y[u];
             X[u] -= yu;
             yy += yu * yu;
         }
@@ -741,7 +803,7 @@ static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
         L.e = (T *)(base ? base + off : nullptr);
         off += bytes;
         nlev++;
-        if (L.n >= 32768) grid_levels = nlev + 1;
+        if (L.n >= w.mg_block_nodes) grid_levels = nlev + 1;
         if (L.n <= 64 || (nx <= 2 && ny <= 2 && nz <= 2)) break;
         nx = (nx + 1) / 2;
         ny = (ny + 1) / 2;
@@ -751,6 +813,15 @@ static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
     A.grid_levels = grid_levels;
     A.nu_coarse = 2;
     A.scale = (T)w.mg_scale;
+    /* block 0 works levels lblock-1 .. nlev-1 alone (lblock = min(grid
+     * levels, nlev)); keep them in its shared memory when they fit */
+    A.smem_from = -1;
+    const int lblock = grid_levels < A.nlev ? grid_levels : A.nlev;
+    if (A.nlev > 0 && A.nlev >= grid_levels) {
+        size_t bytes = 0;
+        for (int i = lblock - 1; i < A.nlev; i++) bytes += level_smem_bytes<T>(A.L[i].n);
+        if (bytes <= PCG_SMEM_MAX) A.smem_from = lblock - 1;
+    }
     return off;
 }
 
@@ -800,8 +871,12 @@ static int run_pcg(World &w) {
     }
     const void *fn = (const void *)k_newton_pcg<T>;
     const int threads = 1024;
+    size_t dyn = 0;
+    if (A.smem_from >= 0)
+        for (int i = A.smem_from; i < A.nlev; i++) dyn += level_smem_bytes<T>(A.L[i].n);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, dyn);
     if (per_sm < 1) per_sm = 1;
     int64_t maxb = (int64_t)per_sm * w.sm_count;
     int64_t needb = (w.nn + threads - 1) / threads;
@@ -827,7 +902,7 @@ static int run_pcg(World &w) {
                     &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
                     &ly,   &lb};
     w.nlaunch++;
-    return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, 0, w.stream);
+    return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, dyn, w.stream);
 }
 
 int launch_newton_pcg(World &w, bool fp32) { return fp32 ? run_pcg<float>(w) : run_pcg<double>(w); }
