@@ -542,7 +542,7 @@ def run_ensemble(args, E, torch, dist, rank, world_size):
             "config": {"workload": "ensemble512", "boxes": cfg["nbox"], "particles": npart,
                        "nodes": int(np.prod(nodes, axis=1).sum()), "solver": "red-black SOR, per-box optimal "
                        "omega, tol 1e-4", "launch": {k: tune[k] for k in ("chunk", "push_threads",
-                                                                        "solve_threads")},
+                                                                        "solve_threads", "cluster")},
                        "l2": "flushed between timed steps (256 MB write, outside the events)"},
             "phase_ms_per_step": {"push": tune["push_ms"], "solve": tune["solve_ms"]},
             "sor_sweeps_per_step": {"mean": float(np.mean(sweeps)), "max": int(np.max(sweeps))},

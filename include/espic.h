@@ -274,9 +274,10 @@ int espic_step(espic_world *w, int sort_every, double *row, int len);
  * PotentialSolver) stepped together.  Every box has its own node counts and
  * extents; every (box, species) its own weight mpw0 and capacity.  Particles
  * are in the mixed form.  A step runs push + deposit of all boxes in one
- * launch over a flattened work list, then one launch in which blocks claim
- * boxes and compute charge density, red-black SOR (float32 sweeps under a
- * float64 residual, ch2/PotentialSolver.cpp:11-67 convergence test) and E;
+ * launch over a flattened work list, then one launch in which clusters of
+ * thread blocks claim boxes and compute charge density, red-black SOR
+ * (float32 sweeps under a float64 residual, ch2/PotentialSolver.cpp:11-67
+ * convergence test) and E;
  * espic_ensemble_step replays the step as a captured CUDA graph. */
 typedef struct espic_ensemble espic_ensemble;
 /* nodes[3*b..], x0[3*b..], xm[3*b..] per box; mass[s], charge[s] per species;
@@ -301,10 +302,11 @@ int espic_ensemble_load_box(espic_ensemble *e, int box, int sp, const double x1[
  * hard-codes 1.4) */
 int espic_ensemble_set_solver(espic_ensemble *e, int max_it, double tol, double omega);
 /* launch shape: particles per work item (>= 256), push block (128/256/512),
- * solve block (256/512/1024); results do not depend on it */
-int espic_ensemble_set_launch(espic_ensemble *e, int chunk, int push_threads, int solve_threads);
-int espic_ensemble_get_launch(espic_ensemble *e, int *chunk, int *push_threads, int *solve_threads);
-/* times every launch shape on real steps and keeps the fastest (consumes 18
+ * solve block (256/512/1024), CTAs per box cluster (1/2/4/8); results do
+ * not depend on it */
+int espic_ensemble_set_launch(espic_ensemble *e, int chunk, int push_threads, int solve_threads, int cluster);
+int espic_ensemble_get_launch(espic_ensemble *e, int *chunk, int *push_threads, int *solve_threads, int *cluster);
+/* times every launch shape on real steps and keeps the fastest (consumes 27
  * steps of the run; results do not depend on the shape) */
 int espic_ensemble_autotune(espic_ensemble *e, int *chunk, int *push_threads, int *solve_threads, double *push_ms,
                             double *solve_ms);

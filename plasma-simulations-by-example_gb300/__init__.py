@@ -127,8 +127,8 @@ def lib():
             "espic_ensemble_get_particles": [VP, C.c_int, C.c_int, PD, I64, I64, C.POINTER(I64)],
             "espic_ensemble_load_box": [VP, C.c_int, C.c_int, PD, PD, I64],
             "espic_ensemble_set_solver": [VP, C.c_int, C.c_double, C.c_double],
-            "espic_ensemble_set_launch": [VP, C.c_int, C.c_int, C.c_int],
-            "espic_ensemble_get_launch": [VP, PI, PI, PI],
+            "espic_ensemble_set_launch": [VP, C.c_int, C.c_int, C.c_int, C.c_int],
+            "espic_ensemble_get_launch": [VP, PI, PI, PI, PI],
             "espic_ensemble_autotune": [VP, PI, PI, PI, PD, PD],
             "espic_ensemble_prepare": [VP],
             "espic_ensemble_step": [VP, C.c_int],
@@ -529,21 +529,23 @@ class Ensemble:
     def set_solver(self, max_it=10000, tol=1e-4, omega=0.0):
         check(lib().espic_ensemble_set_solver(self.h, max_it, tol, omega))
 
-    def set_launch(self, chunk, push_threads, solve_threads):
-        check(lib().espic_ensemble_set_launch(self.h, chunk, push_threads, solve_threads))
+    def set_launch(self, chunk, push_threads, solve_threads, cluster=8):
+        check(lib().espic_ensemble_set_launch(self.h, chunk, push_threads, solve_threads, cluster))
 
     def get_launch(self):
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
-        check(lib().espic_ensemble_get_launch(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return a.value, b.value, c.value
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(lib().espic_ensemble_get_launch(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def autotune(self):
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         pm, sm = C.c_double(), C.c_double()
         check(lib().espic_ensemble_autotune(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(pm),
                                             C.byref(sm)))
-        return dict(chunk=a.value, push_threads=b.value, solve_threads=c.value, push_ms=pm.value,
-                    solve_ms=sm.value)
+        cl = C.c_int()
+        check(lib().espic_ensemble_get_launch(self.h, None, None, None, C.byref(cl)))
+        return dict(chunk=a.value, push_threads=b.value, solve_threads=c.value, cluster=cl.value,
+                    push_ms=pm.value, solve_ms=sm.value)
 
     def prepare(self):
         check(lib().espic_ensemble_prepare(self.h))

@@ -18,10 +18,12 @@
  *  1. k_ens_push (k_mixed.cu): push + deposit over a flattened work list of
  *     particle chunks; the walls reflect, so counts never change and the
  *     work list is built once on the host;
- *  2. k_ens_solve: blocks claim boxes, largest first, from an atomic
- *     counter; per box: rho from the accumulators (which it clears), the
- *     red-black SOR of PotentialSolver::solve (ch2/PotentialSolver.cpp:11-67)
- *     as float32 correction sweeps under a float64 residual, then E.
+ *  2. k_ens_solve: thread-block clusters (1 to 8 CTAs on as many SMs) claim
+ *     boxes, largest first, from an atomic counter; per box: rho from the
+ *     accumulators (which it clears), the red-black SOR of
+ *     PotentialSolver::solve (ch2/PotentialSolver.cpp:11-67) as float32
+ *     correction sweeps under a float64 residual, then E, every pass split
+ *     over the cluster's CTAs between cluster barriers.
  *
  * The SOR: the residual R = rho/eps0 + L phi of the reference
  * (ch2/PotentialSolver.cpp:44-61, L2 = sqrt(sum R^2 / (ni nj nk))) is formed
@@ -39,8 +41,12 @@
 #include <algorithm>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "espic.h"
 #include "espic_world.h"
+
+namespace cg = cooperative_groups;
 
 int espic_internal_fail(int code, const char *msg);
 
@@ -137,19 +143,38 @@ __device__ __forceinline__ void ens_efield(const Geo &g, const EfRcp &rc, const 
     e2 = div_rcp(n2, rc.d2[2], rc.y2[2]);
 }
 
+/* cluster barrier between passes that exchange global memory across the
+ * cluster's SMs: barrier.cluster.arrive (release) + wait (acquire) orders
+ * every CTA's global writes before the other CTAs' later reads */
+__device__ __forceinline__ void cluster_sync_global(cg::cluster_group &cl) { cl.sync(); }
+
+/* One box per thread-block cluster of C CTAs (C = 1, 2, 4 or 8, chosen at
+ * launch): the CTAs split every node pass and every half sweep into
+ * contiguous slices and meet at cluster barriers.  The box a cluster works
+ * on is claimed by CTA 0 and read by the others from its shared memory.  The
+ * residual sum uses the fixed layout of ENS_VW virtual threads (node t
+ * belongs to virtual thread t mod ENS_VW; CTA r owns a contiguous range of
+ * virtual threads); CTA 0 gathers the ENS_VW partials through distributed
+ * shared memory and sums them in a fixed tree, so the result depends on
+ * neither C nor the block size. */
 __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ boxes, const EnsSeg *__restrict__ segs,
                                                     int nsp, const int *__restrict__ order, int nbox, int *counter,
                                                     double *phi, double *rho, float *ecor, float *res, float4 *ef4,
                                                     unsigned long long *acc, int64_t total_nodes, int max_it,
                                                     double tol, int solve, EnsStat *stat, int *err) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks();
+    const int rank = (int)cl.block_rank();
     __shared__ double part[ENS_VW];
+    __shared__ double total;
     __shared__ int sb;
     const int tid = threadIdx.x, nt = blockDim.x;
+    const int vper = ENS_VW / C, v0 = rank * vper, v1 = v0 + vper;
     for (;;) {
-        if (tid == 0) sb = atomicAdd(counter, 1);
-        __syncthreads();
-        const int b = sb;
-        __syncthreads();
+        if (rank == 0 && tid == 0) sb = atomicAdd(counter, 1);
+        cluster_sync_global(cl);
+        const int b = *cl.map_shared_rank(&sb, 0);
+        cluster_sync_global(cl);
         if (b >= nbox) break;
         const int bid = order[b];
         const EnsBox B = boxes[bid];
@@ -160,11 +185,12 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
         double *rh = rho + B.node0;
         float *e = ecor + B.node0;
         float *R = res + B.node0;
+        const int64_t n0 = nn * rank / C, n1 = nn * (rank + 1) / C;
         /* 1. rho = sum_s q_s den_s, den_s = counts * unit_s / node_vol; the
          *    accumulators are cleared for the next deposit */
         const double V0 = g.dh[0] * g.dh[1] * g.dh[2];
         const double yV0 = 1.0 / V0;
-        for (int64_t u = tid; u < nn; u += nt) {
+        for (int64_t u = n0 + tid; u < n1; u += nt) {
             const int i = (int)(u % ni), j = (int)((u / ni) % nj), k = (int)(u / ((int64_t)ni * nj));
             double r = 0;
             for (int s = 0; s < nsp; s++) {
@@ -178,7 +204,7 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
             rh[u] = r;
             e[u] = 0.f;
         }
-        __syncthreads();
+        cluster_sync_global(cl);
         /* 2. red-black SOR: float32 correction sweeps under the float64
          *    residual */
         const double idx2 = 1.0 / (g.dh[0] * g.dh[0]);
@@ -192,10 +218,12 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
         const int hx = (ni - 2 + 1) / 2;
         const int count = hx * (nj - 2) * (nk - 2);
         const int interior = (ni - 2) * (nj - 2) * (nk - 2);
+        const int c0 = (int)((int64_t)count * rank / C), c1 = (int)((int64_t)count * (rank + 1) / C);
+        const int i0 = (int)((int64_t)interior * rank / C), i1 = (int)((int64_t)interior * (rank + 1) / C);
         int sweeps = 0, conv = 0;
         double L2 = 0;
         while (solve) {
-            for (int v = tid; v < ENS_VW; v += nt) {
+            for (int v = v0 + tid; v < v1; v += nt) {
                 double acc2 = 0;
                 for (int t = v; t < interior; t += ENS_VW) {
                     const int i = 1 + t % (ni - 2);
@@ -211,10 +239,16 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
                 }
                 part[v] = acc2;
             }
-            const double tot = ens_tree_sum(part);
-            L2 = sqrt(tot / ((double)ni * nj * nk));
+            cluster_sync_global(cl);
+            if (rank == 0) {
+                for (int v = vper + tid; v < ENS_VW; v += nt) part[v] = *cl.map_shared_rank(&part[v], v / vper);
+                const double t = ens_tree_sum(part);
+                if (tid == 0) total = t;
+            }
+            cluster_sync_global(cl);
+            L2 = sqrt(*cl.map_shared_rank(&total, 0) / ((double)ni * nj * nk));
             if (!isfinite(L2)) {
-                if (tid == 0) atomicOr(err, DERR_NONFINITE);
+                if (rank == 0 && tid == 0) atomicOr(err, DERR_NONFINITE);
                 break;
             }
             if (L2 < tol) {
@@ -224,47 +258,45 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
             if (sweeps >= max_it) break;
             /* ENS_SWEEPS float32 sweeps of L e = -R, then phi += e and the
              * float64 residual decides again */
-            {
-                const int ns = max_it - sweeps < ENS_SWEEPS ? max_it - sweeps : ENS_SWEEPS;
-                for (int s = 0; s < ns; s++) {
-                    for (int c = 0; c < 2; c++) {
-                        /* four independent nodes of colour c per thread: all
-                         * loads before any store */
-                        for (int tb = tid; tb < count; tb += 4 * nt) {
-                            int uq[4];
-                            float eo[4], sum[4];
+            const int ns = max_it - sweeps < ENS_SWEEPS ? max_it - sweeps : ENS_SWEEPS;
+            for (int s = 0; s < ns; s++) {
+                for (int c = 0; c < 2; c++) {
+                    /* four independent nodes of colour c per thread: all
+                     * loads before any store */
+                    for (int tb = c0 + tid; tb < c1; tb += 4 * nt) {
+                        int uq[4];
+                        float eo[4], sum[4];
 #pragma unroll
-                            for (int q = 0; q < 4; q++) {
-                                const int t = tb + q * nt;
-                                uq[q] = -1;
-                                eo[q] = 0.f;
-                                sum[q] = 0.f;
-                                if (t >= count) continue;
-                                const int i2 = t % hx;
-                                const int r = t / hx;
-                                const int j = 1 + r % (nj - 2);
-                                const int k = 1 + r / (nj - 2);
-                                const int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
-                                if (i > ni - 2) continue;
-                                const int u = (k * nj + j) * ni + i;
-                                uq[q] = u;
-                                eo[q] = e[u];
-                                sum[q] = R[u] + fcx * (e[u - 1] + e[u + 1]) + fcy * (e[u - sy] + e[u + sy]) +
-                                         fcz * (e[u - sz] + e[u + sz]);
-                            }
-#pragma unroll
-                            for (int q = 0; q < 4; q++) {
-                                if (uq[q] < 0) continue;
-                                const float en = sum[q] * fiD;
-                                e[uq[q]] = eo[q] + fw * (en - eo[q]);
-                            }
+                        for (int q = 0; q < 4; q++) {
+                            const int t = tb + q * nt;
+                            uq[q] = -1;
+                            eo[q] = 0.f;
+                            sum[q] = 0.f;
+                            if (t >= c1) continue;
+                            const int i2 = t % hx;
+                            const int r = t / hx;
+                            const int j = 1 + r % (nj - 2);
+                            const int k = 1 + r / (nj - 2);
+                            const int i = 1 + 2 * i2 + ((1 + j + k + c) & 1);
+                            if (i > ni - 2) continue;
+                            const int u = (k * nj + j) * ni + i;
+                            uq[q] = u;
+                            eo[q] = e[u];
+                            sum[q] = R[u] + fcx * (e[u - 1] + e[u + 1]) + fcy * (e[u - sy] + e[u + sy]) +
+                                     fcz * (e[u - sz] + e[u + sz]);
                         }
-                        __syncthreads();
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            if (uq[q] < 0) continue;
+                            const float en = sum[q] * fiD;
+                            e[uq[q]] = eo[q] + fw * (en - eo[q]);
+                        }
                     }
+                    cluster_sync_global(cl);
                 }
-                sweeps += ns;
             }
-            for (int t = tid; t < interior; t += nt) {
+            sweeps += ns;
+            for (int t = i0 + tid; t < i1; t += nt) {
                 const int i = 1 + t % (ni - 2);
                 const int r = t / (ni - 2);
                 const int j = 1 + r % (nj - 2);
@@ -272,22 +304,22 @@ __global__ void __launch_bounds__(1024) k_ens_solve(const EnsBox *__restrict__ b
                 const int u = (k * nj + j) * ni + i;
                 ph[u] += (double)e[u];
             }
-            __syncthreads();
+            cluster_sync_global(cl);
         }
         /* 3. E = -grad phi, float32 copy for the push */
         const EfRcp rc = ef_rcp(g);
-        for (int64_t u = tid; u < nn; u += nt) {
+        for (int64_t u = n0 + tid; u < n1; u += nt) {
             const int i = (int)(u % ni), j = (int)((u / ni) % nj), k = (int)(u / ((int64_t)ni * nj));
             double e0, e1, e2;
             ens_efield(g, rc, ph, u, i, j, k, e0, e1, e2);
             ef4[B.node0 + u] = make_float4((float)e0, (float)e1, (float)e2, 0.f);
         }
-        if (tid == 0) {
+        if (rank == 0 && tid == 0) {
             stat[bid].sweeps = sweeps;
             stat[bid].converged = conv;
             stat[bid].residual = L2;
         }
-        __syncthreads();
+        cluster_sync_global(cl);
     }
 }
 
@@ -413,7 +445,7 @@ struct espic_ensemble {
     size_t scratch_bytes = 0;
     int max_it = 10000;
     double tol = 1e-4, omega_req = 0;
-    int chunk = 4096, push_threads = 256, solve_threads = 1024;
+    int chunk = 4096, push_threads = 256, solve_threads = 1024, cluster = 8;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t nlaunch = 0, steps = 0;
@@ -522,10 +554,29 @@ static int ens_push_blocks(espic_ensemble &E) {
     return (int)(E.nwork < b ? (E.nwork > 0 ? E.nwork : 1) : b);
 }
 
-static int ens_solve_blocks(espic_ensemble &E) {
-    int per_sm = 2048 / E.solve_threads;
-    int64_t b = (int64_t)E.sm_count * per_sm;
-    return (int)(E.nbox < b ? E.nbox : b);
+/* the solve launch: clusters of E.cluster CTAs, as many as can be resident
+ * (one box each at a time), at most one per box */
+static cudaError_t ens_launch_solve(espic_ensemble &E, int solve) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = E.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(E.solve_threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = E.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(E.cluster);
+    int ncl = 0;
+    cudaError_t ce = cudaOccupancyMaxActiveClusters(&ncl, (void *)k_ens_solve, &cfg);
+    if (ce != cudaSuccess || ncl < 1) ncl = E.sm_count / E.cluster > 0 ? E.sm_count / E.cluster : 1;
+    if (ncl > E.nbox) ncl = E.nbox;
+    cfg.gridDim = dim3(ncl * E.cluster);
+    return cudaLaunchKernelEx(&cfg, k_ens_solve, (const EnsBox *)E.d_boxes, (const EnsSeg *)E.d_segs, E.nsp,
+                              (const int *)E.d_order, E.nbox, E.d_counter, E.phi, E.rho, E.ecor, E.res, E.ef4, E.acc,
+                              E.total_nodes, E.max_it, E.tol, solve, E.d_stat, E.d_err);
 }
 
 /* enqueue one phase sequence: [push +] deposit, then rho / solve / E */
@@ -537,9 +588,7 @@ static int ens_enqueue(espic_ensemble &E, bool push, bool solve) {
     launch_ens_push(E.stream, push, ens_push_blocks(E), E.push_threads, E.d_boxes, E.d_segs, E.d_work, E.nwork,
                     E.ef4, E.cell, E.off, E.vel, E.total_cap, E.acc, E.total_nodes, E.d_err);
     ECK(cudaMemsetAsync(E.d_counter, 0, sizeof(int), E.stream));
-    k_ens_solve<<<ens_solve_blocks(E), E.solve_threads, 0, E.stream>>>(
-        E.d_boxes, E.d_segs, E.nsp, E.d_order, E.nbox, E.d_counter, E.phi, E.rho, E.ecor, E.res, E.ef4, E.acc,
-        E.total_nodes, E.max_it, E.tol, solve ? 1 : 0, E.d_stat, E.d_err);
+    ECK(ens_launch_solve(E, solve ? 1 : 0));
     E.nlaunch += E.nwork ? 2 : 1;
     cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return efail(ESPIC_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(le));
@@ -767,24 +816,29 @@ extern "C" int espic_ensemble_set_solver(espic_ensemble *h, int max_it, double t
     return ens_upload_tables(E);
 }
 
-extern "C" int espic_ensemble_set_launch(espic_ensemble *h, int chunk, int push_threads, int solve_threads) {
+extern "C" int espic_ensemble_set_launch(espic_ensemble *h, int chunk, int push_threads, int solve_threads,
+                                         int cluster) {
     ENSEMBLE(h);
     bool okp = push_threads == 128 || push_threads == 256 || push_threads == 512;
     bool oks = solve_threads == 256 || solve_threads == 512 || solve_threads == 1024;
-    if (chunk < 256 || chunk > (1 << 24) || !okp || !oks) return efail(ESPIC_ERR_ARG, "bad launch shape");
+    bool okc = cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8;
+    if (chunk < 256 || chunk > (1 << 24) || !okp || !oks || !okc) return efail(ESPIC_ERR_ARG, "bad launch shape");
     if (chunk != E.chunk) E.work_valid = false;
     E.chunk = chunk;
     E.push_threads = push_threads;
     E.solve_threads = solve_threads;
+    E.cluster = cluster;
     ens_drop_graph(E);
     return ESPIC_OK;
 }
 
-extern "C" int espic_ensemble_get_launch(espic_ensemble *h, int *chunk, int *push_threads, int *solve_threads) {
+extern "C" int espic_ensemble_get_launch(espic_ensemble *h, int *chunk, int *push_threads, int *solve_threads,
+                                         int *cluster) {
     ENSEMBLE(h);
     if (chunk) *chunk = E.chunk;
     if (push_threads) *push_threads = E.push_threads;
     if (solve_threads) *solve_threads = E.solve_threads;
+    if (cluster) *cluster = E.cluster;
     return ESPIC_OK;
 }
 
@@ -940,13 +994,14 @@ extern "C" int espic_ensemble_diag(espic_ensemble *h, double *out) {
  * depend on the shape: per-particle pushes, integer deposits, colour-ordered
  * sweeps, fixed-width reductions) with CUDA events around the two phases, and
  * keeps the fastest chunk / push block for the push phase and the fastest
- * solve block for the solve phase.  Consumes (candidates) steps. */
+ * cluster size / solve block for the solve phase.  Consumes 27 steps. */
 extern "C" int espic_ensemble_autotune(espic_ensemble *h, int *chunk, int *push_threads, int *solve_threads,
                                        double *push_ms, double *solve_ms) {
     ENSEMBLE(h);
     const int chunks[] = {1024, 2048, 4096, 8192, 16384};
     const int pts[] = {128, 256, 512};
     const int sts[] = {256, 512, 1024};
+    const int cls[] = {1, 2, 4, 8};
     cudaEvent_t a, b, c;
     ECK(cudaEventCreate(&a));
     ECK(cudaEventCreate(&b));
@@ -965,9 +1020,7 @@ extern "C" int espic_ensemble_autotune(espic_ensemble *h, int *chunk, int *push_
                             E.nwork, E.ef4, E.cell, E.off, E.vel, E.total_cap, E.acc, E.total_nodes, E.d_err);
             ECK(cudaEventRecord(b, E.stream));
             ECK(cudaMemsetAsync(E.d_counter, 0, sizeof(int), E.stream));
-            k_ens_solve<<<ens_solve_blocks(E), E.solve_threads, 0, E.stream>>>(
-                E.d_boxes, E.d_segs, E.nsp, E.d_order, E.nbox, E.d_counter, E.phi, E.rho, E.ecor, E.res, E.ef4,
-                E.acc, E.total_nodes, E.max_it, E.tol, 1, E.d_stat, E.d_err);
+            ECK(ens_launch_solve(E, 1));
             E.nlaunch += 2;
             E.steps++;
             ECK(cudaGetLastError());
@@ -985,28 +1038,31 @@ extern "C" int espic_ensemble_autotune(espic_ensemble *h, int *chunk, int *push_
     E.work_valid = false;
     int rc = ens_build_work(E);
     if (rc) return rc;
-    for (int si = 0; si < 3; si++) {
-        E.solve_threads = sts[si];
-        launch_ens_push(E.stream, true, ens_push_blocks(E), E.push_threads, E.d_boxes, E.d_segs, E.d_work, E.nwork,
-                        E.ef4, E.cell, E.off, E.vel, E.total_cap, E.acc, E.total_nodes, E.d_err);
-        ECK(cudaMemsetAsync(E.d_counter, 0, sizeof(int), E.stream));
-        ECK(cudaEventRecord(b, E.stream));
-        k_ens_solve<<<ens_solve_blocks(E), E.solve_threads, 0, E.stream>>>(
-            E.d_boxes, E.d_segs, E.nsp, E.d_order, E.nbox, E.d_counter, E.phi, E.rho, E.ecor, E.res, E.ef4, E.acc,
-            E.total_nodes, E.max_it, E.tol, 1, E.d_stat, E.d_err);
-        ECK(cudaEventRecord(c, E.stream));
-        E.nlaunch += 2;
-        E.steps++;
-        ECK(cudaGetLastError());
-        ECK(cudaEventSynchronize(c));
-        float ms = 0;
-        ECK(cudaEventElapsedTime(&ms, b, c));
-        if (ms < best_solve) {
-            best_solve = ms;
-            bs = E.solve_threads;
+    int bcl = E.cluster;
+    for (int ki = 0; ki < 4; ki++)
+        for (int si = 0; si < 3; si++) {
+            E.cluster = cls[ki];
+            E.solve_threads = sts[si];
+            launch_ens_push(E.stream, true, ens_push_blocks(E), E.push_threads, E.d_boxes, E.d_segs, E.d_work,
+                            E.nwork, E.ef4, E.cell, E.off, E.vel, E.total_cap, E.acc, E.total_nodes, E.d_err);
+            ECK(cudaMemsetAsync(E.d_counter, 0, sizeof(int), E.stream));
+            ECK(cudaEventRecord(b, E.stream));
+            ECK(ens_launch_solve(E, 1));
+            ECK(cudaEventRecord(c, E.stream));
+            E.nlaunch += 2;
+            E.steps++;
+            ECK(cudaGetLastError());
+            ECK(cudaEventSynchronize(c));
+            float ms = 0;
+            ECK(cudaEventElapsedTime(&ms, b, c));
+            if (ms < best_solve) {
+                best_solve = ms;
+                bs = E.solve_threads;
+                bcl = E.cluster;
+            }
         }
-    }
     E.solve_threads = bs;
+    E.cluster = bcl;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaEventDestroy(c);
