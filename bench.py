@@ -46,6 +46,10 @@ CONFIGS = {
                      radius=0.05, phi_s=-100.0, np=4_000_000, mpw0=40.0, dt=1e-7, sort_every=20),
     "sphere256": dict(n=(256, 256, 512), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
                       radius=0.04, phi_s=-100.0, np=500_000_000, mpw0=0.32, dt=1e-7, sort_every=20),
+    # the 256x256x512 plasma on an eighth of the cells (the same ions per
+    # cell): small enough for a full ncu capture of the push at that density
+    "sphere128": dict(n=(128, 128, 256), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
+                      radius=0.04, phi_s=-100.0, np=60_000_000, mpw0=0.32 * 500 / 60, dt=1e-7, sort_every=20),
     # the reference's configuration 1: ch2 grounded box, FP64 plain form
     "box21": dict(n=(21, 21, 21), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.2), np=90_000, dt=2e-10,
                   sort_every=0),
