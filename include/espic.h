@@ -261,6 +261,20 @@ int espic_deposit_noalloc(const double *d_P, int64_t stride, int64_t n, int ni, 
                           const double x0[3], const double xm[3], double weight_bound, double *d_den,
                           void *stream);
 
+/* ---- output snapshots ------------------------------------------------------- */
+/* Output::fields (ch3/ver2/Output.cpp:12-79) without stalling the step: packs
+ * the node fields of the VTK file -- object_id, node_vol, phi, rho, then den
+ * and den_ave of every species, then ef ([nn][3]) -- into a device buffer on
+ * the world's stream (so later steps do not change it) and copies them to
+ * pinned host memory on a second stream; returns a ticket at once.  Two
+ * snapshots can be in flight; a third reuses the oldest slot after its copy
+ * has finished. */
+int espic_snapshot_begin(espic_world *w, int64_t *ticket);
+/* waits for snapshot `ticket`; *host points at its (7 + 2 * nspecies) * nn
+ * doubles in the order above, valid until the slot is reused by the
+ * snapshot two tickets later.  May be called from another host thread. */
+int espic_snapshot_wait(espic_world *w, int64_t ticket, const double **host, int64_t *count);
+
 /* ---- one whole step --------------------------------------------------------- */
 /* One iteration of the ch3/ver2/Main.cpp:50-72 loop body: sample every
  * source, push + deposit every species (sorting mixed species every

@@ -120,6 +120,8 @@ def lib():
             "espic_profile": [VP, C.c_int],
             "espic_profile_read": [VP, PD, C.POINTER(I64), C.POINTER(I64)],
             "espic_solver_totals": [VP, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)],
+            "espic_snapshot_begin": [VP, C.POINTER(I64)],
+            "espic_snapshot_wait": [VP, I64, C.POINTER(PD), C.POINTER(I64)],
             "espic_ensemble_create": [C.c_int, PI, PD, PD, C.c_int, PD, PD, PD, C.POINTER(I64), C.c_double,
                                       C.POINTER(VP)],
             "espic_ensemble_set_seed": [VP, C.c_uint64],
@@ -281,6 +283,28 @@ class World:
         nl = I64()
         check(lib().espic_profile_read(self.h, None, None, C.byref(nl)))
         return nl.value
+
+    def snapshot_begin(self):
+        """Queue an output snapshot (object_id, node_vol, phi, rho, den and
+        den_ave per species, ef) and return its ticket."""
+        t = I64()
+        check(lib().espic_snapshot_begin(self.h, C.byref(t)))
+        return t.value
+
+    def snapshot_wait(self, ticket):
+        """The snapshot's fields as a dict of numpy copies."""
+        ptr, cnt = PD(), I64()
+        check(lib().espic_snapshot_wait(self.h, ticket, C.byref(ptr), C.byref(cnt)))
+        a = np.ctypeslib.as_array(ptr, shape=(cnt.value,)).copy()
+        nn = self.nn
+        ns = (cnt.value // nn - 7) // 2
+        out = {"object_id": a[:nn].astype(np.int32), "node_vol": a[nn:2 * nn], "phi": a[2 * nn:3 * nn],
+               "rho": a[3 * nn:4 * nn]}
+        for s in range(ns):
+            out["den%d" % s] = a[(4 + s) * nn:(5 + s) * nn]
+            out["den_ave%d" % s] = a[(4 + ns + s) * nn:(5 + ns + s) * nn]
+        out["ef"] = a[(4 + 2 * ns) * nn:].reshape(nn, 3)
+        return out
 
     def solver_totals(self):
         a, b, c = I64(), I64(), I64()

@@ -157,6 +157,14 @@ static void free_world(World &w) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (w.h_small) cudaFreeHost(w.h_small);
+    for (auto &sn : w.snap) {
+        if (sn.copied) cudaEventSynchronize(sn.copied);
+        if (sn.dev) cudaFree(sn.dev);
+        if (sn.host) cudaFreeHost(sn.host);
+        if (sn.packed) cudaEventDestroy(sn.packed);
+        if (sn.copied) cudaEventDestroy(sn.copied);
+    }
+    if (w.snap_stream) cudaStreamDestroy(w.snap_stream);
     if (w.stream) cudaStreamSynchronize(w.stream);
     for (auto &r : w.ranges) {
         cudaEventDestroy(r.a);
@@ -1055,6 +1063,50 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
     if (field == ESPIC_FIELD_RHO) w.rho_version++;
     CHECK_LAUNCH();
     CK(cudaStreamSynchronize(w.stream));
+    return ESPIC_OK;
+}
+
+/* ---------------------------------------------------------------- output snapshots */
+extern "C" int espic_snapshot_begin(espic_world *h, int64_t *ticket) {
+    WORLD(h);
+    if (!ticket) return fail(ESPIC_ERR_ARG, "null ticket");
+    const int ns = (int)w.species.size() < 8 ? (int)w.species.size() : 8;
+    const size_t count = (size_t)(7 + 2 * ns) * w.nn;
+    if (!w.snap_stream) CK(cudaStreamCreateWithFlags(&w.snap_stream, cudaStreamNonBlocking));
+    World::Snapshot &sn = w.snap[w.snap_next & 1];
+    if (sn.copied) CK(cudaEventSynchronize(sn.copied)); /* the slot's previous copy is done */
+    if (sn.count < count) {
+        if (sn.dev) cudaFree(sn.dev);
+        if (sn.host) cudaFreeHost(sn.host);
+        sn.dev = nullptr;
+        sn.host = nullptr;
+        sn.count = 0;
+        CK(cudaMalloc(&sn.dev, count * sizeof(double)));
+        CK(cudaMallocHost(&sn.host, count * sizeof(double)));
+        sn.count = count;
+    }
+    if (!sn.packed) CK(cudaEventCreateWithFlags(&sn.packed, cudaEventDisableTiming));
+    if (!sn.copied) CK(cudaEventCreateWithFlags(&sn.copied, cudaEventDisableTiming));
+    launch_snapshot(w, sn.dev);
+    CHECK_LAUNCH();
+    CK(cudaEventRecord(sn.packed, w.stream));
+    CK(cudaStreamWaitEvent(w.snap_stream, sn.packed, 0));
+    CK(cudaMemcpyAsync(sn.host, sn.dev, count * sizeof(double), cudaMemcpyDeviceToHost, w.snap_stream));
+    CK(cudaEventRecord(sn.copied, w.snap_stream));
+    sn.ticket = w.snap_next++;
+    *ticket = sn.ticket;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_snapshot_wait(espic_world *h, int64_t ticket, const double **host, int64_t *count) {
+    if (!h) return fail(ESPIC_ERR_ARG, "null world handle");
+    World &w = h->w;
+    World::Snapshot &sn = w.snap[ticket & 1];
+    if (ticket < 0 || sn.ticket != ticket) return fail(ESPIC_ERR_STATE, "snapshot %lld is no longer held", (long long)ticket);
+    if (cudaSetDevice(w.device) != cudaSuccess) return fail(ESPIC_ERR_CUDA, "cudaSetDevice failed");
+    CK(cudaEventSynchronize(sn.copied));
+    if (host) *host = sn.host;
+    if (count) *count = (int64_t)sn.count;
     return ESPIC_OK;
 }
 

@@ -142,6 +142,7 @@ void launch_node_vol(World &w);
 void launch_ef4(World &w);
 void launch_fill(World &w, double *x, int64_t n, double v);
 void launch_predict(World &w, bool extrapolate);
+void launch_snapshot(World &w, double *out);
 
 /* k_mixed.cu */
 void launch_push_mixed(World &w, Species &s, bool deposit);

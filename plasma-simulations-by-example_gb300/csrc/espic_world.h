@@ -106,6 +106,17 @@ struct World {
     double last_mass = 0, last_mom = 0, last_en = 0;
     std::vector<Species *> species;
     std::vector<Source> sources;
+    /* output snapshots: two slots of packed node fields (device and pinned
+     * host), copied on their own stream */
+    struct Snapshot {
+        double *dev = nullptr, *host = nullptr;
+        size_t count = 0;
+        cudaEvent_t packed = nullptr, copied = nullptr;
+        int64_t ticket = -1;
+    };
+    Snapshot snap[2];
+    cudaStream_t snap_stream = nullptr;
+    int64_t snap_next = 0;
     /* per-phase event timing */
     bool prof = false;
     std::vector<cudaEvent_t> ev_pool;

@@ -1031,6 +1031,43 @@ __global__ void k_ef_to_ef4(int64_t nn, const double *__restrict__ ef, float4 *e
     ef4[u] = make_float4((float)ef[3 * u], (float)ef[3 * u + 1], (float)ef[3 * u + 2], 0.f);
 }
 
+/* output snapshot: object_id, node_vol, phi, rho, den and den_ave of each
+ * species, ef ([nn][3]), one after the other in that order */
+struct SnapArgs {
+    int ns;
+    const double *den[8], *ave[8];
+};
+
+__global__ void k_snapshot(int64_t nn, const int32_t *__restrict__ obj, const double *__restrict__ vol,
+                           const double *__restrict__ phi, const double *__restrict__ rho,
+                           const double *__restrict__ ef, SnapArgs a, double *out) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    out[u] = (double)obj[u];
+    out[nn + u] = vol[u];
+    out[2 * nn + u] = phi[u];
+    out[3 * nn + u] = rho[u];
+    for (int s = 0; s < a.ns; s++) {
+        out[(4 + s) * nn + u] = a.den[s][u];
+        out[(4 + a.ns + s) * nn + u] = a.ave[s][u];
+    }
+    double *e = out + (4 + 2 * (int64_t)a.ns) * nn;
+    e[3 * u] = ef[3 * u];
+    e[3 * u + 1] = ef[3 * u + 1];
+    e[3 * u + 2] = ef[3 * u + 2];
+}
+
+void launch_snapshot(World &w, double *out) {
+    SnapArgs a;
+    a.ns = (int)w.species.size() < 8 ? (int)w.species.size() : 8;
+    for (int s = 0; s < a.ns; s++) {
+        a.den[s] = w.species[s]->den;
+        a.ave[s] = w.species[s]->den_ave;
+    }
+    k_snapshot<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.obj, w.vol, w.phi, w.rho, w.ef, a, out);
+    w.nlaunch++;
+}
+
 /* Newton predictor: on the unknowns phi <- 2 phi - phi_prev and phi_prev <-
  * the old phi (extrapolate), or only phi_prev <- phi */
 __global__ void k_predict(Geo g, const int32_t *__restrict__ obj, double *phi, double *phi_prev, int extrapolate) {

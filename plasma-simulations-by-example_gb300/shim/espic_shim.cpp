@@ -9,6 +9,8 @@
  * species with a default weight in the mixed form), ESPIC_SEED (Philox key).
  */
 #include <cmath>
+#include <deque>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -46,7 +48,10 @@ World::World(int ni, int nj, int nk)
     time_start = std::chrono::high_resolution_clock::now();
 }
 
+static void join_output_writers();
+
 World::~World() {
+    join_output_writers(); /* files still being written read this world's snapshots */
     if (h) espic_world_destroy(h);
 }
 
@@ -473,8 +478,105 @@ namespace Output {
 std::ofstream f_diag;
 }
 
-/* Output::fields, ch3/ver2/Output.cpp:12-79: VTK ImageData, ASCII */
-void Output::fields(World &world, std::vector<Species> &species) {
+/* Output::fields, ch3/ver2/Output.cpp:12-79: VTK ImageData, ASCII.  The
+ * fields are packed on the GPU and copied to pinned memory behind the step
+ * (espic_snapshot_begin); a writer thread formats them with the same stream
+ * output as the reference, so the caller's loop goes on at once.  At most
+ * two files are in progress; ESPIC_OUTPUT_SYNC=1 writes inline instead. */
+namespace {
+
+struct FieldsJob {
+    std::string name;
+    double x0[3], dh[3];
+    int ni, nj, nk;
+    std::vector<std::string> species;
+    int64_t ticket;
+    espic_world *h;
+};
+
+/* one Field_ in the layout of its operator<<: k outer, j, i inner, a space
+ * after every value, a newline after every k plane */
+template <typename T>
+void write_scalar(std::ostream &out, const double *v, int ni, int nj, int nk) {
+    for (int k = 0; k < nk; k++, out << "\n")
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) out << (T)v[((size_t)k * nj + j) * ni + i] << " ";
+}
+
+void write_vector(std::ostream &out, const double *v, int ni, int nj, int nk) {
+    for (int k = 0; k < nk; k++, out << "\n")
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                const double *e = v + 3 * (((size_t)k * nj + j) * ni + i);
+                out << e[0] << " " << e[1] << " " << e[2] << " ";
+            }
+}
+
+void write_fields(const FieldsJob &J, const double *snap) {
+    std::ofstream out(J.name);
+    if (!out.is_open()) {
+        std::cerr << "Could not open " << J.name << std::endl;
+        return;
+    }
+    const size_t nn = (size_t)J.ni * J.nj * J.nk;
+    const size_t ns = J.species.size();
+    out << "<VTKFile type=\"ImageData\">\n";
+    out << "<ImageData Origin=\"" << J.x0[0] << " " << J.x0[1] << " " << J.x0[2] << "\" ";
+    out << "Spacing=\"" << J.dh[0] << " " << J.dh[1] << " " << J.dh[2] << "\" ";
+    out << "WholeExtent=\"0 " << J.ni - 1 << " 0 " << J.nj - 1 << " 0 " << J.nk - 1 << "\">\n";
+    out << "<PointData>\n";
+    auto array = [&out](const std::string &nm, int comps, const char *type) {
+        out << "<DataArray Name=\"" << nm << "\" NumberOfComponents=\"" << comps << "\" format=\"ascii\" type=\""
+            << type << "\">\n";
+    };
+    array("object_id", 1, "Int32");
+    write_scalar<int>(out, snap, J.ni, J.nj, J.nk);
+    out << "</DataArray>\n";
+    array("NodeVol", 1, "Float64");
+    write_scalar<double>(out, snap + nn, J.ni, J.nj, J.nk);
+    out << "</DataArray>\n";
+    array("phi", 1, "Float64");
+    write_scalar<double>(out, snap + 2 * nn, J.ni, J.nj, J.nk);
+    out << "</DataArray>\n";
+    array("rho", 1, "Float64");
+    write_scalar<double>(out, snap + 3 * nn, J.ni, J.nj, J.nk);
+    out << "</DataArray>\n";
+    for (size_t s = 0; s < ns; s++) {
+        array("nd." + J.species[s], 1, "Float64");
+        write_scalar<double>(out, snap + (4 + s) * nn, J.ni, J.nj, J.nk);
+        out << "</DataArray>\n";
+    }
+    for (size_t s = 0; s < ns; s++) {
+        array("nd-ave." + J.species[s], 1, "Float64");
+        write_scalar<double>(out, snap + (4 + ns + s) * nn, J.ni, J.nj, J.nk);
+        out << "</DataArray>\n";
+    }
+    array("ef", 3, "Float64");
+    write_vector(out, snap + (4 + 2 * ns) * nn, J.ni, J.nj, J.nk);
+    out << "</DataArray>\n";
+    out << "</PointData>\n</ImageData>\n</VTKFile>\n";
+}
+
+/* writer threads of the files in progress, oldest first; joined when a
+ * third file starts and at exit */
+struct Writers {
+    std::deque<std::thread> q;
+    void join_all() {
+        while (!q.empty()) {
+            q.front().join();
+            q.pop_front();
+        }
+    }
+    ~Writers() { join_all(); }
+} writers;
+
+}  // namespace
+
+static void join_output_writers() { writers.join_all(); }
+
+namespace {
+
+void fields_sync(World &world, std::vector<Species> &species) {
     std::stringstream name;
     name << "results/fields_" << std::setfill('0') << std::setw(5) << world.getTs() << ".vti";
     std::ofstream out(name.str());
@@ -511,6 +613,52 @@ void Output::fields(World &world, std::vector<Species> &species) {
     array("ef", 3, "Float64");
     out << world.ef << "</DataArray>\n";
     out << "</PointData>\n</ImageData>\n</VTKFile>\n";
+}
+
+}  // namespace
+
+void Output::fields(World &world, std::vector<Species> &species) {
+    const char *sync = std::getenv("ESPIC_OUTPUT_SYNC");
+    if (sync && sync[0] == '1') {
+        fields_sync(world, species);
+        return;
+    }
+    /* host edits reach the device before the snapshot reads it */
+    world.phi.push();
+    world.rho.push();
+    world.ef.push();
+    for (Species &sp : species) {
+        sp.den.push();
+        sp.den_ave.push();
+    }
+    while (writers.q.size() >= 2) {
+        writers.q.front().join();
+        writers.q.pop_front();
+    }
+    FieldsJob J;
+    std::stringstream name;
+    name << "results/fields_" << std::setfill('0') << std::setw(5) << world.getTs() << ".vti";
+    J.name = name.str();
+    double3 x0 = world.getX0(), dh = world.getDh();
+    for (int d = 0; d < 3; d++) {
+        J.x0[d] = x0[d];
+        J.dh[d] = dh[d];
+    }
+    J.ni = world.ni;
+    J.nj = world.nj;
+    J.nk = world.nk;
+    for (Species &sp : species) J.species.push_back(sp.name);
+    J.h = world.handle();
+    ck(espic_snapshot_begin(J.h, &J.ticket), "Output::fields");
+    writers.q.emplace_back([J]() {
+        const double *snap = nullptr;
+        int64_t count = 0;
+        if (espic_snapshot_wait(J.h, J.ticket, &snap, &count) != ESPIC_OK) {
+            std::cerr << "Output::fields: snapshot " << J.ticket << " lost" << std::endl;
+            return;
+        }
+        write_fields(J, snap);
+    });
 }
 
 void Output::screenOutput(World &world, std::vector<Species> &species) {

@@ -90,3 +90,28 @@ def test_drop_in_sphere_runs(tmp_path, espic):
     last = lines[-1].split()
     assert last[0] == "obj" and last[1] == "1"  # node (10,10,15) is inside the sphere
     assert float(last[3]) == -100.0
+
+
+@pytest.mark.gpu
+def test_drop_in_output_async_matches_inline(tmp_path, espic):
+    """Output::fields packs the fields on the GPU and formats them on a writer
+    thread; the files are byte-identical to formatting the host mirrors
+    inline (ESPIC_OUTPUT_SYNC=1)."""
+    E = _espic_module()
+    exe = str(tmp_path / "output_main")
+    r = E.compile_drop_in(os.path.join(DROP, "output_main.cpp"), exe)
+    assert r.returncode == 0, r.stderr[-2000:]
+    files = {}
+    for mode in ("async", "sync"):
+        d = tmp_path / mode
+        (d / "results").mkdir(parents=True)
+        env = dict(os.environ, ESPIC_SEED="7")
+        if mode == "sync":
+            env["ESPIC_OUTPUT_SYNC"] = "1"
+        p = subprocess.run([exe, "17"], capture_output=True, text=True, cwd=d, env=env, timeout=300)
+        assert p.returncode == 0, p.stderr[-2000:]
+        files[mode] = {f: (d / "results" / f).read_bytes() for f in sorted(os.listdir(d / "results"))}
+    assert len(files["async"]) >= 3 and sorted(files["async"]) == sorted(files["sync"])
+    assert files["async"] == files["sync"]
+    body = files["async"][sorted(files["async"])[-1]].decode()
+    assert body.startswith("<VTKFile type=\"ImageData\">") and body.count("<DataArray") == 7

@@ -513,3 +513,29 @@ def test_thermal_loader(espic, po):
         sigma = np.sqrt(K * T / (16 * AMU))
         assert abs(V[2].mean() - 7000.0) < 5 * sigma / np.sqrt(4e5)
         assert abs(V[0].std() / sigma - 1) < 0.01
+
+
+def test_output_snapshot_is_taken_at_begin(espic, po):
+    """espic_snapshot_begin packs the output fields in stream order: later
+    steps do not change a snapshot that is still being copied."""
+    with world(espic, SPH) as w:
+        w.setTime(1e-7, 100)
+        w.addSphere(*SPHERE)
+        w.addInlet()
+        s = espic.Species(w, "O+", 16 * AMU, QE, mpw0=50.0, capacity=1 << 16, form=espic.FORM_MIXED,
+                          walls=espic.WALLS_ABSORB)
+        src = espic.BeamSource(s, 7000.0, 1e10)
+        sol = espic.PotentialSolver(w, espic.SOLVER_GS, 20000, 1e-4)
+        sol.setReferenceValues(0.0, 1.5, 1e10)
+        for _ in range(3):
+            w.step(0)
+        s.updateAverages()
+        want = dict(object_id=w.object_id, node_vol=w.node_vol, phi=w.phi, rho=w.rho, den0=s.den,
+                    den_ave0=s.den_ave, ef=w.ef)
+        t = w.snapshot_begin()
+        for _ in range(3):
+            w.step(0)
+        got = w.snapshot_wait(t)
+        for k, v in want.items():
+            assert np.array_equal(got[k], v), k
+        assert not np.array_equal(w.phi, want["phi"])
