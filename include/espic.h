@@ -139,6 +139,25 @@ int espic_sort(espic_world *w, int sp);
  * (ch4/Source.h:32-46; temp in K) on the z = x0 face. */
 int espic_source_create(espic_world *w, int sp, double v_drift, double den, double temp,
                         int *source_id);
+/* Velocity and count modes of a source.  Velocity: ESPIC_BEAM_COLD (v_drift
+ * along z, ColdBeamSource, ch3/ver2/Source.cpp:4-27), ESPIC_BEAM_WARM (the
+ * ch4 approximation, sampleIsotropicVel x sampleVth, ch4/Species.cpp:149-175;
+ * the default when temp > 0), ESPIC_BEAM_ISOTROPIC (ch9/MPI/src/Source.cpp:
+ * 39-59: isotropic direction at the speed sqrt(2 kT/m), drift added, v_z < 0
+ * reflected) and ESPIC_BEAM_MAXWELLIAN (normal components of deviation
+ * sqrt(kT/m) by Box-Muller, drift added, v_z < 0 reflected).  Count:
+ * ESPIC_COUNT_RANDOM ((int)(N/mpw0 + U), ch3/ver2/Source.cpp:18) or
+ * ESPIC_COUNT_REMAINDER ((int)(N/mpw0 + r), the fraction r carried to the next
+ * sample, ch9/MPI/src/Source.cpp:20-27).  Explicit uniforms
+ * (espic_source_sample_uniforms): one count slot (unused by the remainder
+ * count), then 2 / 13 / 4 / 6 per particle for the four velocity modes. */
+#define ESPIC_BEAM_COLD 0
+#define ESPIC_BEAM_WARM 1
+#define ESPIC_BEAM_ISOTROPIC 2
+#define ESPIC_BEAM_MAXWELLIAN 3
+#define ESPIC_COUNT_RANDOM 0
+#define ESPIC_COUNT_REMAINDER 1
+int espic_source_set_mode(espic_world *w, int source, int velocity_mode, int count_mode);
 /* ColdBeamSource::sample / WarmBeamSource::sample, ch3/ver2/Source.cpp:4-27,
  * ch4/Source.cpp:31-55, drawing from the world's Philox stream. */
 int espic_source_sample(espic_world *w, int source);

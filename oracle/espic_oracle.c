@@ -408,6 +408,61 @@ int64_t eo_inject_warm(const eo_grid *g, const double *ef, double charge, double
     return np;
 }
 
+/* Source::sample of ch9/MPI (ch9/MPI/src/Source.cpp:5-72) and a
+ * drifting-Maxwellian beam.  mode 2: isotropic direction (theta, R) at the
+ * speed sqrt(2 Kb T / m) with ch9/MPI's Kb = 1.3806488e-23 and PI = acos(-1),
+ * drift added to z, v_z < 0 reflected; 4 uniforms per particle (x, y, theta,
+ * R).  mode 3: normal components of deviation sqrt(k T / m) by Box-Muller
+ * (radius sqrt(-2 ln(1 - u)), angle 2 pi u), drift added, v_z < 0 reflected;
+ * 6 uniforms per particle.  The count is the remainder count of ch9/MPI
+ * (*rem carried) when rem != NULL, else (int)(N + u[0]).  The rewind is that
+ * of addParticle here and of ch9/MPI/src/Source.cpp:61-68 (same expression). */
+int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, double temp, int mode, double *rem,
+                       const double *u, int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap) {
+    const double pi = acos(-1.0);
+    double Lx = g->dh[0] * (g->ni - 1);
+    double Ly = g->dh[1] * (g->nj - 1);
+    int num_sim;
+    if (rem) {
+        double A = Lx * Ly;
+        double num_real = den * v_drift * A * dt;
+        double f = num_real / mpw0 + *rem;
+        num_sim = (int)f;
+        *rem = f - num_sim;
+    } else {
+        num_sim = eo_inject_count(g, dt, mpw0, v_drift, den, u[0]);
+    }
+    const int upp = mode == 2 ? 4 : 6;
+    int64_t np = np0;
+    for (int i = 0; i < num_sim; i++) {
+        const double *ui = u + 1 + upp * (int64_t)i;
+        double pos[3] = {g->x0[0] + ui[0] * Lx, g->x0[1] + ui[1] * Ly, g->x0[2]};
+        double vel[3];
+        if (mode == 2) {
+            double v_th = sqrt(2 * 1.3806488e-23 * temp / mass);
+            double theta = 2 * pi * ui[2];
+            double R = -1.0 + 2 * ui[3];
+            double a = sqrt(1 - R * R);
+            vel[0] = v_th * (cos(theta) * a);
+            vel[1] = v_th * (sin(theta) * a);
+            vel[2] = v_th * R + v_drift;
+        } else {
+            double sig = sqrt(EO_K * temp / mass);
+            double r1 = sqrt(-2.0 * log(1.0 - ui[2])), a1 = 2 * pi * ui[3];
+            double r2 = sqrt(-2.0 * log(1.0 - ui[4])), a2 = 2 * pi * ui[5];
+            vel[0] = sig * (r1 * cos(a1));
+            vel[1] = sig * (r1 * sin(a1));
+            vel[2] = sig * (r2 * cos(a2)) + v_drift;
+        }
+        if (vel[2] < 0) vel[2] = -vel[2];
+        np = eo_add_particles(g, ef, charge, mass, dt, pos, vel, &mpw0, 1, P, stride, np, cap);
+        if (np < 0) return -1;
+    }
+    if (u_used) *u_used = 1 + upp * (int64_t)num_sim;
+    return np;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Corner weights of Field_::scatter, ch2/Field.h:164-183, in the reference's
  * corner order: value*(1-di)*(1-dj)*(1-dk) evaluated left to right. */

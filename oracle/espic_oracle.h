@@ -81,6 +81,9 @@ int64_t eo_inject_warm(const eo_grid *g, const double *ef, double charge, double
                        double mpw0, double v_drift, double den, double temp, const double *u,
                        int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap);
 int eo_inject_count(const eo_grid *g, double dt, double mpw0, double v_drift, double den, double u0);
+int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double mass, double dt,
+                       double mpw0, double v_drift, double den, double temp, int mode, double *rem,
+                       const double *u, int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap);
 
 /* ---- deposit --------------------------------------------------------- */
 void eo_deposit_fp64(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *acc);

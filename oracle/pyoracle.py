@@ -68,6 +68,9 @@ def _sig(L):
     L.eo_inject_count.argtypes = [C.POINTER(Grid), D, D, D, D, D]
     L.eo_inject_cold.restype = I64
     L.eo_inject_cold.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, PD, PI64, PD, I64, I64, I64]
+    L.eo_inject_beam.restype = I64
+    L.eo_inject_beam.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, C.c_int, PD, PD, PI64, PD, I64, I64,
+                                 I64]
     L.eo_inject_warm.restype = I64
     L.eo_inject_warm.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, PD, PI64, PD, I64, I64,
                                  I64]
@@ -220,6 +223,19 @@ def inject(g, ef, charge, mass, dt, mpw0, v_drift, den, u, temp=None, P=None):
     else:
         m = L.eo_inject_warm(C.byref(g), pd(ef), charge, mass, dt, mpw0, v_drift, den, temp, pd(u),
                              C.byref(used), pd(B), B.shape[1], np0, B.shape[1])
+    return np.ascontiguousarray(B[:, :m]), used.value
+
+
+def inject_beam(g, ef, charge, mass, dt, mpw0, v_drift, den, temp, mode, u, rem=None, max_new=100000):
+    """eo_inject_beam: mode 2 (ch9/MPI isotropic) or 3 (Maxwellian); with rem
+    (a one-element float64 array) the remainder count, updated in place."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    B = np.zeros((7, max_new))
+    used = C.c_int64(0)
+    rp = None if rem is None else rem.ctypes.data_as(PD)
+    m = lib().eo_inject_beam(C.byref(g), pd(ef), charge, mass, dt, mpw0, v_drift, den, temp, mode, rp, pd(u),
+                             C.byref(used), pd(B), B.shape[1], 0, B.shape[1])
+    assert m >= 0
     return np.ascontiguousarray(B[:, :m]), used.value
 
 

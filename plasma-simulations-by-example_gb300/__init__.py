@@ -23,6 +23,8 @@ FORM_FP64, FORM_MIXED = 0, 1
 WALLS_REFLECT, WALLS_ABSORB = 0, 1
 SOLVER_SOR, SOLVER_GS, SOLVER_PCG, SOLVER_QN = 0, 1, 2, 3
 FIELD_PHI, FIELD_RHO, FIELD_NODE_VOL, FIELD_EF, FIELD_DEN, FIELD_DEN_AVE, FIELD_OBJECT_ID = range(7)
+BEAM_COLD, BEAM_WARM, BEAM_ISOTROPIC, BEAM_MAXWELLIAN = range(4)
+COUNT_RANDOM, COUNT_REMAINDER = 0, 1
 
 QE, AMU, ME, K, EPS_0 = 1.602176565e-19, 1.660538921e-27, 9.10938215e-31, 1.380648e-23, 8.85418782e-12
 
@@ -100,6 +102,7 @@ def lib():
             "espic_source_create": [VP, C.c_int, C.c_double, C.c_double, C.c_double, PI],
             "espic_source_sample": [VP, C.c_int],
             "espic_source_sample_uniforms": [VP, C.c_int, PD, I64, C.POINTER(I64)],
+            "espic_source_set_mode": [VP, C.c_int, C.c_int, C.c_int],
             "espic_solver_set": [VP, C.c_int, C.c_int, C.c_double],
             "espic_solver_set_reference": [VP, C.c_double, C.c_double, C.c_double],
             "espic_solver_set_newton": [VP, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int],
@@ -435,6 +438,11 @@ class BeamSource:
         self.world = species.world
         self.id = sid.value
         self.temp = temp
+
+    def set_mode(self, velocity_mode, count_mode=COUNT_RANDOM):
+        """BEAM_COLD / BEAM_WARM (ch4) / BEAM_ISOTROPIC (ch9/MPI) /
+        BEAM_MAXWELLIAN velocities; COUNT_RANDOM or COUNT_REMAINDER (ch9/MPI)."""
+        check(lib().espic_source_set_mode(self.world.h, self.id, velocity_mode, count_mode))
 
     def sample(self, u=None):
         if u is None:

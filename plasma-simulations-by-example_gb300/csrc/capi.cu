@@ -711,17 +711,28 @@ extern "C" int espic_source_create(espic_world *h, int sp, double v_drift, doubl
     src.v_drift = v_drift;
     src.den = den;
     src.temp = temp;
+    src.vmode = temp > 0 ? ESPIC_BEAM_WARM : ESPIC_BEAM_COLD;
+    src.count_mode = ESPIC_COUNT_RANDOM;
     w.sources.push_back(src);
     *source_id = (int)w.sources.size() - 1;
     return ESPIC_OK;
 }
 
 /* ColdBeamSource::sample, ch3/ver2/Source.cpp:7-18: (int)(n v A dt/mpw0 + U) */
-static int inject_count(const World &w, const Source &src, double mpw0, double u0) {
+/* macroparticles of one sample: (int)(N_real / mpw0 + U) (ch3/ver2/Source.cpp:
+ * 18) or, with the remainder count, (int)(N_real / mpw0 + remainder) with the
+ * fraction carried to the next call (ch9/MPI/src/Source.cpp:20-27) */
+static int inject_count(const World &w, Source &src, double mpw0, double u0) {
     double Lx = w.g.dh[0] * (w.g.ni - 1);
     double Ly = w.g.dh[1] * (w.g.nj - 1);
     double A = Lx * Ly;
     double num_real = src.den * src.v_drift * A * w.dt;
+    if (src.count_mode == ESPIC_COUNT_REMAINDER) {
+        double f = num_real / mpw0 + src.remainder;
+        int n = (int)f;
+        src.remainder = f - n;
+        return n;
+    }
     return (int)(num_real / mpw0 + u0);
 }
 
@@ -736,7 +747,7 @@ extern "C" int espic_source_sample(espic_world *h, int source) {
     int num_sim = inject_count(w, src, s.mpw0, u0);
     if (num_sim <= 0) return ESPIC_OK;
     PhaseScope ph(w, ESPIC_PHASE_INJECT);
-    launch_inject(w, s, num_sim, src.v_drift, src.temp, nullptr, stream_id);
+    launch_inject(w, s, num_sim, src.v_drift, src.temp, src.vmode, nullptr, stream_id);
     CHECK_LAUNCH();
     return ESPIC_OK;
 }
@@ -749,7 +760,7 @@ extern "C" int espic_source_sample_uniforms(espic_world *h, int source, const do
     Source &src = w.sources[source];
     Species &s = *w.species[src.sp];
     int num_sim = inject_count(w, src, s.mpw0, u[0]);
-    int64_t upp = src.temp > 0 ? 13 : 2;
+    int64_t upp = beam_uniforms(src.vmode);
     int64_t need = 1 + upp * (int64_t)(num_sim > 0 ? num_sim : 0);
     if (nu < need) return fail(ESPIC_ERR_ARG, "%lld uniforms given, %lld needed", (long long)nu, (long long)need);
     if (used) *used = need;
@@ -758,10 +769,26 @@ extern "C" int espic_source_sample_uniforms(espic_world *h, int source, const do
     if (rc != ESPIC_OK) return rc;
     CK(cudaMemcpyAsync(w.d_u, u, need * sizeof(double), cudaMemcpyHostToDevice, w.stream));
     PhaseScope ph(w, ESPIC_PHASE_INJECT);
-    launch_inject(w, s, num_sim, src.v_drift, src.temp, w.d_u, 0);
+    launch_inject(w, s, num_sim, src.v_drift, src.temp, src.vmode, w.d_u, 0);
     CHECK_LAUNCH();
     CK(cudaStreamSynchronize(w.stream));
     return take_device_errors(w);
+}
+
+extern "C" int espic_source_set_mode(espic_world *h, int source, int velocity_mode, int count_mode) {
+    WORLD(h);
+    if (source < 0 || source >= (int)w.sources.size()) return fail(ESPIC_ERR_ARG, "bad source id");
+    if (velocity_mode < ESPIC_BEAM_COLD || velocity_mode > ESPIC_BEAM_MAXWELLIAN)
+        return fail(ESPIC_ERR_ARG, "unknown velocity mode");
+    if (count_mode != ESPIC_COUNT_RANDOM && count_mode != ESPIC_COUNT_REMAINDER)
+        return fail(ESPIC_ERR_ARG, "unknown count mode");
+    Source &src = w.sources[source];
+    if (velocity_mode != ESPIC_BEAM_COLD && !(src.temp > 0))
+        return fail(ESPIC_ERR_ARG, "a thermal velocity mode needs a temperature > 0");
+    src.vmode = velocity_mode;
+    src.count_mode = count_mode;
+    src.remainder = 0;
+    return ESPIC_OK;
 }
 
 /* ---------------------------------------------------------------- solver */

@@ -130,7 +130,7 @@ void launch_load_qs(World &w, Species &s, const double x1[3], const double x2[3]
                     const int num_mp[3]);
 void launch_load_thermal(World &w, Species &s, const double x1[3], const double x2[3], double mpw,
                          int64_t num_mp, const double vd[3], double temp, const double *d_u, uint64_t stream_id);
-void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp,
+void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp, int vmode,
                    const double *d_u, uint64_t stream_id);
 void launch_diag(World &w, Species &s, double *d_out5);
 void launch_pe(World &w, double *d_out1);

@@ -49,7 +49,13 @@ struct Source {
     int sp = 0;
     double v_drift = 0, den = 0, temp = 0;
     uint64_t calls = 0;
+    int vmode = 0;         /* ESPIC_BEAM_*: cold, ch4 warm, ch9 isotropic, Maxwellian */
+    int count_mode = 0;    /* ESPIC_COUNT_*: random, remainder */
+    double remainder = 0;  /* carried fraction of a macroparticle (remainder count) */
 };
+
+/* uniforms a beam particle consumes, by velocity mode */
+__host__ __device__ inline int beam_uniforms(int vmode) { return vmode == 1 ? 13 : (vmode == 2 ? 4 : (vmode == 3 ? 6 : 2)); }
 
 struct World {
     Geo g{};

@@ -420,14 +420,16 @@ struct GenQS { /* Species::loadParticlesBoxQS, ch2/Species.cpp:101-141 */
     }
 };
 
-struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27) and
-                    WarmBeamSource::sample (ch4/Source.cpp:31-55) */
+struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27),
+                    WarmBeamSource::sample (ch4/Source.cpp:31-55),
+                    Source::sample of ch9/MPI (ch9/MPI/src/Source.cpp:5-72)
+                    and a drifting-Maxwellian beam */
     double x0[3], Lx, Ly, v_drift, mpw0, v_th;
-    int warm;
-    const double *u; /* count draw at 0, then 2 or 13 per particle */
+    int mode; /* 0 cold, 1 ch4 warm, 2 ch9 isotropic, 3 Maxwellian */
+    const double *u; /* count draw at 0, then beam_uniforms(mode) per particle */
     uint64_t seed, stream;
     __device__ double U(int64_t k) const { return u ? u[k] : philox_uniform(seed, stream, (uint64_t)k); }
-    __device__ int64_t base(int64_t i) const { return 1 + (warm ? 13 : 2) * i; }
+    __device__ int64_t base(int64_t i) const { return 1 + (int64_t)beam_uniforms(mode) * i; }
     __device__ void pos(int64_t i, double x[3]) const {
         int64_t b = base(i);
         x[0] = x0[0] + U(b) * Lx;
@@ -437,10 +439,35 @@ struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27) and
     __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
         pos(i, x);
         w_ = mpw0;
-        if (!warm) {
+        if (mode == 0) {
             v[0] = 0;
             v[1] = 0;
             v[2] = v_drift;
+            return;
+        }
+        if (mode == 2) {
+            /* isotropic direction at speed v_th, drift added, v_z < 0
+             * reflected (ch9/MPI/src/Source.cpp:39-59, PI = acos(-1)) */
+            int64_t b = base(i) + 2;
+            double theta = 2 * 3.141592653589793 * U(b);
+            double r = -1.0 + 2 * U(b + 1);
+            double a = sqrt(1 - r * r);
+            v[0] = v_th * (cos(theta) * a);
+            v[1] = v_th * (sin(theta) * a);
+            v[2] = v_th * r + v_drift;
+            if (v[2] < 0) v[2] = -v[2];
+            return;
+        }
+        if (mode == 3) {
+            /* drifting Maxwellian: normal components by Box-Muller with
+             * sigma = v_th (here sqrt(kT/m)), v_z < 0 reflected as above */
+            int64_t b = base(i) + 2;
+            double r1 = sqrt(-2.0 * log(1.0 - U(b))), a1 = 2 * 3.141592653589793 * U(b + 1);
+            double r2 = sqrt(-2.0 * log(1.0 - U(b + 2))), a2 = 2 * 3.141592653589793 * U(b + 3);
+            v[0] = v_th * (r1 * cos(a1));
+            v[1] = v_th * (r1 * sin(a1));
+            v[2] = v_th * (r2 * cos(a2)) + v_drift;
+            if (v[2] < 0) v[2] = -v[2];
             return;
         }
         /* Species::sampleIsotropicVel and sampleVth, ch4/Species.cpp:149-175 */
@@ -1291,7 +1318,7 @@ void launch_load_thermal(World &w, Species &s, const double x1[3], const double 
     append(w, s, g, num_mp, s.uniform_w ? 0 : 1);
 }
 
-void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp, const double *d_u,
+void launch_inject(World &w, Species &s, int num_sim, double v_drift, double temp, int vmode, const double *d_u,
                    uint64_t stream_id) {
     GenBeam b;
     for (int d = 0; d < 3; d++) b.x0[d] = w.g.x0[d];
@@ -1299,8 +1326,13 @@ void launch_inject(World &w, Species &s, int num_sim, double v_drift, double tem
     b.Ly = w.g.dh[1] * (w.g.nj - 1);
     b.v_drift = v_drift;
     b.mpw0 = s.mpw0;
-    b.warm = temp > 0;
-    b.v_th = b.warm ? sqrt(2 * KB * temp / s.mass) : 0;
+    b.mode = vmode;
+    /* thermal speed: sqrt(2 k T / m) of ch4 (KB) and of ch9/MPI (its own
+     * Kb = 1.3806488e-23, ch9/MPI/include/World.h:17); sqrt(k T / m) per
+     * component for the Maxwellian */
+    b.v_th = vmode == 1 ? sqrt(2 * KB * temp / s.mass)
+                        : (vmode == 2 ? sqrt(2 * 1.3806488e-23 * temp / s.mass)
+                                      : (vmode == 3 ? sqrt(KB * temp / s.mass) : 0.0));
     b.u = d_u;
     b.seed = w.seed;
     b.stream = stream_id;
