@@ -137,6 +137,14 @@ int main(int argc, char **argv) {
             solver.computeEF();
         }
         std::vector<double> hist, us, ucount;
+        /* optional batch means of den (species 0) and phi: avg = [first ts, steps per batch, batches] */
+        int a_from = 0, a_len = 0, a_nb = 0;
+        if (kv_has(in, "avg")) {
+            const std::vector<double> &a = kv_get(in, "avg");
+            a_from = (int)a[0]; a_len = (int)a[1]; a_nb = (int)a[2];
+        }
+        size_t nn = (size_t)ni * nj * nk;
+        std::vector<double> den_b((size_t)a_nb * nn, 0.0), phi_b((size_t)a_nb * nn, 0.0);
         while (world.advanceTime()) {
             Rnd before = rnd;
             for (ColdBeamSource &s : sources) s.sample();
@@ -165,6 +173,20 @@ int main(int argc, char **argv) {
             }
             hist.push_back(world.getPE());
             hist.push_back(ss);
+            int ts = world.getTs();
+            if (a_len > 0 && ts >= a_from && (ts - a_from) / a_len < a_nb) {
+                size_t b = (size_t)((ts - a_from) / a_len) * nn;
+                std::vector<double> d = field_out(species[0].den, ni, nj, nk);
+                std::vector<double> p = field_out(world.phi, ni, nj, nk);
+                for (size_t n = 0; n < nn; n++) {
+                    den_b[b + n] += d[n] / a_len;
+                    phi_b[b + n] += p[n] / a_len;
+                }
+            }
+        }
+        if (a_nb > 0) {
+            out["sp0_den_batches"] = den_b;
+            out["phi_batches"] = phi_b;
         }
         out["hist"] = hist;
         out["u"] = us;
@@ -174,6 +196,7 @@ int main(int argc, char **argv) {
         for (int s = 0; s < ns; s++) {
             out["sp" + std::to_string(s) + "_P"] = particles_out(species[s]);
             out["sp" + std::to_string(s) + "_den"] = field_out(species[s].den, ni, nj, nk);
+            out["sp" + std::to_string(s) + "_den_ave"] = field_out(species[s].den_ave, ni, nj, nk);
         }
     } else {
         fprintf(stderr, "unknown op %s\n", op.c_str());

@@ -2,7 +2,8 @@
 CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
-Run here, where the reference checkout exists:  python tests/golden/make_golden.py
+Run here, where the reference checkout exists:
+    python tests/golden/make_golden.py [base] [steady]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -13,7 +14,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 from oracle import build_ref, pyoracle as po  # noqa: E402
+import steady_stats as ss  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 QE, AMU, ME, K = 1.602176565e-19, 1.660538921e-27, 9.10938215e-31, 1.380648e-23
@@ -207,8 +210,48 @@ def sphere_cases(rng):
          mpw0=5e2)
 
 
+def steady_run(seed):
+    """One 600-step run of the ch3/ver2 main loop at the reference's own
+    macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
+    phi over time steps 200-599 and the reference's den_ave."""
+    st = base_inputs(SPH, ss.DT, steps=[ss.STEPS], ns=[1], sp0_mq=[16 * AMU, QE, ss.MPW0], seed=[seed],
+                     sphere=SPHERE, inlet=[1], source=[7000.0, 1e10], ref=[0.0, 1.5, 1e10],
+                     max_it=[20000], tol=[1e-4], initial_solve=[1], avg=list(ss.AVG))
+    o = po.run_reference("ref_ch3", "steps", st)
+    hist = o["hist"].reshape(-1, 9)     # ts, np, real count, momentum (3), KE, PE, steady
+    nb = ss.AVG[2]
+    out = ss.batch_profiles(o["sp0_den_batches"].reshape(nb, -1), o["phi_batches"].reshape(nb, -1))
+    tot = np.zeros((nb, 3))
+    for row in hist:
+        b = ss.batch_index(int(row[0]))
+        if b >= 0:
+            tot[b] += row[[1, 6, 7]] / ss.AVG[1]
+    out["totals"] = tot
+    ave = ss.profiles(o["sp0_den_ave"], o["phi"])
+    out.update({"ave_" + k: ave[k] for k in ("axial", "wake", "radial")})
+    out["steady_ts"] = hist[np.nonzero(hist[:, 8])[0][0], 0]
+    return out
+
+
+def steady_cases():
+    """Steady-state statistics of the sphere run, two seeds (run concurrently)."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(2) as ex:
+        runs = list(ex.map(steady_run, (1, 2)))
+    arrays = {}
+    for seed, r in zip((1, 2), runs):
+        arrays.update({"%s_s%d" % (k, seed): v for k, v in r.items()})
+    save("sphere_steady", steps=ss.STEPS, dt=ss.DT, mpw0=ss.MPW0, avg=np.array(ss.AVG), **arrays)
+
+
 if __name__ == "__main__":
+    # optional arguments select cases: "base" (box and sphere, one random
+    # stream), "steady" (default: both)
+    cases = sys.argv[1:] or ["base", "steady"]
     build_ref.build_reference()
-    rng = np.random.default_rng(20261203)
-    box_cases(rng)
-    sphere_cases(rng)
+    if "base" in cases:
+        rng = np.random.default_rng(20261203)
+        box_cases(rng)
+        sphere_cases(rng)
+    if "steady" in cases:
+        steady_cases()
