@@ -254,50 +254,80 @@ __device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &
 
 /* node-grid half sweep of colour c over the unknowns; with C != null the
  * neighbours are read with the coarse correction added (post-smoothing);
- * adds r*z and z*z of the nodes it updated to rz and zz */
+ * adds r*z and z*z of the nodes it updated to rz and zz.  Each thread takes
+ * two list entries per pass and issues every load of both before any store
+ * (a padding entry reads the interior node (1,1,1) and stores nothing), so
+ * twice as many loads are in flight as with one node per pass. */
 template <typename T>
 __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale, T &rz, T &zz) {
     int64_t t0, ts;
     span(true, t0, ts);
     const int32_t *list = F.list[c], *pk = F.pk[c];
-    for (int64_t t = t0; t < F.nlist; t += ts) {
-        int32_t uu = list[t];
-        if (uu < 0) continue;
-        int64_t u = uu;
+    const Geo &g = F.g;
+    const int64_t safe = ((int64_t)g.nj + 1) * g.ni + 1;
+    for (int64_t t = t0; t < F.nlist; t += 2 * ts) {
+        const int64_t tq[2] = {t, t + ts};
+        int64_t u[2];
+        bool ok[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int32_t uu = tq[q] < F.nlist ? list[tq[q]] : -1;
+            ok[q] = uu >= 0;
+            u[q] = ok[q] ? (int64_t)uu : safe;
+        }
         /* interior node: all six neighbours are in bounds, so their loads
          * are issued before the code word arrives; the code only selects */
-        uint16_t cc = F.code[u];
-        T ru = F.r[u];
-        T dBu = F.dg[u];
-        T zn[6];
+        uint16_t cc[2];
+        T ru[2], dBu[2], zn[2][6];
 #pragma unroll
-        for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
-        if (C) {
-            const MgLevel<T> &Cc = *C;
-            int32_t p = pk[t];
-            int i = p & 1023, j = (p >> 10) & 1023, k = p >> 20;
-            int32_t row = ((k >> 1) * Cc.ny + (j >> 1)) * Cc.nx;
-            int32_t ci = i >> 1;
-            int32_t Ix0 = row + ((i - 1) >> 1), Ix1 = row + ((i + 1) >> 1);
-            int32_t Iy0 = ((k >> 1) * Cc.ny + ((j - 1) >> 1)) * Cc.nx + ci;
-            int32_t Iy1 = ((k >> 1) * Cc.ny + ((j + 1) >> 1)) * Cc.nx + ci;
-            int32_t Iz0 = (((k - 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ci;
-            int32_t Iz1 = (((k + 1) >> 1) * Cc.ny + (j >> 1)) * Cc.nx + ci;
-            zn[0] += scale * Cc.e[Ix0];
-            zn[1] += scale * Cc.e[Ix1];
-            zn[2] += scale * Cc.e[Iy0];
-            zn[3] += scale * Cc.e[Iy1];
-            zn[4] += scale * Cc.e[Iz0];
-            zn[5] += scale * Cc.e[Iz1];
+        for (int q = 0; q < 2; q++) {
+            cc[q] = F.code[u[q]];
+            ru[q] = F.r[u[q]];
+            dBu[q] = F.dg[u[q]];
+#pragma unroll
+            for (int m = 0; m < 6; m++) zn[q][m] = F.z[u[q] + F.off[m]];
         }
-        if (!(cc & SELF)) continue;
-        T s = ru;
+        if (C) {
+            /* the coarse correction at the six neighbours: for each axis one
+             * neighbour shares the node's aggregate, the other is the next
+             * aggregate on the side of the node's parity */
+            const MgLevel<T> &Cc = *C;
+            T ea[2], ex[2], ey[2], ez[2];
+            int par[2];
 #pragma unroll
-        for (int m = 0; m < 6; m++) s += (cc & (1u << m)) ? F.ct[m >> 1] * zn[m] : (T)0;
-        T zu = s / full_diag(cc, dBu, F.ct);
-        F.z[u] = zu;
-        rz += ru * zu;
-        zz += zu * zu;
+            for (int q = 0; q < 2; q++) {
+                const int32_t p = ok[q] ? pk[tq[q]] : (1 | (1 << 10) | (1 << 20));
+                const int i = p & 1023, j = (p >> 10) & 1023, k = p >> 20;
+                const int32_t sy = Cc.nx, sz = Cc.nx * Cc.ny;
+                const int32_t A = ((k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1);
+                par[q] = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
+                ea[q] = Cc.e[A];
+                ex[q] = Cc.e[(i & 1) ? A + 1 : A - 1];
+                ey[q] = Cc.e[(j & 1) ? A + sy : A - sy];
+                ez[q] = Cc.e[(k & 1) ? A + sz : A - sz];
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const bool oi = par[q] & 1, oj = par[q] & 2, ok_ = par[q] & 4;
+                zn[q][0] += scale * (oi ? ea[q] : ex[q]);
+                zn[q][1] += scale * (oi ? ex[q] : ea[q]);
+                zn[q][2] += scale * (oj ? ea[q] : ey[q]);
+                zn[q][3] += scale * (oj ? ey[q] : ea[q]);
+                zn[q][4] += scale * (ok_ ? ea[q] : ez[q]);
+                zn[q][5] += scale * (ok_ ? ez[q] : ea[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (!ok[q] || !(cc[q] & SELF)) continue;
+            T s = ru[q];
+#pragma unroll
+            for (int m = 0; m < 6; m++) s += (cc[q] & (1u << m)) ? F.ct[m >> 1] * zn[q][m] : (T)0;
+            const T zu = s / full_diag(cc[q], dBu[q], F.ct);
+            F.z[u[q]] = zu;
+            rz += ru[q] * zu;
+            zz += zu * zu;
+        }
     }
 }
 
@@ -560,6 +590,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
     const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
     const int64_t off[6] = {-1, 1, -sy, sy, -sz, sz};
+    const int64_t safe = sz + sy + 1; /* the interior node (1,1,1) */
     const double cd[3] = {1.0 / (g.dh[0] * g.dh[0]), 1.0 / (g.dh[1] * g.dh[1]), 1.0 / (g.dh[2] * g.dh[2])};
     const T ct[3] = {(T)cd[0], (T)cd[1], (T)cd[2]};
     const double A0 = PCG_QE * n0 / PCG_EPS_0;
@@ -605,7 +636,20 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 L += on ? cd[m >> 1] * (xu - pn[m]) : 0.0;
                 dL += on ? cd[m >> 1] : 0.0;
             }
-            double e = exp((phi[u] - phi0) * inv_te0);
+            const double xa = (phi[u] - phi0) * inv_te0;
+            double e;
+            if (sizeof(T) == sizeof(float)) {
+                /* with the float inner solve, the Boltzmann factor is the
+                 * float exponential of the leading part of the argument times
+                 * a first-order factor for the rest: relative error ~1e-7,
+                 * which moves phi by ~Te 1e-7 (far below the Newton
+                 * tolerance), at a fraction of the float64 exp's cost on a
+                 * GPU with a narrow float64 pipe */
+                const float xh = (float)xa;
+                e = (double)expf(xh) * (1.0 + (xa - (double)xh));
+            } else {
+                e = exp(xa);
+            }
             double dB = A0_te0 * e;
             double Fv = linear ? L + dB * xu - lin_b[u] : L + A0 * e - rho[u] * inv_eps0;
             T rv = (T)Fv;
@@ -636,38 +680,79 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 /* p = z + beta p (on the fly at the node and its neighbours),
                  * q = J p */
                 T pq = 0;
-                for (int64_t u = gtid; u < nn; u += gsize) {
-                    uint16_t c = code[u];
-                    if (!(c & SELF)) continue;
-                    /* an unknown is interior: neighbour loads need no code bit */
-                    T zc = z[u], pc = it ? pold[u] : (T)0, dB = dg[u];
-                    T zn[6], pn[6];
+                /* two nodes per pass, every load before any store; a node
+                 * that is not an unknown (or past the end) reads the
+                 * interior node (1,1,1) and stores nothing */
+                for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
+                    const int64_t uq[2] = {u0, u0 + gsize};
+                    bool on[2];
+                    uint16_t c[2];
+                    int64_t u[2];
 #pragma unroll
-                    for (int m = 0; m < 6; m++) {
-                        zn[m] = z[u + off[m]];
-                        pn[m] = it ? pold[u + off[m]] : (T)0;
+                    for (int h = 0; h < 2; h++) {
+                        c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
+                        on[h] = c[h] & SELF;
+                        u[h] = on[h] ? uq[h] : safe;
                     }
-                    T pu = zc + beta * pc;
+                    /* an unknown is interior: neighbour loads need no code bit */
+                    T zc[2], pc[2], dB[2], zn[2][6], pn[2][6];
 #pragma unroll
-                    for (int m = 0; m < 6; m++) pn[m] = zn[m] + beta * pn[m];
-                    T s = jacobian_apply(c, dB, ct, pu, pn);
-                    pnew[u] = pu;
-                    q[u] = s;
-                    pq += pu * s;
+                    for (int h = 0; h < 2; h++) {
+                        zc[h] = z[u[h]];
+                        pc[h] = it ? pold[u[h]] : (T)0;
+                        dB[h] = dg[u[h]];
+#pragma unroll
+                        for (int m = 0; m < 6; m++) {
+                            zn[h][m] = z[u[h] + off[m]];
+                            pn[h][m] = it ? pold[u[h] + off[m]] : (T)0;
+                        }
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (!on[h]) continue;
+                        T pu = zc[h] + beta * pc[h];
+#pragma unroll
+                        for (int m = 0; m < 6; m++) pn[h][m] = zn[h][m] + beta * pn[h][m];
+                        T s = jacobian_apply(c[h], dB[h], ct, pu, pn[h]);
+                        pnew[u[h]] = pu;
+                        q[u[h]] = s;
+                        pq += pu * s;
+                    }
                 }
                 double s3[1] = {(double)pq};
                 grid_sum_n<1>(grid, s3, partials, round);
                 const T alpha = (T)(RZ / s3[0]);
                 /* y += alpha p, r -= alpha q, and the first red half sweep */
                 T rr = 0;
-                for (int64_t u = gtid; u < nn; u += gsize) {
-                    uint16_t c = code[u];
-                    if (!(c & SELF)) continue;
-                    y[u] += alpha * pnew[u];
-                    T ru = r[u] - alpha * q[u];
-                    r[u] = ru;
-                    rr += ru * ru;
-                    if (jacobi || !(c & BLACK)) z[u] = ru / full_diag(c, dg[u], ct);
+                for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
+                    const int64_t uq[2] = {u0, u0 + gsize};
+                    bool on[2];
+                    uint16_t c[2];
+                    int64_t u[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
+                        on[h] = c[h] & SELF;
+                        u[h] = on[h] ? uq[h] : safe;
+                    }
+                    T yv[2], pv[2], rv[2], qv[2], dv[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        yv[h] = y[u[h]];
+                        pv[h] = pnew[u[h]];
+                        rv[h] = r[u[h]];
+                        qv[h] = q[u[h]];
+                        dv[h] = dg[u[h]];
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (!on[h]) continue;
+                        y[u[h]] = yv[h] + alpha * pv[h];
+                        T ru = rv[h] - alpha * qv[h];
+                        r[u[h]] = ru;
+                        rr += ru * ru;
+                        if (jacobi || !(c[h] & BLACK)) z[u[h]] = ru / full_diag(c[h], dv[h], ct);
+                    }
                 }
                 double s4[1] = {(double)rr};
                 grid_sum_n<1>(grid, s4, partials, round);
