@@ -245,19 +245,26 @@ __device__ __forceinline__ T jacobian_apply(uint16_t cc, T dB, const T ct[3], T 
  * fly to the red neighbours read by the following black half sweep (the red
  * nodes are overwritten next anyway); and the dot products r.z and z.z are
  * accumulated by the last two half sweeps, which produce the final z. */
-template <typename T>
-__device__ __forceinline__ int64_t fine_agg(const Fine<T> &F, const MgLevel<T> &C, int64_t u) {
-    const Geo &g = F.g;
-    int i = (int)(u % g.ni), j = (int)((u / g.ni) % g.nj), k = (int)(u / ((int64_t)g.ni * g.nj));
-    return ((int64_t)(k >> 1) * C.ny + (j >> 1)) * C.nx + (i >> 1);
+/* n / d for n < 2^24 without an integer division: the float estimate is
+ * within one of the quotient (n is exact in float and 1/d is rounded once),
+ * and one remainder test corrects it */
+__device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float inv_d) {
+    uint32_t q = __float2uint_rz((float)n * inv_d);
+    const int32_t r = (int32_t)(n - q * d);
+    if (r < 0) q--;
+    else if (r >= (int32_t)d) q++;
+    return q;
 }
 
 /* node-grid half sweep of colour c over the unknowns; with C != null the
  * neighbours are read with the coarse correction added (post-smoothing);
  * adds r*z and z*z of the nodes it updated to rz and zz.  Each thread takes
- * two list entries per pass and issues every load of both before any store
- * (a padding entry reads the interior node (1,1,1) and stores nothing), so
- * twice as many loads are in flight as with one node per pass. */
+ * two entries of the colour's enumeration per pass and issues every load of
+ * both before any store (a padding entry reads the interior node (1,1,1) and
+ * stores nothing), so twice as many loads are in flight as with one node per
+ * pass.  Entry t is node i = 1 + 2 i2 + ((1+j+k+c)&1) of interior row
+ * (j, k), with i2 = t mod hx; below 2^24 entries the coordinates come from
+ * float-estimated divisions, above from the precomputed lists. */
 template <typename T>
 __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale, T &rz, T &zz) {
     int64_t t0, ts;
@@ -265,15 +272,32 @@ __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale,
     const int32_t *list = F.list[c], *pk = F.pk[c];
     const Geo &g = F.g;
     const int64_t safe = ((int64_t)g.nj + 1) * g.ni + 1;
+    const bool arith = F.nlist < (1 << 24);
+    const uint32_t hx = (uint32_t)((g.ni - 1) / 2), rj = (uint32_t)(g.nj - 2);
+    const float inv_hx = 1.f / (float)hx, inv_rj = 1.f / (float)rj;
     for (int64_t t = t0; t < F.nlist; t += 2 * ts) {
         const int64_t tq[2] = {t, t + ts};
         int64_t u[2];
         bool ok[2];
+        int32_t pq[2];
 #pragma unroll
         for (int q = 0; q < 2; q++) {
-            const int32_t uu = tq[q] < F.nlist ? list[tq[q]] : -1;
-            ok[q] = uu >= 0;
-            u[q] = ok[q] ? (int64_t)uu : safe;
+            if (arith) {
+                const bool in = tq[q] < F.nlist;
+                const uint32_t tt = in ? (uint32_t)tq[q] : 0u;
+                const uint32_t row = div_small(tt, hx, inv_hx);
+                const uint32_t kk = div_small(row, rj, inv_rj);
+                const int j = 1 + (int)(row - kk * rj), k = 1 + (int)kk;
+                const int i = 1 + 2 * (int)(tt - row * hx) + ((1 + j + k + c) & 1);
+                ok[q] = in && i <= g.ni - 2;
+                u[q] = ok[q] ? ((int64_t)k * g.nj + j) * g.ni + i : safe;
+                pq[q] = i | (j << 10) | (k << 20);
+            } else {
+                const int32_t uu = tq[q] < F.nlist ? list[tq[q]] : -1;
+                ok[q] = uu >= 0;
+                u[q] = ok[q] ? (int64_t)uu : safe;
+                pq[q] = C && ok[q] ? pk[tq[q]] : 0;
+            }
         }
         /* interior node: all six neighbours are in bounds, so their loads
          * are issued before the code word arrives; the code only selects */
@@ -296,7 +320,7 @@ __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale,
             int par[2];
 #pragma unroll
             for (int q = 0; q < 2; q++) {
-                const int32_t p = ok[q] ? pk[tq[q]] : (1 | (1 << 10) | (1 << 20));
+                const int32_t p = ok[q] ? pq[q] : (1 | (1 << 10) | (1 << 20));
                 const int i = p & 1023, j = (p >> 10) & 1023, k = p >> 20;
                 const int32_t sy = Cc.nx, sz = Cc.nx * Cc.ny;
                 const int32_t A = ((k >> 1) * Cc.ny + (j >> 1)) * Cc.nx + (i >> 1);
@@ -331,40 +355,50 @@ __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale,
     }
 }
 
-template <typename T>
-__device__ __forceinline__ int32_t coarse_agg(const MgLevel<T> &L, const MgLevel<T> &C, int64_t u) {
-    uint32_t uu = (uint32_t)u, nx = (uint32_t)L.nx, ny = (uint32_t)L.ny;
-    uint32_t i = uu % nx, r = uu / nx, j = r % ny, k = r / ny;
-    return (int32_t)(((k >> 1) * (uint32_t)C.ny + (j >> 1)) * (uint32_t)C.nx + (i >> 1));
-}
-
+/* one half sweep of colour c on a coarse level; with C != null the
+ * neighbours are read with C's correction added.  Coordinates come from the
+ * sweep index by float-estimated divisions (levels below 2^24 nodes), the
+ * neighbours' aggregates from the coordinates. */
 template <typename T>
 __device__ void coarse_half(const MgLevel<T> &L, int c, bool whole, const MgLevel<T> *C, T scale) {
-    int hx = (L.nx + 1) / 2;
-    int64_t count = (int64_t)hx * L.ny * L.nz;
-    int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
+    const int hx = (L.nx + 1) / 2;
+    const int64_t count = (int64_t)hx * L.ny * L.nz;
+    const int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
+    const bool fast = count < (1 << 24);
+    const float inv_hx = 1.f / (float)hx, inv_ny = 1.f / (float)L.ny;
     int64_t t0, ts;
     span(whole, t0, ts);
     for (int64_t t = t0; t < count; t += ts) {
-        uint32_t tt = (uint32_t)t;
-        uint32_t i2 = tt % (uint32_t)hx, rr = tt / (uint32_t)hx;
-        int j = (int)(rr % (uint32_t)L.ny);
-        int k = (int)(rr / (uint32_t)L.ny);
-        int i = 2 * (int)i2 + ((j + k + c) & 1);
+        const uint32_t tt = (uint32_t)t;
+        uint32_t rr, kk;
+        if (fast) {
+            rr = div_small(tt, (uint32_t)hx, inv_hx);
+            kk = div_small(rr, (uint32_t)L.ny, inv_ny);
+        } else {
+            rr = tt / (uint32_t)hx;
+            kk = rr / (uint32_t)L.ny;
+        }
+        const int i2 = (int)(tt - rr * (uint32_t)hx);
+        const int j = (int)(rr - kk * (uint32_t)L.ny);
+        const int k = (int)kk;
+        const int i = 2 * i2 + ((j + k + c) & 1);
         if (i >= L.nx) continue;
-        int64_t I = ((int64_t)k * L.ny + j) * L.nx + i;
-        /* all loads first (neighbour indices clamped into the level; a zero
-         * weight deselects them), then the arithmetic */
+        const int64_t I = ((int64_t)k * L.ny + j) * L.nx + i;
+        /* all loads first (a missing neighbour reads a clamped node; its zero
+         * weight deselects it), then the arithmetic */
         T d = L.diag[I];
         T s = L.b[I];
         T wm[6], en[6];
+        const int ci[6] = {i > 0 ? i - 1 : 0, i + 1 < L.nx ? i + 1 : i, i, i, i, i};
+        const int cj[6] = {j, j, j > 0 ? j - 1 : 0, j + 1 < L.ny ? j + 1 : j, j, j};
+        const int ck[6] = {k, k, k, k, k > 0 ? k - 1 : 0, k + 1 < L.nz ? k + 1 : k};
 #pragma unroll
         for (int m = 0; m < 6; m++) {
             int64_t nb = I + offs[m];
             nb = nb < 0 ? 0 : (nb >= L.n ? L.n - 1 : nb);
             wm[m] = L.w[m * L.n + I];
             en[m] = L.e[nb];
-            if (C) en[m] += scale * C->e[coarse_agg(L, *C, nb)];
+            if (C) en[m] += scale * C->e[((ck[m] >> 1) * C->ny + (cj[m] >> 1)) * C->nx + (ci[m] >> 1)];
         }
         if (d == (T)0) continue;
 #pragma unroll
@@ -373,80 +407,185 @@ __device__ void coarse_half(const MgLevel<T> &L, int c, bool whole, const MgLeve
     }
 }
 
-/* b of level l+1 = sum of the children's residuals (b - A e); the first red
- * half sweep of level l+1 (e = b / diag) is fused in */
+/* The red children of a coarse node (its 2x2x2 block), in the order in which
+ * their residuals are summed: offsets dx | dy<<1 | dz<<2 with dx+dy+dz even
+ * (black residuals are zero after the black half sweep). */
+__device__ __forceinline__ int red_child(int q) { return q == 0 ? 0 : (q == 1 ? 3 : (q == 2 ? 5 : 6)); }
+
+/* Coordinates of coarse node I (float-estimated divisions below 2^24 nodes). */
 template <typename T>
-__device__ void restrict_fine(const Fine<T> &F, const MgLevel<T> &C) {
-    const Geo &g = F.g;
-    int64_t t0, ts;
-    span(true, t0, ts);
-    for (int64_t I = t0; I < C.n; I += ts) {
-        uint32_t I32 = (uint32_t)I, cr = I32 / (uint32_t)C.nx;
-        int ci = (int)(I32 % (uint32_t)C.nx);
-        int cj = (int)(cr % (uint32_t)C.ny);
-        int ck = (int)(cr / (uint32_t)C.ny);
-        T sum = 0;
-        /* the four red children (black residuals are zero after the black
-         * sweep); a child off the grid or not an unknown contributes 0 */
-        int64_t uu[4];
-        uint16_t cc[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            int d = (q << 1) | (((q & 1) + (q >> 1)) & 1); /* dx makes dx+dy+dz even: a red child */
-            int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
-            bool in = i < g.ni && j < g.nj && k < g.nk;
-            uu[q] = in ? ((int64_t)k * g.nj + j) * g.ni + i : 0;
-            cc[q] = in ? F.code[uu[q]] : (uint16_t)0;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (!(cc[q] & SELF)) continue;
-            int64_t u = uu[q];
-            T zn[6];
-#pragma unroll
-            for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
-            T res = F.r[u] - jacobian_apply(cc[q], F.dg[u], F.ct, F.z[u], zn);
-            sum += res;
-        }
-        C.b[I] = sum;
-        if (((ci + cj + ck) & 1) == 0) {
-            T d = C.diag[I];
-            if (d != (T)0) C.e[I] = sum / d;
-        }
+__device__ __forceinline__ void coarse_coords(const MgLevel<T> &C, int64_t I, bool fast, float inv_nx, float inv_ny,
+                                              int &ci, int &cj, int &ck) {
+    const uint32_t I32 = (uint32_t)I;
+    const uint32_t cr = fast ? div_small(I32, (uint32_t)C.nx, inv_nx) : I32 / (uint32_t)C.nx;
+    const uint32_t ckk = fast ? div_small(cr, (uint32_t)C.ny, inv_ny) : cr / (uint32_t)C.ny;
+    ci = (int)(I32 - cr * (uint32_t)C.nx);
+    cj = (int)(cr - ckk * (uint32_t)C.ny);
+    ck = (int)ckk;
+}
+
+/* The sum of four lanes' residuals (lanes 4g..4g+3, in lane order) into
+ * b of the coarse node, and the fused first red half sweep (e = b / diag).
+ * Every lane of the warp calls it. */
+template <typename T>
+__device__ __forceinline__ void restrict_store(const MgLevel<T> &C, bool valid, int64_t I, int ci, int cj, int ck,
+                                               T res) {
+    const T r1 = __shfl_down_sync(0xffffffffu, res, 1);
+    const T r2 = __shfl_down_sync(0xffffffffu, res, 2);
+    const T r3 = __shfl_down_sync(0xffffffffu, res, 3);
+    if (!valid || (threadIdx.x & 3)) return;
+    T sum = 0;
+    sum += res;
+    sum += r1;
+    sum += r2;
+    sum += r3;
+    C.b[I] = sum;
+    if (((ci + cj + ck) & 1) == 0) {
+        const T d = C.diag[I];
+        if (d != (T)0) C.e[I] = sum / d;
     }
 }
 
+/* b of level 1 = sum of the node-grid children's residuals (r - J z).  When
+ * the level has fewer nodes than the grid has threads (latency-bound),
+ * four consecutive threads take the four red children of a coarse node,
+ * each issuing all its loads at once (neighbour indices clamped into the
+ * grid; a child that is not an unknown contributes zero); otherwise
+ * (bandwidth-bound) a thread takes a coarse node and its four children, so
+ * that a warp's loads of one child cover consecutive nodes of a row. */
+template <typename T>
+__device__ void restrict_fine(const Fine<T> &F, const MgLevel<T> &C) {
+    const Geo &g = F.g;
+    const int64_t nn = (int64_t)g.ni * g.nj * g.nk;
+    const int64_t safe = ((int64_t)g.nj + 1) * g.ni + 1;
+    int64_t t0, ts;
+    span(true, t0, ts);
+    const bool fast = C.n < (1 << 24);
+    const float inv_nx = 1.f / (float)C.nx, inv_ny = 1.f / (float)C.ny;
+    if (C.n > ts) {
+        for (int64_t I = t0; I < C.n; I += ts) {
+            int ci, cj, ck;
+            coarse_coords(C, I, fast, inv_nx, inv_ny, ci, cj, ck);
+            T sum = 0;
+            int64_t uu[4];
+            uint16_t cc[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int d = red_child(q);
+                const int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+                const bool in = i < g.ni && j < g.nj && k < g.nk;
+                uu[q] = in ? ((int64_t)k * g.nj + j) * g.ni + i : 0;
+                cc[q] = in ? F.code[uu[q]] : (uint16_t)0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (!(cc[q] & SELF)) continue;
+                const int64_t u = uu[q];
+                T zn[6];
+#pragma unroll
+                for (int m = 0; m < 6; m++) zn[m] = F.z[u + F.off[m]];
+                sum += F.r[u] - jacobian_apply(cc[q], F.dg[u], F.ct, F.z[u], zn);
+            }
+            C.b[I] = sum;
+            if (((ci + cj + ck) & 1) == 0) {
+                const T d = C.diag[I];
+                if (d != (T)0) C.e[I] = sum / d;
+            }
+        }
+        return;
+    }
+    const int64_t total = 4 * C.n, padded = (total + 31) & ~(int64_t)31;
+    for (int64_t t = t0; t < padded; t += ts) {
+        const bool valid = t < total;
+        const int64_t I = valid ? (t >> 2) : 0;
+        int ci, cj, ck;
+        coarse_coords(C, I, fast, inv_nx, inv_ny, ci, cj, ck);
+        const int d = red_child((int)(t & 3));
+        const int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+        const bool in = valid && i < g.ni && j < g.nj && k < g.nk;
+        const int64_t u = in ? ((int64_t)k * g.nj + j) * g.ni + i : safe;
+        const uint16_t cc = F.code[u];
+        const T ru = F.r[u], dBu = F.dg[u], zu = F.z[u];
+        T zn[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            int64_t nb = u + F.off[m];
+            nb = nb < 0 ? 0 : (nb >= nn ? nn - 1 : nb);
+            zn[m] = F.z[nb];
+        }
+        const T res = (in && (cc & SELF)) ? ru - jacobian_apply(cc, dBu, F.ct, zu, zn) : (T)0;
+        restrict_store(C, valid, I, ci, cj, ck, res);
+    }
+}
+
+/* b of level l+1 from level l, laid out like restrict_fine */
 template <typename T>
 __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool whole) {
-    int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
+    const int64_t offs[6] = {-1, 1, -(int64_t)L.nx, L.nx, -(int64_t)L.nx * L.ny, (int64_t)L.nx * L.ny};
     int64_t t0, ts;
     span(whole, t0, ts);
-    for (int64_t I = t0; I < C.n; I += ts) {
-        uint32_t I32 = (uint32_t)I, cr = I32 / (uint32_t)C.nx;
-        int ci = (int)(I32 % (uint32_t)C.nx);
-        int cj = (int)(cr % (uint32_t)C.ny);
-        int ck = (int)(cr / (uint32_t)C.ny);
-        T sum = 0;
-        for (int d = 0; d < 8; d++) {
-            int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
-            if (i >= L.nx || j >= L.ny || k >= L.nz) continue;
-            if (((i + j + k) & 1) == 1) continue;
-            int64_t u = ((int64_t)k * L.ny + j) * L.nx + i;
-            T dd = L.diag[u];
-            if (dd == (T)0) continue;
-            T res = L.b[u] - dd * L.e[u];
+    const bool fast = C.n < (1 << 24);
+    const float inv_nx = 1.f / (float)C.nx, inv_ny = 1.f / (float)C.ny;
+    if (C.n > ts) {
+        for (int64_t I = t0; I < C.n; I += ts) {
+            int ci, cj, ck;
+            coarse_coords(C, I, fast, inv_nx, inv_ny, ci, cj, ck);
+            T sum = 0;
 #pragma unroll
-            for (int m = 0; m < 6; m++) {
-                T wm = L.w[m * L.n + u];
-                if (wm != (T)0) res += wm * L.e[u + offs[m]];
+            for (int q = 0; q < 4; q++) {
+                const int d = red_child(q);
+                const int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+                const bool in = i < L.nx && j < L.ny && k < L.nz;
+                const int64_t u = in ? ((int64_t)k * L.ny + j) * L.nx + i : 0;
+                const T dd = L.diag[u], bu = L.b[u], eu = L.e[u];
+                T wm[6], en[6];
+#pragma unroll
+                for (int m = 0; m < 6; m++) {
+                    int64_t nb = u + offs[m];
+                    nb = nb < 0 ? 0 : (nb >= L.n ? L.n - 1 : nb);
+                    wm[m] = L.w[m * L.n + u];
+                    en[m] = L.e[nb];
+                }
+                if (!in || dd == (T)0) continue;
+                T res = bu - dd * eu;
+#pragma unroll
+                for (int m = 0; m < 6; m++) res += (wm[m] != (T)0) ? wm[m] * en[m] : (T)0;
+                sum += res;
             }
-            sum += res;
+            C.b[I] = sum;
+            if (((ci + cj + ck) & 1) == 0) {
+                const T d = C.diag[I];
+                if (d != (T)0) C.e[I] = sum / d;
+            }
         }
-        C.b[I] = sum;
-        if (((ci + cj + ck) & 1) == 0) {
-            T d = C.diag[I];
-            if (d != (T)0) C.e[I] = sum / d;
+        return;
+    }
+    const int64_t total = 4 * C.n, padded = (total + 31) & ~(int64_t)31;
+    for (int64_t t = t0; t < padded; t += ts) {
+        const bool valid = t < total;
+        const int64_t I = valid ? (t >> 2) : 0;
+        int ci, cj, ck;
+        coarse_coords(C, I, fast, inv_nx, inv_ny, ci, cj, ck);
+        const int d = red_child((int)(t & 3));
+        const int i = 2 * ci + (d & 1), j = 2 * cj + ((d >> 1) & 1), k = 2 * ck + (d >> 2);
+        const bool in = valid && i < L.nx && j < L.ny && k < L.nz;
+        const int64_t u = in ? ((int64_t)k * L.ny + j) * L.nx + i : 0;
+        const T dd = L.diag[u], bu = L.b[u], eu = L.e[u];
+        T wm[6], en[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            int64_t nb = u + offs[m];
+            nb = nb < 0 ? 0 : (nb >= L.n ? L.n - 1 : nb);
+            wm[m] = L.w[m * L.n + u];
+            en[m] = L.e[nb];
         }
+        T res = 0;
+        if (in && dd != (T)0) {
+            res = bu - dd * eu;
+#pragma unroll
+            for (int m = 0; m < 6; m++) res += (wm[m] != (T)0) ? wm[m] * en[m] : (T)0;
+        }
+        restrict_store(C, valid, I, ci, cj, ck, res);
     }
 }
 
@@ -623,41 +762,67 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
          * diagonal; the first red smoothing half sweep (or Jacobi) of the
          * preconditioner rides along */
         double ff = 0;
-        for (int64_t u = gtid; u < nn; u += gsize) {
-            uint16_t c = code[u];
-            if (!(c & SELF)) continue;
-            const double *X = linear ? lin_y : phi;
-            double xu = X[u], L = 0, dL = 0, pn[6];
+        const double *XR = linear ? lin_y : phi;
+        /* two nodes per pass, every load before any store (a node that is
+         * not an unknown reads the interior node (1,1,1) and stores nothing) */
+        for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
+            const int64_t uq[2] = {u0, u0 + gsize};
+            bool onq[2];
+            uint16_t c[2];
+            int64_t u[2];
 #pragma unroll
-            for (int m = 0; m < 6; m++) pn[m] = X[u + off[m]];
+            for (int h = 0; h < 2; h++) {
+                c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
+                onq[h] = c[h] & SELF;
+                u[h] = onq[h] ? uq[h] : safe;
+            }
+            double xu[2], pn[2][6], ph[2], bv[2];
 #pragma unroll
-            for (int m = 0; m < 6; m++) {
-                bool on = c & ((1u << m) | (1u << (6 + m)));
-                L += on ? cd[m >> 1] * (xu - pn[m]) : 0.0;
-                dL += on ? cd[m >> 1] : 0.0;
+            for (int h = 0; h < 2; h++) {
+                xu[h] = XR[u[h]];
+#pragma unroll
+                for (int m = 0; m < 6; m++) pn[h][m] = XR[u[h] + off[m]];
+                ph[h] = phi[u[h]];
+                bv[h] = linear ? lin_b[u[h]] : rho[u[h]];
             }
-            const double xa = (phi[u] - phi0) * inv_te0;
-            double e;
-            if (sizeof(T) == sizeof(float)) {
-                /* with the float inner solve, the Boltzmann factor is the
-                 * float exponential of the leading part of the argument times
-                 * a first-order factor for the rest: relative error ~1e-7,
-                 * which moves phi by ~Te 1e-7 (far below the Newton
-                 * tolerance), at a fraction of the float64 exp's cost on a
-                 * GPU with a narrow float64 pipe */
-                const float xh = (float)xa;
-                e = (double)expf(xh) * (1.0 + (xa - (double)xh));
-            } else {
-                e = exp(xa);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (!onq[h]) continue;
+                double L = 0, dL = 0;
+#pragma unroll
+                for (int m = 0; m < 6; m++) {
+                    const bool on = c[h] & ((1u << m) | (1u << (6 + m)));
+                    L += on ? cd[m >> 1] * (xu[h] - pn[h][m]) : 0.0;
+                    if (sizeof(T) != sizeof(float)) dL += on ? cd[m >> 1] : 0.0;
+                }
+                const double xa = (ph[h] - phi0) * inv_te0;
+                double e;
+                if (sizeof(T) == sizeof(float)) {
+                    /* with the float inner solve, the Boltzmann factor is the
+                     * float exponential of the leading part of the argument
+                     * times a first-order factor for the rest: relative error
+                     * ~1e-7, which moves phi by ~Te 1e-7 (far below the
+                     * Newton tolerance), at a fraction of the float64 exp's
+                     * cost on a GPU with a narrow float64 pipe */
+                    const float xh = (float)xa;
+                    e = (double)expf(xh) * (1.0 + (xa - (double)xh));
+                } else {
+                    e = exp(xa);
+                }
+                const double dB = A0_te0 * e;
+                const double Fv = linear ? L + dB * xu[h] - bv[h] : L + A0 * e - bv[h] * inv_eps0;
+                const T rv = (T)Fv;
+                dg[u[h]] = (T)dB;
+                r[u[h]] = rv;
+                y[u[h]] = 0;
+                if (jacobi || !(c[h] & BLACK)) {
+                    /* the float form takes the diagonal in float, the float64
+                     * form keeps its float64 sum */
+                    const T d = sizeof(T) == sizeof(float) ? full_diag(c[h], (T)dB, ct) : (T)(dL + dB);
+                    z[u[h]] = rv / d;
+                }
+                ff += Fv * Fv;
             }
-            double dB = A0_te0 * e;
-            double Fv = linear ? L + dB * xu - lin_b[u] : L + A0 * e - rho[u] * inv_eps0;
-            T rv = (T)Fv;
-            dg[u] = (T)dB;
-            r[u] = rv;
-            y[u] = 0;
-            if (jacobi || !(c & BLACK)) z[u] = rv / (T)(dL + dB);
-            ff += Fv * Fv;
         }
         double s1[1] = {ff};
         grid_sum_n<1>(grid, s1, partials, round);
