@@ -135,6 +135,17 @@ struct World {
     int64_t prof_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
+/* n / d for n < 2^24 without an integer division: the float estimate is
+ * within one of the quotient (n is exact in float and 1/d is rounded once),
+ * and one remainder test corrects it */
+__device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float inv_d) {
+    uint32_t q = __float2uint_rz((float)n * inv_d);
+    const int32_t r = (int32_t)(n - q * d);
+    if (r < 0) q--;
+    else if (r >= (int32_t)d) q++;
+    return q;
+}
+
 inline int blocks_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;

@@ -621,15 +621,18 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
  * central inside.  Also writes the float32 copy used by the mixed push. */
+/* grid: x over the nodes of a k-plane, y over the planes (no 64-bit index
+ * division per node) */
 __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double *__restrict__ phi, double *ef,
                                                 float4 *ef4) {
-    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t nn = (int64_t)g.ni * g.nj * g.nk;
-    if (u >= nn) return;
-    int i = (int)(u % g.ni);
-    int j = (int)((u / g.ni) % g.nj);
-    int k = (int)(u / ((int64_t)g.ni * g.nj));
+    const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nplane = (uint32_t)g.ni * (uint32_t)g.nj;
+    if (pl >= nplane) return;
+    const int k = blockIdx.y;
+    const uint32_t jj = div_small(pl, (uint32_t)g.ni, 1.f / (float)g.ni);
+    const int j = (int)jj, i = (int)(pl - jj * (uint32_t)g.ni);
     int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    const int64_t u = (int64_t)k * sz + pl;
     const double d2x = 2 * g.dh[0], d2y = 2 * g.dh[1], d2z = 2 * g.dh[2];
     double n0, n1, n2;
     if (i == 0)
@@ -1143,7 +1146,8 @@ void launch_efield(World &w) {
     for (Species *s : w.species) mixed |= (s->form == 1);
     /* RN(1 / (2 dh)) per axis, for div_rcp */
     double3 y2 = make_double3(1.0 / (2 * w.g.dh[0]), 1.0 / (2 * w.g.dh[1]), 1.0 / (2 * w.g.dh[2]));
-    k_efield<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, mixed ? w.ef4 : nullptr);
+    dim3 grid((unsigned)blocks_for((int64_t)w.g.ni * w.g.nj, 256), (unsigned)w.g.nk);
+    k_efield<<<grid, 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, mixed ? w.ef4 : nullptr);
     w.nlaunch++;
     if (mixed) w.ef4_valid = true;
     else w.ef4_valid = false;

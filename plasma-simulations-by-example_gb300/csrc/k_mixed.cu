@@ -397,16 +397,31 @@ __device__ __forceinline__ int32_t linear_cell(int32_t key, int ni, int nj) {
     return (k * (nj - 1) + j) * (ni - 1) + i;
 }
 
+/* Runs of equal cells in lane order (the particles are nearly sorted, so a
+ * warp holds a few long runs): each lane gets the first lane of its run and
+ * the run length.  A cell that appears in several runs is counted once per
+ * run, which leaves sums and slot ranges exact.  Every lane of the warp
+ * calls it; lanes without a particle pass -1 and form runs of their own. */
+__device__ __forceinline__ void cell_runs(int32_t lc, int &head, int &len) {
+    const int lane = threadIdx.x & 31;
+    const int32_t prev = __shfl_up_sync(0xffffffffu, lc, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != lc || lc < 0);
+    const unsigned le = 0xffffffffu >> (31 - lane);
+    head = 31 - __clz(heads & le);
+    const unsigned after = heads & ~le;
+    const int next = after ? __ffs(after) - 1 : 32;
+    len = next - head;
+}
+
 __global__ void __launch_bounds__(256) k_sort_hist(const int32_t *__restrict__ cell,
                                                    const int64_t *__restrict__ d_count, int ni, int nj,
                                                    int32_t *counts) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool me = p < d_count[0];
     int32_t lc = me ? linear_cell(cell[p], ni, nj) : -1;
-    unsigned active = __ballot_sync(0xffffffffu, me);
-    if (!me) return;
-    unsigned peers = __match_any_sync(active, lc);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counts + lc, __popc(peers));
+    int head, len;
+    cell_runs(lc, head, len);
+    if (me && (int)(threadIdx.x & 31) == head) atomicAdd(counts + lc, len);
 }
 
 constexpr int SCAN_PER_BLOCK = 8192; /* 1024 threads x 8 */
@@ -488,15 +503,14 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict_
     bool me = p < d_count[0];
     int32_t key = me ? cell[p] : -1;
     int32_t lc = me ? linear_cell(key, ni, nj) : -1;
-    unsigned active = __ballot_sync(0xffffffffu, me);
-    if (!me) return;
-    unsigned peers = __match_any_sync(active, lc);
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(peers) - 1;
+    int head, len;
+    cell_runs(lc, head, len);
+    const int lane = threadIdx.x & 31;
     int32_t base = 0;
-    if (lane == leader) base = atomicAdd(cursor + lc, __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    int64_t dst = base + __popc(peers & ((1u << lane) - 1u));
+    if (me && lane == head) base = atomicAdd(cursor + lc, len);
+    base = __shfl_sync(0xffffffffu, base, head);
+    if (!me) return;
+    const int64_t dst = base + (lane - head);
     cell2[dst] = key;
 #pragma unroll
     for (int d = 0; d < 3; d++) {

@@ -245,17 +245,6 @@ __device__ __forceinline__ T jacobian_apply(uint16_t cc, T dB, const T ct[3], T 
  * fly to the red neighbours read by the following black half sweep (the red
  * nodes are overwritten next anyway); and the dot products r.z and z.z are
  * accumulated by the last two half sweeps, which produce the final z. */
-/* n / d for n < 2^24 without an integer division: the float estimate is
- * within one of the quotient (n is exact in float and 1/d is rounded once),
- * and one remainder test corrects it */
-__device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float inv_d) {
-    uint32_t q = __float2uint_rz((float)n * inv_d);
-    const int32_t r = (int32_t)(n - q * d);
-    if (r < 0) q--;
-    else if (r >= (int32_t)d) q++;
-    return q;
-}
-
 /* node-grid half sweep of colour c over the unknowns; with C != null the
  * neighbours are read with the coarse correction added (post-smoothing);
  * adds r*z and z*z of the nodes it updated to rz and zz.  Each thread takes
