@@ -198,6 +198,11 @@ int espic_solver_set_predictor(espic_world *w, int enable);
  * between two grid barriers (default 4096); larger levels run on the whole
  * grid.  A tuning knob with no reference counterpart. */
 int espic_solver_set_coarse(espic_world *w, int64_t block_nodes);
+/* The first multigrid level with at most max_nodes nodes (<= 4096; default
+ * 1024) becomes the coarsest and is solved by its dense inverse, computed
+ * once per geometry; 0 keeps smoothing sweeps on the coarsest level.  A
+ * tuning knob with no reference counterpart. */
+int espic_solver_set_dense(espic_world *w, int64_t max_nodes);
 /* PotentialSolver::solve, ch2/PotentialSolver.cpp:11-67 and
  * ch3/ver2/PotentialSolver.h:66-75.  With all out-pointers NULL the solve is
  * only enqueued; otherwise the call waits and reports iterations and the

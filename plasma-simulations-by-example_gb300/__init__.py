@@ -109,6 +109,7 @@ def lib():
             "espic_solver_set_multigrid": [VP, C.c_int, C.c_double],
             "espic_solver_set_launch": [VP, C.c_int],
             "espic_solver_set_coarse": [VP, I64],
+            "espic_solver_set_dense": [VP, I64],
             "espic_solver_set_predictor": [VP, C.c_int],
             "espic_solve": [VP, PI, PI, PD],
             "espic_efield": [VP],
@@ -483,6 +484,11 @@ class PotentialSolver:
     def setCoarse(self, block_nodes):
         """Multigrid levels with fewer nodes than this run on one block."""
         check(lib().espic_solver_set_coarse(self.world.h, int(block_nodes)))
+
+    def setDense(self, max_nodes):
+        """The first multigrid level with at most max_nodes nodes is the
+        coarsest, solved by its dense inverse (0: smoothing sweeps)."""
+        check(lib().espic_solver_set_dense(self.world.h, int(max_nodes)))
 
     def solve(self, wait=True):
         """Returns (converged, iterations, inner_iterations, residual)."""

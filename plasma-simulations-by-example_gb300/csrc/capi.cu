@@ -826,6 +826,7 @@ extern "C" int espic_solver_set_newton(espic_world *h, int nr_max, double nr_tol
 extern "C" int espic_solver_set_multigrid(espic_world *h, int levels, double scale) {
     WORLD(h);
     if (levels < 0 || levels > 12 || !(scale > 0 && scale < 2)) return fail(ESPIC_ERR_ARG, "bad multigrid controls");
+    if (levels != w.mg_levels_max) w.pcg_codes_valid = false; /* levels to set up change */
     w.mg_levels_max = levels;
     w.mg_scale = scale;
     return ESPIC_OK;
@@ -835,6 +836,16 @@ extern "C" int espic_solver_set_coarse(espic_world *h, int64_t block_nodes) {
     WORLD(h);
     if (block_nodes < 0) return fail(ESPIC_ERR_ARG, "bad coarse-level size");
     w.mg_block_nodes = block_nodes;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_solver_set_dense(espic_world *h, int64_t max_nodes) {
+    WORLD(h);
+    if (max_nodes < 0 || max_nodes > 4096) return fail(ESPIC_ERR_ARG, "bad dense coarse-level size");
+    if (max_nodes != w.mg_dense_max) {
+        w.mg_dense_max = max_nodes;
+        w.pcg_codes_valid = false; /* the hierarchy and its setup change */
+    }
     return ESPIC_OK;
 }
 

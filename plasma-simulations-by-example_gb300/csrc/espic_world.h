@@ -94,6 +94,8 @@ struct World {
     int mg_levels_max = 12; /* multigrid levels of the PCG preconditioner (0: Jacobi) */
     double mg_scale = 1.6;  /* coarse-correction scale */
     int64_t mg_block_nodes = 4096; /* multigrid levels smaller than this run on one block */
+    int64_t mg_dense_max = 1024;   /* coarsest level solved by its dense inverse when it has at most this
+                                      many nodes (0: smoothing sweeps on block 0) */
     int solver_blocks = 0;  /* cap on cooperative solver blocks (0: occupancy limit) */
     double *phi_prev = nullptr;    /* the potential before the last Newton solve (predictor) */
     bool phi_prev_valid = false;

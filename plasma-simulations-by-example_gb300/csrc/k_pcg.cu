@@ -135,6 +135,10 @@ struct MgArgs {
     int nu_coarse;   /* sweeps each way on the coarsest level */
     T scale;         /* coarse-correction scale */
     int smem_from;   /* block 0 keeps levels L[smem_from..] in shared memory (-1: none) */
+    int dense_n;     /* nodes of the coarsest level when it is solved by its dense inverse */
+    T *dense;        /* that inverse, row-major (null: smoothing sweeps on the coarsest level) */
+    const int *dense_ok; /* 0 when the inversion met a vanishing pivot (a singular coarse operator,
+                            e.g. without Dirichlet nodes): the coarsest level is smoothed instead */
     MgLevel<T> L[MG_MAX];
 };
 
@@ -578,6 +582,24 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
     }
 }
 
+/* e = A^-1 b on the coarsest level by its dense inverse, on the whole grid:
+ * a warp per row, lanes over the columns in a fixed order, a fixed shuffle
+ * tree over the lanes */
+template <typename T>
+__device__ void dense_apply(const MgLevel<T> &L, const T *__restrict__ Ainv, int n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < n; r += nwarps) {
+        const T *row = Ainv + r * n;
+        T acc = 0;
+        for (int j = lane; j < n; j += 32) acc += row[j] * L.b[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) L.e[r] = acc;
+    }
+}
+
 /* The V-cycle z = M r after its first red half sweep on the node grid
  * (done by the caller, fused with the CG update of r).  Every block executes
  * the same grid barriers; returns the grid-wide r.z of the final z and puts
@@ -664,6 +686,9 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
                 for (int64_t t = threadIdx.x; t < G0.n; t += blockDim.x) G0.e[t] = S0.e[t];
             }
         }
+        grid.sync();
+    } else if (A.dense && *A.dense_ok) {
+        dense_apply(A.L[NL - 1], A.dense, A.dense_n);
         grid.sync();
     } else {
         const MgLevel<T> &Lc = A.L[NL - 1];
@@ -1019,6 +1044,76 @@ __global__ void k_mg_setup(Geo g, const uint16_t *__restrict__ code, MgLevel<T> 
     for (int m = 0; m < 6; m++) C.w[m * C.n + I] = (T)w[m];
 }
 
+/* The coarsest level's operator as a dense float64 matrix (A e = diag e -
+ * sum_m w_m e_nb(m)); an aggregate without unknowns (diag 0) gets an
+ * identity row. */
+template <typename T>
+__global__ void k_dense_build(MgLevel<T> L, double *M, double *diag0) {
+    const int64_t n = L.n;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t / n, j = t - i * n;
+    const double di = (double)L.diag[i];
+    double v = 0;
+    if (di == 0) {
+        v = i == j ? 1.0 : 0.0;
+    } else if (i == j) {
+        v = di;
+    } else if ((double)L.diag[j] != 0) {
+        const int xi = (int)(i % L.nx), yi = (int)((i / L.nx) % L.ny), zi = (int)(i / ((int64_t)L.nx * L.ny));
+        const int xj = (int)(j % L.nx), yj = (int)((j / L.nx) % L.ny), zj = (int)(j / ((int64_t)L.nx * L.ny));
+        const int dx = xj - xi, dy = yj - yi, dz = zj - zi;
+        int m = -1;
+        if (dy == 0 && dz == 0 && (dx == -1 || dx == 1)) m = dx < 0 ? 0 : 1;
+        if (dx == 0 && dz == 0 && (dy == -1 || dy == 1)) m = dy < 0 ? 2 : 3;
+        if (dx == 0 && dy == 0 && (dz == -1 || dz == 1)) m = dz < 0 ? 4 : 5;
+        if (m >= 0) v = -(double)L.w[m * n + i];
+    }
+    M[t] = v;
+    if (i == j) diag0[i] = v;
+}
+
+/* in-place Gauss-Jordan inversion without pivoting (the operator is
+ * symmetric positive definite), step k: save column k, scale row k ... */
+__global__ void k_gj_pivot(double *M, int n, int k, double *col, const double *__restrict__ diag0, int *ok) {
+    __shared__ double piv;
+    if (threadIdx.x == 0) {
+        piv = M[(int64_t)k * n + k];
+        /* a pivot that vanished against the original diagonal: singular */
+        if (!(piv > 1e-9 * diag0[k])) {
+            *ok = 0;
+            piv = 1.0;
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = M[(int64_t)i * n + k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double a = j == k ? 1.0 : M[(int64_t)k * n + j];
+        M[(int64_t)k * n + j] = a / piv;
+    }
+}
+
+/* ... and eliminate column k from every other row */
+__global__ void k_gj_update(double *M, int n, int k, const double *__restrict__ col) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n * n) return;
+    const int64_t i = t / n, j = t - i * n;
+    if (i == k) return;
+    M[t] = (j == k ? 0.0 : M[t]) - col[i] * M[(int64_t)k * n + j];
+}
+
+/* the inverse in T, symmetrised; rows and columns of aggregates without
+ * unknowns are zero */
+template <typename T>
+__global__ void k_dense_store(MgLevel<T> L, const double *__restrict__ M, T *out) {
+    const int64_t n = L.n;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t / n, j = t - i * n;
+    const bool live = (double)L.diag[i] != 0 && (double)L.diag[j] != 0;
+    out[t] = live ? (T)(0.5 * (M[t] + M[j * n + i])) : (T)0;
+}
+
 /* ======================================================================== */
 template <typename T>
 static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
@@ -1049,6 +1144,30 @@ static size_t mg_layout(World &w, MgArgs<T> &A, char *base) {
         nz = (nz + 1) / 2;
     }
     A.nlev = w.mg_levels_max < nlev ? w.mg_levels_max : nlev;
+    /* the first level with at most mg_dense_max nodes becomes the coarsest,
+     * solved by its dense inverse on the whole grid (every level above it
+     * runs on the whole grid too); the float64 work matrix of the inversion
+     * and its column buffer follow the levels */
+    A.dense = nullptr;
+    A.dense_n = 0;
+    if (w.mg_dense_max > 0)
+        for (int i = 0; i < A.nlev; i++)
+            if (A.L[i].n <= w.mg_dense_max) {
+                A.nlev = i + 1;
+                A.dense_n = (int)A.L[i].n;
+                grid_levels = A.nlev + 1;
+                break;
+            }
+    if (A.dense_n > 0) {
+        const size_t nsq = (size_t)A.dense_n * A.dense_n;
+        A.dense = (T *)(base ? base + off : nullptr);
+        off += (nsq * sizeof(T) + 255) / 256 * 256;
+        off += (nsq * sizeof(double) + 255) / 256 * 256 + 2 * (((size_t)A.dense_n * sizeof(double) + 255) / 256 * 256);
+        A.dense_ok = (const int *)(base ? base + off : nullptr);
+        off += 256;
+    } else {
+        A.dense_ok = nullptr;
+    }
     A.grid_levels = grid_levels;
     A.nu_coarse = 2;
     A.scale = (T)w.mg_scale;
@@ -1105,6 +1224,24 @@ static int run_pcg(World &w) {
             MgLevel<T> prev = l ? A.L[l - 1] : A.L[0];
             k_mg_setup<T><<<blocks_for(A.L[l].n, 256), 256, 0, w.stream>>>(w.g, code, prev, A.L[l], l == 0);
             w.nlaunch++;
+        }
+        if (A.dense) {
+            const int n = A.dense_n;
+            const int64_t nsq = (int64_t)n * n;
+            double *M = (double *)((char *)A.dense + (nsq * sizeof(T) + 255) / 256 * 256);
+            double *col = (double *)((char *)M + (nsq * sizeof(double) + 255) / 256 * 256);
+            double *diag0 = col + ((size_t)n * sizeof(double) + 255) / 256 * 256 / sizeof(double);
+            int *ok = (int *)A.dense_ok;
+            const int one = 1;
+            cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, w.stream);
+            const MgLevel<T> &Lc = A.L[A.nlev - 1];
+            k_dense_build<T><<<blocks_for(nsq, 256), 256, 0, w.stream>>>(Lc, M, diag0);
+            for (int k = 0; k < n; k++) {
+                k_gj_pivot<<<1, 1024, 0, w.stream>>>(M, n, k, col, diag0, ok);
+                k_gj_update<<<blocks_for(nsq, 256), 256, 0, w.stream>>>(M, n, k, col);
+            }
+            k_dense_store<T><<<blocks_for(nsq, 256), 256, 0, w.stream>>>(Lc, M, A.dense);
+            w.nlaunch += 2 + 2 * n;
         }
         w.pcg_codes_valid = true;
     }

@@ -323,6 +323,56 @@ def test_newton_pcg(espic, po, fp32, levels):
             assert inner < 40 * nr, (nr, inner)
 
 
+def test_newton_pcg_dense_coarsest_level(espic, po):
+    """The coarsest multigrid level (here 6x6x11) solved by its dense inverse,
+    the default, or by smoothing sweeps on one block: the same converged phi,
+    within 1e-8 of the reference's solveGS, and no more PCG iterations with
+    the exact coarse solve."""
+    f = golden("sphere_solve")
+    phi0, te0, n0 = f["ref"]
+    res = {}
+    for dense in (0, 1024):
+        with world(espic, SPH) as w:
+            _sphere_solver_setup(espic, f, w)
+            sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 1000, 1e-4)
+            sol.setReferenceValues(phi0, te0, n0)
+            sol.setNewton(nr_max=50, nr_tol=1e-10, pcg_max=20000, pcg_tol=1e-12, fp32_inner=False)
+            sol.setDense(dense)
+            conv, nr, inner, norm = sol.solve()
+            assert conv, (dense, nr, inner, norm)
+            res[dense] = (w.phi.copy(), inner)
+    assert rel(res[1024][0], f["phi_tight"]) <= 1e-8
+    assert rel(res[1024][0], res[0][0]) <= 1e-9
+    assert res[1024][1] <= res[0][1], (res[1024][1], res[0][1])
+
+
+def test_newton_pcg_without_dirichlet_nodes(espic, po):
+    """A domain with no Dirichlet node at all: the Galerkin Laplacian of the
+    coarsest level is singular, the dense inversion detects the vanishing
+    pivot and that level is smoothed instead; the Boltzmann term keeps the
+    Newton problem definite, so float and float64 inner solves converge to the
+    same phi as the smoothing-only hierarchy."""
+    geo = ([17, 17, 33], [-0.1, -0.1, 0.0], [0.1, 0.1, 0.4])
+    ni, nj, nk = geo[0]
+    z = np.repeat(np.linspace(0, 1, nk), ni * nj)
+    rho = QE * 1e10 * (1.0 + 0.2 * np.cos(3 * z))
+    out = {}
+    for fp32 in (False, True):
+        for dense in (0, 1024):
+            with world(espic, geo) as w:
+                w.write(espic.FIELD_RHO, rho)
+                sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 100, 1e-4)
+                sol.setReferenceValues(0.0, 3.0, 1e10)
+                # the float inner solve resolves the Newton update to ~1e-8 V here
+                sol.setNewton(nr_max=50, nr_tol=1e-7 if fp32 else 1e-9, pcg_max=5000, pcg_tol=1e-10,
+                              fp32_inner=fp32)
+                sol.setDense(dense)
+                conv, nr, inner, norm = sol.solve()
+                assert conv and np.all(np.isfinite(w.phi)), (fp32, dense, nr, inner, norm)
+                out[fp32, dense] = w.phi.copy()
+        assert rel(out[fp32, 1024], out[fp32, 0]) <= (1e-6 if fp32 else 1e-7)
+
+
 def test_newton_pcg_fp32_inner_accuracy(espic, po):
     """One Newton step from a perturbed solution on a fine grid: the FP32 inner
     solve reaches the same accuracy as the FP64 one.  (A float Jacobian
