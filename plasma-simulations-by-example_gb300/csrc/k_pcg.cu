@@ -802,39 +802,58 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 if (!onq[h]) continue;
-                double L = 0, dL = 0;
-#pragma unroll
-                for (int m = 0; m < 6; m++) {
-                    const bool on = c[h] & ((1u << m) | (1u << (6 + m)));
-                    L += on ? cd[m >> 1] * (xu[h] - pn[h][m]) : 0.0;
-                    if (sizeof(T) != sizeof(float)) dL += on ? cd[m >> 1] : 0.0;
-                }
-                const double xa = (ph[h] - phi0) * inv_te0;
-                double e;
+                double Fv;
+                T rv, dBt;
                 if (sizeof(T) == sizeof(float)) {
-                    /* with the float inner solve, the Boltzmann factor is the
-                     * float exponential of the leading part of the argument
-                     * times a first-order factor for the rest: relative error
-                     * ~1e-7, which moves phi by ~Te 1e-7 (far below the
-                     * Newton tolerance), at a fraction of the float64 exp's
-                     * cost on a GPU with a narrow float64 pipe */
+                    /* the float-inner form spends fewer float64 operations
+                     * (the float64 pipe is narrow here): per axis
+                     * c (2 x_u - x_w - x_e) with a missing link reading x_u
+                     * itself; the Boltzmann factor as the float exponential of
+                     * the leading part of the argument times a first-order
+                     * factor for the rest (relative error ~1e-7, which moves
+                     * phi by ~Te 1e-7, far below the Newton tolerance); the
+                     * Jacobian's Boltzmann diagonal in float */
+                    double L = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        const unsigned mw = (1u << (2 * a)) | (1u << (6 + 2 * a));
+                        const unsigned me = (1u << (2 * a + 1)) | (1u << (7 + 2 * a));
+                        const double pw = (c[h] & mw) ? pn[h][2 * a] : xu[h];
+                        const double pe = (c[h] & me) ? pn[h][2 * a + 1] : xu[h];
+                        L = fma(cd[a], fma(2.0, xu[h], -(pw + pe)), L);
+                    }
+                    const double xa = (ph[h] - phi0) * inv_te0;
                     const float xh = (float)xa;
-                    e = (double)expf(xh) * (1.0 + (xa - (double)xh));
+                    const float ef = expf(xh);
+                    const double e = fma((double)ef, xa - (double)xh, (double)ef);
+                    if (linear) {
+                        const double dB = A0_te0 * e;
+                        Fv = fma(dB, xu[h], L) - bv[h];
+                        dBt = (T)dB;
+                    } else {
+                        Fv = fma(-bv[h], inv_eps0, fma(A0, e, L));
+                        dBt = (T)((float)A0_te0 * ef);
+                    }
+                    rv = (T)Fv;
+                    if (jacobi || !(c[h] & BLACK)) z[u[h]] = rv / full_diag(c[h], dBt, ct);
                 } else {
-                    e = exp(xa);
+                    double L = 0, dL = 0;
+#pragma unroll
+                    for (int m = 0; m < 6; m++) {
+                        const bool on = c[h] & ((1u << m) | (1u << (6 + m)));
+                        L += on ? cd[m >> 1] * (xu[h] - pn[h][m]) : 0.0;
+                        dL += on ? cd[m >> 1] : 0.0;
+                    }
+                    const double e = exp((ph[h] - phi0) * inv_te0);
+                    const double dB = A0_te0 * e;
+                    Fv = linear ? L + dB * xu[h] - bv[h] : L + A0 * e - bv[h] * inv_eps0;
+                    rv = (T)Fv;
+                    dBt = (T)dB;
+                    if (jacobi || !(c[h] & BLACK)) z[u[h]] = rv / (T)(dL + dB);
                 }
-                const double dB = A0_te0 * e;
-                const double Fv = linear ? L + dB * xu[h] - bv[h] : L + A0 * e - bv[h] * inv_eps0;
-                const T rv = (T)Fv;
-                dg[u[h]] = (T)dB;
+                dg[u[h]] = dBt;
                 r[u[h]] = rv;
                 y[u[h]] = 0;
-                if (jacobi || !(c[h] & BLACK)) {
-                    /* the float form takes the diagonal in float, the float64
-                     * form keeps its float64 sum */
-                    const T d = sizeof(T) == sizeof(float) ? full_diag(c[h], (T)dB, ct) : (T)(dL + dB);
-                    z[u[h]] = rv / d;
-                }
                 ff += Fv * Fv;
             }
         }
