@@ -96,10 +96,14 @@ __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV]
     }
     __syncthreads();
     double *slot = partials + (size_t)(round & 1) * gridDim.x * NV;
-    if (threadIdx.x < NV) {
-        double s = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[threadIdx.x][k];
-        slot[(size_t)blockIdx.x * NV + threadIdx.x] = s;
+    if (wid == 0) {
+        /* the warps' sums by a fixed shuffle tree (blocks of 32 warps) */
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double s = lane < (int)(blockDim.x >> 5) ? sh[q][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) slot[(size_t)blockIdx.x * NV + q] = s;
+        }
     }
     round++;
     grid.sync();
@@ -107,6 +111,7 @@ __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV]
 #pragma unroll
         for (int q = 0; q < NV; q++) {
             double s = 0;
+#pragma unroll 4
             for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + (size_t)b * NV + q);
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) tot[q] = s;
@@ -583,20 +588,39 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
 }
 
 /* e = A^-1 b on the coarsest level by its dense inverse, on the whole grid:
- * a warp per row, lanes over the columns in a fixed order, a fixed shuffle
- * tree over the lanes */
+ * block b takes a contiguous range of rows, eight at a time, four warps per
+ * row, each warp a quarter of the columns (lanes in a fixed order, a fixed
+ * shuffle tree); the four quarter sums are added in order.  Every thread of
+ * every block calls it (blocks of 1024 threads). */
 template <typename T>
 __device__ void dense_apply(const MgLevel<T> &L, const T *__restrict__ Ainv, int n) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < n; r += nwarps) {
-        const T *row = Ainv + r * n;
+    __shared__ T part[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int WPR = 4, RPP = 8; /* warps per row, rows per pass */
+    const int64_t rpb = ((int64_t)n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = (int64_t)blockIdx.x * rpb;
+    const int64_t r1 = r0 + rpb < n ? r0 + rpb : n;
+    for (int64_t rb = r0; rb < r1; rb += RPP) {
+        const int64_t r = rb + wid / WPR;
+        const int q = wid % WPR;
         T acc = 0;
-        for (int j = lane; j < n; j += 32) acc += row[j] * L.b[j];
+        if (r < r1) {
+            const int64_t c0 = (int64_t)q * n / WPR, c1 = (int64_t)(q + 1) * n / WPR;
+            const T *row = Ainv + r * n;
+#pragma unroll 8
+            for (int64_t j = c0 + lane; j < c1; j += 32) acc += row[j] * L.b[j];
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) L.e[r] = acc;
+        if (lane == 0) part[wid] = acc;
+        __syncthreads();
+        if (threadIdx.x < RPP && rb + threadIdx.x < r1) {
+            T sum = 0;
+#pragma unroll
+            for (int k = 0; k < WPR; k++) sum += part[threadIdx.x * WPR + k];
+            L.e[rb + threadIdx.x] = sum;
+        }
+        __syncthreads();
     }
 }
 
