@@ -1116,33 +1116,41 @@ __global__ void k_dense_build(MgLevel<T> L, double *M, double *diag0) {
     if (i == j) diag0[i] = v;
 }
 
-/* in-place Gauss-Jordan inversion without pivoting (the operator is
- * symmetric positive definite), step k: save column k, scale row k ... */
-__global__ void k_gj_pivot(double *M, int n, int k, double *col, const double *__restrict__ diag0, int *ok) {
+/* In-place Gauss-Jordan inversion without pivoting (the operator is
+ * symmetric positive definite), in one cooperative launch: for each k,
+ * block 0 saves column k and scales row k by the pivot, then every thread
+ * eliminates column k from the other rows.  A pivot that vanished against
+ * the original diagonal (a singular operator) clears *ok. */
+__global__ void __launch_bounds__(1024) k_gauss_jordan(double *M, int n, double *col,
+                                                       const double *__restrict__ diag0, int *ok) {
+    cg::grid_group grid = cg::this_grid();
     __shared__ double piv;
-    if (threadIdx.x == 0) {
-        piv = M[(int64_t)k * n + k];
-        /* a pivot that vanished against the original diagonal: singular */
-        if (!(piv > 1e-9 * diag0[k])) {
-            *ok = 0;
-            piv = 1.0;
+    for (int k = 0; k < n; k++) {
+        if (blockIdx.x == 0) {
+            if (threadIdx.x == 0) {
+                piv = __ldcg(M + (int64_t)k * n + k);
+                if (!(piv > 1e-9 * diag0[k])) {
+                    *ok = 0;
+                    piv = 1.0;
+                }
+            }
+            for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = __ldcg(M + (int64_t)i * n + k);
+            __syncthreads();
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                const double a = j == k ? 1.0 : __ldcg(M + (int64_t)k * n + j);
+                M[(int64_t)k * n + j] = a / piv;
+            }
         }
+        grid.sync();
+        for (int i = blockIdx.x; i < n; i += gridDim.x) {
+            if (i == k) continue;
+            const double f = __ldcg(col + i);
+            double *Mi = M + (int64_t)i * n;
+            for (int j = threadIdx.x; j < n; j += blockDim.x)
+                Mi[j] = (j == k ? 0.0 : __ldcg(Mi + j)) - f * __ldcg(M + (int64_t)k * n + j);
+        }
+        grid.sync();
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = M[(int64_t)i * n + k];
-    __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double a = j == k ? 1.0 : M[(int64_t)k * n + j];
-        M[(int64_t)k * n + j] = a / piv;
-    }
-}
-
-/* ... and eliminate column k from every other row */
-__global__ void k_gj_update(double *M, int n, int k, const double *__restrict__ col) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)n * n) return;
-    const int64_t i = t / n, j = t - i * n;
-    if (i == k) return;
-    M[t] = (j == k ? 0.0 : M[t]) - col[i] * M[(int64_t)k * n + j];
 }
 
 /* the inverse in T, symmetrised; rows and columns of aggregates without
@@ -1279,12 +1287,15 @@ static int run_pcg(World &w) {
             cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, w.stream);
             const MgLevel<T> &Lc = A.L[A.nlev - 1];
             k_dense_build<T><<<blocks_for(nsq, 256), 256, 0, w.stream>>>(Lc, M, diag0);
-            for (int k = 0; k < n; k++) {
-                k_gj_pivot<<<1, 1024, 0, w.stream>>>(M, n, k, col, diag0, ok);
-                k_gj_update<<<blocks_for(nsq, 256), 256, 0, w.stream>>>(M, n, k, col);
-            }
+            int gj_per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gj_per_sm, k_gauss_jordan, 1024, 0);
+            int gj_grid = (gj_per_sm < 1 ? 1 : gj_per_sm) * w.sm_count;
+            if (gj_grid > n) gj_grid = n;
+            int nn_ = n;
+            void *gj_args[] = {&M, &nn_, &col, &diag0, &ok};
+            cudaLaunchCooperativeKernel((const void *)k_gauss_jordan, gj_grid, 1024, gj_args, 0, w.stream);
             k_dense_store<T><<<blocks_for(nsq, 256), 256, 0, w.stream>>>(Lc, M, A.dense);
-            w.nlaunch += 2 + 2 * n;
+            w.nlaunch += 3;
         }
         w.pcg_codes_valid = true;
     }
