@@ -21,9 +21,10 @@
  * order, so every block takes the same branch.  The inner PCG stops when
  * |r| <= pcg_tol |F|, or earlier once the RMS of the preconditioned residual
  * z = M r (an estimate of the error left in the Newton update y) is below
- * nr_tol / 10: the Newton test RMS(y) < nr_tol cannot then depend on more
- * inner accuracy, and the last Newton step stops needing a full solve; when
- * the first V-cycle's z is already that small, z itself is the update.
+ * nr_tol / 3 (nr_tol / 10 in linear mode): the Newton test RMS(y) < nr_tol
+ * cannot then depend on more inner accuracy, and the last Newton step stops
+ * needing a full solve; when the first V-cycle's z is already that small,
+ * z itself is the update.
  *
  * Preconditioner: an aggregation multigrid V-cycle.  Level l+1 groups the
  * level-l unknowns in 2x2x2 blocks of the structured index space; its
@@ -794,7 +795,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
      * phi solves J y = b; the stopping test is relative to the first update */
     const bool linear = lin_y != nullptr;
     double nr_scale = linear ? 0.0 : 1.0;
-    double zz_stop = 0.01 * nr_tol * nr_tol * (double)nn * nr_scale;
+    double zz_stop = nr_tol * nr_tol / 9.0 * (double)nn * nr_scale;
     for (nr = 0; nr < nr_max; nr++) {
         /* Newton residual (float64) and the Boltzmann part of the Jacobian
          * diagonal; the first red smoothing half sweep (or Jacobi) of the
@@ -894,7 +895,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             double ZZ;
             double RZ = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
             /* the first preconditioned residual already estimates an update
-             * below a tenth of the Newton tolerance: it is the update */
+             * below the inner stop: it is the update */
             take_z = ZZ < zz_stop;
             T beta = 0;
             T *pold = p0, *pnew = p1;
@@ -982,7 +983,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 if (!(s4[0] > stop2)) break; /* also leaves on NaN */
                 double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
                 /* z = M r estimates the remaining error of y: once its RMS is
-                 * below a tenth of the Newton tolerance, further inner
+                 * below a third of the Newton tolerance, further inner
                  * iterations cannot change the outcome of the Newton test */
                 if (ZZ < zz_stop) break;
                 beta = (T)(RZn / RZ);
