@@ -152,7 +152,7 @@ static void free_species(Species *s) {
 static void free_world(World &w) {
     for (Species *s : w.species) free_species(s);
     w.species.clear();
-    void *ptrs[] = {w.phi, w.rho, w.vol, w.ef, w.ef4, w.obj, w.target, w.d_err, w.d_status, w.d_partials,
+    void *ptrs[] = {w.phi, w.rho, w.vol, w.ivol, w.ef, w.ef4, w.obj, w.target, w.d_err, w.d_status, w.d_partials,
                     w.d_small, w.d_u, w.d_stage, w.d_blockcnt, w.pcg_buf, w.phi_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -213,6 +213,7 @@ extern "C" int espic_world_create(int ni, int nj, int nk, const double x0[3], co
     TRY(dalloc(&w.phi, w.nn));
     TRY(dalloc(&w.rho, w.nn));
     TRY(dalloc(&w.vol, w.nn));
+    TRY(dalloc(&w.ivol, w.nn));
     TRY(dalloc(&w.ef, 3 * w.nn));
     TRY(dalloc(&w.ef4, w.nn));
     TRY(dalloc(&w.obj, w.nn));
@@ -1097,6 +1098,7 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
     if (n < cnt) return fail(ESPIC_ERR_ARG, "buffer holds %lld of %lld values", (long long)n, (long long)cnt);
     CK(cudaMemcpyAsync(p, host, cnt * sizeof(double), cudaMemcpyHostToDevice, w.stream));
     if (field == ESPIC_FIELD_EF) launch_ef4(w);
+    if (field == ESPIC_FIELD_NODE_VOL) launch_inv_vol(w);
     if (field == ESPIC_FIELD_PHI) w.phi_prev_valid = false;
     if (field == ESPIC_FIELD_RHO) w.rho_version++;
     CHECK_LAUNCH();

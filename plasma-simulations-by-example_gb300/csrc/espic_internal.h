@@ -121,6 +121,7 @@ void launch_push_fp64(World &w, Species &s, bool deposit);
 void launch_deposit_fp64(World &w, Species &s);
 void launch_compact(World &w, Species &s);
 void launch_density(World &w, Species &s);
+void launch_inv_vol(World &w);
 void launch_charge(World &w);
 void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3,
                      const double *d_w, int64_t n, int rewind);

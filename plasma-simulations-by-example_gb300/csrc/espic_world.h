@@ -65,6 +65,7 @@ struct World {
     cudaStream_t stream = nullptr;
     int device = 0, sm_count = 0;
     double *phi = nullptr, *rho = nullptr, *vol = nullptr, *ef = nullptr;
+    double *ivol = nullptr; /* RN(1 / node_vol), 0 where the volume is 0: the density's divisor */
     float4 *ef4 = nullptr;
     bool ef4_valid = false;
     int32_t *obj = nullptr, *target = nullptr;

@@ -722,12 +722,13 @@ __global__ void k_targets(Geo g, const int32_t *__restrict__ obj, int32_t *targe
 /* den = acc * unit / node_vol (0 where the volume is 0): the fixed-point sum
  * followed by Field_::operator/=, ch2/Field.h:125-134 */
 __global__ void k_density(int64_t nn, const unsigned long long *__restrict__ acc, double unit,
-                          const double *__restrict__ vol, double *den) {
+                          const double *__restrict__ vol, const double *__restrict__ ivol, double *den) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nn) return;
     double d = __ll2double_rn((long long)acc[u]) * unit;
     double v = vol[u];
-    den[u] = (v != 0) ? d / v : 0.0;
+    /* d / v, correctly rounded, from RN(1/v) (the float64 pipe is narrow) */
+    den[u] = (v != 0) ? div_rcp(d, v, ivol[u]) : 0.0;
 }
 
 struct ChargeArgs {
@@ -1055,6 +1056,14 @@ __global__ void k_node_vol(Geo g, double *vol) {
     vol[u] = V;
 }
 
+/* RN(1 / node_vol) for the density's division (0 where the volume is 0) */
+__global__ void k_inv_vol(int64_t nn, const double *__restrict__ vol, double *ivol) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    const double v = vol[u];
+    ivol[u] = v != 0 ? 1.0 / v : 0.0;
+}
+
 __global__ void k_ef_to_ef4(int64_t nn, const double *__restrict__ ef, float4 *ef4) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nn) return;
@@ -1212,7 +1221,7 @@ void launch_compact(World &w, Species &s) {
 }
 
 void launch_density(World &w, Species &s) {
-    k_density<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, s.acc, s.unit, w.vol, s.den);
+    k_density<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, s.acc, s.unit, w.vol, w.ivol, s.den);
     w.nlaunch++;
 }
 
@@ -1403,8 +1412,14 @@ int launch_gs_sphere(World &w, int max_it, double tol) {
     return (int)cudaLaunchCooperativeKernel((const void *)k_gs_sphere, grid, 256, args, 0, w.stream);
 }
 
+void launch_inv_vol(World &w) {
+    k_inv_vol<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.vol, w.ivol);
+    w.nlaunch++;
+}
+
 void launch_node_vol(World &w) {
     k_node_vol<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.vol);
+    launch_inv_vol(w);
     w.nlaunch++;
 }
 
