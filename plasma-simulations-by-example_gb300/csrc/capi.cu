@@ -88,6 +88,7 @@ static int take_device_errors(World &w) {
     if (bits & DERR_NONFINITE) return fail(ESPIC_ERR_NONFINITE, "non-finite value in the step");
     if (bits & DERR_FIXED_RANGE) return fail(ESPIC_ERR_FIXED, "weight outside the fixed-point range");
     if (bits & DERR_TIMEOUT) return fail(ESPIC_ERR_CUDA, "a bounded wait on a bulk copy timed out");
+    if (bits & DERR_SORT) return fail(ESPIC_ERR_CUDA, "the cell sort lost track of a particle");
     return ESPIC_OK;
 }
 

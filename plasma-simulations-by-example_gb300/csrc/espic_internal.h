@@ -27,7 +27,8 @@ enum : int {
     DERR_CAPACITY = 1,   /* particle buffer full: injection or load truncated */
     DERR_NONFINITE = 2,  /* NaN / Inf met in a solve */
     DERR_FIXED_RANGE = 4, /* a weight too large for the fixed-point scale */
-    DERR_TIMEOUT = 8      /* a bounded wait on an asynchronous copy ran out */
+    DERR_TIMEOUT = 8,     /* a bounded wait on an asynchronous copy ran out */
+    DERR_SORT = 16        /* a sort slot named no particle of the species */
 };
 
 struct Geo {

@@ -505,10 +505,15 @@ struct GenThermal { /* uniform box with a drifting Maxwellian (no reference coun
     }
 };
 
+/* Candidates per block of the append passes: small blocks spread an
+ * injection of a few thousand candidates, whose float64 Box-Muller
+ * transcendentals dominate, over many SMs. */
+constexpr int APPEND_THREADS = 64;
+
 /* Pass 1: accepted candidates per block (addParticle rejects x outside
  * [x0,xm)). */
 template <class Gen>
-__global__ void __launch_bounds__(256) k_append_count(Geo g, Gen gen, int64_t ncand, int32_t *blockcnt) {
+__global__ void __launch_bounds__(APPEND_THREADS) k_append_count(Geo g, Gen gen, int64_t ncand, int32_t *blockcnt) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool ok = false;
     if (i < ncand) {
@@ -555,13 +560,13 @@ __global__ void __launch_bounds__(1024) k_append_scan(int32_t *blockcnt, int64_t
  * n_old + (number of accepted candidates before it), so the order is the
  * candidates' order, as the reference's emplace_back. */
 template <class Gen, int FORM>
-__global__ void __launch_bounds__(256) k_append_write(Geo g, Gen gen, int64_t ncand,
+__global__ void __launch_bounds__(APPEND_THREADS) k_append_write(Geo g, Gen gen, int64_t ncand,
                                                       const int32_t *__restrict__ blockpre,
                                                       const int64_t *__restrict__ d_count,
                                                       const double *__restrict__ ef, double qm, double dt,
                                                       double *P, int32_t *cell, float *off, float *vel,
                                                       int64_t stride, int64_t cap, int write_w) {
-    __shared__ int32_t sh[8];
+    __shared__ int32_t sh[APPEND_THREADS / 32];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t s_base = d_count[1] + blockpre[blockIdx.x];
     double x[3], v[3], w = 0;
@@ -570,7 +575,7 @@ __global__ void __launch_bounds__(256) k_append_write(Geo g, Gen gen, int64_t nc
         gen.make(i, x, v, w);
         ok = in_bounds(g, x);
     }
-    /* block exclusive rank of ok (256 threads = 8 warps) */
+    /* block exclusive rank of ok */
     unsigned bal = __ballot_sync(0xffffffffu, ok);
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) sh[wid] = __popc(bal);
@@ -1248,7 +1253,7 @@ void launch_update_average(World &w, Species &s) {
 template <class Gen>
 static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int write_w) {
     if (ncand <= 0) return;
-    int64_t blocks = (ncand + 255) / 256;
+    int64_t blocks = (ncand + APPEND_THREADS - 1) / APPEND_THREADS;
     if (blocks > w.blockcnt_cap) {
         if (w.d_blockcnt) {
             cudaStreamSynchronize(w.stream);
@@ -1262,14 +1267,14 @@ static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int writ
         }
     }
     double qm = s.charge / s.mass;
-    k_append_count<Gen><<<(unsigned)blocks, 256, 0, w.stream>>>(w.g, gen, ncand, w.d_blockcnt);
+    k_append_count<Gen><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(w.g, gen, ncand, w.d_blockcnt);
     k_append_scan<<<1, 1024, 0, w.stream>>>(w.d_blockcnt, blocks, s.d_count, s.cap, w.d_err);
     if (s.form == 0)
-        k_append_write<Gen, 0><<<(unsigned)blocks, 256, 0, w.stream>>>(
+        k_append_write<Gen, 0><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(
             w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, s.P, nullptr, nullptr, nullptr, s.cap, s.cap,
             write_w);
     else
-        k_append_write<Gen, 1><<<(unsigned)blocks, 256, 0, w.stream>>>(
+        k_append_write<Gen, 1><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(
             w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, nullptr, s.cell, s.off, s.vel, s.ms, s.cap,
             0);
     w.nlaunch += 3;

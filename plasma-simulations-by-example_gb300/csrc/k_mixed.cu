@@ -518,21 +518,35 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict_
     perm[base + (lane - head)] = (int32_t)p;
 }
 
-/* out[q] = in[perm[q]] for one float array */
+/* out[q] = in[perm[q]] for one float array (an index outside the species,
+ * which the histogram and scatter cannot produce, is flagged, not read) */
 __global__ void __launch_bounds__(256) k_sort_gather(const float *__restrict__ in, const int32_t *__restrict__ perm,
-                                                     const int64_t *__restrict__ d_count, float *out) {
+                                                     const int64_t *__restrict__ d_count, float *out, int *err) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d_count[0]) return;
-    out[q] = in[perm[q]];
+    const int64_t n = d_count[0];
+    if (q >= n) return;
+    const int64_t p = perm[q];
+    if (p < 0 || p >= n) {
+        atomicOr(err, DERR_SORT);
+        return;
+    }
+    out[q] = in[p];
 }
 
 /* the keys last: perm is overwritten in place (each thread reads its slot
  * before writing it) */
 __global__ void __launch_bounds__(256) k_sort_gather_keys(const int32_t *__restrict__ cell,
-                                                          const int64_t *__restrict__ d_count, int32_t *perm_key) {
+                                                          const int64_t *__restrict__ d_count, int32_t *perm_key,
+                                                          int *err) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d_count[0]) return;
-    perm_key[q] = cell[perm_key[q]];
+    const int64_t n = d_count[0];
+    if (q >= n) return;
+    const int64_t p = perm_key[q];
+    if (p < 0 || p >= n) {
+        atomicOr(err, DERR_SORT);
+        return;
+    }
+    perm_key[q] = cell[p];
 }
 
 /* per block: {count, mx, my, mz, sum w v^2} for the mixed form: float sums
@@ -682,11 +696,11 @@ void launch_sort_mixed(World &w, Species &s) {
     k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, w.g.ni, w.g.nj, counts, s.cell2);
     for (int d = 0; d < 3; d++) {
         k_sort_gather<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.off + d * s.ms, s.cell2, s.d_count,
-                                                                s.off2 + d * s.ms);
+                                                                s.off2 + d * s.ms, w.d_err);
         k_sort_gather<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.vel + d * s.ms, s.cell2, s.d_count,
-                                                                s.vel2 + d * s.ms);
+                                                                s.vel2 + d * s.ms, w.d_err);
     }
-    k_sort_gather_keys<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, s.cell2);
+    k_sort_gather_keys<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, s.cell2, w.d_err);
     w.nlaunch += 12;
     int32_t *tc = s.cell;
     s.cell = s.cell2;

@@ -1245,7 +1245,10 @@ static int run_pcg(World &w) {
     MgArgs<T> A;
     size_t mgb = mg_layout<T>(w, A, nullptr);
     int64_t nlist = (int64_t)((w.g.ni - 1) / 2) * (w.g.nj - 2) * (w.g.nk - 2);
-    size_t listb = ((4 * nlist * sizeof(int32_t) + 255) / 256) * 256;
+    /* the colour lists are only read when the sweeps cannot enumerate their
+     * nodes arithmetically (2^24 entries or more, see fine_half) */
+    const bool need_lists = nlist >= (1 << 24);
+    size_t listb = need_lists ? ((4 * nlist * sizeof(int32_t) + 255) / 256) * 256 : 0;
     size_t need = 7 * vec + codeb + mgb + listb;
     if (w.pcg_bytes < need || w.pcg_elem != (int)es) {
         if (w.pcg_buf) {
@@ -1267,7 +1270,7 @@ static int run_pcg(World &w) {
     if (!w.pcg_codes_valid) {
         k_pcg_codes<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.g, w.obj, code);
         w.nlaunch++;
-        for (int c = 0; c < 2; c++) {
+        for (int c = 0; c < 2 && need_lists; c++) {
             k_pcg_lists<<<blocks_for(nlist, 256), 256, 0, w.stream>>>(w.g, c, lists + 2 * c * nlist,
                                                                       lists + (2 * c + 1) * nlist);
             w.nlaunch++;
