@@ -247,6 +247,10 @@ __device__ __forceinline__ T jacobian_apply(uint16_t cc, T dB, const T ct[3], T 
     return s;
 }
 
+/* a node index clamped into the grid (loads of a boundary node's missing
+ * neighbours, whose values are never used) */
+__device__ __forceinline__ int64_t clamp_node(int64_t v, int64_t nn) { return v < 0 ? 0 : (v >= nn ? nn - 1 : v); }
+
 /* red-black half sweep on the node grid: z = (r + sum c z_nb) / diag */
 /* Red-black Gauss-Seidel pieces.  A Gauss-Seidel update never reads the
  * node's own old value, which allows three fusions: the first red half
@@ -802,8 +806,10 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
          * preconditioner rides along */
         double ff = 0;
         const double *XR = linear ? lin_y : phi;
-        /* two nodes per pass, every load before any store (a node that is
-         * not an unknown reads the interior node (1,1,1) and stores nothing) */
+        /* two nodes per pass, every load before any store; the loads do not
+         * wait for the code word (neighbour indices are clamped into the
+         * grid, a node past the end reads the interior node (1,1,1)), and
+         * a node that is not an unknown stores nothing */
         for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
             const int64_t uq[2] = {u0, u0 + gsize};
             bool onq[2];
@@ -813,14 +819,14 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             for (int h = 0; h < 2; h++) {
                 c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
                 onq[h] = c[h] & SELF;
-                u[h] = onq[h] ? uq[h] : safe;
+                u[h] = uq[h] < nn ? uq[h] : safe;
             }
             double xu[2], pn[2][6], ph[2], bv[2];
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 xu[h] = XR[u[h]];
 #pragma unroll
-                for (int m = 0; m < 6; m++) pn[h][m] = XR[u[h] + off[m]];
+                for (int m = 0; m < 6; m++) pn[h][m] = XR[clamp_node(u[h] + off[m], nn)];
                 ph[h] = phi[u[h]];
                 bv[h] = linear ? lin_b[u[h]] : rho[u[h]];
             }
@@ -903,9 +909,10 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 /* p = z + beta p (on the fly at the node and its neighbours),
                  * q = J p */
                 T pq = 0;
-                /* two nodes per pass, every load before any store; a node
-                 * that is not an unknown (or past the end) reads the
-                 * interior node (1,1,1) and stores nothing */
+                /* two nodes per pass, every load before any store; the loads
+                 * do not wait for the code word (neighbour indices clamped
+                 * into the grid, a node past the end reads the interior node
+                 * (1,1,1)); a node that is not an unknown stores nothing */
                 for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
                     const int64_t uq[2] = {u0, u0 + gsize};
                     bool on[2];
@@ -915,7 +922,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                     for (int h = 0; h < 2; h++) {
                         c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
                         on[h] = c[h] & SELF;
-                        u[h] = on[h] ? uq[h] : safe;
+                        u[h] = uq[h] < nn ? uq[h] : safe;
                     }
                     /* an unknown is interior: neighbour loads need no code bit */
                     T zc[2], pc[2], dB[2], zn[2][6], pn[2][6];
@@ -926,8 +933,9 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                         dB[h] = dg[u[h]];
 #pragma unroll
                         for (int m = 0; m < 6; m++) {
-                            zn[h][m] = z[u[h] + off[m]];
-                            pn[h][m] = it ? pold[u[h] + off[m]] : (T)0;
+                            const int64_t nb = clamp_node(u[h] + off[m], nn);
+                            zn[h][m] = z[nb];
+                            pn[h][m] = it ? pold[nb] : (T)0;
                         }
                     }
 #pragma unroll
@@ -956,7 +964,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                     for (int h = 0; h < 2; h++) {
                         c[h] = uq[h] < nn ? code[uq[h]] : (uint16_t)0;
                         on[h] = c[h] & SELF;
-                        u[h] = on[h] ? uq[h] : safe;
+                        u[h] = uq[h] < nn ? uq[h] : safe;
                     }
                     T yv[2], pv[2], rv[2], qv[2], dv[2];
 #pragma unroll
