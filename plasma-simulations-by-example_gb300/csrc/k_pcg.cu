@@ -124,6 +124,56 @@ __device__ __forceinline__ void grid_sum_n(cg::grid_group &grid, double (&v)[NV]
 }
 
 
+/* The same for per-thread values of the inner-solve type T: the warp stage
+ * adds in T (for float, five float shuffle steps instead of five float64
+ * ones in each of a block's 32 warps, which the narrow float64 pipe
+ * serialised), then the warps' sums, the blocks' partials and the grid
+ * total are float64 as above. */
+template <int NV, typename T>
+__device__ __forceinline__ void grid_sum_t(cg::grid_group &grid, const T (&v)[NV], double (&out)[NV],
+                                           double *partials, int &round) {
+    if (sizeof(T) == sizeof(double)) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) out[q] = (double)v[q];
+        grid_sum_n<NV>(grid, out, partials, round);
+        return;
+    }
+    __shared__ double shw[NV][32];
+    __shared__ double tot[NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        T x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) shw[q][wid] = (double)x;
+    }
+    __syncthreads();
+    double *slot = partials + (size_t)(round & 1) * gridDim.x * NV;
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double sum = lane < (int)(blockDim.x >> 5) ? shw[q][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            if (lane == 0) slot[(size_t)blockIdx.x * NV + q] = sum;
+        }
+    }
+    round++;
+    grid.sync();
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double sum = 0;
+#pragma unroll 4
+            for (unsigned b = lane; b < gridDim.x; b += 32) sum += __ldcg(slot + (size_t)b * NV + q);
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            if (lane == 0) tot[q] = sum;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = tot[q];
+}
+
 constexpr int MG_MAX = 12;
 constexpr size_t PCG_SMEM_MAX = 160 * 1024; /* shared memory for block 0's coarse levels */
 
@@ -648,8 +698,9 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
                 rz += F.r[u] * zu;
                 z2 += zu * zu;
             }
-        double v[2] = {(double)rz, (double)z2};
-        grid_sum_n<2>(grid, v, partials, round);
+        const T vt[2] = {rz, z2};
+        double v[2];
+        grid_sum_t<2, T>(grid, vt, v, partials, round);
         zz = v[1];
         return v[0];
     }
@@ -746,8 +797,9 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
     fine_half(F, 1, &A.L[0], sc, rz, z2);
     grid.sync();
     fine_half(F, 0, (const MgLevel<T> *)nullptr, sc, rz, z2);
-    double v[2] = {(double)rz, (double)z2};
-    grid_sum_n<2>(grid, v, partials, round);
+    const T vt[2] = {rz, z2};
+    double v[2];
+    grid_sum_t<2, T>(grid, vt, v, partials, round);
     zz = v[1];
     return v[0];
 }
@@ -950,8 +1002,9 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                         pq += pu * s;
                     }
                 }
-                double s3[1] = {(double)pq};
-                grid_sum_n<1>(grid, s3, partials, round);
+                const T t3[1] = {pq};
+                double s3[1];
+                grid_sum_t<1, T>(grid, t3, s3, partials, round);
                 const T alpha = (T)(RZ / s3[0]);
                 /* y += alpha p, r -= alpha q, and the first red half sweep */
                 T rr = 0;
@@ -985,8 +1038,9 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                         if (jacobi || !(c[h] & BLACK)) z[u[h]] = ru / full_diag(c[h], dv[h], ct);
                     }
                 }
-                double s4[1] = {(double)rr};
-                grid_sum_n<1>(grid, s4, partials, round);
+                const T t4[1] = {rr};
+                double s4[1];
+                grid_sum_t<1, T>(grid, t4, s4, partials, round);
                 inner++;
                 if (!(s4[0] > stop2)) break; /* also leaves on NaN */
                 double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
