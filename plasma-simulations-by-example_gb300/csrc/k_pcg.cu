@@ -815,6 +815,8 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         double *lin_y, const double *__restrict__ lin_b) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char pcg_smem[];
+    __shared__ T bc_alpha, bc_beta;
+    __shared__ int bc_stop;
     __shared__ MgArgs<T> smem_args;
     const MgArgs<T> *SB = nullptr;
     if (mg.smem_from >= 0 && mg.nlev > 0 && blockIdx.x == 0) {
@@ -1005,7 +1007,12 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 const T t3[1] = {pq};
                 double s3[1];
                 grid_sum_t<1, T>(grid, t3, s3, partials, round);
-                const T alpha = (T)(RZ / s3[0]);
+                /* block-uniform scalars are computed by one thread and
+                 * broadcast: 32 warps each dividing in float64 would queue
+                 * on the narrow float64 pipe */
+                if (threadIdx.x == 0) bc_alpha = (T)(RZ / s3[0]);
+                __syncthreads();
+                const T alpha = bc_alpha;
                 /* y += alpha p, r -= alpha q, and the first red half sweep */
                 T rr = 0;
                 for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
@@ -1042,13 +1049,20 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 double s4[1];
                 grid_sum_t<1, T>(grid, t4, s4, partials, round);
                 inner++;
-                if (!(s4[0] > stop2)) break; /* also leaves on NaN */
+                if (threadIdx.x == 0) bc_stop = !(s4[0] > stop2); /* also leaves on NaN */
+                __syncthreads();
+                if (bc_stop) break;
                 double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
                 /* z = M r estimates the remaining error of y: once its RMS is
                  * below a third of the Newton tolerance, further inner
                  * iterations cannot change the outcome of the Newton test */
-                if (ZZ < zz_stop) break;
-                beta = (T)(RZn / RZ);
+                if (threadIdx.x == 0) {
+                    bc_stop = ZZ < zz_stop;
+                    bc_beta = (T)(RZn / RZ);
+                }
+                __syncthreads();
+                if (bc_stop) break;
+                beta = bc_beta;
                 RZ = RZn;
                 T *tp = pold;
                 pold = pnew;
