@@ -621,7 +621,9 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
     const double q = a * y;
     const double r = __fma_rn(-q, b, a);
     const double q2 = __fma_rn(r, y, q);
-    return a == 0.0 ? q : q2;
+    /* a == +-0 tested on the bits: an integer compare keeps the narrow
+     * float64 pipe for the arithmetic */
+    return (__double_as_longlong(a) << 1) == 0 ? q : q2;
 }
 
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
@@ -733,7 +735,7 @@ __global__ void k_density(int64_t nn, const unsigned long long *__restrict__ acc
     double d = __ll2double_rn((long long)acc[u]) * unit;
     double v = vol[u];
     /* d / v, correctly rounded, from RN(1/v) (the float64 pipe is narrow) */
-    den[u] = (v != 0) ? div_rcp(d, v, ivol[u]) : 0.0;
+    den[u] = (__double_as_longlong(v) << 1) != 0 ? div_rcp(d, v, ivol[u]) : 0.0;
 }
 
 struct ChargeArgs {

@@ -1072,11 +1072,27 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         /* Newton update */
         double yy = 0;
         double *X = linear ? lin_y : phi;
-        for (int64_t u = gtid; u < nn; u += gsize) {
-            if (!(code[u] & SELF)) continue;
-            double yu = take_z ? (double)z[u] : (double)y[u];
-            X[u] -= yu;
-            yy += yu * yu;
+        /* two nodes per pass, loads ahead of the code test and the stores */
+        for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
+            const int64_t uq[2] = {u0, u0 + gsize};
+            int64_t u[2];
+            uint16_t c[2];
+            T yv[2];
+            double xv[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                u[h] = uq[h] < nn ? uq[h] : safe;
+                c[h] = uq[h] < nn ? code[u[h]] : (uint16_t)0;
+                yv[h] = take_z ? z[u[h]] : y[u[h]];
+                xv[h] = X[u[h]];
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (!(c[h] & SELF)) continue;
+                const double yu = (double)yv[h];
+                X[u[h]] = xv[h] - yu;
+                yy += yu * yu;
+            }
         }
         double s6[1] = {yy};
         grid_sum_n<1>(grid, s6, partials, round);
