@@ -32,11 +32,14 @@
  * (a 7-point stencil again, with per-node weights), built once per geometry
  * by a deterministic gather.  Smoothing is red-black Gauss-Seidel (red then
  * black before the coarse correction, black then red after), restriction is
- * P^T, prolongation P scaled by a constant, and the coarsest level gets
- * symmetric sweeps, so the preconditioner is symmetric as CG requires.
- * Levels with fewer than World::mg_block_nodes nodes (default 4096) run on
- * block 0 alone between two grid barriers.  Without levels, the
- * preconditioner is Jacobi.
+ * P^T, prolongation P scaled by a constant.  The first level with at most
+ * World::mg_dense_max nodes (default 1024) is the coarsest and is solved by
+ * its dense inverse (computed once per geometry by k_gauss_jordan), every
+ * level above it on the whole grid.  With mg_dense_max 0 (or a singular
+ * coarse operator) the coarsest level gets symmetric sweeps instead and
+ * levels with fewer than World::mg_block_nodes nodes (default 4096) run on
+ * block 0 alone between two grid barriers.  Either way the preconditioner
+ * is symmetric, as CG requires.  Without levels, it is Jacobi.
  */
 #include <cooperative_groups.h>
 
