@@ -216,6 +216,23 @@ int espic_efield(espic_world *w);
 /* Species::getRealCount, getMomentum, getKE, ch2/Species.cpp:144-168:
  * out = {real count, px, py, pz, KE} */
 int espic_species_diag(espic_world *w, int sp, double out[5]);
+
+/* DSMC_MEX, ch4/Collisions.h:51-75 and ch4/Collisions.cpp:84-183:
+ * neutral-neutral collisions of a species in the float64 form by Bird's
+ * no-time-counter scheme with the variable-hard-sphere cross-section.
+ * c = {d_ref, omega, 2 K T_ref / m_r, Gamma(5/2 - omega)}, or NULL for the
+ * reference's constructor values (d_ref 4.07e-10 m, omega 0.77, T_ref
+ * 273.15 K); sigma_cr_max is the member's starting value (1e-14 in the
+ * reference).  DSMC_MEX::apply(dt) is espic_dsmc_apply with u NULL: each
+ * cell draws its uniforms from the world's counter-based stream.  With u
+ * non-NULL (parity checks) cell c draws u[cell_off[c]], u[cell_off[c] + 1],
+ * ... in the reference's rnd() order (cell_off: n_cells + 1 entries); the
+ * call then waits.  espic_dsmc_status reads sigma_cr_max and the collision
+ * counts of the last call and of all calls. */
+int espic_dsmc_enable(espic_world *w, int sp, const double *c, double sigma_cr_max);
+int espic_dsmc_apply(espic_world *w, int sp, double dt, const double *u, int64_t nu, const int64_t *cell_off);
+int espic_dsmc_status(espic_world *w, int sp, double *sigma_cr_max, int64_t *collisions_last,
+                      int64_t *collisions_total);
 /* World::getPE, ch2/World.cpp:72-84 */
 int espic_potential_energy(espic_world *w, double *pe);
 /* The per-step columns of Output::diagOutput, ch3/ver2/Output.cpp:96-132, with

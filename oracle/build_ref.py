@@ -22,7 +22,7 @@ REF_TARGETS = {
     "ref_ch2": ("ch2", ["World.cpp", "Species.cpp", "PotentialSolver.cpp"], "ch2_harness.cpp"),
     "ref_ch3": ("ch3/ver2", ["World.cpp", "Species.cpp", "PotentialSolver.cpp", "Source.cpp"],
                 "ch3_harness.cpp"),
-    "ref_ch4": ("ch4", ["World.cpp", "Species.cpp", "Source.cpp"], "ch4_harness.cpp"),
+    "ref_ch4": ("ch4", ["World.cpp", "Species.cpp", "Source.cpp", "Collisions.cpp"], "ch4_harness.cpp"),
 }
 
 

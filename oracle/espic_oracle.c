@@ -417,6 +417,109 @@ int64_t eo_inject_warm(const eo_grid *g, const double *ef, double charge, double
  * 6 uniforms per particle.  The count is the remainder count of ch9/MPI
  * (*rem carried) when rem != NULL, else (int)(N + u[0]).  The rewind is that
  * of addParticle here and of ch9/MPI/src/Source.cpp:61-68 (same expression). */
+/* World::XtoC, ch4/World.h:79-98: truncated logical coordinates */
+static int64_t dsmc_cell(const eo_grid *g, const double x[3]) {
+    int ijk[3];
+    for (int d = 0; d < 3; d++) ijk[d] = (int)((x[d] - g->x0[d]) / g->dh[d]);
+    return (int64_t)ijk[2] * (g->nj - 1) * (g->ni - 1) + (int64_t)ijk[1] * (g->ni - 1) + ijk[0];
+}
+
+/* vec3 magnitude, ch4/Field.h:21-26: sqrt of ((0 + x x) + y y) + z z */
+static double dsmc_mag(const double v[3]) {
+    double s = 0;
+    for (int i = 0; i < 3; i++) s += v[i] * v[i];
+    return sqrt(s);
+}
+
+/* DSMC_MEX::collide, ch4/Collisions.cpp:84-105 (isotropic scattering) */
+static void dsmc_collide(double *v1, double *v2, double m1, double m2, double u_chi, double u_eps) {
+    double cm[3], cr[3];
+    for (int i = 0; i < 3; i++) cm[i] = (v1[i] * m1 + v2[i] * m2) / (m1 + m2);
+    for (int i = 0; i < 3; i++) cr[i] = v1[i] - v2[i];
+    const double cr_mag = dsmc_mag(cr);
+    const double cos_chi = 2 * u_chi - 1;
+    const double sin_chi = sqrt(1 - cos_chi * cos_chi);
+    const double eps = 2 * EO_PI * u_eps;
+    cr[0] = cr_mag * cos_chi;
+    cr[1] = cr_mag * sin_chi * cos(eps);
+    cr[2] = cr_mag * sin_chi * sin(eps);
+    const double s1 = m2 / (m1 + m2), s2 = m1 / (m1 + m2);
+    for (int i = 0; i < 3; i++) {
+        v1[i] = cm[i] + cr[i] * s1;
+        v2[i] = cm[i] - cr[i] * s2;
+    }
+}
+
+int64_t eo_dsmc_mex(const eo_grid *g, double mass, double mpw0, double dt, const double c[4],
+                    double *sigma_cr_max, double *P, int64_t stride, int64_t n, const double *u, int64_t nu,
+                    int64_t *u_used, int64_t *cell_off) {
+    const int64_t n_cells = (int64_t)(g->ni - 1) * (g->nj - 1) * (g->nk - 1);
+    int64_t *start = (int64_t *)calloc((size_t)n_cells + 1, sizeof(int64_t));
+    int64_t *fill = (int64_t *)calloc((size_t)n_cells + 1, sizeof(int64_t));
+    int64_t *cellof = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    int64_t *list = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    /* the particles of each cell in particle order (parts_in_cell) */
+    for (int64_t p = 0; p < n; p++) {
+        const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        cellof[p] = dsmc_cell(g, x);
+        start[cellof[p] + 1]++;
+    }
+    for (int64_t cc = 0; cc < n_cells; cc++) start[cc + 1] += start[cc];
+    for (int64_t p = 0; p < n; p++) list[start[cellof[p]] + fill[cellof[p]]++] = p;
+    double sigma_cr_max_temp = 0;
+    const double dV = g->dh[0] * g->dh[1] * g->dh[2];
+    const double Fn = mpw0;
+    int64_t num_cols = 0, k = 0;
+#define DSMC_U() (k < nu ? u[k++] : (k++, -1.0))
+    for (int64_t cc = 0; cc < n_cells; cc++) {
+        if (cell_off) cell_off[cc] = k;
+        const int64_t *parts = list + start[cc];
+        const int np = (int)(start[cc + 1] - start[cc]);
+        if (np < 2) continue;
+        const double ng_f = 0.5 * np * np * Fn * (*sigma_cr_max) * dt / dV;
+        const int ng = (int)(ng_f + 0.5);
+        for (int gg = 0; gg < ng; gg++) {
+            const int p1 = (int)(DSMC_U() * np);
+            int p2;
+            do {
+                p2 = (int)(DSMC_U() * np);
+            } while (p2 == p1 && k <= nu);
+            const int64_t a = parts[p1], b = parts[p2];
+            double cr_vec[3];
+            for (int d = 0; d < 3; d++) cr_vec[d] = P[(3 + d) * stride + a] - P[(3 + d) * stride + b];
+            const double cr = dsmc_mag(cr_vec);
+            /* DSMC_MEX::evalSigma, ch4/Collisions.h:64-67 */
+            const double sigma = EO_PI * c[0] * c[0] * pow(c[2] / (cr * cr), c[1] - 0.5) / c[3];
+            const double sigma_cr = sigma * cr;
+            if (sigma_cr > sigma_cr_max_temp) sigma_cr_max_temp = sigma_cr;
+            const double Pc = sigma_cr / (*sigma_cr_max);
+            if (Pc > DSMC_U()) {
+                num_cols++;
+                double v1[3], v2[3];
+                for (int d = 0; d < 3; d++) {
+                    v1[d] = P[(3 + d) * stride + a];
+                    v2[d] = P[(3 + d) * stride + b];
+                }
+                const double u_chi = DSMC_U(), u_eps = DSMC_U();
+                dsmc_collide(v1, v2, mass, mass, u_chi, u_eps);
+                for (int d = 0; d < 3; d++) {
+                    P[(3 + d) * stride + a] = v1[d];
+                    P[(3 + d) * stride + b] = v2[d];
+                }
+            }
+        }
+    }
+#undef DSMC_U
+    if (cell_off) cell_off[n_cells] = k;
+    if (num_cols) *sigma_cr_max = sigma_cr_max_temp;
+    free(start);
+    free(fill);
+    free(cellof);
+    free(list);
+    if (u_used) *u_used = k;
+    return k > nu ? -1 : num_cols;
+}
+
 int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double mass, double dt,
                        double mpw0, double v_drift, double den, double temp, int mode, double *rem,
                        const double *u, int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap) {

@@ -85,6 +85,19 @@ int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double
                        double mpw0, double v_drift, double den, double temp, int mode, double *rem,
                        const double *u, int64_t *u_used, double *P, int64_t stride, int64_t np0, int64_t cap);
 
+/* ---- collisions: DSMC_MEX, ch4/Collisions.h:51-75, ch4/Collisions.cpp:84-183 ----
+ * One DSMC_MEX::apply(dt) on one species (mass, specific weight mpw0) with the
+ * VHS parameters c[4] = {d_ref, omega, 2 K T_ref / m_r, Gamma(5/2 - omega)}:
+ * particles grouped by World::XtoC in particle order, NTC group counts from
+ * *sigma_cr_max, pairs, collision tests and post-collision angles drawn from
+ * u[0..nu) in the reference's rnd() order.  *sigma_cr_max becomes the largest
+ * sigma*cr tested when a collision happened.  cell_off (n_cells + 1 entries,
+ * optional) receives the index of each cell's first uniform.  Returns the
+ * number of collisions, -1 when the uniforms run out. */
+int64_t eo_dsmc_mex(const eo_grid *g, double mass, double mpw0, double dt, const double c[4],
+                    double *sigma_cr_max, double *P, int64_t stride, int64_t n, const double *u, int64_t nu,
+                    int64_t *u_used, int64_t *cell_off);
+
 /* ---- deposit --------------------------------------------------------- */
 void eo_deposit_fp64(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *acc);
 void eo_deposit_fixed(const eo_grid *g, const double *P, int64_t stride, int64_t n, double fx,

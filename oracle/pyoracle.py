@@ -71,6 +71,8 @@ def _sig(L):
     L.eo_inject_beam.restype = I64
     L.eo_inject_beam.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, C.c_int, PD, PD, PI64, PD, I64, I64,
                                  I64]
+    L.eo_dsmc_mex.restype = I64
+    L.eo_dsmc_mex.argtypes = [C.POINTER(Grid), D, D, D, PD, PD, PD, I64, I64, PD, I64, PI64, PI64]
     L.eo_inject_warm.restype = I64
     L.eo_inject_warm.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, PD, PI64, PD, I64, I64,
                                  I64]
@@ -237,6 +239,23 @@ def inject_beam(g, ef, charge, mass, dt, mpw0, v_drift, den, temp, mode, u, rem=
                              C.byref(used), pd(B), B.shape[1], 0, B.shape[1])
     assert m >= 0
     return np.ascontiguousarray(B[:, :m]), used.value
+
+
+def dsmc_mex(g, mass, mpw0, dt, c, sigma_cr_max, P, u):
+    """eo_dsmc_mex: one DSMC_MEX::apply on a copy of P with the uniforms u.
+    Returns (P after, sigma_cr_max after, collisions, uniforms used, the
+    per-cell offsets of the first uniform, n_cells + 1 entries)."""
+    P = np.array(P, dtype=np.float64, order="C", copy=True)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    smax = np.array([sigma_cr_max], dtype=np.float64)
+    ncell = (g.ni - 1) * (g.nj - 1) * (g.nk - 1)
+    off = np.zeros(ncell + 1, dtype=np.int64)
+    used = C.c_int64(0)
+    ncol = lib().eo_dsmc_mex(C.byref(g), mass, mpw0, dt, pd(c), pd(smax), pd(P), P.shape[1], P.shape[1], pd(u),
+                             u.size, C.byref(used), off.ctypes.data_as(PI64))
+    assert ncol >= 0, "uniforms ran out"
+    return P, float(smax[0]), int(ncol), used.value, off
 
 
 def deposit_fp64(g, P):

@@ -1,8 +1,9 @@
 /*
  * ch4_harness.cpp -- drives the reference's ch4 WarmBeamSource (drifting
- * isotropic thermal injector) through its public API for golden vectors.
+ * isotropic thermal injector) and DSMC_MEX (neutral-neutral collisions)
+ * through their public API for golden vectors.
  * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
- * oracle/build_ref.py.  Usage: ref_ch4 inject_warm <in.kv> <out.kv>
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc <in.kv> <out.kv>
  */
 #include <chrono>
 #include <cmath>
@@ -15,6 +16,7 @@
 #include "World.h"
 #include "Species.h"
 #include "Source.h"
+#include "Collisions.h"
 #undef protected
 
 int main(int argc, char **argv) {
@@ -31,6 +33,39 @@ int main(int argc, char **argv) {
     if (kv_has(in, "ef")) field3_in(world.ef, kv_get(in, "ef"), ni, nj, nk);
     const std::vector<double> &mq = kv_get(in, "sp0_mq");
     Species sp("sp0", mq[0], mq[1], mq[2], world);
+    if (op == "dsmc") {
+        /* DSMC_MEX::apply(dt) `steps` times on the given particles; the
+         * uniforms it drew are recorded by replaying the generator */
+        const std::vector<double> &P = kv_get(in, "sp0_P");
+        size_t n = P.size() / 7;
+        for (size_t p = 0; p < n; p++)
+            sp.particles.emplace_back(double3(P[p], P[n + p], P[2 * n + p]),
+                                      double3(P[3 * n + p], P[4 * n + p], P[5 * n + p]), 0.0, P[6 * n + p]);
+        DSMC_MEX dsmc(sp, world);
+        if (kv_has(in, "sigma_cr_max")) dsmc.sigma_cr_max = kv_s(in, "sigma_cr_max");
+        int steps = kv_has(in, "steps") ? (int)kv_s(in, "steps") : 1;
+        std::vector<double> us, smax;
+        for (int s = 0; s < steps; s++) {
+            Rnd before = rnd;
+            dsmc.apply(kv_s(in, "dt"));
+            for (long g = 0; g < 2000000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+            smax.push_back(dsmc.sigma_cr_max);
+        }
+        std::vector<double> v(7 * n);
+        for (size_t p = 0; p < n; p++) {
+            for (int d = 0; d < 3; d++) {
+                v[d * n + p] = sp.particles[p].pos[d];
+                v[(3 + d) * n + p] = sp.particles[p].vel[d];
+            }
+            v[6 * n + p] = sp.particles[p].mpw;
+        }
+        out["u"] = us;
+        out["sigma_cr_max"] = smax;
+        out["c"] = std::vector<double>(dsmc.c, dsmc.c + 4);
+        out["sp0_P"] = v;
+        kv_write(argv[3], out);
+        return 0;
+    }
     if (op != "inject_warm") { fprintf(stderr, "unknown op\n"); return 1; }
     const std::vector<double> &src = kv_get(in, "source"); /* v_drift den T */
     WarmBeamSource source(sp, world, src[0], src[1], src[2]);

@@ -114,6 +114,9 @@ def lib():
             "espic_solve": [VP, PI, PI, PD],
             "espic_efield": [VP],
             "espic_species_diag": [VP, C.c_int, PD],
+            "espic_dsmc_enable": [VP, C.c_int, PD, C.c_double],
+            "espic_dsmc_apply": [VP, C.c_int, C.c_double, PD, I64, C.POINTER(C.c_int64)],
+            "espic_dsmc_status": [VP, C.c_int, PD, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
             "espic_potential_energy": [VP, PD],
             "espic_diag_row": [VP, PD, C.c_int],
             "espic_update_average": [VP, C.c_int],
@@ -415,6 +418,31 @@ class Species:
         out = np.zeros(5)
         check(lib().espic_species_diag(self.world.h, self.id, _pd(out)))
         return out
+
+    # DSMC_MEX, ch4/Collisions.h:51-75 (float64 form)
+    def enable_dsmc(self, c=None, sigma_cr_max=1e-14):
+        """Neutral-neutral collisions of this species (the reference's VHS
+        parameters when c is None)."""
+        cc = None if c is None else np.ascontiguousarray(c, dtype=np.float64)
+        check(lib().espic_dsmc_enable(self.world.h, self.id, None if cc is None else _pd(cc), sigma_cr_max))
+
+    def dsmc(self, dt, u=None, cell_off=None):
+        """DSMC_MEX::apply(dt); with u and cell_off the uniforms are replayed
+        (cell c starts at u[cell_off[c]])."""
+        if u is None:
+            check(lib().espic_dsmc_apply(self.world.h, self.id, dt, None, 0, None))
+            return
+        uu = np.ascontiguousarray(u, dtype=np.float64)
+        off = np.ascontiguousarray(cell_off, dtype=np.int64)
+        check(lib().espic_dsmc_apply(self.world.h, self.id, dt, _pd(uu), uu.size,
+                                     off.ctypes.data_as(C.POINTER(C.c_int64))))
+
+    def dsmc_status(self):
+        """(sigma_cr_max, collisions of the last call, collisions of all calls)"""
+        smax = C.c_double()
+        last, total = C.c_int64(), C.c_int64()
+        check(lib().espic_dsmc_status(self.world.h, self.id, C.byref(smax), C.byref(last), C.byref(total)))
+        return smax.value, last.value, total.value
 
     def updateAverages(self):
         check(lib().espic_update_average(self.world.h, self.id))

@@ -89,6 +89,8 @@ static int take_device_errors(World &w) {
     if (bits & DERR_FIXED_RANGE) return fail(ESPIC_ERR_FIXED, "weight outside the fixed-point range");
     if (bits & DERR_TIMEOUT) return fail(ESPIC_ERR_CUDA, "a bounded wait on a bulk copy timed out");
     if (bits & DERR_SORT) return fail(ESPIC_ERR_CUDA, "the cell sort lost track of a particle");
+    if (bits & DERR_DSMC)
+        return fail(ESPIC_ERR_ARG, "DSMC: a particle outside the domain, or the replayed uniforms ran out");
     return ESPIC_OK;
 }
 
@@ -144,7 +146,8 @@ struct PhaseScope {
 static void free_species(Species *s) {
     if (!s) return;
     void *ptrs[] = {s->P, s->cell, s->cell2, s->off, s->off2, s->vel, s->vel2, s->sort_count, s->deadmask,
-                    s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave};
+                    s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
+                    s->dsmc_cell, s->dsmc_perm, s->dsmc_count, s->dsmc_cursor, s->dsmc_bsum};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -941,6 +944,86 @@ extern "C" int espic_efield(espic_world *h) {
 }
 
 /* ---------------------------------------------------------------- diagnostics */
+/* ---------------------------------------------------------------- DSMC_MEX */
+extern "C" int espic_dsmc_enable(espic_world *h, int sp, const double *c, double sigma_cr_max) {
+    WORLD(h);
+    SPECIES(sp);
+    if (s.form != 0) return fail(ESPIC_ERR_ARG, "DSMC works on a species in the float64 form");
+    if (!(sigma_cr_max > 0)) return fail(ESPIC_ERR_ARG, "sigma_cr_max must be positive");
+    if (c) {
+        for (int d = 0; d < 4; d++) s.dsmc_c[d] = c[d];
+    } else {
+        /* the reference's constructor, ch4/Collisions.h:53-60 (Bird's VHS
+         * parameters at 273.15 K; m_r of a like pair) */
+        const double K = 1.380648e-23;
+        const double mr = s.mass * s.mass / (s.mass + s.mass);
+        s.dsmc_c[0] = 4.07e-10;
+        s.dsmc_c[1] = 0.77;
+        s.dsmc_c[2] = 2 * K * 273.15 / mr;
+        s.dsmc_c[3] = tgamma(2.5 - s.dsmc_c[1]);
+    }
+    const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    if (!s.dsmc_on) {
+        if (dalloc(&s.d_dsmc, 4) != ESPIC_OK || dalloc(&s.dsmc_cell, s.cap) != ESPIC_OK ||
+            dalloc(&s.dsmc_perm, s.cap) != ESPIC_OK || dalloc(&s.dsmc_count, n_cells + 1) != ESPIC_OK ||
+            dalloc(&s.dsmc_cursor, n_cells + 1) != ESPIC_OK ||
+            dalloc(&s.dsmc_bsum, int_scan_blocks(n_cells) + 1) != ESPIC_OK)
+            return ESPIC_ERR_CUDA;
+        s.dsmc_on = true;
+    }
+    unsigned long long st[4] = {0, 0, 0, 0};
+    memcpy(&st[0], &sigma_cr_max, sizeof(double));
+    CK(cudaMemcpyAsync(s.d_dsmc, st, sizeof st, cudaMemcpyHostToDevice, w.stream));
+    CK(cudaStreamSynchronize(w.stream));
+    return ESPIC_OK;
+}
+
+extern "C" int espic_dsmc_apply(espic_world *h, int sp, double dt, const double *u, int64_t nu,
+                                const int64_t *cell_off) {
+    WORLD(h);
+    SPECIES(sp);
+    if (!s.dsmc_on) return fail(ESPIC_ERR_ARG, "DSMC not enabled on species %d", sp);
+    if (!(dt > 0)) return fail(ESPIC_ERR_ARG, "bad time step");
+    if (!u) {
+        launch_dsmc(w, s, dt, nullptr, 0, nullptr);
+        CHECK_LAUNCH();
+        return ESPIC_OK;
+    }
+    /* replayed uniforms (parity checks): staged for this call */
+    if (!cell_off || nu < 0) return fail(ESPIC_ERR_ARG, "replayed uniforms need their cell offsets");
+    const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    double *du = nullptr;
+    int64_t *doff = nullptr;
+    if (dalloc(&du, nu) != ESPIC_OK) return ESPIC_ERR_CUDA;
+    if (dalloc(&doff, n_cells + 1) != ESPIC_OK) {
+        cudaFree(du);
+        return ESPIC_ERR_CUDA;
+    }
+    cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+    cudaMemcpyAsync(doff, cell_off, (n_cells + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, w.stream);
+    launch_dsmc(w, s, dt, du, nu, doff);
+    cudaError_t e = cudaStreamSynchronize(w.stream);
+    cudaFree(du);
+    cudaFree(doff);
+    if (e != cudaSuccess) return fail(ESPIC_ERR_CUDA, "%s", cudaGetErrorString(e));
+    CHECK_LAUNCH();
+    return take_device_errors(w);
+}
+
+extern "C" int espic_dsmc_status(espic_world *h, int sp, double *sigma_cr_max, int64_t *collisions_last,
+                                 int64_t *collisions_total) {
+    WORLD(h);
+    SPECIES(sp);
+    if (!s.dsmc_on) return fail(ESPIC_ERR_ARG, "DSMC not enabled on species %d", sp);
+    unsigned long long st[4];
+    CK(cudaMemcpyAsync(st, s.d_dsmc, sizeof st, cudaMemcpyDeviceToHost, w.stream));
+    CK(cudaStreamSynchronize(w.stream));
+    if (sigma_cr_max) memcpy(sigma_cr_max, &st[0], sizeof(double));
+    if (collisions_last) *collisions_last = (int64_t)st[2];
+    if (collisions_total) *collisions_total = (int64_t)st[3];
+    return take_device_errors(w);
+}
+
 extern "C" int espic_species_diag(espic_world *h, int sp, double out[5]) {
     WORLD(h);
     SPECIES(sp);

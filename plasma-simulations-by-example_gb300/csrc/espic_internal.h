@@ -28,7 +28,8 @@ enum : int {
     DERR_NONFINITE = 2,  /* NaN / Inf met in a solve */
     DERR_FIXED_RANGE = 4, /* a weight too large for the fixed-point scale */
     DERR_TIMEOUT = 8,     /* a bounded wait on an asynchronous copy ran out */
-    DERR_SORT = 16        /* a sort slot named no particle of the species */
+    DERR_SORT = 16,       /* a sort slot named no particle of the species */
+    DERR_DSMC = 32        /* a collision partner outside the domain, or replayed uniforms ran out */
 };
 
 struct Geo {
@@ -122,6 +123,9 @@ void launch_push_fp64(World &w, Species &s, bool deposit);
 void launch_deposit_fp64(World &w, Species &s);
 void launch_compact(World &w, Species &s);
 void launch_density(World &w, Species &s);
+void launch_int_excl_scan(cudaStream_t st, int32_t *x, int64_t n, int32_t *bsum);
+int64_t int_scan_blocks(int64_t n);
+void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu, const int64_t *d_cell_off);
 void launch_inv_vol(World &w);
 void launch_charge(World &w);
 void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3,

@@ -43,6 +43,14 @@ struct Species {
     double unit = 1.0;    /* real particles per accumulator count: 1/fx or mpw0*2^-24 */
     double weight_bound = 0;
     bool deposit_valid = false;
+    /* DSMC_MEX collisions (float64 form) */
+    bool dsmc_on = false;
+    double dsmc_c[4] = {0, 0, 0, 0}; /* VHS: d_ref, omega, 2 K T_ref / m_r, Gamma(5/2 - omega) */
+    uint64_t dsmc_calls = 0;
+    unsigned long long *d_dsmc = nullptr; /* [0] sigma_cr_max (bits), [1] largest sigma*cr of the call
+                                             (bits), [2] collisions of the call, [3] all collisions */
+    int32_t *dsmc_cell = nullptr, *dsmc_perm = nullptr;                       /* [cap] */
+    int32_t *dsmc_count = nullptr, *dsmc_cursor = nullptr, *dsmc_bsum = nullptr; /* [ncells + 1], scan */
 };
 
 struct Source {

@@ -1370,6 +1370,204 @@ void launch_diag(World &w, Species &s, double *d_out5) {
     w.nlaunch += 2;
 }
 
+/* ------------------------------------------------------------------------ */
+/* DSMC_MEX (ch4/Collisions.h:51-75, ch4/Collisions.cpp:84-183): neutral-
+ * neutral collisions by Bird's no-time-counter scheme with the variable-
+ * hard-sphere cross-section, in the float64 form.  Particles are grouped by
+ * World::XtoC (ch4/World.h:79-98); each cell's list is put in particle order
+ * (parts_in_cell) and worked by one thread, drawing its uniforms in the
+ * reference's rnd() order: from a counter-based stream keyed by (call, cell),
+ * or, for parity checks, from the caller's array at the cell's offset.
+ * Every operation keeps the reference's operand order (unit built with
+ * -fmad=false). */
+struct DsmcArgs {
+    Geo g;
+    double mass, Fn, dt, dV, c[4];
+    int64_t n_cells;
+    const int32_t *count, *cursor; /* cursor: one past each cell's last slot */
+    int32_t *perm;
+    double *P;
+    int64_t stride;
+    unsigned long long *state;
+    const double *u;
+    int64_t nu;
+    const int64_t *cell_off;
+    uint64_t seed, stream;
+    int *err;
+};
+
+__global__ void k_dsmc_cells(Geo g, const double *__restrict__ P, int64_t stride, const int64_t *__restrict__ d_count,
+                             int64_t n_cells, int32_t *cell, int32_t *count, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    int ijk[3];
+    for (int d = 0; d < 3; d++) ijk[d] = (int)((P[d * stride + p] - g.x0[d]) / g.dh[d]);
+    const int64_t c = (int64_t)ijk[2] * (g.nj - 1) * (g.ni - 1) + (int64_t)ijk[1] * (g.ni - 1) + ijk[0];
+    const bool in = ijk[0] >= 0 && ijk[1] >= 0 && ijk[2] >= 0 && ijk[0] < g.ni - 1 && ijk[1] < g.nj - 1 &&
+                    ijk[2] < g.nk - 1 && c < n_cells;
+    if (!in) {
+        atomicOr(err, DERR_DSMC);
+        cell[p] = -1;
+        return;
+    }
+    cell[p] = (int32_t)c;
+    atomicAdd(count + c, 1);
+}
+
+__global__ void k_dsmc_scatter(const int32_t *__restrict__ cell, const int64_t *__restrict__ d_count, int32_t *cursor,
+                               int32_t *perm) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    const int32_t c = cell[p];
+    if (c < 0) return;
+    perm[atomicAdd(cursor + c, 1)] = (int32_t)p;
+}
+
+__global__ void k_dsmc_begin(unsigned long long *state) {
+    state[1] = 0ull;
+    state[2] = 0ull;
+}
+
+/* sqrt of ((0 + x x) + y y) + z z, vec3 mag of ch4/Field.h:21-26 */
+__device__ __forceinline__ double dsmc_mag(double x, double y, double z) {
+    double s = 0;
+    s += x * x;
+    s += y * y;
+    s += z * z;
+    return sqrt(s);
+}
+
+__global__ void __launch_bounds__(128) k_dsmc_collide(DsmcArgs a) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    const int np = a.count[c];
+    if (np < 2) return;
+    int32_t *parts = a.perm + (a.cursor[c] - np);
+    /* the cell's particles in particle order */
+    for (int i = 1; i < np; i++) {
+        const int32_t v = parts[i];
+        int j = i - 1;
+        while (j >= 0 && parts[j] > v) {
+            parts[j + 1] = parts[j];
+            j--;
+        }
+        parts[j + 1] = v;
+    }
+    const double smax = __longlong_as_double((long long)a.state[0]);
+    const double ng_f = 0.5 * np * np * a.Fn * smax * a.dt / a.dV;
+    const int ng = (int)(ng_f + 0.5);
+    const double *u = a.u ? a.u + a.cell_off[c] : nullptr;
+    const int64_t ulim = a.u ? a.nu - a.cell_off[c] : 0;
+    int64_t k = 0;
+    bool short_u = false;
+    auto U = [&]() -> double {
+        if (u) {
+            if (k >= ulim) {
+                short_u = true;
+                return 0.5;
+            }
+            return u[k++];
+        }
+        return philox_uniform(a.seed, a.stream, ((uint64_t)c << 32) + (uint64_t)(k++));
+    };
+    double local_max = 0;
+    unsigned long long cols = 0;
+    double *V = a.P + 3 * a.stride;
+    for (int gg = 0; gg < ng && !short_u; gg++) {
+        const int p1 = (int)(U() * np);
+        int p2;
+        do {
+            p2 = (int)(U() * np);
+        } while (p2 == p1 && !short_u);
+        if (short_u) break;
+        const int64_t i1 = parts[p1], i2 = parts[p2];
+        const double cr = dsmc_mag(V[i1] - V[i2], V[a.stride + i1] - V[a.stride + i2],
+                                   V[2 * a.stride + i1] - V[2 * a.stride + i2]);
+        /* DSMC_MEX::evalSigma, ch4/Collisions.h:64-67 */
+        const double sigma = REF_PI * a.c[0] * a.c[0] * pow(a.c[2] / (cr * cr), a.c[1] - 0.5) / a.c[3];
+        const double sigma_cr = sigma * cr;
+        if (sigma_cr > local_max) local_max = sigma_cr;
+        const double Pc = sigma_cr / smax;
+        if (Pc > U()) {
+            const double u_chi = U(), u_eps = U();
+            if (short_u) break;
+            cols++;
+            /* DSMC_MEX::collide, ch4/Collisions.cpp:84-105 */
+            const double m1 = a.mass, m2 = a.mass;
+            double v1[3], v2[3], cm[3], crv[3];
+            for (int d = 0; d < 3; d++) {
+                v1[d] = V[d * a.stride + i1];
+                v2[d] = V[d * a.stride + i2];
+            }
+            for (int d = 0; d < 3; d++) cm[d] = (v1[d] * m1 + v2[d] * m2) / (m1 + m2);
+            for (int d = 0; d < 3; d++) crv[d] = v1[d] - v2[d];
+            const double cr_mag = dsmc_mag(crv[0], crv[1], crv[2]);
+            const double cos_chi = 2 * u_chi - 1;
+            const double sin_chi = sqrt(1 - cos_chi * cos_chi);
+            const double eps = 2 * REF_PI * u_eps;
+            crv[0] = cr_mag * cos_chi;
+            crv[1] = cr_mag * sin_chi * cos(eps);
+            crv[2] = cr_mag * sin_chi * sin(eps);
+            const double s1 = m2 / (m1 + m2), s2 = m1 / (m1 + m2);
+            for (int d = 0; d < 3; d++) {
+                V[d * a.stride + i1] = cm[d] + crv[d] * s1;
+                V[d * a.stride + i2] = cm[d] - crv[d] * s2;
+            }
+        }
+    }
+    if (short_u) atomicOr(a.err, DERR_DSMC);
+    /* sigma*cr >= 0: the order of the bit patterns is the order of the values */
+    if (local_max > 0) atomicMax(a.state + 1, (unsigned long long)__double_as_longlong(local_max));
+    if (cols) atomicAdd(a.state + 2, cols);
+}
+
+/* sigma_cr_max takes the call's largest sigma*cr when a collision happened */
+__global__ void k_dsmc_finish(unsigned long long *state) {
+    if (state[2]) state[0] = state[1];
+    state[3] += state[2];
+}
+
+void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu, const int64_t *d_cell_off) {
+    const int64_t n = s.host_bound;
+    const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    cudaMemsetAsync(s.dsmc_count, 0, (n_cells + 1) * sizeof(int32_t), w.stream);
+    if (n > 0)
+        k_dsmc_cells<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, n_cells, s.dsmc_cell,
+                                                                s.dsmc_count, w.d_err);
+    cudaMemcpyAsync(s.dsmc_cursor, s.dsmc_count, (n_cells + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                    w.stream);
+    launch_int_excl_scan(w.stream, s.dsmc_cursor, n_cells, s.dsmc_bsum);
+    if (n > 0)
+        k_dsmc_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.dsmc_cell, s.d_count, s.dsmc_cursor,
+                                                                  s.dsmc_perm);
+    k_dsmc_begin<<<1, 1, 0, w.stream>>>(s.d_dsmc);
+    DsmcArgs a;
+    a.g = w.g;
+    a.mass = s.mass;
+    a.Fn = s.mpw0;
+    a.dt = dt;
+    a.dV = w.g.dh[0] * w.g.dh[1] * w.g.dh[2];
+    for (int d = 0; d < 4; d++) a.c[d] = s.dsmc_c[d];
+    a.n_cells = n_cells;
+    a.count = s.dsmc_count;
+    a.cursor = s.dsmc_cursor;
+    a.perm = s.dsmc_perm;
+    a.P = s.P;
+    a.stride = s.cap;
+    a.state = s.d_dsmc;
+    a.u = d_u;
+    a.nu = nu;
+    a.cell_off = d_cell_off;
+    a.seed = w.seed;
+    /* one stream per (species, call); cell c draws index (c << 32) + k */
+    a.stream = (0xD5ull << 56) | ((uint64_t)(s.id & 0xff) << 48) | (s.dsmc_calls & 0xffffffffffffull);
+    a.err = w.d_err;
+    k_dsmc_collide<<<blocks_for(n_cells, 128), 128, 0, w.stream>>>(a);
+    k_dsmc_finish<<<1, 1, 0, w.stream>>>(s.d_dsmc);
+    w.nlaunch += 6 + 3;
+    s.dsmc_calls++;
+}
+
 void launch_pe(World &w, double *d_out1) {
     k_pe_partials<<<RED_BLOCKS, RED_THREADS, 0, w.stream>>>(w.nn, w.ef, w.vol, w.d_partials);
     k_pe_final<<<1, 32, 0, w.stream>>>(w.d_partials, d_out1);

@@ -713,6 +713,17 @@ void launch_sort_mixed(World &w, Species &s) {
     s.vel2 = tv;
 }
 
+/* exclusive prefix sum of x[0..n) in place (bsum: int_scan_blocks(n) entries) */
+int64_t int_scan_blocks(int64_t n) { return (n + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK; }
+
+void launch_int_excl_scan(cudaStream_t st, int32_t *x, int64_t n, int32_t *bsum) {
+    const int64_t nb = int_scan_blocks(n);
+    if (nb <= 0) return;
+    k_scan_reduce<<<(unsigned)nb, 1024, 0, st>>>(x, n, bsum);
+    k_scan_bsum<<<1, 1024, 0, st>>>(bsum, nb);
+    k_scan_down<<<(unsigned)nb, 1024, 0, st>>>(x, n, bsum);
+}
+
 void launch_diag_mixed(World &w, Species &s, double *d_out5) {
     const int nb = 592;
     k_diag_mixed<<<nb, 256, 0, w.stream>>>(s.vel, s.ms, s.d_count, w.d_partials, nb);

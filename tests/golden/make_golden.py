@@ -3,7 +3,7 @@ CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
 Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py [base] [steady]
+    python tests/golden/make_golden.py [base] [steady] [dsmc]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -210,6 +210,25 @@ def sphere_cases(rng):
          mpw0=5e2)
 
 
+def dsmc_cases():
+    """Three DSMC_MEX::apply calls (ch4/Collisions.cpp:108-183) on 3000 oxygen
+    atoms in 125 cells: a 7 km/s beam with anisotropic thermal spread, specific
+    weight 1e14, the reference's starting sigma_cr_max (1e-14)."""
+    geo = dict(grid=[6, 6, 6], x0=[0.0, 0.0, 0.0], xm=[0.05, 0.05, 0.05])
+    rng = np.random.default_rng(20261204)
+    n, mass, mpw0, dt = 3000, 16 * AMU, 1e14, 1e-7
+    P = np.zeros((7, n))
+    P[0:3] = rng.random((3, n)) * 0.05 * 0.999999
+    P[3] = 7000 + 300 * rng.standard_normal(n)
+    P[4] = 300 * rng.standard_normal(n)
+    P[5] = 150 * rng.standard_normal(n)
+    P[6] = mpw0
+    o = po.run_reference("ref_ch4", "dsmc", base_inputs(geo, dt, seed=[77], sp0_mq=[mass, 0.0, mpw0],
+                                                        sp0_P=P.ravel(), steps=[3]))
+    save("dsmc_steps", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, mpw0=mpw0, dt=dt, P0=P,
+         P=o["sp0_P"].reshape(7, -1), u=o["u"], sigma_cr_max=o["sigma_cr_max"], c=o["c"])
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -246,8 +265,8 @@ def steady_cases():
 
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
-    # stream), "steady" (default: both)
-    cases = sys.argv[1:] or ["base", "steady"]
+    # stream), "steady", "dsmc" (default: all)
+    cases = sys.argv[1:] or ["base", "steady", "dsmc"]
     build_ref.build_reference()
     if "base" in cases:
         rng = np.random.default_rng(20261203)
@@ -255,3 +274,5 @@ if __name__ == "__main__":
         sphere_cases(rng)
     if "steady" in cases:
         steady_cases()
+    if "dsmc" in cases:
+        dsmc_cases()

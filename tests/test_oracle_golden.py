@@ -253,3 +253,20 @@ def test_sphere_main_loop_bitexact(po):
         assert np.array_equal(np.array(row), f["hist"][st]), st
     assert np.array_equal(phi, f["phi"])
     assert np.array_equal(P, f["P"])
+
+
+def test_dsmc_bitexact(po):
+    """Three DSMC_MEX::apply calls of the reference (ch4/Collisions.cpp:
+    108-183), replayed with its recorded uniforms: velocities, sigma_cr_max
+    and the uniform count reproduced bit for bit."""
+    f = golden("dsmc_steps")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    P, smax, off = f["P0"], 1e-14, 0
+    for st in range(3):
+        P, smax, ncol, used, _ = po.dsmc_mex(g, float(f["mass"]), float(f["mpw0"]), float(f["dt"]), f["c"], smax,
+                                             P, f["u"][off:])
+        off += used
+        assert ncol > 0
+        assert smax == f["sigma_cr_max"][st], st
+    assert off == f["u"].size
+    assert np.array_equal(P, f["P"])
