@@ -55,6 +55,11 @@ CONFIGS = {
                   sort_every=0),
     # batched ensemble: 512 ch2 boxes with drawn sizes, counts and densities
     "ensemble512": dict(nbox=512, x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.2), dt=2e-10, seed=2024),
+    # ch4 neutral gas (ch4/Main.cpp:21-58): O atoms at 2e20 m^-3, 1000 K,
+    # 7 km/s along z, mpw0 1e12 on a 41x21x41-node box; a step is one
+    # DSMC_MEX::apply (Bird's NTC pairs, VHS cross-section) over all atoms
+    "dsmc41": dict(n=(41, 21, 41), x0=(-0.2, -0.1, 0.0), xm=(0.2, 0.1, 0.4), nda=2e20, temp=1000.0, mpw0=1e12,
+                   dt=1e-7),
     # differentiable sphere run: gradients by the adjoint kernels
     "diff32": dict(n=(32, 32, 64), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.3), center=(0, 0, 0.15), radius=0.05,
                    phi_s=-100.0, np=500_000, dt=1e-7, steps=400, checkpoint=20, wake=(0.2, 0.3)),
@@ -657,6 +662,100 @@ def run_diff(args, E, torch):
     print(json.dumps(line))
 
 
+def run_dsmc(args, E, torch):
+    """DSMC_MEX::apply (ch4/Collisions.cpp:108-183) over the ch4 neutral gas:
+    6.4M O atoms in 32,000 cells (about 200 per cell) with the counter-based
+    stream, timed with CUDA events on the library's stream; the L2 is
+    flushed between timed calls.  The CPU baseline is the oracle's
+    restatement of the same call on the same atoms (one thread)."""
+    cfg = CONFIGS["dsmc41"]
+    x0, xm = np.array(cfg["x0"]), np.array(cfg["xm"])
+    n = int(round(cfg["nda"] * np.prod(xm - x0) / cfg["mpw0"]))
+    mass, dt = 16 * AMU, cfg["dt"]
+    w = E.World(*cfg["n"], cfg["x0"], cfg["xm"])
+    w.set_seed(7)
+    w.setTime(dt, 1 << 30)
+    s = E.Species(w, "O", mass, 0.0, mpw0=cfg["mpw0"], capacity=n + 1024, form=E.FORM_FP64)
+    s.loadParticlesBoxThermal(cfg["x0"], cfg["xm"], 0.0, n, (0.0, 0.0, V_DRIFT), cfg["temp"])
+    s.enable_dsmc()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(w.stream_handle())
+    for _ in range(max(args.warmup, 3)):
+        s.dsmc(dt)
+    w.sync()
+    smax_w, _, tot0 = s.dsmc_status()
+    l0 = w.launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = Clocks()
+    clocks.start()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[i][0].record(stream)
+        s.dsmc(dt)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    launches = w.launches() - l0
+    smax, _, tot1 = s.dsmc_status()
+    # e2e: the call through the C-ABI plus the read of its status
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.dsmc(dt)
+        s.dsmc_status()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    P = s.particles()
+    w.close()
+    # CPU: the oracle on the same atoms, starting from the warmed-up sigma_cr_max
+    from oracle import pyoracle as po
+    g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
+    ijk = ((P[0:3] - x0[:, None]) / ((xm - x0) / (np.array(cfg["n"]) - 1))[:, None]).astype(np.int64)
+    ci, cj = cfg["n"][0] - 1, cfg["n"][1] - 1
+    cnt = np.bincount(ijk[2] * cj * ci + ijk[1] * ci + ijk[0], minlength=ci * cj * (cfg["n"][2] - 1))
+    dV = np.prod((xm - x0) / (np.array(cfg["n"]) - 1))
+    # uniforms for two calls with room for sigma_cr_max to grow fourfold
+    ng = np.floor(0.5 * cnt * cnt * cfg["mpw0"] * (4 * smax) * dt / dV + 0.5)
+    u = np.random.default_rng(3).random(int(8 * ng.sum()) + 100_000)
+    cpu_t, sm = [], smax
+    for _ in range(2):
+        t0 = time.perf_counter()
+        P, sm, _, used, _ = po.dsmc_mex(g, mass, cfg["mpw0"], dt, po_c(mass), sm, P, u)
+        cpu_t.append(time.perf_counter() - t0)
+        assert used <= u.size
+    hbm, peak_kind = peaks()
+    alg = 40.0 * n
+    achieved = alg / (ms * 1e-3) / 1e9
+    line = {"metric": "DSMC_MEX particle-calls/s (ch4 neutral gas)", "value": n / (ms * 1e-3),
+            "unit": "particle-calls/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "dsmc41", "grid": list(cfg["n"]), "particles": n, "cells": int(cnt.size),
+                       "density": cfg["nda"], "temp_K": cfg["temp"], "mpw0": cfg["mpw0"], "dt": dt,
+                       "l2": "flushed between timed calls (256 MB write, outside the events)"},
+            "collisions_per_call": (tot1 - tot0) / args.steps, "sigma_cr_max": smax,
+            "e2e": {"value": n / e2e_s, "unit": "particle-calls/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 24},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "one DSMC call (k_dsmc_cells, scan, k_dsmc_scatter, "
+                         "k_dsmc_collide)", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": alg, "bytes_per_particle": 40},
+            "clocks": ck,
+            "cpu_baseline": {"value": n / float(np.mean(cpu_t)), "unit": "particle-calls/s", "cores": 1,
+                             "kind": "port", "sample": "2 calls of the oracle's DSMC_MEX over all %d atoms" % n}}
+    print(json.dumps(line))
+
+
+def po_c(mass):
+    """DSMC_MEX's VHS parameters for one species (ch4/Collisions.h:53-60)"""
+    import math
+    mr = mass * mass / (mass + mass)
+    return np.array([4.07e-10, 0.77, 2 * K * 273.15 / mr, math.gamma(2.5 - 0.77)])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -700,6 +799,9 @@ def main():
         return
     if args.config == "diff32":
         run_diff(args, E, torch)
+        return
+    if args.config == "dsmc41":
+        run_dsmc(args, E, torch)
         return
     if args.config == "ensemble512":
         run_ensemble(args, E, torch, dist, rank, world_size)

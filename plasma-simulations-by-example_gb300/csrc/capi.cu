@@ -147,7 +147,7 @@ static void free_species(Species *s) {
     if (!s) return;
     void *ptrs[] = {s->P, s->cell, s->cell2, s->off, s->off2, s->vel, s->vel2, s->sort_count, s->deadmask,
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
-                    s->dsmc_cell, s->dsmc_perm, s->dsmc_count, s->dsmc_cursor, s->dsmc_bsum};
+                    s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -965,8 +965,8 @@ extern "C" int espic_dsmc_enable(espic_world *h, int sp, const double *c, double
     const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
     if (!s.dsmc_on) {
         if (dalloc(&s.d_dsmc, 4) != ESPIC_OK || dalloc(&s.dsmc_cell, s.cap) != ESPIC_OK ||
-            dalloc(&s.dsmc_perm, s.cap) != ESPIC_OK || dalloc(&s.dsmc_count, n_cells + 1) != ESPIC_OK ||
-            dalloc(&s.dsmc_cursor, n_cells + 1) != ESPIC_OK ||
+            dalloc(&s.dsmc_rank, s.cap) != ESPIC_OK || dalloc(&s.dsmc_perm, s.cap) != ESPIC_OK ||
+            dalloc(&s.dsmc_count, n_cells + 1) != ESPIC_OK || dalloc(&s.dsmc_start, n_cells + 1) != ESPIC_OK ||
             dalloc(&s.dsmc_bsum, int_scan_blocks(n_cells) + 1) != ESPIC_OK)
             return ESPIC_ERR_CUDA;
         s.dsmc_on = true;

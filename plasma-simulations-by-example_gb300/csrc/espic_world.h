@@ -49,8 +49,8 @@ struct Species {
     uint64_t dsmc_calls = 0;
     unsigned long long *d_dsmc = nullptr; /* [0] sigma_cr_max (bits), [1] largest sigma*cr of the call
                                              (bits), [2] collisions of the call, [3] all collisions */
-    int32_t *dsmc_cell = nullptr, *dsmc_perm = nullptr;                       /* [cap] */
-    int32_t *dsmc_count = nullptr, *dsmc_cursor = nullptr, *dsmc_bsum = nullptr; /* [ncells + 1], scan */
+    int32_t *dsmc_cell = nullptr, *dsmc_rank = nullptr, *dsmc_perm = nullptr; /* [cap] */
+    int32_t *dsmc_count = nullptr, *dsmc_start = nullptr, *dsmc_bsum = nullptr; /* [ncells + 1], scan */
 };
 
 struct Source {

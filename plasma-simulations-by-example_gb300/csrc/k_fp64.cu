@@ -17,6 +17,7 @@
  *   solveQN          ch3/ver2/PotentialSolver.cpp:204-222 k_qn
  */
 #include <cooperative_groups.h>
+#include <limits.h>
 #include <stdio.h>
 
 #include "espic_world.h"
@@ -1374,18 +1375,20 @@ void launch_diag(World &w, Species &s, double *d_out5) {
 /* DSMC_MEX (ch4/Collisions.h:51-75, ch4/Collisions.cpp:84-183): neutral-
  * neutral collisions by Bird's no-time-counter scheme with the variable-
  * hard-sphere cross-section, in the float64 form.  Particles are grouped by
- * World::XtoC (ch4/World.h:79-98); each cell's list is put in particle order
- * (parts_in_cell) and worked by one thread, drawing its uniforms in the
- * reference's rnd() order: from a counter-based stream keyed by (call, cell),
- * or, for parity checks, from the caller's array at the cell's offset.
+ * World::XtoC (ch4/World.h:79-98) with a counting sort (cell and arrival slot
+ * per atom, a scan of the cell counts, a scatter); one warp per cell then
+ * puts the cell's list in particle order (parts_in_cell) with a bitonic
+ * network, and one thread per cell works the pairs, drawing its uniforms in
+ * the reference's rnd() order: from a counter-based stream keyed by (call,
+ * cell), or, for parity checks, from the caller's array at the cell's offset.
  * Every operation keeps the reference's operand order (unit built with
  * -fmad=false). */
 struct DsmcArgs {
     Geo g;
     double mass, Fn, dt, dV, c[4];
     int64_t n_cells;
-    const int32_t *count, *cursor; /* cursor: one past each cell's last slot */
-    int32_t *perm;
+    const int32_t *count, *start;
+    const int32_t *perm;
     double *P;
     int64_t stride;
     unsigned long long *state;
@@ -1396,31 +1399,151 @@ struct DsmcArgs {
     int *err;
 };
 
-__global__ void k_dsmc_cells(Geo g, const double *__restrict__ P, int64_t stride, const int64_t *__restrict__ d_count,
-                             int64_t n_cells, int32_t *cell, int32_t *count, int *err) {
+/* World::XtoIJK (ch4/World.h:79-92) along one axis without a float64
+ * division: x is cut to a float (24 leading bits, by integer operations so
+ * that nothing queues on the narrow float64 pipe), q = (x_f - x0_f) / dh in
+ * float, and q's integer part is the reference's (int)((x - x0) / dh)
+ * whenever q lies farther than tol from an integer; tol bounds the error of
+ * the float estimate (host side, dsmc_axis).  Anything else (near a cell
+ * face, outside the grid, huge or not finite) takes the float64 division. */
+struct DsmcAxis {
+    float x0f, invf, tol;
+    int nc;
+};
+
+__device__ __forceinline__ int dsmc_coord(double x, double x0, double dh, DsmcAxis ax) {
+    const int hi = __double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const int fe = ((hi >> 20) & 0x7ff) - 896; /* float exponent field */
+    float xf = 0.0f;                            /* |x| < 2^-126: zero */
+    if (fe >= 1) xf = __int_as_float((hi & (int)0x80000000) | (fe << 23) | ((hi & 0xfffff) << 3) | (int)(lo >> 29));
+    const float q = (xf - ax.x0f) * ax.invf;
+    if (fe <= 254 && q >= 0.0f && q < (float)ax.nc) {
+        const int k = (int)q;
+        const float fr = q - (float)k; /* exact: k <= q < k + 1 */
+        if (fr > ax.tol && fr < 1.0f - ax.tol) return k;
+    }
+    return (int)((x - x0) / dh);
+}
+
+static DsmcAxis dsmc_axis(double x0, double xm, double dh, int nc) {
+    /* |q - (x - x0)/dh| <= 2^-23 |x| / dh + 2^-24 |x0| / dh (x and x0 to
+     * float) + 3 roundings of 2^-24 relative on q (the subtraction, 1/dh,
+     * the product) for 0 <= q < nc; doubled, plus the float64 quotient's
+     * own rounding */
+    const double L = fmax(fabs(x0), fabs(xm)) + dh;
+    const double err = 3.01 * ldexp(1.0, -24) * (nc + 1.0) + (ldexp(1.0, -23) * L + ldexp(1.0, -24) * fabs(x0)) / dh;
+    const double tol = 2 * err + 1e-12;
+    DsmcAxis a;
+    a.x0f = (float)x0;
+    a.invf = (float)(1.0 / dh);
+    a.tol = tol < 0.01 ? (float)tol : 2.0f; /* 2: always the division */
+    a.nc = nc;
+    return a;
+}
+
+/* each atom's cell and its slot among the cell's atoms (arrival order) */
+__global__ void k_dsmc_cells(Geo g, DsmcAxis ax, DsmcAxis ay, DsmcAxis az, const double *__restrict__ P,
+                             int64_t stride, const int64_t *__restrict__ d_count, int64_t n_cells, int32_t *cell,
+                             int32_t *rank, int32_t *count, int *err) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d_count[0]) return;
-    int ijk[3];
-    for (int d = 0; d < 3; d++) ijk[d] = (int)((P[d * stride + p] - g.x0[d]) / g.dh[d]);
-    const int64_t c = (int64_t)ijk[2] * (g.nj - 1) * (g.ni - 1) + (int64_t)ijk[1] * (g.ni - 1) + ijk[0];
-    const bool in = ijk[0] >= 0 && ijk[1] >= 0 && ijk[2] >= 0 && ijk[0] < g.ni - 1 && ijk[1] < g.nj - 1 &&
-                    ijk[2] < g.nk - 1 && c < n_cells;
+    const int i = dsmc_coord(P[p], g.x0[0], g.dh[0], ax);
+    const int j = dsmc_coord(P[stride + p], g.x0[1], g.dh[1], ay);
+    const int k = dsmc_coord(P[2 * stride + p], g.x0[2], g.dh[2], az);
+    const int64_t c = (int64_t)k * (g.nj - 1) * (g.ni - 1) + (int64_t)j * (g.ni - 1) + i;
+    const bool in = i >= 0 && j >= 0 && k >= 0 && i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1 && c < n_cells;
     if (!in) {
         atomicOr(err, DERR_DSMC);
         cell[p] = -1;
         return;
     }
     cell[p] = (int32_t)c;
-    atomicAdd(count + c, 1);
+    rank[p] = atomicAdd(count + c, 1);
 }
 
-__global__ void k_dsmc_scatter(const int32_t *__restrict__ cell, const int64_t *__restrict__ d_count, int32_t *cursor,
+__global__ void k_dsmc_scatter(const int32_t *__restrict__ cell, const int32_t *__restrict__ rank,
+                               const int64_t *__restrict__ d_count, const int32_t *__restrict__ start,
                                int32_t *perm) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d_count[0]) return;
     const int32_t c = cell[p];
     if (c < 0) return;
-    perm[atomicAdd(cursor + c, 1)] = (int32_t)p;
+    perm[start[c] + rank[p]] = (int32_t)p;
+}
+
+/* Bitonic sort of 32 R values held R per lane (element i*32 + lane in a[i]),
+ * ascending: exchanges between lanes by shuffles, within a lane by swaps. */
+template <int R>
+__device__ __forceinline__ void warp_bitonic(int32_t (&a)[R], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jj = j >> 5;
+#pragma unroll
+                for (int i = 0; i < R; i++) {
+                    if ((i & jj) == 0) {
+                        const bool up = ((i * 32 + lane) & k) == 0;
+                        const int32_t x = a[i], y = a[i | jj];
+                        const bool sw = up ? (x > y) : (x < y);
+                        a[i] = sw ? y : x;
+                        a[i | jj] = sw ? x : y;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < R; i++) {
+                    const int32_t y = __shfl_xor_sync(0xffffffffu, a[i], j);
+                    const bool lower = (lane & j) == 0;
+                    const bool up = ((i * 32 + lane) & k) == 0;
+                    a[i] = (lower == up) ? min(a[i], y) : max(a[i], y);
+                }
+            }
+        }
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void order_segment(int32_t *parts, int np, int lane) {
+    int32_t a[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) a[i] = i * 32 + lane < np ? parts[i * 32 + lane] : INT_MAX;
+    warp_bitonic<R>(a, lane);
+#pragma unroll
+    for (int i = 0; i < R; i++)
+        if (i * 32 + lane < np) parts[i * 32 + lane] = a[i];
+}
+
+/* each cell's atoms in particle order (the order of parts_in_cell,
+ * ch4/Collisions.cpp:114-120): one warp per cell */
+__global__ void __launch_bounds__(256) k_dsmc_order(const int32_t *__restrict__ count,
+                                                    const int32_t *__restrict__ start, int32_t *perm,
+                                                    int64_t n_cells) {
+    const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= n_cells) return; /* whole warps */
+    const int np = count[c];
+    if (np < 2) return;
+    int32_t *parts = perm + start[c];
+    if (np <= 32) order_segment<1>(parts, np, lane);
+    else if (np <= 64) order_segment<2>(parts, np, lane);
+    else if (np <= 128) order_segment<4>(parts, np, lane);
+    else if (np <= 256) order_segment<8>(parts, np, lane);
+    else if (np <= 512) order_segment<16>(parts, np, lane);
+    else if (np <= 1024) order_segment<32>(parts, np, lane);
+    else if (lane == 0) {
+        for (int i = 1; i < np; i++) {
+            const int32_t v = parts[i];
+            int j = i - 1;
+            while (j >= 0 && parts[j] > v) {
+                parts[j + 1] = parts[j];
+                j--;
+            }
+            parts[j + 1] = v;
+        }
+    }
 }
 
 __global__ void k_dsmc_begin(unsigned long long *state) {
@@ -1442,17 +1565,7 @@ __global__ void __launch_bounds__(128) k_dsmc_collide(DsmcArgs a) {
     if (c >= a.n_cells) return;
     const int np = a.count[c];
     if (np < 2) return;
-    int32_t *parts = a.perm + (a.cursor[c] - np);
-    /* the cell's particles in particle order */
-    for (int i = 1; i < np; i++) {
-        const int32_t v = parts[i];
-        int j = i - 1;
-        while (j >= 0 && parts[j] > v) {
-            parts[j + 1] = parts[j];
-            j--;
-        }
-        parts[j + 1] = v;
-    }
+    const int32_t *parts = a.perm + a.start[c]; /* in particle order */
     const double smax = __longlong_as_double((long long)a.state[0]);
     const double ng_f = 0.5 * np * np * a.Fn * smax * a.dt / a.dV;
     const int ng = (int)(ng_f + 0.5);
@@ -1530,16 +1643,21 @@ __global__ void k_dsmc_finish(unsigned long long *state) {
 void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu, const int64_t *d_cell_off) {
     const int64_t n = s.host_bound;
     const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    const DsmcAxis ax = dsmc_axis(w.g.x0[0], w.g.xm[0], w.g.dh[0], w.g.ni - 1);
+    const DsmcAxis ay = dsmc_axis(w.g.x0[1], w.g.xm[1], w.g.dh[1], w.g.nj - 1);
+    const DsmcAxis az = dsmc_axis(w.g.x0[2], w.g.xm[2], w.g.dh[2], w.g.nk - 1);
     cudaMemsetAsync(s.dsmc_count, 0, (n_cells + 1) * sizeof(int32_t), w.stream);
     if (n > 0)
-        k_dsmc_cells<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, n_cells, s.dsmc_cell,
-                                                                s.dsmc_count, w.d_err);
-    cudaMemcpyAsync(s.dsmc_cursor, s.dsmc_count, (n_cells + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+        k_dsmc_cells<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, ax, ay, az, s.P, s.cap, s.d_count, n_cells,
+                                                                s.dsmc_cell, s.dsmc_rank, s.dsmc_count, w.d_err);
+    cudaMemcpyAsync(s.dsmc_start, s.dsmc_count, (n_cells + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice,
                     w.stream);
-    launch_int_excl_scan(w.stream, s.dsmc_cursor, n_cells, s.dsmc_bsum);
+    launch_int_excl_scan(w.stream, s.dsmc_start, n_cells, s.dsmc_bsum);
     if (n > 0)
-        k_dsmc_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.dsmc_cell, s.d_count, s.dsmc_cursor,
-                                                                  s.dsmc_perm);
+        k_dsmc_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.dsmc_cell, s.dsmc_rank, s.d_count,
+                                                                  s.dsmc_start, s.dsmc_perm);
+    k_dsmc_order<<<blocks_for(n_cells * 32, 256), 256, 0, w.stream>>>(s.dsmc_count, s.dsmc_start, s.dsmc_perm,
+                                                                       n_cells);
     k_dsmc_begin<<<1, 1, 0, w.stream>>>(s.d_dsmc);
     DsmcArgs a;
     a.g = w.g;
@@ -1550,7 +1668,7 @@ void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu,
     for (int d = 0; d < 4; d++) a.c[d] = s.dsmc_c[d];
     a.n_cells = n_cells;
     a.count = s.dsmc_count;
-    a.cursor = s.dsmc_cursor;
+    a.start = s.dsmc_start;
     a.perm = s.dsmc_perm;
     a.P = s.P;
     a.stride = s.cap;
@@ -1564,7 +1682,7 @@ void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu,
     a.err = w.d_err;
     k_dsmc_collide<<<blocks_for(n_cells, 128), 128, 0, w.stream>>>(a);
     k_dsmc_finish<<<1, 1, 0, w.stream>>>(s.d_dsmc);
-    w.nlaunch += 6 + 3;
+    w.nlaunch += 7 + 3;
     s.dsmc_calls++;
 }
 
