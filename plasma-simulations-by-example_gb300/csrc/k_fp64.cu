@@ -1517,7 +1517,7 @@ __device__ __forceinline__ void order_segment(int32_t *parts, int np, int lane) 
 }
 
 /* each cell's atoms in particle order (the order of parts_in_cell,
- * ch4/Collisions.cpp:114-120): one warp per cell */
+ * ch4/Collisions.cpp:116-121): one warp per cell */
 __global__ void __launch_bounds__(256) k_dsmc_order(const int32_t *__restrict__ count,
                                                     const int32_t *__restrict__ start, int32_t *perm,
                                                     int64_t n_cells) {

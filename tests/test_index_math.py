@@ -29,3 +29,51 @@ def test_float_estimated_division_is_exact_below_2_pow_24():
         want = n // d
         assert np.all(np.abs(est - want) <= 1), d
         assert np.array_equal(q, want), d
+
+
+def dsmc_axis(x0, xm, dh, nc):
+    """host side of the DSMC cell estimate (dsmc_axis in csrc/k_fp64.cu)"""
+    L = max(abs(x0), abs(xm)) + dh
+    err = 3.01 * 2.0 ** -24 * (nc + 1.0) + (2.0 ** -23 * L + 2.0 ** -24 * abs(x0)) / dh
+    tol = 2 * err + 1e-12
+    return np.float32(x0), np.float32(1.0 / dh), np.float32(tol if tol < 0.01 else 2.0), nc
+
+
+def dsmc_coord(x, x0, dh, ax):
+    """device side (dsmc_coord): x cut to 24 leading bits by integer
+    operations, q = (x_f - x0_f) * (1/dh)_f in float, accepted when q lies
+    farther than tol from an integer, else the float64 division"""
+    x0f, invf, tol, nc = ax
+    bits = x.view(np.uint64)
+    hi = (bits >> np.uint64(32)).astype(np.uint32)
+    lo = (bits & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    fe = ((hi >> 20) & 0x7FF).astype(np.int64) - 896
+    fb = (hi & 0x80000000) | (np.clip(fe, 0, 255).astype(np.uint32) << 23) | ((hi & 0xFFFFF) << 3) | (lo >> 29)
+    xf = np.where(fe >= 1, fb.astype(np.uint32).view(np.float32), np.float32(0))
+    q = ((xf - x0f).astype(np.float32) * invf).astype(np.float32)
+    k = np.trunc(q).astype(np.int64)
+    fr = (q - k.astype(np.float32)).astype(np.float32)
+    fast = (fe <= 254) & (q >= 0) & (q < np.float32(nc)) & (fr > tol) & (fr < np.float32(1) - tol)
+    exact = np.trunc((x - x0) / dh).astype(np.int64)
+    return np.where(fast, k, exact), exact, fast
+
+
+def test_dsmc_cell_index():
+    """World::XtoIJK (ch4/World.h:79-92) by the float estimate equals the
+    float64 division for random positions and for positions within a few
+    ulps of every cell face, on grids near and far from the origin."""
+    rng = np.random.default_rng(41)
+    for x0, xm, n in [(-0.2, 0.2, 41), (-0.1, 0.1, 21), (0.0, 0.4, 41), (0.0, 0.05, 6), (0.0, 0.4, 512),
+                      (1000.0, 1000.5, 101), (-3e-3, 5e-3, 2049)]:
+        dh = (xm - x0) / (n - 1)
+        ax = dsmc_axis(x0, xm, dh, n - 1)
+        x = x0 + rng.random(400_000) * (xm - x0)
+        f = x0 + rng.integers(0, n, 40_000) * dh
+        near = np.concatenate([f, np.nextafter(f, np.inf), np.nextafter(f, -np.inf), f + dh * 1e-9,
+                               f - dh * 1e-9, f + dh * 1e-6, f - dh * 3e-6])
+        near = near[(near >= x0) & (near < xm)]
+        for xs in (x, near):
+            got, want, _ = dsmc_coord(xs, x0, dh, ax)
+            assert np.array_equal(got, want), (x0, xm, n)
+        if ax[2] < 1:
+            assert dsmc_coord(x, x0, dh, ax)[2].mean() > 0.99
