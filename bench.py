@@ -707,6 +707,29 @@ def run_dsmc(args, E, torch):
         s.dsmc(dt)
         s.dsmc_status()
     e2e_s = (time.perf_counter() - t0) / args.steps
+
+    def timed(fn):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        fn()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                evs[i][0].record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+    # ch4 species moments (Species::sampleMoments) and MCC_CEX::apply with
+    # the same atoms as source and target (den and stream velocity of the gas)
+    ms_mom = timed(s.sampleMoments)
+    s.computeGasProperties()
+    s.computeNumberDensity()
+    mcc = E.MCC_CEX(s, s, w)
+    ms_mcc = timed(lambda: mcc.apply(dt))
     P = s.particles()
     w.close()
     # CPU: the oracle on the same atoms, starting from the warmed-up sigma_cr_max
@@ -745,7 +768,12 @@ def run_dsmc(args, E, torch):
                          "algorithmic_bytes_per_launch": alg, "bytes_per_particle": 40},
             "clocks": ck,
             "cpu_baseline": {"value": n / float(np.mean(cpu_t)), "unit": "particle-calls/s", "cores": 1,
-                             "kind": "port", "sample": "2 calls of the oracle's DSMC_MEX over all %d atoms" % n}}
+                             "kind": "port", "sample": "2 calls of the oracle's DSMC_MEX over all %d atoms" % n},
+            "sample_moments": {"ms_per_call": ms_mom, "particles_per_s": n / (ms_mom * 1e-3),
+                               "bytes_per_particle": 56,
+                               "hbm_frac": 56.0 * n / (ms_mom * 1e-3) / 1e9 / hbm},
+            "mcc_cex": {"ms_per_call": ms_mcc, "particles_per_s": n / (ms_mcc * 1e-3), "bytes_per_particle": 48,
+                        "hbm_frac": 48.0 * n / (ms_mcc * 1e-3) / 1e9 / hbm}}
     print(json.dumps(line))
 
 

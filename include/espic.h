@@ -53,6 +53,11 @@ extern "C" {
 #define ESPIC_FIELD_DEN 4     /* number density of one species */
 #define ESPIC_FIELD_DEN_AVE 5 /* running average of den */
 #define ESPIC_FIELD_OBJECT_ID 6 /* int32 values travelled as float64 */
+/* ch4 species fields (float64 form; ch4/Species.h:84-95) */
+#define ESPIC_FIELD_VEL 7     /* stream velocity, 3 values per node, interleaved */
+#define ESPIC_FIELD_TEMP 8    /* temperature (K) */
+#define ESPIC_FIELD_MPC 9     /* macroparticles per cell, (ni-1)(nj-1)(nk-1) values, i fastest */
+#define ESPIC_FIELD_MOMENTS 10 /* sampled sums n, nu, nv, nw, nuu, nvv, nww: 7 planes of nn (read only) */
 
 typedef struct espic_world espic_world;
 
@@ -233,6 +238,31 @@ int espic_dsmc_enable(espic_world *w, int sp, const double *c, double sigma_cr_m
 int espic_dsmc_apply(espic_world *w, int sp, double dt, const double *u, int64_t nu, const int64_t *cell_off);
 int espic_dsmc_status(espic_world *w, int sp, double *sigma_cr_max, int64_t *collisions_last,
                       int64_t *collisions_total);
+/* Species::sampleMoments (ch4/Species.cpp:191-201): adds each particle's
+ * mpw, mpw v and mpw v_d v_d to the sampled sums with the CIC corner weights
+ * of Field_::scatter.  Each corner product is rounded to a 64-bit integer
+ * count of 2^-S (S per sum and call, from the call's largest value, so no
+ * node overflows) and summed exactly: deterministic, within ~1e-13 relative
+ * of the reference's float64 sums. */
+int espic_sample_moments(espic_world *w, int sp);
+/* Species::computeGasProperties (ch4/Species.cpp:204-225): ESPIC_FIELD_VEL
+ * and ESPIC_FIELD_TEMP from the sampled sums */
+int espic_gas_properties(espic_world *w, int sp);
+/* Species::clearSamples (ch4/Species.cpp:238-240) */
+int espic_clear_samples(espic_world *w, int sp);
+/* Species::computeMPC (ch4/Species.cpp:228-235): ESPIC_FIELD_MPC */
+int espic_compute_mpc(espic_world *w, int sp);
+/* MCC_CEX(source, target).apply(dt) (ch4/Collisions.h:40-50,
+ * ch4/Collisions.cpp:43-80): each source particle collides with the target
+ * gas (den and ESPIC_FIELD_VEL of species tgt, gathered at the particle)
+ * with probability 1 - exp(-n sigma |v - v_t| dt), sigma = 1e-16 m^2, and a
+ * colliding particle's velocity is set to 0, as in the reference.  u NULL:
+ * particle p draws index p of the call's counter-based stream.  u non-NULL
+ * (parity checks): particle p draws u[p_off[p]] (p_off: one entry per
+ * particle) and the call waits.  collisions (may be NULL; non-NULL waits):
+ * the number of colliding particles. */
+int espic_mcc_cex(espic_world *w, int src, int tgt, double dt, const double *u, int64_t nu, const int64_t *p_off,
+                  int64_t *collisions);
 /* World::getPE, ch2/World.cpp:72-84 */
 int espic_potential_energy(espic_world *w, double *pe);
 /* The per-step columns of Output::diagOutput, ch3/ver2/Output.cpp:96-132, with

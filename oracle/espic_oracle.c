@@ -1179,6 +1179,114 @@ void eo_update_average(int64_t nn, double *ave, const double *inst, int samples)
 }
 
 /* ------------------------------------------------------------------------ */
+/* ch4 species moments.  Species::sampleMoments, ch4/Species.cpp:191-201:
+ * n_sum += mpw, nv_sum += mpw vel, nuu_sum += (mpw u) u, ... each with
+ * Field_::scatter (ch4/Field.h:212-232; a double3 value scatters per
+ * component), float64 sums in particle order.  mom: 7 planes of nn (n, nu,
+ * nv, nw, nuu, nvv, nww). */
+void eo_sample_moments(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *mom) {
+    const int64_t nn = (int64_t)g->ni * g->nj * g->nk;
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double lc[3], f[3], w[8];
+        int c[3];
+        int64_t idx[8];
+        eo_xtol(g, x, lc);
+        cell_of(g, lc, c, f);
+        cic_nodes(g, c, idx);
+        const double mpw = P[6 * stride + p], u = P[3 * stride + p], v = P[4 * stride + p], ww = P[5 * stride + p];
+        const double val[7] = {mpw, mpw * u, mpw * v, mpw * ww, mpw * u * u, mpw * v * v, mpw * ww * ww};
+        for (int q = 0; q < 7; q++) {
+            cic_weights(val[q], f[0], f[1], f[2], w);
+            for (int m = 0; m < 8; m++) mom[q * nn + idx[m]] += w[m];
+        }
+    }
+}
+
+/* Species::computeGasProperties, ch4/Species.cpp:204-225: vel = nv/n (0 where
+ * n == 0, Field_ operator/ ch4/Field.h:182-196), T = m/(2K) (uu + vv + ww)
+ * with uu = nuu/n - u u (T = 0 where n <= 0).  vel: [nn][3]. */
+void eo_gas_properties(const eo_grid *g, double mass, const double *mom, double *vel, double *T) {
+    const double K = 1.380648e-23;
+    const int64_t nn = (int64_t)g->ni * g->nj * g->nk;
+    for (int64_t u = 0; u < nn; u++) {
+        const double count = mom[u];
+        double ave[3];
+        for (int d = 0; d < 3; d++) {
+            ave[d] = count != 0 ? mom[(1 + d) * nn + u] / count : 0.0;
+            vel[3 * u + d] = ave[d];
+        }
+        if (count <= 0) {
+            T[u] = 0;
+            continue;
+        }
+        const double uu = mom[4 * nn + u] / count - ave[0] * ave[0];
+        const double vv = mom[5 * nn + u] / count - ave[1] * ave[1];
+        const double ww = mom[6 * nn + u] / count - ave[2] * ave[2];
+        T[u] = mass / (2 * K) * (uu + vv + ww);
+    }
+}
+
+/* Species::computeMPC, ch4/Species.cpp:228-235: particles per cell by
+ * World::XtoIJK (ch4/World.h:88-92); mpc[(k (nj-1) + j) (ni-1) + i] */
+void eo_compute_mpc(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *mpc) {
+    const int64_t n_cells = (int64_t)(g->ni - 1) * (g->nj - 1) * (g->nk - 1);
+    for (int64_t c = 0; c < n_cells; c++) mpc[c] = 0;
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]}, lc[3];
+        eo_xtol(g, x, lc);
+        const int i = (int)lc[0], j = (int)lc[1], k = (int)lc[2];
+        mpc[((int64_t)k * (g->nj - 1) + j) * (g->ni - 1) + i] += 1;
+    }
+}
+
+/* Field_<double>::gather, ch4/Field.h:234-253, with the index clamp */
+static double gather1(const eo_grid *g, const double *f, const double lc[3]) {
+    int c[3];
+    double fr[3];
+    int64_t idx[8];
+    cell_of(g, lc, c, fr);
+    cic_nodes(g, c, idx);
+    const double di = fr[0], dj = fr[1], dk = fr[2];
+    return f[idx[0]] * (1 - di) * (1 - dj) * (1 - dk) + f[idx[1]] * (di) * (1 - dj) * (1 - dk) +
+           f[idx[2]] * (di) * (dj) * (1 - dk) + f[idx[3]] * (1 - di) * (dj) * (1 - dk) +
+           f[idx[4]] * (1 - di) * (1 - dj) * (dk) + f[idx[5]] * (di) * (1 - dj) * (dk) +
+           f[idx[6]] * (di) * (dj) * (dk) + f[idx[7]] * (1 - di) * (dj) * (dk);
+}
+
+/* MCC_CEX::apply, ch4/Collisions.cpp:43-80: for each source particle in
+ * order, vt = target vel gathered, nn = target den gathered, P = 1 -
+ * exp(-nn sigma |v - vt| dt) with sigma = 1e-16; one rnd() per particle and,
+ * on a collision (P >= rnd()), the 11 of target.sampleIsotropicVel
+ * (ch4/Species.cpp:149-174: theta, r, then 9 in sampleVth), whose velocity
+ * the reference discards; the particle's velocity becomes 0.  p_off[p]: the
+ * index in u of particle p's uniform.  Returns the collisions. */
+int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const double *den, const double *vel,
+                   double dt, const double *u, int64_t nu, int64_t *u_used, int64_t *p_off) {
+    int64_t k = 0, ncol = 0;
+    for (int64_t p = 0; p < n; p++) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]}, lc[3], vt[3], vr[3];
+        eo_xtol(g, x, lc);
+        eo_gather3(g, vel, lc, vt);
+        const double nn = gather1(g, den, lc);
+        for (int d = 0; d < 3; d++) vr[d] = P[(3 + d) * stride + p] - vt[d];
+        const double v_rel_mag = dsmc_mag(vr);
+        const double sigma = 1e-16;
+        const double Pc = 1 - exp(-nn * sigma * v_rel_mag * dt);
+        if (p_off) p_off[p] = k;
+        const double U = k < nu ? u[k] : -1.0;
+        k++;
+        if (Pc >= U) {
+            k += 11;
+            ncol++;
+            for (int d = 0; d < 3; d++) P[(3 + d) * stride + p] = 0;
+        }
+    }
+    if (u_used) *u_used = k;
+    return ncol;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Threaded CPU baseline: the per-thread particle ranges and private deposit
  * buffers of ch9/MT (Species.cpp:9-110), for the sphere push + compaction +
  * fixed-point deposit.  Returns seconds of wall time. */

@@ -136,6 +136,12 @@ void eo_efield(const eo_grid *g, const double *phi, double *ef);
 void eo_species_diag(const double *P, int64_t stride, int64_t n, double mass, double out[5]);
 double eo_potential_energy(const eo_grid *g, const double *ef, const double *vol);
 void eo_update_average(int64_t nn, double *ave, const double *inst, int samples);
+/* ch4 species moments and MCC (ch4/Species.cpp:191-235, ch4/Collisions.cpp:43-80) */
+void eo_sample_moments(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *mom);
+void eo_gas_properties(const eo_grid *g, double mass, const double *mom, double *vel, double *T);
+void eo_compute_mpc(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *mpc);
+int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const double *den, const double *vel,
+                   double dt, const double *u, int64_t nu, int64_t *u_used, int64_t *p_off);
 
 /* ---- CPU baseline (threaded like ch9/MT) ------------------------------ */
 double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],

@@ -73,6 +73,11 @@ def _sig(L):
                                  I64]
     L.eo_dsmc_mex.restype = I64
     L.eo_dsmc_mex.argtypes = [C.POINTER(Grid), D, D, D, PD, PD, PD, I64, I64, PD, I64, PI64, PI64]
+    L.eo_sample_moments.argtypes = [C.POINTER(Grid), PD, I64, I64, PD]
+    L.eo_gas_properties.argtypes = [C.POINTER(Grid), D, PD, PD, PD]
+    L.eo_compute_mpc.argtypes = [C.POINTER(Grid), PD, I64, I64, PD]
+    L.eo_mcc_cex.restype = I64
+    L.eo_mcc_cex.argtypes = [C.POINTER(Grid), PD, I64, I64, PD, PD, D, PD, I64, PI64, PI64]
     L.eo_inject_warm.restype = I64
     L.eo_inject_warm.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, PD, PI64, PD, I64, I64,
                                  I64]
@@ -256,6 +261,46 @@ def dsmc_mex(g, mass, mpw0, dt, c, sigma_cr_max, P, u):
                              u.size, C.byref(used), off.ctypes.data_as(PI64))
     assert ncol >= 0, "uniforms ran out"
     return P, float(smax[0]), int(ncol), used.value, off
+
+
+def sample_moments(g, P, mom=None):
+    """eo_sample_moments: adds P's samples to mom (7 planes of nn: n, nu, nv,
+    nw, nuu, nvv, nww; zeros when None) and returns it."""
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    nn = g.ni * g.nj * g.nk
+    mom = np.zeros(7 * nn) if mom is None else np.ascontiguousarray(mom, dtype=np.float64).copy()
+    lib().eo_sample_moments(C.byref(g), pd(P), P.shape[1], P.shape[1], pd(mom))
+    return mom
+
+
+def gas_properties(g, mass, mom):
+    """eo_gas_properties: (vel [nn][3] flattened, T [nn])"""
+    nn = g.ni * g.nj * g.nk
+    mom = np.ascontiguousarray(mom, dtype=np.float64)
+    vel, T = np.zeros(3 * nn), np.zeros(nn)
+    lib().eo_gas_properties(C.byref(g), mass, pd(mom), pd(vel), pd(T))
+    return vel, T
+
+
+def compute_mpc(g, P):
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    mpc = np.zeros((g.ni - 1) * (g.nj - 1) * (g.nk - 1))
+    lib().eo_compute_mpc(C.byref(g), pd(P), P.shape[1], P.shape[1], pd(mpc))
+    return mpc
+
+
+def mcc_cex(g, P, den, vel, dt, u):
+    """eo_mcc_cex on a copy of P: (P after, collisions, uniforms used, the
+    per-particle offset of its uniform in u)"""
+    P = np.array(P, dtype=np.float64, order="C", copy=True)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    den = np.ascontiguousarray(den, dtype=np.float64)
+    vel = np.ascontiguousarray(vel, dtype=np.float64)
+    off = np.zeros(max(P.shape[1], 1), dtype=np.int64)
+    used = C.c_int64(0)
+    ncol = lib().eo_mcc_cex(C.byref(g), pd(P), P.shape[1], P.shape[1], pd(den), pd(vel), dt, pd(u), u.size,
+                            C.byref(used), off.ctypes.data_as(PI64))
+    return P, int(ncol), used.value, off[:P.shape[1]]
 
 
 def deposit_fp64(g, P):

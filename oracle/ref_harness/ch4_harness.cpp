@@ -1,9 +1,10 @@
 /*
  * ch4_harness.cpp -- drives the reference's ch4 WarmBeamSource (drifting
- * isotropic thermal injector) and DSMC_MEX (neutral-neutral collisions)
- * through their public API for golden vectors.
+ * isotropic thermal injector), DSMC_MEX (neutral-neutral collisions),
+ * Species moment sampling and MCC_CEX (charge exchange) through their
+ * public API for golden vectors.
  * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
- * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc <in.kv> <out.kv>
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc <in.kv> <out.kv>
  */
 #include <chrono>
 #include <cmath>
@@ -62,6 +63,66 @@ int main(int argc, char **argv) {
         out["u"] = us;
         out["sigma_cr_max"] = smax;
         out["c"] = std::vector<double>(dsmc.c, dsmc.c + 4);
+        out["sp0_P"] = v;
+        kv_write(argv[3], out);
+        return 0;
+    }
+    if (op == "moments" || op == "mcc") {
+        const std::vector<double> &P = kv_get(in, "sp0_P");
+        size_t n = P.size() / 7;
+        for (size_t p = 0; p < n; p++)
+            sp.particles.emplace_back(double3(P[p], P[n + p], P[2 * n + p]),
+                                      double3(P[3 * n + p], P[4 * n + p], P[5 * n + p]), 0.0, P[6 * n + p]);
+        if (op == "moments") {
+            /* sampleMoments `calls` times (particles unchanged), then
+             * computeGasProperties and computeMPC */
+            int calls = kv_has(in, "calls") ? (int)kv_s(in, "calls") : 1;
+            for (int c = 0; c < calls; c++) sp.sampleMoments();
+            sp.computeGasProperties();
+            sp.computeMPC();
+            std::vector<double> mom;
+            for (Field *f : {&sp.n_sum}) {
+                std::vector<double> a = field_out(*f, ni, nj, nk);
+                mom.insert(mom.end(), a.begin(), a.end());
+            }
+            std::vector<double> nv = field3_out(sp.nv_sum, ni, nj, nk); /* [nn][3] */
+            for (int d = 0; d < 3; d++)
+                for (size_t u = 0; u < nv.size() / 3; u++) mom.push_back(nv[3 * u + d]);
+            for (Field *f : {&sp.nuu_sum, &sp.nvv_sum, &sp.nww_sum}) {
+                std::vector<double> a = field_out(*f, ni, nj, nk);
+                mom.insert(mom.end(), a.begin(), a.end());
+            }
+            out["mom"] = mom;
+            out["vel"] = field3_out(sp.vel, ni, nj, nk);
+            out["T"] = field_out(sp.T, ni, nj, nk);
+            out["mpc"] = field_out(sp.mpc, ni - 1, nj - 1, nk - 1);
+            kv_write(argv[3], out);
+            return 0;
+        }
+        /* MCC_CEX(sp0 -> sp1).apply(dt) `steps` times; sp1's den and vel are
+         * given; the uniforms drawn are recorded by replaying the generator */
+        const std::vector<double> &mq1 = kv_get(in, "sp1_mq");
+        Species tgt("sp1", mq1[0], mq1[1], mq1[2], world);
+        field_in(tgt.den, kv_get(in, "sp1_den"), ni, nj, nk);
+        field3_in(tgt.vel, kv_get(in, "sp1_vel"), ni, nj, nk);
+        field_in(tgt.T, kv_get(in, "sp1_T"), ni, nj, nk);
+        MCC_CEX mcc(sp, tgt, world);
+        int steps = kv_has(in, "steps") ? (int)kv_s(in, "steps") : 1;
+        std::vector<double> us;
+        for (int s = 0; s < steps; s++) {
+            Rnd before = rnd;
+            mcc.apply(kv_s(in, "dt"));
+            for (long g = 0; g < 2000000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+        }
+        std::vector<double> v(7 * n);
+        for (size_t p = 0; p < n; p++) {
+            for (int d = 0; d < 3; d++) {
+                v[d * n + p] = sp.particles[p].pos[d];
+                v[(3 + d) * n + p] = sp.particles[p].vel[d];
+            }
+            v[6 * n + p] = sp.particles[p].mpw;
+        }
+        out["u"] = us;
         out["sp0_P"] = v;
         kv_write(argv[3], out);
         return 0;

@@ -23,6 +23,7 @@ FORM_FP64, FORM_MIXED = 0, 1
 WALLS_REFLECT, WALLS_ABSORB = 0, 1
 SOLVER_SOR, SOLVER_GS, SOLVER_PCG, SOLVER_QN = 0, 1, 2, 3
 FIELD_PHI, FIELD_RHO, FIELD_NODE_VOL, FIELD_EF, FIELD_DEN, FIELD_DEN_AVE, FIELD_OBJECT_ID = range(7)
+FIELD_VEL, FIELD_TEMP, FIELD_MPC, FIELD_MOMENTS = range(7, 11)
 BEAM_COLD, BEAM_WARM, BEAM_ISOTROPIC, BEAM_MAXWELLIAN = range(4)
 COUNT_RANDOM, COUNT_REMAINDER = 0, 1
 
@@ -117,6 +118,12 @@ def lib():
             "espic_dsmc_enable": [VP, C.c_int, PD, C.c_double],
             "espic_dsmc_apply": [VP, C.c_int, C.c_double, PD, I64, C.POINTER(C.c_int64)],
             "espic_dsmc_status": [VP, C.c_int, PD, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+            "espic_sample_moments": [VP, C.c_int],
+            "espic_gas_properties": [VP, C.c_int],
+            "espic_clear_samples": [VP, C.c_int],
+            "espic_compute_mpc": [VP, C.c_int],
+            "espic_mcc_cex": [VP, C.c_int, C.c_int, C.c_double, PD, I64, C.POINTER(C.c_int64),
+                              C.POINTER(C.c_int64)],
             "espic_potential_energy": [VP, PD],
             "espic_diag_row": [VP, PD, C.c_int],
             "espic_update_average": [VP, C.c_int],
@@ -320,8 +327,12 @@ class World:
 
     # fields
     def read(self, field, sp=0):
-        if field == FIELD_EF:
+        if field in (FIELD_EF, FIELD_VEL):
             out = np.zeros((self.nn, 3))
+        elif field == FIELD_MPC:
+            out = np.zeros((self.ni - 1) * (self.nj - 1) * (self.nk - 1))
+        elif field == FIELD_MOMENTS:
+            out = np.zeros((7, self.nn))
         else:
             out = np.zeros(self.nn)
         check(lib().espic_field_read(self.h, field, sp, _pd(out), out.size))
@@ -444,6 +455,37 @@ class Species:
         check(lib().espic_dsmc_status(self.world.h, self.id, C.byref(smax), C.byref(last), C.byref(total)))
         return smax.value, last.value, total.value
 
+    # ch4 species moments (ch4/Species.cpp:191-240, float64 form)
+    def sampleMoments(self):
+        check(lib().espic_sample_moments(self.world.h, self.id))
+
+    def computeGasProperties(self):
+        check(lib().espic_gas_properties(self.world.h, self.id))
+
+    def clearSamples(self):
+        check(lib().espic_clear_samples(self.world.h, self.id))
+
+    def computeMPC(self):
+        check(lib().espic_compute_mpc(self.world.h, self.id))
+
+    @property
+    def vel(self):
+        """stream velocity [nn][3] (computeGasProperties)"""
+        return self.world.read(FIELD_VEL, self.id)
+
+    @property
+    def T(self):
+        return self.world.read(FIELD_TEMP, self.id)
+
+    @property
+    def mpc(self):
+        return self.world.read(FIELD_MPC, self.id)
+
+    @property
+    def moments(self):
+        """sampled sums [7][nn]: n, nu, nv, nw, nuu, nvv, nww"""
+        return self.world.read(FIELD_MOMENTS, self.id)
+
     def updateAverages(self):
         check(lib().espic_update_average(self.world.h, self.id))
 
@@ -454,6 +496,32 @@ class Species:
     @property
     def den_ave(self):
         return self.world.read(FIELD_DEN_AVE, self.id)
+
+
+class MCC_CEX:
+    """MCC_CEX(source, target, world) (ch4/Collisions.h:40-50): source
+    particles collide with the target gas (its den and vel fields)."""
+
+    def __init__(self, source, target, world=None):
+        self.source, self.target = source, target
+        self.world = world or source.world
+        self.last = None
+
+    def apply(self, dt, u=None, p_off=None, count=False):
+        """MCC_CEX::apply(dt); with u and p_off the uniforms are replayed
+        (particle p draws u[p_off[p]]); count=True waits and returns the
+        number of colliding particles."""
+        n = C.c_int64(0)
+        pn = C.byref(n) if (count or u is not None) else None
+        if u is None:
+            check(lib().espic_mcc_cex(self.world.h, self.source.id, self.target.id, dt, None, 0, None, pn))
+        else:
+            uu = np.ascontiguousarray(u, dtype=np.float64)
+            off = np.ascontiguousarray(p_off, dtype=np.int64)
+            check(lib().espic_mcc_cex(self.world.h, self.source.id, self.target.id, dt, _pd(uu), uu.size,
+                                      off.ctypes.data_as(C.POINTER(C.c_int64)), pn))
+        self.last = n.value if pn is not None else None
+        return self.last
 
 
 class BeamSource:

@@ -91,6 +91,9 @@ static int take_device_errors(World &w) {
     if (bits & DERR_SORT) return fail(ESPIC_ERR_CUDA, "the cell sort lost track of a particle");
     if (bits & DERR_DSMC)
         return fail(ESPIC_ERR_ARG, "DSMC: a particle outside the domain, or the replayed uniforms ran out");
+    if (bits & DERR_NEUTRAL)
+        return fail(ESPIC_ERR_ARG, "moments / MCC: a particle outside the grid, a non-finite moment, or a "
+                                   "replayed uniform out of range");
     return ESPIC_OK;
 }
 
@@ -147,7 +150,8 @@ static void free_species(Species *s) {
     if (!s) return;
     void *ptrs[] = {s->P, s->cell, s->cell2, s->off, s->off2, s->vel, s->vel2, s->sort_count, s->deadmask,
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
-                    s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum};
+                    s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum,
+                    s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -1024,6 +1028,90 @@ extern "C" int espic_dsmc_status(espic_world *h, int sp, double *sigma_cr_max, i
     return take_device_errors(w);
 }
 
+/* ---------------------------------------------------------------- ch4 moments, MCC */
+static int ensure_ch4(World &w, Species &s);
+
+extern "C" int espic_sample_moments(espic_world *h, int sp) {
+    WORLD(h);
+    SPECIES(sp);
+    int rc = ensure_ch4(w, s);
+    if (rc != ESPIC_OK) return rc;
+    launch_moments(w, s);
+    CHECK_LAUNCH();
+    return ESPIC_OK;
+}
+
+extern "C" int espic_gas_properties(espic_world *h, int sp) {
+    WORLD(h);
+    SPECIES(sp);
+    int rc = ensure_ch4(w, s);
+    if (rc != ESPIC_OK) return rc;
+    launch_gas_props(w, s);
+    CHECK_LAUNCH();
+    return ESPIC_OK;
+}
+
+extern "C" int espic_clear_samples(espic_world *h, int sp) {
+    WORLD(h);
+    SPECIES(sp);
+    int rc = ensure_ch4(w, s);
+    if (rc != ESPIC_OK) return rc;
+    CK(cudaMemsetAsync(s.mom, 0, NMOM * w.nn * sizeof(double), w.stream));
+    return ESPIC_OK;
+}
+
+extern "C" int espic_compute_mpc(espic_world *h, int sp) {
+    WORLD(h);
+    SPECIES(sp);
+    int rc = ensure_ch4(w, s);
+    if (rc != ESPIC_OK) return rc;
+    launch_mpc(w, s);
+    CHECK_LAUNCH();
+    return ESPIC_OK;
+}
+
+extern "C" int espic_mcc_cex(espic_world *h, int src, int tgt, double dt, const double *u, int64_t nu,
+                             const int64_t *p_off, int64_t *collisions) {
+    WORLD(h);
+    if (src < 0 || src >= (int)w.species.size() || tgt < 0 || tgt >= (int)w.species.size())
+        return fail(ESPIC_ERR_ARG, "bad species id");
+    Species &s = *w.species[src], &t = *w.species[tgt];
+    int rc = ensure_ch4(w, s);
+    if (rc == ESPIC_OK) rc = ensure_ch4(w, t);
+    if (rc != ESPIC_OK) return rc;
+    if (!(dt > 0)) return fail(ESPIC_ERR_ARG, "bad time step");
+    double *du = nullptr;
+    int64_t *doff = nullptr;
+    if (u) {
+        if (!p_off || nu < 0) return fail(ESPIC_ERR_ARG, "replayed uniforms need their particle offsets");
+        int64_t np = 0; /* p_off holds one entry per particle: the exact count */
+        CK(cudaMemcpyAsync(&np, s.d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaStreamSynchronize(w.stream));
+        s.host_bound = np;
+        if (dalloc(&du, nu > 0 ? nu : 1) != ESPIC_OK) return ESPIC_ERR_CUDA;
+        if (dalloc(&doff, np > 0 ? np : 1) != ESPIC_OK) {
+            cudaFree(du);
+            return ESPIC_ERR_CUDA;
+        }
+        if (nu > 0) cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        if (np > 0) cudaMemcpyAsync(doff, p_off, np * sizeof(int64_t), cudaMemcpyHostToDevice, w.stream);
+    }
+    launch_mcc(w, s, t, dt, du, nu, doff, s.mcc_ncol);
+    cudaError_t e = cudaSuccess;
+    if (u || collisions) e = cudaStreamSynchronize(w.stream);
+    if (du) cudaFree(du);
+    if (doff) cudaFree(doff);
+    if (e != cudaSuccess) return fail(ESPIC_ERR_CUDA, "%s", cudaGetErrorString(e));
+    CHECK_LAUNCH();
+    if (collisions) {
+        unsigned long long c = 0;
+        CK(cudaMemcpy(&c, s.mcc_ncol, sizeof c, cudaMemcpyDeviceToHost));
+        *collisions = (int64_t)c;
+    }
+    if (u || collisions) return take_device_errors(w);
+    return ESPIC_OK;
+}
+
 extern "C" int espic_species_diag(espic_world *h, int sp, double out[5]) {
     WORLD(h);
     SPECIES(sp);
@@ -1123,6 +1211,25 @@ extern "C" int espic_steady_state(espic_world *h, int *steady) {
 }
 
 /* ---------------------------------------------------------------- fields */
+/* the ch4 species fields, allocated (zeroed) on first use */
+static int ensure_ch4(World &w, Species &s) {
+    if (s.ch4_on) return ESPIC_OK;
+    if (s.form != 0) return fail(ESPIC_ERR_ARG, "moments and MCC work on a species in the float64 form");
+    const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    if (dalloc(&s.mom, NMOM * w.nn) != ESPIC_OK || dalloc(&s.mom_acc, NMOM * w.nn) != ESPIC_OK ||
+        dalloc(&s.mom_scale, 2 * NMOM) != ESPIC_OK || dalloc(&s.mom_bound, NMOM) != ESPIC_OK ||
+        dalloc(&s.gvel, 3 * w.nn) != ESPIC_OK || dalloc(&s.gtemp, w.nn) != ESPIC_OK ||
+        dalloc(&s.mpc, n_cells) != ESPIC_OK || dalloc(&s.mcc_ncol, 1) != ESPIC_OK)
+        return ESPIC_ERR_CUDA;
+    CK(cudaMemsetAsync(s.mom, 0, NMOM * w.nn * sizeof(double), w.stream));
+    CK(cudaMemsetAsync(s.mom_acc, 0, NMOM * w.nn * sizeof(unsigned long long), w.stream));
+    CK(cudaMemsetAsync(s.gvel, 0, 3 * w.nn * sizeof(double), w.stream));
+    CK(cudaMemsetAsync(s.gtemp, 0, w.nn * sizeof(double), w.stream));
+    CK(cudaMemsetAsync(s.mpc, 0, n_cells * sizeof(double), w.stream));
+    s.ch4_on = true;
+    return ESPIC_OK;
+}
+
 static int field_ptr(World &w, int field, int sp, double **p, int64_t *count) {
     switch (field) {
         case ESPIC_FIELD_PHI: *p = w.phi; *count = w.nn; return ESPIC_OK;
@@ -1135,6 +1242,21 @@ static int field_ptr(World &w, int field, int sp, double **p, int64_t *count) {
             *p = field == ESPIC_FIELD_DEN ? w.species[sp]->den : w.species[sp]->den_ave;
             *count = w.nn;
             return ESPIC_OK;
+        case ESPIC_FIELD_VEL:
+        case ESPIC_FIELD_TEMP:
+        case ESPIC_FIELD_MPC:
+        case ESPIC_FIELD_MOMENTS: {
+            if (sp < 0 || sp >= (int)w.species.size()) return fail(ESPIC_ERR_ARG, "bad species id");
+            Species &s = *w.species[sp];
+            int rc = ensure_ch4(w, s);
+            if (rc != ESPIC_OK) return rc;
+            const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+            if (field == ESPIC_FIELD_VEL) *p = s.gvel, *count = 3 * w.nn;
+            if (field == ESPIC_FIELD_TEMP) *p = s.gtemp, *count = w.nn;
+            if (field == ESPIC_FIELD_MPC) *p = s.mpc, *count = n_cells;
+            if (field == ESPIC_FIELD_MOMENTS) *p = s.mom, *count = NMOM * w.nn;
+            return ESPIC_OK;
+        }
         default:
             return fail(ESPIC_ERR_ARG, "unknown field %d", field);
     }
@@ -1175,6 +1297,7 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
         w.phi_prev_valid = false;
         return ESPIC_OK;
     }
+    if (field == ESPIC_FIELD_MOMENTS) return fail(ESPIC_ERR_ARG, "the sampled sums are read only");
     double *p;
     int64_t cnt;
     int rc = field_ptr(w, field, sp, &p, &cnt);

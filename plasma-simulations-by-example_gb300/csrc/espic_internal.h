@@ -29,7 +29,9 @@ enum : int {
     DERR_FIXED_RANGE = 4, /* a weight too large for the fixed-point scale */
     DERR_TIMEOUT = 8,     /* a bounded wait on an asynchronous copy ran out */
     DERR_SORT = 16,       /* a sort slot named no particle of the species */
-    DERR_DSMC = 32        /* a collision partner outside the domain, or replayed uniforms ran out */
+    DERR_DSMC = 32,       /* a collision partner outside the domain, or replayed uniforms ran out */
+    DERR_NEUTRAL = 64     /* moments / MCC: a particle outside the grid, a non-finite moment, or replayed
+                             uniforms out of range */
 };
 
 struct Geo {
@@ -39,6 +41,9 @@ struct Geo {
 
 /* particles per dead-count tile of the compaction */
 constexpr int TILE_PARTICLES = 32768;
+
+/* sampled velocity moments of a ch4 species: n, n u, n v, n w, n u u, n v v, n w w */
+constexpr int NMOM = 7;
 
 struct SolveStatus {
     int converged;
@@ -126,6 +131,12 @@ void launch_density(World &w, Species &s);
 void launch_int_excl_scan(cudaStream_t st, int32_t *x, int64_t n, int32_t *bsum);
 int64_t int_scan_blocks(int64_t n);
 void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu, const int64_t *d_cell_off);
+/* ch4 species moments and MCC charge exchange (float64 form) */
+void launch_moments(World &w, Species &s);
+void launch_gas_props(World &w, Species &s);
+void launch_mpc(World &w, Species &s);
+void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const double *d_u, int64_t nu,
+                const int64_t *d_off, unsigned long long *d_ncol);
 void launch_inv_vol(World &w);
 void launch_charge(World &w);
 void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3,

@@ -51,6 +51,13 @@ struct Species {
                                              (bits), [2] collisions of the call, [3] all collisions */
     int32_t *dsmc_cell = nullptr, *dsmc_rank = nullptr, *dsmc_perm = nullptr; /* [cap] */
     int32_t *dsmc_count = nullptr, *dsmc_start = nullptr, *dsmc_bsum = nullptr; /* [ncells + 1], scan */
+    /* ch4 moments (allocated on first use): sampled sums [NMOM][nn], the
+     * call's integer sums, scales, stream velocity [nn][3], temperature,
+     * macroparticles per cell [ncells]; MCC: calls and collision count */
+    bool ch4_on = false;
+    double *mom = nullptr, *mom_scale = nullptr, *gvel = nullptr, *gtemp = nullptr, *mpc = nullptr;
+    unsigned long long *mom_acc = nullptr, *mom_bound = nullptr, *mcc_ncol = nullptr;
+    uint64_t mcc_calls = 0;
 };
 
 struct Source {

@@ -1763,4 +1763,259 @@ void launch_qn(World &w) {
     w.nlaunch++;
 }
 
+/* ------------------------------------------------------------------------ */
+/* ch4 species moments (float64 form): Species::sampleMoments,
+ * computeGasProperties, computeMPC, clearSamples (ch4/Species.cpp:191-240).
+ * The seven sampled sums (n, n u, n v, n w, n u u, n v v, n w w) are
+ * scattered with the reference's corner products, each product rounded once
+ * to a 64-bit integer count of 2^-S_q and added exactly (order independent,
+ * deterministic); S_q is chosen per call from the call's largest |value| and
+ * particle count so that no node can overflow, and each call's integer sums
+ * are folded into float64 accumulators. */
+__device__ __forceinline__ void mom_values(const double *__restrict__ P, int64_t stride, int64_t p, double v[NMOM]) {
+    const double w = P[6 * stride + p], u = P[3 * stride + p], vv = P[4 * stride + p], ww = P[5 * stride + p];
+    v[0] = w;
+    v[1] = w * u;
+    v[2] = w * vv;
+    v[3] = w * ww;
+    v[4] = w * u * u;
+    v[5] = w * vv * vv;
+    v[6] = w * ww * ww;
+}
+
+/* largest |value| of each sum over the particles, as float64 bits (the bits
+ * of non-negative values order like the values: integer max, no float64) */
+__global__ void __launch_bounds__(256) k_mom_bound(const double *__restrict__ P, int64_t stride,
+                                                   const int64_t *__restrict__ d_count, unsigned long long *bound) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long b[NMOM];
+    for (int q = 0; q < NMOM; q++) b[q] = 0;
+    if (p < d_count[0]) {
+        double v[NMOM];
+        mom_values(P, stride, p, v);
+        for (int q = 0; q < NMOM; q++) b[q] = (unsigned long long)__double_as_longlong(v[q]) & 0x7fffffffffffffffull;
+    }
+    for (int q = 0; q < NMOM; q++) {
+        unsigned long long x = b[q];
+        for (int o = 16; o; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+            x = y > x ? y : x;
+        }
+        if ((threadIdx.x & 31) == 0 && x) atomicMax(bound + q, x);
+    }
+}
+
+/* scale[q] = 2^S_q with count * max_q * 2^S_q < 2^62; scale[NMOM + q] = 2^-S_q */
+__global__ void k_mom_scale(const unsigned long long *bound, const int64_t *d_count, double *scale, int *err) {
+    const int q = threadIdx.x;
+    if (q >= NMOM) return;
+    const double b = __longlong_as_double((long long)bound[q]);
+    const double t = b * (double)(d_count[0] > 0 ? d_count[0] : 1);
+    int S = 0;
+    if (!isfinite(t)) {
+        atomicOr(err, DERR_NEUTRAL);
+    } else if (t > 0) {
+        int e;
+        frexp(t, &e); /* t < 2^e */
+        S = 62 - e;
+        S = S > 1000 ? 1000 : (S < -1000 ? -1000 : S);
+    }
+    scale[q] = ldexp(1.0, S);
+    scale[NMOM + q] = ldexp(1.0, -S);
+}
+
+__global__ void __launch_bounds__(256) k_mom_scatter(Geo g, const double *__restrict__ P, int64_t stride,
+                                                     const int64_t *__restrict__ d_count,
+                                                     const double *__restrict__ scale, unsigned long long *acc,
+                                                     int64_t nn, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+    double lc[3];
+    xtol(g, x, lc);
+    if (!(lc[0] >= 0 && lc[1] >= 0 && lc[2] >= 0 && lc[0] <= g.ni - 1 && lc[1] <= g.nj - 1 && lc[2] <= g.nk - 1)) {
+        atomicOr(err, DERR_NEUTRAL);
+        return;
+    }
+    const int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj), k = clamp_cell((int)lc[2], g.nk);
+    const double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+    const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    const int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+    double v[NMOM];
+    mom_values(P, stride, p, v);
+#pragma unroll
+    for (int q = 0; q < NMOM; q++) {
+        const double value = v[q], f = scale[q];
+        double w[8];
+        w[0] = value * (1 - di) * (1 - dj) * (1 - dk);
+        w[1] = value * (di) * (1 - dj) * (1 - dk);
+        w[2] = value * (di) * (dj) * (1 - dk);
+        w[3] = value * (1 - di) * (dj) * (1 - dk);
+        w[4] = value * (1 - di) * (1 - dj) * (dk);
+        w[5] = value * (di) * (1 - dj) * (dk);
+        w[6] = value * (di) * (dj) * (dk);
+        w[7] = value * (1 - di) * (dj) * (dk);
+        unsigned long long *a = acc + q * nn;
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const long long c = __double2ll_rn(w[m] * f);
+            if (c) atomicAdd(a + idx[m], (unsigned long long)c);
+        }
+    }
+}
+
+/* the call's exact integer sums into the float64 accumulators */
+__global__ void __launch_bounds__(256) k_mom_fold(int64_t nn, unsigned long long *acc, const double *scale,
+                                                  double *mom) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NMOM * nn) return;
+    const int q = (int)(t / nn);
+    const long long c = (long long)acc[t];
+    if (c) {
+        mom[t] += (double)c * scale[NMOM + q];
+        acc[t] = 0;
+    }
+}
+
+/* Species::computeGasProperties (ch4/Species.cpp:204-225): stream velocity
+ * nv/n (0 where n == 0, Field_ operator/ at ch4/Field.h:182-196) and
+ * T = m / (2 K) ((uu + vv) + ww) with uu = <u u> - u u (0 where n <= 0) */
+__global__ void __launch_bounds__(256) k_gas_props(int64_t nn, double mass, const double *__restrict__ mom,
+                                                   double *vel, double *T) {
+    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nn) return;
+    const double count = mom[u];
+    double ave[3];
+    for (int d = 0; d < 3; d++) {
+        ave[d] = count != 0 ? mom[(1 + d) * nn + u] / count : 0.0;
+        vel[3 * u + d] = ave[d];
+    }
+    if (count <= 0) {
+        T[u] = 0;
+        return;
+    }
+    const double uu = mom[4 * nn + u] / count - ave[0] * ave[0];
+    const double vv = mom[5 * nn + u] / count - ave[1] * ave[1];
+    const double ww = mom[6 * nn + u] / count - ave[2] * ave[2];
+    T[u] = mass / (2 * KB) * (uu + vv + ww);
+}
+
+/* Species::computeMPC (ch4/Species.cpp:228-235): macroparticles per cell
+ * (World::XtoIJK); counts below 2^53 are exact in float64 */
+__global__ void __launch_bounds__(256) k_mpc(Geo g, const double *__restrict__ P, int64_t stride,
+                                             const int64_t *__restrict__ d_count, double *mpc, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d_count[0]) return;
+    const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+    double lc[3];
+    xtol(g, x, lc);
+    const int i = (int)lc[0], j = (int)lc[1], k = (int)lc[2];
+    if (!(lc[0] >= 0 && lc[1] >= 0 && lc[2] >= 0 && i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1)) {
+        atomicOr(err, DERR_NEUTRAL);
+        return;
+    }
+    atomicAdd(mpc + ((int64_t)k * (g.nj - 1) + j) * (g.ni - 1) + i, 1.0);
+}
+
+/* MCC_CEX::apply (ch4/Collisions.cpp:43-80): each source particle meets
+ * the target gas (density and stream velocity gathered at its position)
+ * with probability 1 - exp(-n sigma |v - v_t| dt), sigma = 1e-16 m^2, and
+ * then stops (the reference sets vel = 0; its sampled target velocity is
+ * never used, so it is not drawn).  One uniform per particle: index p of
+ * the call's counter-based stream, or u[p_off[p]] when replaying. */
+__global__ void __launch_bounds__(256) k_mcc_cex(Geo g, double *P, int64_t stride,
+                                                 const int64_t *__restrict__ d_count, const double *__restrict__ den,
+                                                 const double *__restrict__ vel, double dt, const double *__restrict__ u,
+                                                 int64_t nu, const int64_t *__restrict__ p_off, uint64_t seed,
+                                                 uint64_t stream, unsigned long long *ncol, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool hit = false;
+    if (p < d_count[0]) {
+        const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double lc[3];
+        xtol(g, x, lc);
+        if (!(lc[0] >= 0 && lc[1] >= 0 && lc[2] >= 0 && lc[0] <= g.ni - 1 && lc[1] <= g.nj - 1 &&
+              lc[2] <= g.nk - 1)) {
+            atomicOr(err, DERR_NEUTRAL);
+        } else {
+            double vt[3];
+            gather3(g, vel, lc, vt);
+            const int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj),
+                      k = clamp_cell((int)lc[2], g.nk);
+            const double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+            const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
+            const double nn = den[n0] * (1 - di) * (1 - dj) * (1 - dk) + den[n0 + 1] * (di) * (1 - dj) * (1 - dk) +
+                              den[n0 + 1 + sy] * (di) * (dj) * (1 - dk) + den[n0 + sy] * (1 - di) * (dj) * (1 - dk) +
+                              den[n0 + sz] * (1 - di) * (1 - dj) * (dk) + den[n0 + 1 + sz] * (di) * (1 - dj) * (dk) +
+                              den[n0 + 1 + sy + sz] * (di) * (dj) * (dk) + den[n0 + sy + sz] * (1 - di) * (dj) * (dk);
+            const double v_rel_mag = dsmc_mag(P[3 * stride + p] - vt[0], P[4 * stride + p] - vt[1],
+                                              P[5 * stride + p] - vt[2]);
+            const double sigma = 1e-16;
+            const double Pc = 1 - exp(-nn * sigma * v_rel_mag * dt);
+            double U;
+            if (u) {
+                const int64_t o = p_off[p];
+                if (o < 0 || o >= nu) {
+                    atomicOr(err, DERR_NEUTRAL);
+                    U = 2.0;
+                } else {
+                    U = u[o];
+                }
+            } else {
+                U = philox_uniform(seed, stream, (uint64_t)p);
+            }
+            if (Pc >= U) {
+                hit = true;
+                P[3 * stride + p] = 0;
+                P[4 * stride + p] = 0;
+                P[5 * stride + p] = 0;
+            }
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(ncol, (unsigned long long)__popc(m));
+}
+
+void launch_moments(World &w, Species &s) {
+    const int64_t n = s.host_bound;
+    cudaMemsetAsync(s.mom_bound, 0, NMOM * sizeof(unsigned long long), w.stream);
+    if (n > 0) k_mom_bound<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.P, s.cap, s.d_count, s.mom_bound);
+    k_mom_scale<<<1, 32, 0, w.stream>>>(s.mom_bound, s.d_count, s.mom_scale, w.d_err);
+    if (n > 0)
+        k_mom_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, s.mom_scale, s.mom_acc,
+                                                                 w.nn, w.d_err);
+    k_mom_fold<<<blocks_for(NMOM * w.nn, 256), 256, 0, w.stream>>>(w.nn, s.mom_acc, s.mom_scale, s.mom);
+    w.nlaunch += 2 + 2 * (n > 0);
+}
+
+void launch_gas_props(World &w, Species &s) {
+    k_gas_props<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, s.mass, s.mom, s.gvel, s.gtemp);
+    w.nlaunch++;
+}
+
+void launch_mpc(World &w, Species &s) {
+    const int64_t n = s.host_bound;
+    const int64_t n_cells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    cudaMemsetAsync(s.mpc, 0, n_cells * sizeof(double), w.stream);
+    if (n > 0) {
+        k_mpc<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, s.mpc, w.d_err);
+        w.nlaunch++;
+    }
+}
+
+void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const double *d_u, int64_t nu,
+                const int64_t *d_off, unsigned long long *d_ncol) {
+    const int64_t n = src.host_bound;
+    cudaMemsetAsync(d_ncol, 0, sizeof(unsigned long long), w.stream);
+    if (n > 0) {
+        /* one stream per (species, call); particle p draws index p */
+        const uint64_t stream = (0xCEull << 56) | ((uint64_t)(src.id & 0xff) << 48) |
+                                (src.mcc_calls & 0xffffffffffffull);
+        k_mcc_cex<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, src.P, src.cap, src.d_count, tgt.den, tgt.gvel, dt,
+                                                             d_u, nu, d_off, w.seed, stream, d_ncol, w.d_err);
+        w.nlaunch++;
+    }
+    src.mcc_calls++;
+}
+
 }  // namespace espic

@@ -3,7 +3,7 @@ CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
 Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py [base] [steady] [dsmc]
+    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -229,6 +229,44 @@ def dsmc_cases():
          P=o["sp0_P"].reshape(7, -1), u=o["u"], sigma_cr_max=o["sigma_cr_max"], c=o["c"])
 
 
+def neutral_cases():
+    """ch4 species moments (Species::sampleMoments twice, computeGasProperties,
+    computeMPC, ch4/Species.cpp:191-235) of 2000 weighted atoms, and two
+    MCC_CEX::apply calls (ch4/Collisions.cpp:43-80) of 2000 ions in a given
+    neutral gas (density 0.5-3e19 m^-3, stream velocity about 7 km/s)."""
+    geo = dict(grid=[6, 6, 6], x0=[0.0, 0.0, 0.0], xm=[0.05, 0.05, 0.05])
+    rng = np.random.default_rng(20261205)
+    n, mass = 2000, 16 * AMU
+    P = np.zeros((7, n))
+    P[0:3] = rng.random((3, n)) * 0.05 * 0.999999
+    P[3] = 7000 + 500 * rng.standard_normal(n)
+    P[4] = 200 * rng.standard_normal(n)
+    P[5] = -300 + 400 * rng.standard_normal(n)
+    P[6] = 1e12 * (0.5 + rng.random(n))
+    o = po.run_reference("ref_ch4", "moments", base_inputs(geo, 1e-7, seed=[5], sp0_mq=[mass, 0.0, 1e12],
+                                                           sp0_P=P.ravel(), calls=[2]))
+    save("neutral_moments", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, calls=2, P=P,
+         mom=o["mom"], vel=o["vel"], T=o["T"], mpc=o["mpc"])
+    nn = int(np.prod(geo["grid"]))
+    X = np.stack(np.meshgrid(*[np.linspace(geo["x0"][d], geo["xm"][d], geo["grid"][d]) for d in range(3)],
+                             indexing="ij"), axis=-1).transpose(2, 1, 0, 3).reshape(nn, 3)
+    den = 1e19 * (1.75 + 1.25 * np.sin(X[:, 0] * 90) * np.cos(X[:, 2] * 60))
+    vel = np.zeros((nn, 3))
+    vel[:, 2] = 7000 + 300 * np.sin(X[:, 1] * 70)
+    vel[:, 0] = 100 * rng.standard_normal(nn)
+    T = 1000 + 50 * rng.random(nn)
+    Pi = np.zeros((7, n))
+    Pi[0:3] = rng.random((3, n)) * 0.05 * 0.999999
+    Pi[3:6] = 2000 * rng.standard_normal((3, n))
+    Pi[6] = 5e2
+    dt = 1e-8
+    o = po.run_reference("ref_ch4", "mcc", base_inputs(geo, dt, seed=[41], sp0_mq=[mass, QE, 5e2], sp0_P=Pi.ravel(),
+                                                       sp1_mq=[mass, 0.0, 1e12], sp1_den=den, sp1_vel=vel.ravel(),
+                                                       sp1_T=T, steps=[2]))
+    save("neutral_mcc", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], dt=dt, P0=Pi, den=den, vel=vel.ravel(),
+         T=T, u=o["u"], P=o["sp0_P"].reshape(7, -1), steps=2)
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -265,8 +303,8 @@ def steady_cases():
 
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
-    # stream), "steady", "dsmc" (default: all)
-    cases = sys.argv[1:] or ["base", "steady", "dsmc"]
+    # stream), "steady", "dsmc", "neutral" (default: all)
+    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral"]
     build_ref.build_reference()
     if "base" in cases:
         rng = np.random.default_rng(20261203)
@@ -276,3 +314,5 @@ if __name__ == "__main__":
         steady_cases()
     if "dsmc" in cases:
         dsmc_cases()
+    if "neutral" in cases:
+        neutral_cases()

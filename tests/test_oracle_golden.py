@@ -270,3 +270,32 @@ def test_dsmc_bitexact(po):
         assert smax == f["sigma_cr_max"][st], st
     assert off == f["u"].size
     assert np.array_equal(P, f["P"])
+
+
+def test_neutral_moments_bitexact(po):
+    """Species::sampleMoments twice, computeGasProperties and computeMPC of
+    the reference (ch4/Species.cpp:191-235) reproduced bit for bit."""
+    f = golden("neutral_moments")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    mom = None
+    for _ in range(int(f["calls"])):
+        mom = po.sample_moments(g, f["P"], mom)
+    assert np.array_equal(mom, f["mom"])
+    vel, T = po.gas_properties(g, float(f["mass"]), mom)
+    assert np.array_equal(vel, f["vel"]) and np.array_equal(T, f["T"])
+    assert np.array_equal(po.compute_mpc(g, f["P"]), f["mpc"])
+
+
+def test_mcc_cex_bitexact(po):
+    """Two MCC_CEX::apply calls of the reference (ch4/Collisions.cpp:43-80)
+    replayed with its recorded uniforms: velocities and the uniform count
+    reproduced bit for bit."""
+    f = golden("neutral_mcc")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    P, off = f["P0"], 0
+    for _ in range(int(f["steps"])):
+        P, ncol, used, _ = po.mcc_cex(g, P, f["den"], f["vel"], float(f["dt"]), f["u"][off:])
+        off += used
+        assert ncol > 0
+    assert off == f["u"].size
+    assert np.array_equal(P, f["P"])
