@@ -1767,11 +1767,11 @@ void launch_qn(World &w) {
 /* ch4 species moments (float64 form): Species::sampleMoments,
  * computeGasProperties, computeMPC, clearSamples (ch4/Species.cpp:191-240).
  * The seven sampled sums (n, n u, n v, n w, n u u, n v v, n w w) are
- * scattered with the reference's corner products, each product rounded once
- * to a 64-bit integer count of 2^-S_q and added exactly (order independent,
- * deterministic); S_q is chosen per call from the call's largest |value| and
- * particle count so that no node can overflow, and each call's integer sums
- * are folded into float64 accumulators. */
+ * scattered with the CIC corner weights, each product value * weight rounded
+ * once to a 64-bit integer count of 2^-S_q and added exactly (order
+ * independent, deterministic); S_q is chosen per call from the call's
+ * largest |value| and particle count so that no node can overflow, and each
+ * call's integer sums are folded into float64 accumulators. */
 __device__ __forceinline__ void mom_values(const double *__restrict__ P, int64_t stride, int64_t p, double v[NMOM]) {
     const double w = P[6 * stride + p], u = P[3 * stride + p], vv = P[4 * stride + p], ww = P[5 * stride + p];
     v[0] = w;
@@ -1805,7 +1805,9 @@ __global__ void __launch_bounds__(256) k_mom_bound(const double *__restrict__ P,
     }
 }
 
-/* scale[q] = 2^S_q with count * max_q * 2^S_q < 2^62; scale[NMOM + q] = 2^-S_q */
+/* scale[q] = 2^S_q with count * max_q * 2^S_q < 2^62 (no node overflows)
+ * and max_q * 2^S_q < 2^51 (each product converts by one FMA, see
+ * fix_round); scale[NMOM + q] = 2^-S_q */
 __global__ void k_mom_scale(const unsigned long long *bound, const int64_t *d_count, double *scale, int *err) {
     const int q = threadIdx.x;
     if (q >= NMOM) return;
@@ -1815,16 +1817,52 @@ __global__ void k_mom_scale(const unsigned long long *bound, const int64_t *d_co
     if (!isfinite(t)) {
         atomicOr(err, DERR_NEUTRAL);
     } else if (t > 0) {
-        int e;
-        frexp(t, &e); /* t < 2^e */
-        S = 62 - e;
+        int e, em;
+        frexp(t, &e);  /* t < 2^e */
+        frexp(b, &em); /* b < 2^em */
+        S = 62 - e < 51 - em ? 62 - e : 51 - em;
         S = S > 1000 ? 1000 : (S < -1000 ? -1000 : S);
     }
     scale[q] = ldexp(1.0, S);
     scale[NMOM + q] = ldexp(1.0, -S);
 }
 
-__global__ void __launch_bounds__(256) k_mom_scatter(Geo g, const double *__restrict__ P, int64_t stride,
+/* RN(a b) as a 64-bit integer for |a b| < 2^51: adding 1.5 * 2^52 inside one
+ * FMA puts the exact product's nearest integer (ties to even) in the low
+ * bits of a number in [2^52, 2^53), whose bit pattern then differs from the
+ * constant's by that integer (one float64 operation instead of a product and
+ * a conversion) */
+__device__ __forceinline__ long long fix_round(double a, double b) {
+    const double magic = 6755399441055744.0;
+    return __double_as_longlong(__fma_rn(a, b, magic)) - __double_as_longlong(magic);
+}
+
+/* corner weights (1-di)(1-dj)(1-dk), di(1-dj)(1-dk), ... in Field_::scatter's
+ * corner order (ch4/Field.h:212-232), the dj, dk factors shared */
+__device__ __forceinline__ void corner_weights(double di, double dj, double dk, double W[8]) {
+    const double a0 = (1 - di) * (1 - dj), a1 = di * (1 - dj), a2 = di * dj, a3 = (1 - di) * dj;
+    W[0] = a0 * (1 - dk);
+    W[1] = a1 * (1 - dk);
+    W[2] = a2 * (1 - dk);
+    W[3] = a3 * (1 - dk);
+    W[4] = a0 * dk;
+    W[5] = a1 * dk;
+    W[6] = a2 * dk;
+    W[7] = a3 * dk;
+}
+
+/* x to logical coordinates with the correctly rounded reciprocal of dh:
+ * equal to World::XtoL's division bit for bit (div_rcp) */
+__device__ __forceinline__ void xtol_rcp(const Geo &g, double3 rdh, const double x[3], double lc[3]) {
+    lc[0] = div_rcp(x[0] - g.x0[0], g.dh[0], rdh.x);
+    lc[1] = div_rcp(x[1] - g.x0[1], g.dh[1], rdh.y);
+    lc[2] = div_rcp(x[2] - g.x0[2], g.dh[2], rdh.z);
+}
+
+/* each sum's 8 corner contributions value * W_m, rounded once (from the exact
+ * product) to a count of 2^-S_q and added exactly; within one weight
+ * rounding of the reference's left-to-right product */
+__global__ void __launch_bounds__(256) k_mom_scatter(Geo g, double3 rdh, const double *__restrict__ P, int64_t stride,
                                                      const int64_t *__restrict__ d_count,
                                                      const double *__restrict__ scale, unsigned long long *acc,
                                                      int64_t nn, int *err) {
@@ -1832,33 +1870,25 @@ __global__ void __launch_bounds__(256) k_mom_scatter(Geo g, const double *__rest
     if (p >= d_count[0]) return;
     const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
     double lc[3];
-    xtol(g, x, lc);
+    xtol_rcp(g, rdh, x, lc);
     if (!(lc[0] >= 0 && lc[1] >= 0 && lc[2] >= 0 && lc[0] <= g.ni - 1 && lc[1] <= g.nj - 1 && lc[2] <= g.nk - 1)) {
         atomicOr(err, DERR_NEUTRAL);
         return;
     }
     const int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj), k = clamp_cell((int)lc[2], g.nk);
-    const double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+    double W[8];
+    corner_weights(lc[0] - i, lc[1] - j, lc[2] - k, W);
     const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
     const int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
     double v[NMOM];
     mom_values(P, stride, p, v);
 #pragma unroll
     for (int q = 0; q < NMOM; q++) {
-        const double value = v[q], f = scale[q];
-        double w[8];
-        w[0] = value * (1 - di) * (1 - dj) * (1 - dk);
-        w[1] = value * (di) * (1 - dj) * (1 - dk);
-        w[2] = value * (di) * (dj) * (1 - dk);
-        w[3] = value * (1 - di) * (dj) * (1 - dk);
-        w[4] = value * (1 - di) * (1 - dj) * (dk);
-        w[5] = value * (di) * (1 - dj) * (dk);
-        w[6] = value * (di) * (dj) * (dk);
-        w[7] = value * (1 - di) * (dj) * (dk);
+        const double vf = v[q] * scale[q]; /* exact: a power of two */
         unsigned long long *a = acc + q * nn;
 #pragma unroll
         for (int m = 0; m < 8; m++) {
-            const long long c = __double2ll_rn(w[m] * f);
+            const long long c = fix_round(vf, W[m]);
             if (c) atomicAdd(a + idx[m], (unsigned long long)c);
         }
     }
@@ -1922,8 +1952,12 @@ __global__ void __launch_bounds__(256) k_mpc(Geo g, const double *__restrict__ P
  * with probability 1 - exp(-n sigma |v - v_t| dt), sigma = 1e-16 m^2, and
  * then stops (the reference sets vel = 0; its sampled target velocity is
  * never used, so it is not drawn).  One uniform per particle: index p of
- * the call's counter-based stream, or u[p_off[p]] when replaying. */
-__global__ void __launch_bounds__(256) k_mcc_cex(Geo g, double *P, int64_t stride,
+ * the call's counter-based stream, or u[p_off[p]] when replaying.  The
+ * gathers share one set of corner weights and accumulate with FMAs, so n and
+ * v_t lie within a few ulps of the reference's left-to-right sums; a
+ * decision can differ only for a uniform within those ulps of the
+ * probability. */
+__global__ void __launch_bounds__(256) k_mcc_cex(Geo g, double3 rdh, double *P, int64_t stride,
                                                  const int64_t *__restrict__ d_count, const double *__restrict__ den,
                                                  const double *__restrict__ vel, double dt, const double *__restrict__ u,
                                                  int64_t nu, const int64_t *__restrict__ p_off, uint64_t seed,
@@ -1933,23 +1967,28 @@ __global__ void __launch_bounds__(256) k_mcc_cex(Geo g, double *P, int64_t strid
     if (p < d_count[0]) {
         const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
         double lc[3];
-        xtol(g, x, lc);
+        xtol_rcp(g, rdh, x, lc);
         if (!(lc[0] >= 0 && lc[1] >= 0 && lc[2] >= 0 && lc[0] <= g.ni - 1 && lc[1] <= g.nj - 1 &&
               lc[2] <= g.nk - 1)) {
             atomicOr(err, DERR_NEUTRAL);
         } else {
-            double vt[3];
-            gather3(g, vel, lc, vt);
             const int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj),
                       k = clamp_cell((int)lc[2], g.nk);
-            const double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+            double W[8];
+            corner_weights(lc[0] - i, lc[1] - j, lc[2] - k, W);
             const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
-            const double nn = den[n0] * (1 - di) * (1 - dj) * (1 - dk) + den[n0 + 1] * (di) * (1 - dj) * (1 - dk) +
-                              den[n0 + 1 + sy] * (di) * (dj) * (1 - dk) + den[n0 + sy] * (1 - di) * (dj) * (1 - dk) +
-                              den[n0 + sz] * (1 - di) * (1 - dj) * (dk) + den[n0 + 1 + sz] * (di) * (1 - dj) * (dk) +
-                              den[n0 + 1 + sy + sz] * (di) * (dj) * (dk) + den[n0 + sy + sz] * (1 - di) * (dj) * (dk);
-            const double v_rel_mag = dsmc_mag(P[3 * stride + p] - vt[0], P[4 * stride + p] - vt[1],
-                                              P[5 * stride + p] - vt[2]);
+            const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                    n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+            double nn = 0, vt0 = 0, vt1 = 0, vt2 = 0;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                nn = __fma_rn(den[idx[m]], W[m], nn);
+                vt0 = __fma_rn(vel[3 * idx[m]], W[m], vt0);
+                vt1 = __fma_rn(vel[3 * idx[m] + 1], W[m], vt1);
+                vt2 = __fma_rn(vel[3 * idx[m] + 2], W[m], vt2);
+            }
+            const double v_rel_mag = dsmc_mag(P[3 * stride + p] - vt0, P[4 * stride + p] - vt1,
+                                              P[5 * stride + p] - vt2);
             const double sigma = 1e-16;
             const double Pc = 1 - exp(-nn * sigma * v_rel_mag * dt);
             double U;
@@ -1976,14 +2015,18 @@ __global__ void __launch_bounds__(256) k_mcc_cex(Geo g, double *P, int64_t strid
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(ncol, (unsigned long long)__popc(m));
 }
 
+static double3 rcp_dh(const World &w) {
+    return make_double3(1.0 / w.g.dh[0], 1.0 / w.g.dh[1], 1.0 / w.g.dh[2]);
+}
+
 void launch_moments(World &w, Species &s) {
     const int64_t n = s.host_bound;
     cudaMemsetAsync(s.mom_bound, 0, NMOM * sizeof(unsigned long long), w.stream);
     if (n > 0) k_mom_bound<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.P, s.cap, s.d_count, s.mom_bound);
     k_mom_scale<<<1, 32, 0, w.stream>>>(s.mom_bound, s.d_count, s.mom_scale, w.d_err);
     if (n > 0)
-        k_mom_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, s.P, s.cap, s.d_count, s.mom_scale, s.mom_acc,
-                                                                 w.nn, w.d_err);
+        k_mom_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, rcp_dh(w), s.P, s.cap, s.d_count, s.mom_scale,
+                                                                 s.mom_acc, w.nn, w.d_err);
     k_mom_fold<<<blocks_for(NMOM * w.nn, 256), 256, 0, w.stream>>>(w.nn, s.mom_acc, s.mom_scale, s.mom);
     w.nlaunch += 2 + 2 * (n > 0);
 }
@@ -2011,8 +2054,9 @@ void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const dou
         /* one stream per (species, call); particle p draws index p */
         const uint64_t stream = (0xCEull << 56) | ((uint64_t)(src.id & 0xff) << 48) |
                                 (src.mcc_calls & 0xffffffffffffull);
-        k_mcc_cex<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, src.P, src.cap, src.d_count, tgt.den, tgt.gvel, dt,
-                                                             d_u, nu, d_off, w.seed, stream, d_ncol, w.d_err);
+        k_mcc_cex<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, rcp_dh(w), src.P, src.cap, src.d_count, tgt.den,
+                                                             tgt.gvel, dt, d_u, nu, d_off, w.seed, stream, d_ncol,
+                                                             w.d_err);
         w.nlaunch++;
     }
     src.mcc_calls++;
