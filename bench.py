@@ -305,6 +305,9 @@ def cpu_baseline(cfg, P0, inner_per_step, threads, steps=2, it_cap=8):
 
 
 def run_reference(args):
+    if args.config == "dsmc41":
+        run_reference_dsmc(args)
+        return
     if not args.config.startswith("sphere"):
         print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the sphere workloads "
                           "(the workload the metric is quoted on); run it with --config sphere64 or sphere256"}))
@@ -683,7 +686,7 @@ def run_dsmc(args, E, torch):
     for _ in range(max(args.warmup, 3)):
         s.dsmc(dt)
     w.sync()
-    smax_w, _, tot0 = s.dsmc_status()
+    _, _, tot0 = s.dsmc_status()
     l0 = w.launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = Clocks()
@@ -733,21 +736,8 @@ def run_dsmc(args, E, torch):
     P = s.particles()
     w.close()
     # CPU: the oracle on the same atoms, starting from the warmed-up sigma_cr_max
-    from oracle import pyoracle as po
-    g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
-    ijk = ((P[0:3] - x0[:, None]) / ((xm - x0) / (np.array(cfg["n"]) - 1))[:, None]).astype(np.int64)
-    ci, cj = cfg["n"][0] - 1, cfg["n"][1] - 1
-    cnt = np.bincount(ijk[2] * cj * ci + ijk[1] * ci + ijk[0], minlength=ci * cj * (cfg["n"][2] - 1))
-    dV = np.prod((xm - x0) / (np.array(cfg["n"]) - 1))
-    # uniforms for two calls with room for sigma_cr_max to grow fourfold
-    ng = np.floor(0.5 * cnt * cnt * cfg["mpw0"] * (4 * smax) * dt / dV + 0.5)
-    u = np.random.default_rng(3).random(int(8 * ng.sum()) + 100_000)
-    cpu_t, sm = [], smax
-    for _ in range(2):
-        t0 = time.perf_counter()
-        P, sm, _, used, _ = po.dsmc_mex(g, mass, cfg["mpw0"], dt, po_c(mass), sm, P, u)
-        cpu_t.append(time.perf_counter() - t0)
-        assert used <= u.size
+    _, _, cpu_t = dsmc_cpu_calls(cfg, P, smax, 2)
+    n_cells = (cfg["n"][0] - 1) * (cfg["n"][1] - 1) * (cfg["n"][2] - 1)
     hbm, peak_kind = peaks()
     alg = 40.0 * n
     achieved = alg / (ms * 1e-3) / 1e9
@@ -755,7 +745,7 @@ def run_dsmc(args, E, torch):
             "unit": "particle-calls/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "dsmc41", "grid": list(cfg["n"]), "particles": n, "cells": int(cnt.size),
+            "config": {"workload": "dsmc41", "grid": list(cfg["n"]), "particles": n, "cells": n_cells,
                        "density": cfg["nda"], "temp_K": cfg["temp"], "mpw0": cfg["mpw0"], "dt": dt,
                        "l2": "flushed between timed calls (256 MB write, outside the events)"},
             "collisions_per_call": (tot1 - tot0) / args.steps, "sigma_cr_max": smax,
@@ -774,6 +764,66 @@ def run_dsmc(args, E, torch):
                                "hbm_frac": 56.0 * n / (ms_mom * 1e-3) / 1e9 / hbm},
             "mcc_cex": {"ms_per_call": ms_mcc, "particles_per_s": n / (ms_mcc * 1e-3), "bytes_per_particle": 48,
                         "hbm_frac": 48.0 * n / (ms_mcc * 1e-3) / 1e9 / hbm}}
+    print(json.dumps(line))
+
+
+def dsmc_cpu_calls(cfg, P, smax, calls, seed=3):
+    """`calls` DSMC_MEX::apply calls of the oracle's restatement on the atoms P
+    (one host thread), each with fresh uniforms drawn beforehand (room for
+    sigma_cr_max to grow fourfold).  Returns (P, sigma_cr_max, seconds per
+    call)."""
+    from oracle import pyoracle as po
+    x0, xm, n3 = np.array(cfg["x0"]), np.array(cfg["xm"]), np.array(cfg["n"])
+    g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
+    mass, dt, dh = 16 * AMU, cfg["dt"], (xm - x0) / (n3 - 1)
+    ci, cj = cfg["n"][0] - 1, cfg["n"][1] - 1
+    rng = np.random.default_rng(seed)
+    times = []
+    for _ in range(calls):
+        ijk = ((P[0:3] - x0[:, None]) / dh[:, None]).astype(np.int64)
+        cnt = np.bincount(ijk[2] * cj * ci + ijk[1] * ci + ijk[0], minlength=ci * cj * (cfg["n"][2] - 1))
+        ng = np.floor(0.5 * cnt * cnt * cfg["mpw0"] * (4 * smax) * dt / np.prod(dh) + 0.5)
+        u = rng.random(int(8 * ng.sum()) + 100_000)
+        t0 = time.perf_counter()
+        P, smax, _, used, _ = po.dsmc_mex(g, mass, cfg["mpw0"], dt, po_c(mass), smax, P, u)
+        times.append(time.perf_counter() - t0)
+        assert used <= u.size
+    return P, smax, times
+
+
+def dsmc_state(cfg, seed):
+    """the dsmc41 gas on the host: atoms uniform in the box, drifting
+    Maxwellian velocities (7 km/s along z, 1000 K), weight mpw0"""
+    x0, xm = np.array(cfg["x0"]), np.array(cfg["xm"])
+    n = int(round(cfg["nda"] * np.prod(xm - x0) / cfg["mpw0"]))
+    rng = np.random.default_rng(seed)
+    P = np.empty((7, n))
+    P[0:3] = x0[:, None] + rng.random((3, n)) * (xm - x0)[:, None]
+    P[3:6] = rng.standard_normal((3, n)) * np.sqrt(K * cfg["temp"] / (16 * AMU))
+    P[5] += V_DRIFT
+    P[6] = cfg["mpw0"]
+    return P
+
+
+def run_reference_dsmc(args):
+    """--impl reference on dsmc41: the oracle's DSMC_MEX restatement on the
+    host (the reference's own ch4 code is not on the GPU host), warm-up
+    calls from the reference's starting sigma_cr_max, then timed calls."""
+    cfg = CONFIGS["dsmc41"]
+    P = dsmc_state(cfg, 7)
+    n = P.shape[1]
+    P, sm, _ = dsmc_cpu_calls(cfg, P, 1e-14, max(args.warmup, 0), seed=5)
+    _, _, t = dsmc_cpu_calls(cfg, P, sm, args.steps, seed=6)
+    v = n / float(np.mean(t))
+    line = {"metric": "DSMC_MEX particle-calls/s (ch4 neutral gas)", "value": v, "unit": "particle-calls/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * float(np.mean(t)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "dsmc41", "grid": list(cfg["n"]), "particles": n},
+            "cpu_baseline": {"value": v, "unit": "particle-calls/s", "cores": 1, "kind": "port",
+                             "sample": "%d timed calls of the oracle's DSMC_MEX over all %d atoms after %d warm-up "
+                                       "calls" % (args.steps, n, args.warmup)},
+            "e2e": {"value": v, "unit": "particle-calls/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
