@@ -24,6 +24,13 @@ injection uniforms copied from pinned host memory and the diagnostics row
 cores (the C restatement in oracle/: threaded push + deposit as ch9/MT does,
 serial Newton-PCG timed per iteration and scaled to the iteration count the
 GPU needed at this state).
+
+Other workloads (--config): sphere256 and sphere128 (the same step on
+larger grids), box21 (the ch2 box, FP64 form), ensemble512 (512 ch2 boxes
+stepped together), diff32 (forward + adjoint of the sphere run), dsmc41
+(one DSMC_MEX::apply over the 6.4M-atom ch4 neutral gas, with the ch4
+moment sampling and MCC timed beside it; its reference arm runs the
+oracle's DSMC_MEX on the host).
 """
 import argparse
 import json
