@@ -1287,6 +1287,136 @@ int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const
 }
 
 /* ------------------------------------------------------------------------ */
+/* ch4 neutral push: Species::advance(neutrals, spherium) for a species of
+ * charge 0, ch4/Species.cpp:8-91.  Each particle carries its own time left
+ * (pdt, ch4/Species.h:15): the step adds the world's dt, the particle moves
+ * for its whole time, leaves the domain (killed), or hits the sphere: it is
+ * put 0.999 of the way to the intersection (World::lineSphereIntersect,
+ * ch4/World.cpp:160-182), its time becomes the time used so far, and it
+ * leaves with the thermal speed of a 1000 K wall in a diffuse direction
+ * (Species::sampleReflectedVelocity, ch4/Species.cpp:94-100;
+ * World::sphereDiffuseVector, ch4/World.cpp:185-199), then moves again.
+ * The E-field kick is q/m E dt = 0 for a neutral and is left out.  Dead
+ * particles are removed by swap-with-last (ch4/Species.cpp:76-89).
+ * u: 11 uniforms per bounce (9 of sampleVth(1000), then sin_theta and psi).
+ * sphere: centre and radius^2.  Returns the particle count after removal;
+ * -1 when u runs out. */
+static double dot3(const double a[3], const double b[3]) {
+    double s = 0;
+    for (int i = 0; i < 3; i++) s += a[i] * b[i];
+    return s;
+}
+
+static void cross3(const double a[3], const double b[3], double o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static double line_sphere(const double sphere[4], const double x1[3], const double x2[3]) {
+    double B[3], A[3];
+    for (int i = 0; i < 3; i++) {
+        B[i] = x2[i] - x1[i];
+        A[i] = x1[i] - sphere[i];
+    }
+    const double a = dot3(B, B), b = 2 * dot3(A, B), c = dot3(A, A) - sphere[3];
+    const double det = b * b - 4 * a * c;
+    if (det < 0) return 0.5;
+    double tp = (-b + sqrt(det)) / (2 * a);
+    if (tp < 0 || tp > 1.0) {
+        tp = (-b - sqrt(det)) / (2 * a);
+        if (tp < 0 || tp > 1.0) tp = 0.5;
+    }
+    return tp;
+}
+
+static int in_sphere_ch4(const double sphere[4], const double x[3]) {
+    double r[3] = {x[0] - sphere[0], x[1] - sphere[1], x[2] - sphere[2]};
+    return (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) <= sphere[3];
+}
+
+/* sampleVth(T) (ch4/Species.cpp:149-158) from 9 uniforms */
+static double sample_vth(double mass, double temp, const double *u) {
+    double v_th = sqrt(2 * EO_K * temp / mass);
+    double v1 = v_th * (u[0] + u[1] + u[2] - 1.5);
+    double v2 = v_th * (u[3] + u[4] + u[5] - 1.5);
+    double v3 = v_th * (u[6] + u[7] + u[8] - 1.5);
+    return 3 / sqrt(2 + 2 + 2) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+}
+
+/* sampleReflectedVelocity(pos, v_mag1) with sphereDiffuseVector(pos) */
+static void reflect_diffuse(const double sphere[4], double mass, const double x[3], double v_mag1,
+                            const double *u, double vel[3]) {
+    const double v_th = sample_vth(mass, 1000, u);
+    const double a_th = 1;
+    const double v_mag2 = v_mag1 + a_th * (v_th - v_mag1);
+    const double sin_theta = u[9];
+    const double cos_theta = sqrt(1 - sin_theta * sin_theta);
+    const double psi = 2 * EO_PI * u[10];
+    double r[3] = {x[0] - sphere[0], x[1] - sphere[1], x[2] - sphere[2]}, n[3], t1[3], t2[3];
+    const double m = sqrt(dot3(r, r));
+    for (int i = 0; i < 3; i++) n[i] = r[i] / m;
+    const double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0};
+    if (dot3(n, ex) != 0)
+        cross3(n, ex, t1);
+    else
+        cross3(n, ey, t1);
+    cross3(n, t1, t2);
+    for (int i = 0; i < 3; i++)
+        vel[i] = v_mag2 * (sin_theta * cos(psi) * t1[i] + sin_theta * sin(psi) * t2[i] + cos_theta * n[i]);
+}
+
+int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double mass, double dt, double *P,
+                               int64_t stride, int64_t n, double *pdt, const double *u, int64_t nu,
+                               int64_t *u_used) {
+    int64_t k = 0;
+    for (int64_t p = 0; p < n; p++) {
+        pdt[p] += dt;
+        int n_bounces = 0;
+        while (pdt[p] > 0 && P[6 * stride + p] > 0) {
+            double old[3], x[3], v[3];
+            for (int i = 0; i < 3; i++) {
+                old[i] = P[i * stride + p];
+                v[i] = P[(3 + i) * stride + p];
+                x[i] = old[i] + v[i] * pdt[p];
+                P[i * stride + p] = x[i];
+            }
+            if (!eo_in_bounds(g, x)) {
+                P[6 * stride + p] = 0;
+            } else if (in_sphere_ch4(sphere, x)) {
+                const double tp = line_sphere(sphere, old, x);
+                const double dt_rem = (1 - tp) * pdt[p];
+                pdt[p] -= dt_rem;
+                const double s = 0.999 * tp;
+                for (int i = 0; i < 3; i++) {
+                    x[i] = old[i] + s * (x[i] - old[i]);
+                    P[i * stride + p] = x[i];
+                }
+                const double v_mag1 = sqrt(dot3(v, v));
+                if (k + 11 > nu) return -1;
+                reflect_diffuse(sphere, mass, x, v_mag1, u + k, v);
+                k += 11;
+                for (int i = 0; i < 3; i++) P[(3 + i) * stride + p] = v[i];
+                continue;
+            }
+            pdt[p] = 0;
+            if (++n_bounces > 20) P[6 * stride + p] = 0;
+        }
+    }
+    /* removal: a dead slot takes the last particle and is checked again */
+    int64_t np = n;
+    for (int64_t p = 0; p < np; p++) {
+        if (P[6 * stride + p] > 0) continue;
+        copy_particle(P, stride, p, np - 1);
+        pdt[p] = pdt[np - 1];
+        np--;
+        p--;
+    }
+    if (u_used) *u_used = k;
+    return np;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Threaded CPU baseline: the per-thread particle ranges and private deposit
  * buffers of ch9/MT (Species.cpp:9-110), for the sphere push + compaction +
  * fixed-point deposit.  Returns seconds of wall time. */

@@ -142,6 +142,11 @@ void eo_gas_properties(const eo_grid *g, double mass, const double *mom, double 
 void eo_compute_mpc(const eo_grid *g, const double *P, int64_t stride, int64_t n, double *mpc);
 int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const double *den, const double *vel,
                    double dt, const double *u, int64_t nu, int64_t *u_used, int64_t *p_off);
+/* ch4 Species::advance of a neutral species with the sphere's diffuse
+ * reflection (ch4/Species.cpp:8-100); pdt: per-particle time left */
+int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double mass, double dt, double *P,
+                               int64_t stride, int64_t n, double *pdt, const double *u, int64_t nu,
+                               int64_t *u_used);
 
 /* ---- CPU baseline (threaded like ch9/MT) ------------------------------ */
 double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],

@@ -1,10 +1,11 @@
 /*
  * ch4_harness.cpp -- drives the reference's ch4 WarmBeamSource (drifting
  * isotropic thermal injector), DSMC_MEX (neutral-neutral collisions),
- * Species moment sampling and MCC_CEX (charge exchange) through their
- * public API for golden vectors.
+ * Species moment sampling, MCC_CEX (charge exchange) and the neutral push
+ * with the sphere's diffuse reflection through their public API for golden
+ * vectors.
  * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
- * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc <in.kv> <out.kv>
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc|advance <in.kv> <out.kv>
  */
 #include <chrono>
 #include <cmath>
@@ -124,6 +125,39 @@ int main(int argc, char **argv) {
         }
         out["u"] = us;
         out["sp0_P"] = v;
+        kv_write(argv[3], out);
+        return 0;
+    }
+    if (op == "advance") {
+        /* Species::advance(sp, sp) of a neutral species `steps` times with the
+         * sphere's diffuse reflection; sp0_dt: each particle's time left */
+        const std::vector<double> &P = kv_get(in, "sp0_P"), &pdt = kv_get(in, "sp0_dt");
+        const std::vector<double> &sph = kv_get(in, "sphere"); /* cx cy cz r phi */
+        world.addSphere(double3(sph[0], sph[1], sph[2]), sph[3], sph[4]);
+        size_t n = P.size() / 7;
+        for (size_t p = 0; p < n; p++)
+            sp.particles.emplace_back(double3(P[p], P[n + p], P[2 * n + p]),
+                                      double3(P[3 * n + p], P[4 * n + p], P[5 * n + p]), pdt[p], P[6 * n + p]);
+        int steps = kv_has(in, "steps") ? (int)kv_s(in, "steps") : 1;
+        std::vector<double> us;
+        for (int s = 0; s < steps; s++) {
+            Rnd before = rnd;
+            sp.advance(sp, sp);
+            for (long g = 0; g < 2000000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+        }
+        n = sp.particles.size();
+        std::vector<double> v(7 * n), dts(n);
+        for (size_t p = 0; p < n; p++) {
+            for (int d = 0; d < 3; d++) {
+                v[d * n + p] = sp.particles[p].pos[d];
+                v[(3 + d) * n + p] = sp.particles[p].vel[d];
+            }
+            v[6 * n + p] = sp.particles[p].mpw;
+            dts[p] = sp.particles[p].dt;
+        }
+        out["u"] = us;
+        out["sp0_P"] = v;
+        out["sp0_dt"] = dts;
         kv_write(argv[3], out);
         return 0;
     }

@@ -3,7 +3,7 @@ CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
 Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral]
+    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral] [ch4push]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -267,6 +267,31 @@ def neutral_cases():
          T=T, u=o["u"], P=o["sp0_P"].reshape(7, -1), steps=2)
 
 
+def ch4_push_cases():
+    """Five Species::advance(neutrals, neutrals) steps (ch4/Species.cpp:8-91)
+    of 3000 oxygen atoms flowing at 7 km/s past the sphere: diffuse
+    reflection off its surface at the 1000 K wall speed, removal at the
+    domain faces; half of the atoms start with a full step of time left (as
+    a source leaves them), half with none."""
+    geo = SPH
+    rng = np.random.default_rng(20261206)
+    n, mass, dt = 3000, 16 * AMU, 2e-6
+    x0, xm = np.array(geo["x0"]), np.array(geo["xm"])
+    P = np.zeros((7, n))
+    c = np.array(SPHERE[:3])
+    pos = x0 + rng.random((3 * n, 3)) * (xm - x0)
+    pos = pos[np.sum((pos - c) ** 2, axis=1) > (SPHERE[3] + 1e-3) ** 2][:n]
+    P[0:3] = pos.T
+    P[3:6] = 300 * rng.standard_normal((3, n))
+    P[5] += 7000
+    P[6] = 1e12
+    pdt = np.where(rng.random(n) < 0.5, dt, 0.0)
+    o = po.run_reference("ref_ch4", "advance", base_inputs(geo, dt, seed=[13], sp0_mq=[mass, 0.0, 1e12],
+                                                           sp0_P=P.ravel(), sp0_dt=pdt, sphere=SPHERE, steps=[5]))
+    save("ch4_push", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, dt=dt, sphere=SPHERE, P0=P,
+         dt0=pdt, steps=5, u=o["u"], P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"])
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -303,8 +328,8 @@ def steady_cases():
 
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
-    # stream), "steady", "dsmc", "neutral" (default: all)
-    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral"]
+    # stream), "steady", "dsmc", "neutral", "ch4push" (default: all)
+    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral", "ch4push"]
     build_ref.build_reference()
     if "base" in cases:
         rng = np.random.default_rng(20261203)
@@ -316,3 +341,5 @@ if __name__ == "__main__":
         dsmc_cases()
     if "neutral" in cases:
         neutral_cases()
+    if "ch4push" in cases:
+        ch4_push_cases()

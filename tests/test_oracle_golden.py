@@ -299,3 +299,21 @@ def test_mcc_cex_bitexact(po):
         assert ncol > 0
     assert off == f["u"].size
     assert np.array_equal(P, f["P"])
+
+
+def test_ch4_neutral_push_bitexact(po):
+    """Five Species::advance(neutrals, neutrals) steps of the reference
+    (ch4/Species.cpp:8-100): positions, velocities, per-particle time left,
+    removal order and the uniforms of every sphere bounce reproduced bit
+    for bit."""
+    f = golden("ch4_push")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    sph = f["sphere"]
+    P, pdt, off, bounces = f["P0"], f["dt0"], 0, 0
+    for _ in range(int(f["steps"])):
+        P, pdt, used = po.advance_ch4_neutral(g, tuple(sph[:4]), float(f["mass"]), float(f["dt"]), P, pdt,
+                                              f["u"][off:])
+        off += used
+        bounces += used // 11
+    assert bounces > 50 and off == f["u"].size
+    assert np.array_equal(P, f["P"]) and np.array_equal(pdt, f["pdt"])
