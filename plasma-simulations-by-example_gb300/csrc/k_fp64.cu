@@ -1772,8 +1772,11 @@ void launch_qn(World &w) {
  * independent, deterministic); S_q is chosen per call from the call's
  * largest |value| and particle count so that no node can overflow, and each
  * call's integer sums are folded into float64 accumulators. */
-__device__ __forceinline__ void mom_values(const double *__restrict__ P, int64_t stride, int64_t p, double v[NMOM]) {
-    const double w = P[6 * stride + p], u = P[3 * stride + p], vv = P[4 * stride + p], ww = P[5 * stride + p];
+/* w0 > 0: every particle carries w0 and the weight row is not stored */
+__device__ __forceinline__ void mom_values(const double *__restrict__ P, int64_t stride, int64_t p, double w0,
+                                           double v[NMOM]) {
+    const double w = w0 > 0 ? w0 : P[6 * stride + p];
+    const double u = P[3 * stride + p], vv = P[4 * stride + p], ww = P[5 * stride + p];
     v[0] = w;
     v[1] = w * u;
     v[2] = w * vv;
@@ -1785,14 +1788,14 @@ __device__ __forceinline__ void mom_values(const double *__restrict__ P, int64_t
 
 /* largest |value| of each sum over the particles, as float64 bits (the bits
  * of non-negative values order like the values: integer max, no float64) */
-__global__ void __launch_bounds__(256) k_mom_bound(const double *__restrict__ P, int64_t stride,
+__global__ void __launch_bounds__(256) k_mom_bound(const double *__restrict__ P, int64_t stride, double w0,
                                                    const int64_t *__restrict__ d_count, unsigned long long *bound) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long b[NMOM];
     for (int q = 0; q < NMOM; q++) b[q] = 0;
     if (p < d_count[0]) {
         double v[NMOM];
-        mom_values(P, stride, p, v);
+        mom_values(P, stride, p, w0, v);
         for (int q = 0; q < NMOM; q++) b[q] = (unsigned long long)__double_as_longlong(v[q]) & 0x7fffffffffffffffull;
     }
     for (int q = 0; q < NMOM; q++) {
@@ -1863,7 +1866,7 @@ __device__ __forceinline__ void xtol_rcp(const Geo &g, double3 rdh, const double
  * product) to a count of 2^-S_q and added exactly; within one weight
  * rounding of the reference's left-to-right product */
 __global__ void __launch_bounds__(256) k_mom_scatter(Geo g, double3 rdh, const double *__restrict__ P, int64_t stride,
-                                                     const int64_t *__restrict__ d_count,
+                                                     double w0, const int64_t *__restrict__ d_count,
                                                      const double *__restrict__ scale, unsigned long long *acc,
                                                      int64_t nn, int *err) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1881,7 +1884,7 @@ __global__ void __launch_bounds__(256) k_mom_scatter(Geo g, double3 rdh, const d
     const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
     const int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
     double v[NMOM];
-    mom_values(P, stride, p, v);
+    mom_values(P, stride, p, w0, v);
 #pragma unroll
     for (int q = 0; q < NMOM; q++) {
         const double vf = v[q] * scale[q]; /* exact: a power of two */
@@ -2022,11 +2025,12 @@ static double3 rcp_dh(const World &w) {
 void launch_moments(World &w, Species &s) {
     const int64_t n = s.host_bound;
     cudaMemsetAsync(s.mom_bound, 0, NMOM * sizeof(unsigned long long), w.stream);
-    if (n > 0) k_mom_bound<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.P, s.cap, s.d_count, s.mom_bound);
+    const double w0 = s.uniform_w ? s.mpw0 : 0.0;
+    if (n > 0) k_mom_bound<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.P, s.cap, w0, s.d_count, s.mom_bound);
     k_mom_scale<<<1, 32, 0, w.stream>>>(s.mom_bound, s.d_count, s.mom_scale, w.d_err);
     if (n > 0)
-        k_mom_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, rcp_dh(w), s.P, s.cap, s.d_count, s.mom_scale,
-                                                                 s.mom_acc, w.nn, w.d_err);
+        k_mom_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, rcp_dh(w), s.P, s.cap, w0, s.d_count,
+                                                                 s.mom_scale, s.mom_acc, w.nn, w.d_err);
     k_mom_fold<<<blocks_for(NMOM * w.nn, 256), 256, 0, w.stream>>>(w.nn, s.mom_acc, s.mom_scale, s.mom);
     w.nlaunch += 2 + 2 * (n > 0);
 }

@@ -7,7 +7,8 @@
   fixed-point products, summed exactly, against float64 sums in particle
   order), the stream velocity within 1e-10 of its largest component, the
   temperature within 1e-6 of its largest value (T subtracts two terms about
-  150x larger than itself at this drift), macroparticles per cell exact.
+  150x larger than itself at this drift), macroparticles per cell exact;
+  a species of uniform weight (no stored weight row) against the oracle.
 * MCC_CEX::apply (ch4/Collisions.cpp:43-80) replaying the reference's
   uniforms (tests/golden/neutral_mcc.npz, two calls on 2000 ions): the same
   particles collide and the velocities match bit for bit.
@@ -58,6 +59,25 @@ def test_moments_gas_properties_mpc(espic):
         one = s.moments
         for q in range(7):
             assert np.max(np.abs(2 * one[q] - ref[q])) <= 1e-12 * np.max(np.abs(ref[q])), q
+
+
+def test_moments_uniform_weights(espic, po):
+    """A species whose particles all carry mpw0 stores no weight row: the
+    moments take mpw0 (checked against the oracle on the same atoms)."""
+    f = golden("neutral_moments")
+    nn = int(np.prod(f["grid"]))
+    P = f["P"].copy()
+    P[6] = 1e12
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    ref = po.sample_moments(g, P).reshape(7, nn)
+    with world_of(espic, f) as w:
+        w.setTime(1e-7, 10)
+        s = espic.Species(w, "O", float(f["mass"]), 0.0, mpw0=1e12, capacity=4096, form=espic.FORM_FP64)
+        s.set_particles(P)
+        s.sampleMoments()
+        mom = s.moments
+        for q in range(7):
+            assert np.max(np.abs(mom[q] - ref[q])) <= 1e-12 * np.max(np.abs(ref[q])), q
 
 
 def mcc_world(espic, f, ions):
