@@ -263,6 +263,21 @@ int espic_compute_mpc(espic_world *w, int sp);
  * the number of colliding particles. */
 int espic_mcc_cex(espic_world *w, int src, int tgt, double dt, const double *u, int64_t nu, const int64_t *p_off,
                   int64_t *collisions);
+/* Species::advance(neutrals, spherium) of a species of charge 0
+ * (ch4/Species.cpp:8-100) with the world's dt: each particle moves for its
+ * time left plus dt; leaving the domain removes it; striking the sphere
+ * re-emits it diffusely at the speed of a 1000 K wall and it moves on for the
+ * time it had used (the reference's arithmetic).  pdt NULL: particles
+ * appended since the last call (sources, loaders, espic_species_set) have
+ * one dt left, as addParticle leaves them (ch4/Species.h:65), the others
+ * none; pdt non-NULL: each particle's time left (one per particle).  u NULL:
+ * particle p draws from the call's counter-based stream; u non-NULL (parity
+ * checks): particle p's k-th uniform is u[p_off[p] + k], 11 per bounce.  The
+ * removal keeps this library's compaction order (the survivors of the
+ * reference's swap-with-last).  bounces (may be NULL; non-NULL waits): sphere
+ * strikes of the call.  Charged species (ch4's ion branch) are refused. */
+int espic_advance_ch4(espic_world *w, int sp, const double *pdt, const double *u, int64_t nu, const int64_t *p_off,
+                      int64_t *bounces);
 /* World::getPE, ch2/World.cpp:72-84 */
 int espic_potential_energy(espic_world *w, double *pe);
 /* The per-step columns of Output::diagOutput, ch3/ver2/Output.cpp:96-132, with

@@ -1298,9 +1298,11 @@ int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const
  * World::sphereDiffuseVector, ch4/World.cpp:185-199), then moves again.
  * The E-field kick is q/m E dt = 0 for a neutral and is left out.  Dead
  * particles are removed by swap-with-last (ch4/Species.cpp:76-89).
- * u: 11 uniforms per bounce (9 of sampleVth(1000), then sin_theta and psi).
- * sphere: centre and radius^2.  Returns the particle count after removal;
- * -1 when u runs out. */
+ * u: 11 uniforms per bounce (9 of sampleVth(1000), then sin_theta and psi);
+ * p_off[p] (may be NULL): the index in u of particle p's first uniform.
+ * sphere: centre and radius^2.  holes != 0 removes the dead in the CUDA
+ * path's order instead.  Returns the particle count after removal; -1 when u
+ * runs out. */
 static double dot3(const double a[3], const double b[3]) {
     double s = 0;
     for (int i = 0; i < 3; i++) s += a[i] * b[i];
@@ -1368,9 +1370,10 @@ static void reflect_diffuse(const double sphere[4], double mass, const double x[
 
 int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double mass, double dt, double *P,
                                int64_t stride, int64_t n, double *pdt, const double *u, int64_t nu,
-                               int64_t *u_used) {
+                               int64_t *u_used, int64_t *p_off, int holes) {
     int64_t k = 0;
     for (int64_t p = 0; p < n; p++) {
+        if (p_off) p_off[p] = k;
         pdt[p] += dt;
         int n_bounces = 0;
         while (pdt[p] > 0 && P[6 * stride + p] > 0) {
@@ -1403,6 +1406,22 @@ int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double 
             if (++n_bounces > 20) P[6 * stride + p] = 0;
         }
     }
+    if (u_used) *u_used = k;
+    if (holes) {
+        /* the CUDA path's order: the r-th dead slot below the new count takes
+         * the r-th live particle at or above it */
+        int64_t alive = 0;
+        for (int64_t p = 0; p < n; p++) alive += P[6 * stride + p] > 0;
+        int64_t hole = 0;
+        for (int64_t src = alive; src < n; src++) {
+            if (!(P[6 * stride + src] > 0)) continue;
+            while (P[6 * stride + hole] > 0) hole++;
+            copy_particle(P, stride, hole, src);
+            pdt[hole] = pdt[src];
+            hole++;
+        }
+        return alive;
+    }
     /* removal: a dead slot takes the last particle and is checked again */
     int64_t np = n;
     for (int64_t p = 0; p < np; p++) {
@@ -1412,7 +1431,6 @@ int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double 
         np--;
         p--;
     }
-    if (u_used) *u_used = k;
     return np;
 }
 

@@ -146,7 +146,7 @@ int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const
  * reflection (ch4/Species.cpp:8-100); pdt: per-particle time left */
 int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double mass, double dt, double *P,
                                int64_t stride, int64_t n, double *pdt, const double *u, int64_t nu,
-                               int64_t *u_used);
+                               int64_t *u_used, int64_t *p_off, int holes);
 
 /* ---- CPU baseline (threaded like ch9/MT) ------------------------------ */
 double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],

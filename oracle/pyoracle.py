@@ -79,7 +79,7 @@ def _sig(L):
     L.eo_mcc_cex.restype = I64
     L.eo_mcc_cex.argtypes = [C.POINTER(Grid), PD, I64, I64, PD, PD, D, PD, I64, PI64, PI64]
     L.eo_advance_ch4_neutral.restype = I64
-    L.eo_advance_ch4_neutral.argtypes = [C.POINTER(Grid), PD, D, D, PD, I64, I64, PD, PD, I64, PI64]
+    L.eo_advance_ch4_neutral.argtypes = [C.POINTER(Grid), PD, D, D, PD, I64, I64, PD, PD, I64, PI64, PI64, C.c_int]
     L.eo_inject_warm.restype = I64
     L.eo_inject_warm.argtypes = [C.POINTER(Grid), PD, D, D, D, D, D, D, D, PD, PI64, PD, I64, I64,
                                  I64]
@@ -305,18 +305,20 @@ def mcc_cex(g, P, den, vel, dt, u):
     return P, int(ncol), used.value, off[:P.shape[1]]
 
 
-def advance_ch4_neutral(g, sphere, mass, dt, P, pdt, u):
+def advance_ch4_neutral(g, sphere, mass, dt, P, pdt, u, holes=False):
     """eo_advance_ch4_neutral on copies of P and pdt: (P, pdt after removal,
-    uniforms used).  sphere: (cx, cy, cz, radius)."""
+    uniforms used, each particle's first uniform index).  sphere: (cx, cy,
+    cz, radius).  holes=True removes the dead in the CUDA path's order."""
     P = np.array(P, dtype=np.float64, order="C", copy=True)
     pdt = np.array(pdt, dtype=np.float64, copy=True)
     u = np.ascontiguousarray(u, dtype=np.float64)
     sph = np.array(list(sphere[:3]) + [sphere[3] ** 2], dtype=np.float64)
     used = C.c_int64(0)
+    off = np.zeros(max(P.shape[1], 1), dtype=np.int64)
     m = lib().eo_advance_ch4_neutral(C.byref(g), pd(sph), mass, dt, pd(P), P.shape[1], P.shape[1], pd(pdt), pd(u),
-                                     u.size, C.byref(used))
+                                     u.size, C.byref(used), off.ctypes.data_as(PI64), 1 if holes else 0)
     assert m >= 0, "uniforms ran out"
-    return np.ascontiguousarray(P[:, :m]), pdt[:m].copy(), used.value
+    return np.ascontiguousarray(P[:, :m]), pdt[:m].copy(), used.value, off[:P.shape[1]]
 
 
 def deposit_fp64(g, P):

@@ -124,6 +124,7 @@ def lib():
             "espic_compute_mpc": [VP, C.c_int],
             "espic_mcc_cex": [VP, C.c_int, C.c_int, C.c_double, PD, I64, C.POINTER(C.c_int64),
                               C.POINTER(C.c_int64)],
+            "espic_advance_ch4": [VP, C.c_int, PD, PD, I64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
             "espic_potential_energy": [VP, PD],
             "espic_diag_row": [VP, PD, C.c_int],
             "espic_update_average": [VP, C.c_int],
@@ -454,6 +455,26 @@ class Species:
         last, total = C.c_int64(), C.c_int64()
         check(lib().espic_dsmc_status(self.world.h, self.id, C.byref(smax), C.byref(last), C.byref(total)))
         return smax.value, last.value, total.value
+
+    def advance_ch4(self, pdt=None, u=None, p_off=None, count=False):
+        """Species::advance(neutrals, spherium) of a neutral species
+        (ch4/Species.cpp:8-100); pdt: each particle's time left (default: a
+        dt for particles appended since the last call); u, p_off: replayed
+        uniforms; count=True (or replay) waits and returns the bounces."""
+        b = C.c_int64(0)
+        pb = C.byref(b) if (count or u is not None or pdt is not None) else None
+        pp = None
+        if pdt is not None:
+            pdt = np.ascontiguousarray(pdt, dtype=np.float64)
+            pp = _pd(pdt)
+        if u is None:
+            check(lib().espic_advance_ch4(self.world.h, self.id, pp, None, 0, None, pb))
+        else:
+            uu = np.ascontiguousarray(u, dtype=np.float64)
+            off = np.ascontiguousarray(p_off, dtype=np.int64)
+            check(lib().espic_advance_ch4(self.world.h, self.id, pp, _pd(uu), uu.size,
+                                          off.ctypes.data_as(C.POINTER(C.c_int64)), pb))
+        return b.value if pb is not None else None
 
     # ch4 species moments (ch4/Species.cpp:191-240, float64 form)
     def sampleMoments(self):

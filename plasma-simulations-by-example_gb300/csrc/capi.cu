@@ -151,7 +151,8 @@ static void free_species(Species *s) {
     void *ptrs[] = {s->P, s->cell, s->cell2, s->off, s->off2, s->vel, s->vel2, s->sort_count, s->deadmask,
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
                     s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum,
-                    s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol};
+                    s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol,
+                    s->ch4_settled, s->ch4_bounces};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -529,6 +530,8 @@ extern "C" int espic_species_set(espic_world *h, int sp, const double *P, int64_
     }
     int64_t cnt[4] = {n, n, 0, 0};
     CK(cudaMemcpyAsync(s.d_count, cnt, sizeof cnt, cudaMemcpyHostToDevice, w.stream));
+    /* for the ch4 push, particles set here have a step's time left */
+    if (s.ch4_settled) CK(cudaMemsetAsync(s.ch4_settled, 0, sizeof(int64_t), w.stream));
     CK(cudaStreamSynchronize(w.stream));
     s.host_bound = n;
     return take_device_errors(w);
@@ -1109,6 +1112,61 @@ extern "C" int espic_mcc_cex(espic_world *h, int src, int tgt, double dt, const 
         *collisions = (int64_t)c;
     }
     if (u || collisions) return take_device_errors(w);
+    return ESPIC_OK;
+}
+
+extern "C" int espic_advance_ch4(espic_world *h, int sp, const double *pdt, const double *u, int64_t nu,
+                                 const int64_t *p_off, int64_t *bounces) {
+    WORLD(h);
+    SPECIES(sp);
+    if (s.form != ESPIC_FORM_FP64) return fail(ESPIC_ERR_ARG, "the ch4 push works on a species in the float64 form");
+    if (s.charge != 0)
+        return fail(ESPIC_ERR_ARG, "the ch4 push of a charged species (ions striking the sphere) is not built");
+    if (!(w.dt > 0)) return fail(ESPIC_ERR_ARG, "set the time step first");
+    if (u && (!p_off || nu < 0)) return fail(ESPIC_ERR_ARG, "replayed uniforms need their particle offsets");
+    if (!s.ch4_settled) {
+        if (dalloc(&s.ch4_settled, 1) != ESPIC_OK || dalloc(&s.ch4_bounces, 1) != ESPIC_OK) return ESPIC_ERR_CUDA;
+        CK(cudaMemsetAsync(s.ch4_settled, 0, sizeof(int64_t), w.stream));
+    }
+    double *dpdt = nullptr, *du = nullptr;
+    int64_t *doff = nullptr;
+    const bool staged = pdt || u;
+    if (staged) {
+        int64_t np = 0; /* pdt and p_off hold one entry per particle: the exact count */
+        CK(cudaMemcpyAsync(&np, s.d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaStreamSynchronize(w.stream));
+        s.host_bound = np;
+        const int64_t m = np > 0 ? np : 1;
+        bool ok = true;
+        if (pdt) ok = ok && dalloc(&dpdt, m) == ESPIC_OK;
+        if (u) ok = ok && dalloc(&du, nu > 0 ? nu : 1) == ESPIC_OK && dalloc(&doff, m) == ESPIC_OK;
+        if (!ok) {
+            if (dpdt) cudaFree(dpdt);
+            if (du) cudaFree(du);
+            if (doff) cudaFree(doff);
+            return ESPIC_ERR_CUDA;
+        }
+        if (pdt && np > 0) cudaMemcpyAsync(dpdt, pdt, np * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        if (u && nu > 0) cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        if (u && np > 0) cudaMemcpyAsync(doff, p_off, np * sizeof(int64_t), cudaMemcpyHostToDevice, w.stream);
+    }
+    {
+        PhaseScope ph(w, ESPIC_PHASE_PUSH);
+        launch_advance_ch4(w, s, w.dt, dpdt, du, nu, doff);
+    }
+    cudaError_t e = cudaSuccess;
+    if (staged || bounces) e = cudaStreamSynchronize(w.stream);
+    if (dpdt) cudaFree(dpdt);
+    if (du) cudaFree(du);
+    if (doff) cudaFree(doff);
+    if (e != cudaSuccess) return fail(ESPIC_ERR_CUDA, "%s", cudaGetErrorString(e));
+    CHECK_LAUNCH();
+    if (bounces) {
+        unsigned long long c = 0;
+        CK(cudaMemcpy(&c, s.ch4_bounces, sizeof c, cudaMemcpyDeviceToHost));
+        *bounces = (int64_t)c;
+    }
+    if (staged || bounces) return take_device_errors(w);
     return ESPIC_OK;
 }
 

@@ -137,6 +137,9 @@ void launch_gas_props(World &w, Species &s);
 void launch_mpc(World &w, Species &s);
 void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const double *d_u, int64_t nu,
                 const int64_t *d_off, unsigned long long *d_ncol);
+/* ch4 Species::advance of a neutral species (sphere diffuse reflection) */
+void launch_advance_ch4(World &w, Species &s, double dt, const double *d_pdt, const double *d_u, int64_t nu,
+                        const int64_t *d_off);
 void launch_inv_vol(World &w);
 void launch_charge(World &w);
 void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3,

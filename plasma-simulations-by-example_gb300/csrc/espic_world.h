@@ -58,6 +58,11 @@ struct Species {
     double *mom = nullptr, *mom_scale = nullptr, *gvel = nullptr, *gtemp = nullptr, *mpc = nullptr;
     unsigned long long *mom_acc = nullptr, *mom_bound = nullptr, *mcc_ncol = nullptr;
     uint64_t mcc_calls = 0;
+    /* ch4 neutral push: particles below *ch4_settled have used their time
+     * (those above were appended since the last push), bounces of the call */
+    int64_t *ch4_settled = nullptr;
+    unsigned long long *ch4_bounces = nullptr;
+    uint64_t ch4_calls = 0;
 };
 
 struct Source {

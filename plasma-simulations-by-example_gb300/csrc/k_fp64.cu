@@ -20,6 +20,7 @@
 #include <limits.h>
 #include <stdio.h>
 
+#include "ch4_push.h"
 #include "espic_world.h"
 
 namespace cg = cooperative_groups;
@@ -2064,6 +2065,101 @@ void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const dou
         w.nlaunch++;
     }
     src.mcc_calls++;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ch4 neutral push (ch4_push.h): one thread per particle; particles that
+ * leave the domain go to the dead mask and the compaction of the other
+ * pushes removes them (the reference's swap-with-last order is not kept;
+ * same survivors).  Time of each particle: pdt[p] + dt when the caller gives
+ * the particles' time left, else 2 dt for particles appended since the last
+ * call (a source's addParticle leaves them one dt, ch4/Species.h:65) and dt
+ * for the others.  Uniforms: u[p_off[p] + k] when replaying, else index
+ * (p << 10) + k of the call's counter-based stream (k < 715). */
+struct Ch4Uniforms {
+    const double *u;
+    int64_t nu, base;
+    uint64_t seed, stream, index0;
+    bool bad;
+    __device__ double operator()(int k) {
+        if (u) {
+            const int64_t o = base + k;
+            if (o < 0 || o >= nu) {
+                bad = true;
+                return 0.5;
+            }
+            return u[o];
+        }
+        return philox_uniform(seed, stream, index0 + (uint64_t)k);
+    }
+};
+
+__global__ void __launch_bounds__(256) k_advance_ch4(Ch4Geo G, double mass, double dt, double *P, int64_t stride,
+                                                     const int64_t *__restrict__ d_count,
+                                                     const int64_t *__restrict__ d_settled,
+                                                     const double *__restrict__ pdt, const double *__restrict__ u,
+                                                     int64_t nu, const int64_t *__restrict__ p_off, uint64_t seed,
+                                                     uint64_t stream, uint32_t *deadmask, int32_t *tiledead,
+                                                     unsigned long long *nbounce, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = d_count[0];
+    bool dead = false;
+    int b = 0;
+    if (p < n) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        const double t = (pdt ? pdt[p] : (p >= d_settled[0] ? dt : 0.0)) + dt;
+        Ch4Uniforms U{u, nu, u ? p_off[p] : 0, seed, stream, (uint64_t)p << 10, false};
+        bool alive = true;
+        b = ch4_advance_one(G, mass, t, x, v, U, alive, 64);
+        if (U.bad) atomicOr(err, DERR_NEUTRAL);
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+            atomicOr(err, DERR_NONFINITE);
+            alive = false;
+        }
+        dead = !alive;
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + p] = x[d];
+            P[(3 + d) * stride + p] = v[d];
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, dead);
+    int bs = b;
+    for (int o = 16; o; o >>= 1) bs += __shfl_xor_sync(0xffffffffu, bs, o);
+    if ((threadIdx.x & 31) == 0 && p < n) {
+        deadmask[p >> 5] = m;
+        if (m) atomicAdd(tiledead + (p / TILE_PARTICLES), __popc(m));
+        if (bs) atomicAdd(nbounce, (unsigned long long)bs);
+    }
+}
+
+/* every particle left after the compaction has used its time */
+__global__ void k_ch4_settle(const int64_t *d_count, int64_t *d_settled) { d_settled[0] = d_count[0]; }
+
+void launch_advance_ch4(World &w, Species &s, double dt, const double *d_pdt, const double *d_u, int64_t nu,
+                        const int64_t *d_off) {
+    cudaMemsetAsync(s.ch4_bounces, 0, sizeof(unsigned long long), w.stream);
+    const int64_t n = s.host_bound;
+    if (n > 0) {
+        Ch4Geo G;
+        for (int d = 0; d < 3; d++) {
+            G.x0[d] = w.g.x0[d];
+            G.xm[d] = w.g.xm[d];
+            G.sph[d] = w.sphere[d];
+        }
+        G.sph[3] = w.has_sphere ? w.sphere[3] : -1.0;
+        /* one stream per (species, call) */
+        const uint64_t stream = (0xC4ull << 56) | ((uint64_t)(s.id & 0xff) << 48) |
+                                (s.ch4_calls & 0xffffffffffffull);
+        k_advance_ch4<<<blocks_for(n, 256), 256, 0, w.stream>>>(G, s.mass, dt, s.P, s.cap, s.d_count, s.ch4_settled,
+                                                                 d_pdt, d_u, nu, d_off, w.seed, stream, s.deadmask,
+                                                                 s.tiledead, s.ch4_bounces, w.d_err);
+        w.nlaunch++;
+        launch_compact(w, s);
+    }
+    k_ch4_settle<<<1, 1, 0, w.stream>>>(s.d_count, s.ch4_settled);
+    w.nlaunch++;
+    s.ch4_calls++;
 }
 
 }  // namespace espic

@@ -311,8 +311,8 @@ def test_ch4_neutral_push_bitexact(po):
     sph = f["sphere"]
     P, pdt, off, bounces = f["P0"], f["dt0"], 0, 0
     for _ in range(int(f["steps"])):
-        P, pdt, used = po.advance_ch4_neutral(g, tuple(sph[:4]), float(f["mass"]), float(f["dt"]), P, pdt,
-                                              f["u"][off:])
+        P, pdt, used, _ = po.advance_ch4_neutral(g, tuple(sph[:4]), float(f["mass"]), float(f["dt"]), P, pdt,
+                                                 f["u"][off:])
         off += used
         bounces += used // 11
     assert bounces > 50 and off == f["u"].size
