@@ -1,6 +1,7 @@
 /*
  * Species.h (drop-in) -- the Species class of the reference
- * (ch2/Species.h:22-65, ch3/ver2/Species.h:22-72) on libespic.
+ * (ch2/Species.h:22-65, ch3/ver2/Species.h:22-72, ch4/Species.h:22-96) on
+ * libespic.
  *
  * The particles live on the GPU.  The public `particles` member is a host
  * mirror with the std::vector<Particle> operations the reference's code uses;
@@ -84,6 +85,14 @@ public:
     /* ch4/Species.cpp:149-175 */
     double sampleVth(double T);
     double3 sampleIsotropicVel(double T);
+    /* ch4 (ch4/Species.h:47-62): the push of a neutral species with the
+     * sphere's diffuse reflection (charged species: not built), moments,
+     * gas properties and macroparticles per cell */
+    void advance(Species &neutrals, Species &spherium);
+    void sampleMoments();
+    void computeGasProperties();
+    void computeMPC();
+    void clearSamples();
 
     const std::string name;
     const double mass;
@@ -93,10 +102,14 @@ public:
     ParticleVector particles;
     Field den;
     Field den_ave;
+    Field T;    /* ch4: temperature (computeGasProperties) */
+    Field3 vel; /* ch4: stream velocity */
+    Field mpc;  /* ch4: macroparticles per cell, (ni-1)(nj-1)(nk-1) */
 
     /* ---- libespic plumbing ---- */
     int id() const { return sid; }
     void settle();               /* run a pending push, push host particle edits */
+    void particles_changed();    /* device work moved or changed the particles */
     void pull_particles(std::vector<Particle> &out);
     World &get_world() { return world; }
 

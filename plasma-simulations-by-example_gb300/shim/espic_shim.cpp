@@ -20,6 +20,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "Collisions.h"
 #include "Output.h"
 #include "PotentialSolver.h"
 #include "Source.h"
@@ -211,20 +212,22 @@ std::vector<Particle> &ParticleVector::host() {
 
 Species::Species(std::string name, double mass, double charge, World &world)
     : name(name), mass(mass), charge(charge), mpw0(0), den(world.ni, world.nj, world.nk),
-      den_ave(world.ni, world.nj, world.nk), world(world) {
+      den_ave(world.ni, world.nj, world.nk), T(world.ni, world.nj, world.nk), vel(world.ni, world.nj, world.nk),
+      mpc(world.ni - 1, world.nj - 1, world.nk - 1), world(world) {
     create(ESPIC_WALLS_REFLECT);
 }
 
 Species::Species(std::string name, double mass, double charge, double mpw0, World &world)
     : name(name), mass(mass), charge(charge), mpw0(mpw0), den(world.ni, world.nj, world.nk),
-      den_ave(world.ni, world.nj, world.nk), world(world) {
+      den_ave(world.ni, world.nj, world.nk), T(world.ni, world.nj, world.nk), vel(world.ni, world.nj, world.nk),
+      mpc(world.ni - 1, world.nj - 1, world.nk - 1), world(world) {
     create(ESPIC_WALLS_ABSORB);
 }
 
 Species::Species(Species &&o) noexcept
     : name(o.name), mass(o.mass), charge(o.charge), mpw0(o.mpw0), particles(std::move(o.particles)),
-      den(std::move(o.den)), den_ave(std::move(o.den_ave)), world(o.world), sid(o.sid),
-      push_pending(o.push_pending), diag_valid(o.diag_valid) {
+      den(std::move(o.den)), den_ave(std::move(o.den_ave)), T(std::move(o.T)), vel(std::move(o.vel)),
+      mpc(std::move(o.mpc)), world(o.world), sid(o.sid), push_pending(o.push_pending), diag_valid(o.diag_valid) {
     particles.owner = this;
     memcpy(diag, o.diag, sizeof diag);
     o.sid = -1;
@@ -255,6 +258,23 @@ void Species::bind_fields() {
         [hh, n, s](const void *d) {
             ck(espic_field_write(hh, ESPIC_FIELD_DEN_AVE, s, (const double *)d, n), "write den_ave");
         });
+    /* ch4 fields: the device copies exist once first used (float64 form) */
+    T.bind([hh, n, s](void *d) { ck(espic_field_read(hh, ESPIC_FIELD_TEMP, s, (double *)d, n), "read T"); },
+           [hh, n, s](const void *d) { ck(espic_field_write(hh, ESPIC_FIELD_TEMP, s, (const double *)d, n), "write T"); });
+    vel.bind([hh, n, s](void *d) { ck(espic_field_read(hh, ESPIC_FIELD_VEL, s, (double *)d, 3 * n), "read vel"); },
+             [hh, n, s](const void *d) {
+                 ck(espic_field_write(hh, ESPIC_FIELD_VEL, s, (const double *)d, 3 * n), "write vel");
+             });
+    int64_t nc = (int64_t)(world.ni - 1) * (world.nj - 1) * (world.nk - 1);
+    mpc.bind([hh, nc, s](void *d) { ck(espic_field_read(hh, ESPIC_FIELD_MPC, s, (double *)d, nc), "read mpc"); },
+             [hh, nc, s](const void *d) {
+                 ck(espic_field_write(hh, ESPIC_FIELD_MPC, s, (const double *)d, nc), "write mpc");
+             });
+}
+
+void Species::particles_changed() {
+    particles.host_valid = false;
+    diag_valid = false;
 }
 
 /* run a pending push and send host edits of the particle mirror */
@@ -381,6 +401,72 @@ void Species::updateAverages() {
     den_ave.push();
     ck(espic_update_average(world.handle(), sid), "espic_update_average");
     den_ave.device_written();
+}
+
+/* ch4 Species::advance(neutrals, spherium), ch4/Species.cpp:8-100: the
+ * neutral branch runs on the GPU; the ion branch (ions striking the sphere
+ * become neutrals and sputter) is not built */
+void Species::advance(Species &, Species &) {
+    if (charge != 0) throw std::runtime_error("Species::advance(neutrals, spherium) of a charged species is not built");
+    settle();
+    world.push_host_edits();
+    ck(espic_advance_ch4(world.handle(), sid, nullptr, nullptr, 0, nullptr, nullptr), "espic_advance_ch4");
+    particles_changed();
+}
+
+/* Species::sampleMoments / computeGasProperties / computeMPC / clearSamples,
+ * ch4/Species.cpp:191-240 */
+void Species::sampleMoments() {
+    settle();
+    ck(espic_sample_moments(world.handle(), sid), "espic_sample_moments");
+}
+
+void Species::computeGasProperties() {
+    T.push();
+    vel.push();
+    ck(espic_gas_properties(world.handle(), sid), "espic_gas_properties");
+    T.device_written();
+    vel.device_written();
+}
+
+void Species::computeMPC() {
+    settle();
+    mpc.push();
+    ck(espic_compute_mpc(world.handle(), sid), "espic_compute_mpc");
+    mpc.device_written();
+}
+
+void Species::clearSamples() { ck(espic_clear_samples(world.handle(), sid), "espic_clear_samples"); }
+
+/* ------------------------------------------------------------ Collisions */
+void MCC_CEX::apply(double dt) {
+    source.settle();
+    target.settle();
+    target.den.push();
+    target.vel.push();
+    world.push_host_edits();
+    ck(espic_mcc_cex(world.handle(), source.id(), target.id(), dt, nullptr, 0, nullptr, nullptr), "espic_mcc_cex");
+    source.particles_changed();
+}
+
+DSMC_MEX::DSMC_MEX(Species &species, World &world) : species{species}, world{world} {
+    ck(espic_dsmc_enable(world.handle(), species.id(), nullptr, 1e-14), "espic_dsmc_enable");
+}
+
+void DSMC_MEX::apply(double dt) {
+    species.settle();
+    ck(espic_dsmc_apply(world.handle(), species.id(), dt, nullptr, 0, nullptr), "espic_dsmc_apply");
+    species.particles_changed();
+}
+
+double DSMC_MEX::sigmaCrMax() {
+    double s = 0;
+    ck(espic_dsmc_status(world.handle(), species.id(), &s, nullptr, nullptr), "espic_dsmc_status");
+    return s;
+}
+
+void ChemistryIonize::apply(double) {
+    throw std::runtime_error("ChemistryIonize is not built in libespic");
 }
 
 /* Species::sampleVth / sampleIsotropicVel, ch4/Species.cpp:149-175 (host) */

@@ -2,8 +2,8 @@
 API build with the headers in plasma-simulations-by-example_gb300/shim/ and
 run on the GPU through libespic.
 
-* CPU: the reference's own ch2/Main.cpp and ch3/ver2/Main.cpp compile and
-  link unchanged (fed on stdin, so their directory's headers are not seen);
+* CPU: the reference's own ch2/Main.cpp, ch3/ver2/Main.cpp and ch4/Main.cpp
+  compile and link unchanged (fed on stdin, so their directory's headers are not seen);
   without a GPU they stop with the library's "no CUDA device" error.
 * GPU: drop-in programs of this repository give, step for step, the same
   diagnostics as the same calls made through the C-ABI from Python.
@@ -20,7 +20,7 @@ REF = os.environ.get("ESPIC_REFERENCE", "/root/reference")
 DROP = os.path.join(ROOT, "tests", "drop_in")
 
 
-@pytest.mark.parametrize("chapter", ["ch2", "ch3/ver2"])
+@pytest.mark.parametrize("chapter", ["ch2", "ch3/ver2", "ch4"])
 def test_reference_main_compiles_unchanged(tmp_path, chapter):
     src = os.path.join(REF, chapter, "Main.cpp")
     if not os.path.exists(src):
