@@ -94,6 +94,8 @@ public:
     bool inSphere(double3 x);
     void addInlet();
     bool steadyState(std::vector<Species> &species);
+    /* ch4/World.h:76 */
+    bool isSteadyState() const { return steady_state; }
 
     /* ch9/MT/World.h: the thread count is accepted and ignored on the GPU */
     void setNumThreads(int n) { num_threads = n; }

@@ -30,6 +30,10 @@
 
 Rnd rnd;
 
+/* set once the program uses the ch4 species API: Output::fields then writes
+ * ch4's file layout (ch4/Output.cpp:11-119) */
+static bool g_ch4_layout = false;
+
 static void ck(int rc, const char *what) {
     if (rc >= 0) return;
     char msg[512];
@@ -408,6 +412,7 @@ void Species::updateAverages() {
  * become neutrals and sputter) is not built */
 void Species::advance(Species &, Species &) {
     if (charge != 0) throw std::runtime_error("Species::advance(neutrals, spherium) of a charged species is not built");
+    g_ch4_layout = true;
     settle();
     world.push_host_edits();
     ck(espic_advance_ch4(world.handle(), sid, nullptr, nullptr, 0, nullptr, nullptr), "espic_advance_ch4");
@@ -417,11 +422,13 @@ void Species::advance(Species &, Species &) {
 /* Species::sampleMoments / computeGasProperties / computeMPC / clearSamples,
  * ch4/Species.cpp:191-240 */
 void Species::sampleMoments() {
+    g_ch4_layout = true;
     settle();
     ck(espic_sample_moments(world.handle(), sid), "espic_sample_moments");
 }
 
 void Species::computeGasProperties() {
+    g_ch4_layout = true;
     T.push();
     vel.push();
     ck(espic_gas_properties(world.handle(), sid), "espic_gas_properties");
@@ -430,6 +437,7 @@ void Species::computeGasProperties() {
 }
 
 void Species::computeMPC() {
+    g_ch4_layout = true;
     settle();
     mpc.push();
     ck(espic_compute_mpc(world.handle(), sid), "espic_compute_mpc");
@@ -440,6 +448,7 @@ void Species::clearSamples() { ck(espic_clear_samples(world.handle(), sid), "esp
 
 /* ------------------------------------------------------------ Collisions */
 void MCC_CEX::apply(double dt) {
+    g_ch4_layout = true;
     source.settle();
     target.settle();
     target.den.push();
@@ -450,6 +459,7 @@ void MCC_CEX::apply(double dt) {
 }
 
 DSMC_MEX::DSMC_MEX(Species &species, World &world) : species{species}, world{world} {
+    g_ch4_layout = true;
     ck(espic_dsmc_enable(world.handle(), species.id(), nullptr, 1e-14), "espic_dsmc_enable");
 }
 
@@ -701,9 +711,75 @@ void fields_sync(World &world, std::vector<Species> &species) {
     out << "</PointData>\n</ImageData>\n</VTKFile>\n";
 }
 
+/* ch4's layout (ch4/Output.cpp:11-119): gas properties first, the stream
+ * velocity and temperature of every species among the node data, the
+ * macroparticles per cell as cell data, and the samples cleared until the
+ * steady state */
+void fields_ch4(World &world, std::vector<Species> &species) {
+    for (Species &sp : species) sp.computeGasProperties();
+    std::stringstream name;
+    name << "results/fields_" << std::setfill('0') << std::setw(5) << world.getTs() << ".vti";
+    std::ofstream out(name.str());
+    if (!out.is_open()) {
+        std::cerr << "Could not open " << name.str() << std::endl;
+        return;
+    }
+    double3 x0 = world.getX0(), dh = world.getDh();
+    out << "<VTKFile type=\"ImageData\">\n";
+    out << "<ImageData Origin=\"" << x0[0] << " " << x0[1] << " " << x0[2] << "\" ";
+    out << "Spacing=\"" << dh[0] << " " << dh[1] << " " << dh[2] << "\" ";
+    out << "WholeExtent=\"0 " << world.ni - 1 << " 0 " << world.nj - 1 << " 0 " << world.nk - 1 << "\">\n";
+    out << "<PointData>\n";
+    auto array = [&out](const std::string &nm, int comps, const char *type) {
+        out << "<DataArray Name=\"" << nm << "\" NumberOfComponents=\"" << comps << "\" format=\"ascii\" type=\""
+            << type << "\">\n";
+    };
+    array("object_id", 1, "Int32");
+    out << world.object_id << "</DataArray>\n";
+    array("NodeVol", 1, "Float64");
+    out << world.node_vol << "</DataArray>\n";
+    array("phi", 1, "Float64");
+    out << world.phi << "</DataArray>\n";
+    array("rho", 1, "Float64");
+    out << world.rho << "</DataArray>\n";
+    for (Species &sp : species) {
+        array("nd." + sp.name, 1, "Float64");
+        out << sp.den << "</DataArray>\n";
+    }
+    for (Species &sp : species) {
+        array("nd-ave." + sp.name, 1, "Float64");
+        out << sp.den_ave << "</DataArray>\n";
+    }
+    for (Species &sp : species) {
+        array("vel." + sp.name, 3, "Float64");
+        out << sp.vel << "</DataArray>\n";
+    }
+    for (Species &sp : species) {
+        array("T." + sp.name, 1, "Float64");
+        out << sp.T << "</DataArray>\n";
+    }
+    array("ef", 3, "Float64");
+    out << world.ef << "</DataArray>\n";
+    out << "</PointData>\n";
+    out << "<CellData>\n";
+    for (Species &sp : species) {
+        array("mpc." + sp.name, 1, "Float64");
+        out << sp.mpc << "</DataArray>\n";
+    }
+    out << "</CellData>\n";
+    out << "</ImageData>\n</VTKFile>\n";
+    out.close();
+    if (!world.isSteadyState())
+        for (Species &sp : species) sp.clearSamples();
+}
+
 }  // namespace
 
 void Output::fields(World &world, std::vector<Species> &species) {
+    if (g_ch4_layout) {
+        fields_ch4(world, species);
+        return;
+    }
     const char *sync = std::getenv("ESPIC_OUTPUT_SYNC");
     if (sync && sync[0] == '1') {
         fields_sync(world, species);
