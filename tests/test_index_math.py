@@ -77,3 +77,45 @@ def test_dsmc_cell_index():
             assert np.array_equal(got, want), (x0, xm, n)
         if ax[2] < 1:
             assert dsmc_coord(x, x0, dh, ax)[2].mean() > 0.99
+
+
+def warp_bitonic(vals, R):
+    """numpy emulation of warp_bitonic<R> in csrc/k_fp64.cu: element
+    i*32 + lane held in a[i] of that lane; exchanges between lanes by
+    shuffles (j < 32), within a lane by swaps (j >= 32); INT_MAX pads"""
+    a = np.full((R, 32), 2**31 - 1, dtype=np.int64)
+    for e, v in enumerate(vals):
+        a[e // 32, e % 32] = v
+    lanes = np.arange(32)
+    k = 2
+    while k <= 32 * R:
+        j = k >> 1
+        while j > 0:
+            if j >= 32:
+                jj = j >> 5
+                for i in range(R):
+                    if i & jj == 0:
+                        up = ((i * 32 + lanes) & k) == 0
+                        x, y = a[i].copy(), a[i | jj].copy()
+                        sw = np.where(up, x > y, x < y)
+                        a[i], a[i | jj] = np.where(sw, y, x), np.where(sw, x, y)
+            else:
+                for i in range(R):
+                    y = a[i][lanes ^ j]
+                    lower = (lanes & j) == 0
+                    up = ((i * 32 + lanes) & k) == 0
+                    a[i] = np.where(lower == up, np.minimum(a[i], y), np.maximum(a[i], y))
+            j >>= 1
+        k <<= 1
+    return [int(a[e // 32, e % 32]) for e in range(len(vals))]
+
+
+def test_warp_bitonic_sorts_every_size():
+    """the DSMC cell order (k_dsmc_order): each register count R = 1..32
+    sorts lists of 2..32R distinct particle indices ascending"""
+    rng = np.random.default_rng(1024)
+    for R in (1, 2, 4, 8, 16, 32):
+        sizes = {2, 16 * R + 1 if R > 1 else 3, 32 * R, int(rng.integers(2, 32 * R + 1))}
+        for n in sizes:
+            v = rng.choice(1 << 24, n, replace=False)
+            assert warp_bitonic(list(v), R) == sorted(v), (R, n)
