@@ -15,8 +15,8 @@ import numpy as np
 import pytest
 
 from conftest import ROOT, _espic_module
+from oracle.build_ref import REFERENCE as REF  # the reference checkout, where present
 
-REF = os.environ.get("ESPIC_REFERENCE", "/root/reference")
 DROP = os.path.join(ROOT, "tests", "drop_in")
 
 
