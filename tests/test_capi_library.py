@@ -46,3 +46,28 @@ def test_world_create_fails_loudly_without_gpu(libpath):
     with pytest.raises(mod.EspicError) as e:
         mod.World(5, 5, 5, [0, 0, 0], [1, 1, 1])
     assert "no CUDA device" in str(e.value) or e.value.code == -2
+
+
+def test_entry_points_refuse_a_null_world(libpath):
+    """The ch4 entry points (DSMC, moments, MCC, neutral push) return an
+    argument error with a message for a null world handle, on any host."""
+    L = ctypes.CDLL(libpath)
+    L.espic_last_error.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    null = ctypes.c_void_p(None)
+    calls = {
+        "espic_dsmc_enable": (null, 0, None, ctypes.c_double(1e-14)),
+        "espic_dsmc_apply": (null, 0, ctypes.c_double(1e-7), None, ctypes.c_int64(0), None),
+        "espic_dsmc_status": (null, 0, None, None, None),
+        "espic_sample_moments": (null, 0),
+        "espic_gas_properties": (null, 0),
+        "espic_clear_samples": (null, 0),
+        "espic_compute_mpc": (null, 0),
+        "espic_mcc_cex": (null, 0, 1, ctypes.c_double(1e-7), None, ctypes.c_int64(0), None, None),
+        "espic_advance_ch4": (null, 0, None, None, ctypes.c_int64(0), None, None),
+    }
+    for name, args in calls.items():
+        rc = getattr(L, name)(*args)
+        assert rc < 0, name
+        buf = ctypes.create_string_buffer(256)
+        L.espic_last_error(buf, 256)
+        assert b"null world" in buf.value, (name, buf.value)
