@@ -16,6 +16,9 @@ namespace Output {
 void fields(World &world, std::vector<Species> &species);
 void screenOutput(World &world, std::vector<Species> &species);
 void diagOutput(World &world, std::vector<Species> &species);
+/* ch4/Output.cpp:175-228: about num_parts particles per species as VTK
+ * PolyData (positions, velocities) */
+void particles(World &world, std::vector<Species> &species, int num_parts);
 }  // namespace Output
 
 #endif

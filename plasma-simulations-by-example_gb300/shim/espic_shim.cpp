@@ -829,6 +829,49 @@ void Output::screenOutput(World &world, std::vector<Species> &species) {
     std::cout << std::endl;
 }
 
+/* Output::particles, ch4/Output.cpp:175-228: every particle past a running
+ * counter of num_parts / np, from the host mirror of the species */
+void Output::particles(World &world, std::vector<Species> &species, int num_parts) {
+    for (Species &sp : species) {
+        std::stringstream name;
+        name << "results/parts_" << sp.name << "_" << std::setfill('0') << std::setw(5) << world.getTs() << ".vtp";
+        std::ofstream out(name.str());
+        if (!out.is_open()) {
+            std::cerr << "Could not open " << name.str() << std::endl;
+            return;
+        }
+        double dp = num_parts / (double)sp.getNp();
+        double counter = 0;
+        std::vector<Particle *> to_output;
+        for (Particle &part : sp.particles) {
+            counter += dp;
+            if (counter > 1) {
+                to_output.emplace_back(&part);
+                counter = -1;
+            }
+        }
+        out << "<?xml version=\"1.0\"?>\n";
+        out << "<VTKFile type=\"PolyData\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+        out << "<PolyData>\n";
+        out << "<Piece NumberOfPoints=\"" << to_output.size() << "\" NumberOfVerts=\"0\" NumberOfLines=\"0\" ";
+        out << "NumberOfStrips=\"0\" NumberOfCells=\"0\">\n";
+        out << "<Points>\n";
+        out << "<DataArray type=\"Float64\" NumberOfComponents=\"3\" format=\"ascii\">\n";
+        for (Particle *part : to_output) out << part->pos << "\n";
+        out << "</DataArray>\n";
+        out << "</Points>\n";
+        out << "<PointData>\n";
+        out << "<DataArray Name=\"vel." << sp.name << "\" type=\"Float64\" NumberOfComponents=\"3\" format=\"ascii\">\n";
+        for (Particle *part : to_output) out << part->vel << "\n";
+        out << "</DataArray>\n";
+        out << "</PointData>\n";
+        out << "</Piece>\n";
+        out << "</PolyData>\n";
+        out << "</VTKFile>\n";
+        out.close();
+    }
+}
+
 /* Output::diagOutput, ch3/ver2/Output.cpp:96-132: runtime_diags.csv */
 void Output::diagOutput(World &world, std::vector<Species> &species) {
     if (!f_diag.is_open()) {

@@ -115,3 +115,19 @@ def test_drop_in_output_async_matches_inline(tmp_path, espic):
     assert files["async"] == files["sync"]
     body = files["async"][sorted(files["async"])[-1]].decode()
     assert body.startswith("<VTKFile type=\"ImageData\">") and body.count("<DataArray") == 7
+
+
+def test_ch4_main_with_particle_output_compiles(tmp_path):
+    """ch4/Main.cpp with its commented-out Output::particles call restored
+    (ch4/Main.cpp:109) still compiles against the drop-in headers."""
+    src = os.path.join(REF, "ch4", "Main.cpp")
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present")
+    text = open(src).read()
+    call = "//\tOutput::particles(world, species,10000);"
+    assert call in text
+    edited = tmp_path / "main_particles.cpp"
+    edited.write_text(text.replace(call, "Output::particles(world, species,10000);"))
+    E = _espic_module()
+    r = E.compile_drop_in(str(edited), str(tmp_path / "main"), stdin_source=True)
+    assert r.returncode == 0, r.stderr[-2000:]
