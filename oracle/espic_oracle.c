@@ -1434,6 +1434,106 @@ int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double 
     return np;
 }
 
+/* ch4 ion push: Species::advance(neutrals, spherium) for a charged species,
+ * ch4/Species.cpp:8-91.  The E kick uses the particle's whole time left
+ * (v += E (dt q / m)); a particle leaving the domain is killed; one landing
+ * in the sphere is put 0.999 of the way to the intersection and killed, and
+ * creates (int)(mpw0 / neutral mpw0 + U) neutrals and, above 5000 m/s,
+ * (int)(0.1 mpw0 / spherium mpw0 + U) sputtered particles, each with the
+ * diffusely reflected velocity of sampleReflectedVelocity (the ion's mass in
+ * sampleVth) through Species::addParticle (ch4/Species.cpp:103-119: rejected
+ * outside the domain, velocity rewound by the target's q/m E dt/2, one dt
+ * of time left).  New particles go to Q [7][max_new] in creation order with
+ * tag 0 (neutral) or 1 (spherium), their time left in qdt.  Uniform order
+ * per strike: the neutral count, 11 per neutral, the sputter count, 11 per
+ * sputtered particle.  Returns the ion count after swap-with-last removal;
+ * -1 when u runs out, -2 when Q is full. */
+int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphere[4], double charge, double mass,
+                           double mpw0, double dt, double *P, int64_t stride, int64_t n, double *pdt,
+                           double neu_mpw0, double neu_charge, double neu_mass, double sph_mpw0, double sph_charge,
+                           double sph_mass, double *Q, int64_t max_new, int32_t *tag, double *qdt, int64_t *n_new,
+                           const double *u, int64_t nu, int64_t *u_used) {
+    int64_t k = 0, m = 0;
+    for (int64_t p = 0; p < n; p++) {
+        pdt[p] += dt;
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]}, lc[3], e[3];
+        eo_xtol(g, x, lc);
+        eo_gather3(g, ef, lc, e);
+        const double s = pdt[p] * charge / mass;
+        for (int i = 0; i < 3; i++) P[(3 + i) * stride + p] += e[i] * s;
+        int n_bounces = 0;
+        while (pdt[p] > 0 && P[6 * stride + p] > 0) {
+            double old[3], v[3];
+            for (int i = 0; i < 3; i++) {
+                old[i] = P[i * stride + p];
+                v[i] = P[(3 + i) * stride + p];
+                x[i] = old[i] + v[i] * pdt[p];
+                P[i * stride + p] = x[i];
+            }
+            if (!eo_in_bounds(g, x)) {
+                P[6 * stride + p] = 0;
+            } else if (in_sphere_ch4(sphere, x)) {
+                const double tp = line_sphere(sphere, old, x);
+                const double dt_rem = (1 - tp) * pdt[p];
+                pdt[p] -= dt_rem;
+                const double sc = 0.999 * tp;
+                for (int i = 0; i < 3; i++) {
+                    x[i] = old[i] + sc * (x[i] - old[i]);
+                    P[i * stride + p] = x[i];
+                }
+                const double v_mag1 = sqrt(dot3(v, v));
+                P[6 * stride + p] = 0;
+                for (int kind = 0; kind < 2; kind++) {
+                    double ratio;
+                    if (kind == 0) {
+                        ratio = mpw0 / neu_mpw0;
+                    } else {
+                        const double sput_yield = (v_mag1 > 5000) ? 0.1 : 0;
+                        ratio = sput_yield * mpw0 / sph_mpw0;
+                    }
+                    if (k >= nu) return -1;
+                    const int create = (int)(ratio + u[k++]);
+                    const double tq = kind == 0 ? neu_charge : sph_charge, tm = kind == 0 ? neu_mass : sph_mass;
+                    const double tw = kind == 0 ? neu_mpw0 : sph_mpw0;
+                    for (int c = 0; c < create; c++) {
+                        if (k + 11 > nu) return -1;
+                        double vel[3];
+                        reflect_diffuse(sphere, mass, x, v_mag1, u + k, vel);
+                        k += 11;
+                        if (!eo_in_bounds(g, x)) continue;
+                        if (m >= max_new) return -2;
+                        double lc2[3], e2[3];
+                        eo_xtol(g, x, lc2);
+                        eo_gather3(g, ef, lc2, e2);
+                        for (int i = 0; i < 3; i++) {
+                            Q[i * max_new + m] = x[i];
+                            Q[(3 + i) * max_new + m] = vel[i] - tq / tm * e2[i] * (0.5 * dt);
+                        }
+                        Q[6 * max_new + m] = tw;
+                        tag[m] = kind;
+                        qdt[m] = dt;
+                        m++;
+                    }
+                }
+                continue;
+            }
+            pdt[p] = 0;
+            if (++n_bounces > 20) P[6 * stride + p] = 0;
+        }
+    }
+    int64_t np = n;
+    for (int64_t p = 0; p < np; p++) {
+        if (P[6 * stride + p] > 0) continue;
+        copy_particle(P, stride, p, np - 1);
+        pdt[p] = pdt[np - 1];
+        np--;
+        p--;
+    }
+    if (u_used) *u_used = k;
+    if (n_new) *n_new = m;
+    return np;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Threaded CPU baseline: the per-thread particle ranges and private deposit
  * buffers of ch9/MT (Species.cpp:9-110), for the sphere push + compaction +

@@ -78,6 +78,9 @@ def _sig(L):
     L.eo_compute_mpc.argtypes = [C.POINTER(Grid), PD, I64, I64, PD]
     L.eo_mcc_cex.restype = I64
     L.eo_mcc_cex.argtypes = [C.POINTER(Grid), PD, I64, I64, PD, PD, D, PD, I64, PI64, PI64]
+    L.eo_advance_ch4_ion.restype = I64
+    L.eo_advance_ch4_ion.argtypes = [C.POINTER(Grid), PD, PD, D, D, D, D, PD, I64, I64, PD, D, D, D, D, D, D, PD,
+                                     I64, C.POINTER(C.c_int32), PD, PI64, PD, I64, PI64]
     L.eo_advance_ch4_neutral.restype = I64
     L.eo_advance_ch4_neutral.argtypes = [C.POINTER(Grid), PD, D, D, PD, I64, I64, PD, PD, I64, PI64, PI64, C.c_int]
     L.eo_inject_warm.restype = I64
@@ -319,6 +322,31 @@ def advance_ch4_neutral(g, sphere, mass, dt, P, pdt, u, holes=False):
                                      u.size, C.byref(used), off.ctypes.data_as(PI64), 1 if holes else 0)
     assert m >= 0, "uniforms ran out"
     return np.ascontiguousarray(P[:, :m]), pdt[:m].copy(), used.value, off[:P.shape[1]]
+
+
+def advance_ch4_ion(g, ef, sphere, charge, mass, mpw0, dt, P, pdt, neutral, spherium, u, max_new=100000):
+    """eo_advance_ch4_ion on copies of P and pdt.  neutral, spherium:
+    (mpw0, charge, mass) of the target species.  Returns (P, pdt after
+    removal, created particles [7][m], their tags (0 neutral, 1 spherium),
+    their time left, uniforms used)."""
+    P = np.array(P, dtype=np.float64, order="C", copy=True)
+    pdt = np.array(pdt, dtype=np.float64, copy=True)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    ef = np.ascontiguousarray(ef, dtype=np.float64)
+    sph = np.array(list(sphere[:3]) + [sphere[3] ** 2], dtype=np.float64)
+    Q = np.zeros((7, max_new))
+    tag = np.zeros(max_new, dtype=np.int32)
+    qdt = np.zeros(max_new)
+    m, used = C.c_int64(0), C.c_int64(0)
+    npart = lib().eo_advance_ch4_ion(C.byref(g), pd(ef), pd(sph), charge, mass, mpw0, dt, pd(P), P.shape[1],
+                                     P.shape[1], pd(pdt), neutral[0], neutral[1], neutral[2], spherium[0],
+                                     spherium[1], spherium[2], pd(Q), max_new,
+                                     tag.ctypes.data_as(C.POINTER(C.c_int32)), pd(qdt), C.byref(m), pd(u), u.size,
+                                     C.byref(used))
+    assert npart >= 0, "uniforms ran out or the buffer of new particles is full"
+    k = m.value
+    return (np.ascontiguousarray(P[:, :npart]), pdt[:npart].copy(), np.ascontiguousarray(Q[:, :k]), tag[:k].copy(),
+            qdt[:k].copy(), used.value)
 
 
 def deposit_fp64(g, P):

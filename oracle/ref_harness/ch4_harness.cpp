@@ -5,7 +5,7 @@
  * with the sphere's diffuse reflection through their public API for golden
  * vectors.
  * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
- * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc|advance <in.kv> <out.kv>
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc|advance|advance_ion <in.kv> <out.kv>
  */
 #include <chrono>
 #include <cmath>
@@ -158,6 +158,44 @@ int main(int argc, char **argv) {
         out["u"] = us;
         out["sp0_P"] = v;
         out["sp0_dt"] = dts;
+        kv_write(argv[3], out);
+        return 0;
+    }
+    if (op == "advance_ion") {
+        /* Species::advance(sp1, sp1) of a charged species sp0 `steps` times:
+         * ions striking the sphere create neutrals and sputtered particles
+         * in sp1 (as ch4/Main.cpp calls it) */
+        const std::vector<double> &P = kv_get(in, "sp0_P"), &pdt = kv_get(in, "sp0_dt");
+        const std::vector<double> &sph = kv_get(in, "sphere");
+        world.addSphere(double3(sph[0], sph[1], sph[2]), sph[3], sph[4]);
+        const std::vector<double> &mq1 = kv_get(in, "sp1_mq");
+        Species tgt("sp1", mq1[0], mq1[1], mq1[2], world);
+        size_t n = P.size() / 7;
+        for (size_t p = 0; p < n; p++)
+            sp.particles.emplace_back(double3(P[p], P[n + p], P[2 * n + p]),
+                                      double3(P[3 * n + p], P[4 * n + p], P[5 * n + p]), pdt[p], P[6 * n + p]);
+        int steps = kv_has(in, "steps") ? (int)kv_s(in, "steps") : 1;
+        std::vector<double> us;
+        for (int s = 0; s < steps; s++) {
+            Rnd before = rnd;
+            sp.advance(tgt, tgt);
+            for (long g = 0; g < 2000000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+        }
+        for (Species *q : {&sp, &tgt}) {
+            size_t m = q->particles.size();
+            std::vector<double> v(7 * m), dts(m);
+            for (size_t p = 0; p < m; p++) {
+                for (int d = 0; d < 3; d++) {
+                    v[d * m + p] = q->particles[p].pos[d];
+                    v[(3 + d) * m + p] = q->particles[p].vel[d];
+                }
+                v[6 * m + p] = q->particles[p].mpw;
+                dts[p] = q->particles[p].dt;
+            }
+            out[q == &sp ? "sp0_P" : "sp1_P"] = v;
+            out[q == &sp ? "sp0_dt" : "sp1_dt"] = dts;
+        }
+        out["u"] = us;
         kv_write(argv[3], out);
         return 0;
     }

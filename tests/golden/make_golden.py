@@ -3,7 +3,7 @@ CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
 Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral] [ch4push]
+    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral] [ch4push] [ch4ion]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -292,6 +292,34 @@ def ch4_push_cases():
          dt0=pdt, steps=5, u=o["u"], P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"])
 
 
+def ch4_ion_push_cases():
+    """Three Species::advance(neutrals, neutrals) steps of 1500 O+ ions
+    (ch4/Species.cpp:8-91) in a given E field: ions striking the sphere are
+    removed and leave two neutrals each (mpw0 ratio 2) and, above 5000 m/s,
+    a sputtered atom with probability 0.2."""
+    geo = SPH
+    rng = np.random.default_rng(20261207)
+    n, mass, dt = 1500, 16 * AMU, 2e-6
+    x0, xm = np.array(geo["x0"]), np.array(geo["xm"])
+    c = np.array(SPHERE[:3])
+    pos = x0 + rng.random((3 * n, 3)) * (xm - x0)
+    pos = pos[np.sum((pos - c) ** 2, axis=1) > (SPHERE[3] + 1e-3) ** 2][:n]
+    P = np.zeros((7, n))
+    P[0:3] = pos.T
+    P[3:6] = 600 * rng.standard_normal((3, n))
+    P[5] += 6000
+    P[6] = 2e11
+    nn = int(np.prod(geo["grid"]))
+    ef = 200 * rng.standard_normal((nn, 3))
+    pdt = np.where(rng.random(n) < 0.5, dt, 0.0)
+    o = po.run_reference("ref_ch4", "advance_ion", base_inputs(geo, dt, seed=[17], sp0_mq=[mass, QE, 2e11],
+                                                               sp0_P=P.ravel(), sp0_dt=pdt, sp1_mq=[mass, 0.0, 1e11],
+                                                               sphere=SPHERE, ef=ef.ravel(), steps=[3]))
+    save("ch4_ion_push", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, charge=QE, mpw0=2e11, dt=dt,
+         sphere=SPHERE, ef=ef.ravel(), P0=P, dt0=pdt, steps=3, neutral=[1e11, 0.0, mass], u=o["u"],
+         P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"], N=o["sp1_P"].reshape(7, -1), ndt=o["sp1_dt"])
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -328,8 +356,8 @@ def steady_cases():
 
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
-    # stream), "steady", "dsmc", "neutral", "ch4push" (default: all)
-    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral", "ch4push"]
+    # stream), "steady", "dsmc", "neutral", "ch4push", "ch4ion" (default: all)
+    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral", "ch4push", "ch4ion"]
     build_ref.build_reference()
     if "base" in cases:
         rng = np.random.default_rng(20261203)
@@ -343,3 +371,5 @@ if __name__ == "__main__":
         neutral_cases()
     if "ch4push" in cases:
         ch4_push_cases()
+    if "ch4ion" in cases:
+        ch4_ion_push_cases()

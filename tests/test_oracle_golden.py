@@ -317,3 +317,25 @@ def test_ch4_neutral_push_bitexact(po):
         bounces += used // 11
     assert bounces > 50 and off == f["u"].size
     assert np.array_equal(P, f["P"]) and np.array_equal(pdt, f["pdt"])
+
+
+def test_ch4_ion_push_bitexact(po):
+    """Three Species::advance(neutrals, neutrals) steps of an ion species
+    (ch4/Species.cpp:8-91, 103-119): E kick, removal at the faces and at the
+    sphere, and the neutrals and sputtered atoms the strikes create, with
+    their velocities, weights and time left, reproduced bit for bit."""
+    f = golden("ch4_ion_push")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    sph, neu = tuple(f["sphere"][:4]), tuple(f["neutral"])
+    P, pdt, off = f["P0"], f["dt0"], 0
+    N, ndt, sputtered = np.zeros((7, 0)), np.zeros(0), 0
+    for _ in range(int(f["steps"])):
+        P, pdt, Q, tag, qdt, used = po.advance_ch4_ion(g, f["ef"], sph, float(f["charge"]), float(f["mass"]),
+                                                       float(f["mpw0"]), float(f["dt"]), P, pdt, neu, neu,
+                                                       f["u"][off:])
+        off += used
+        N, ndt = np.concatenate([N, Q], axis=1), np.concatenate([ndt, qdt])
+        sputtered += int(np.sum(tag == 1))
+    assert off == f["u"].size and N.shape[1] > 50 and sputtered > 0
+    assert np.array_equal(P, f["P"]) and np.array_equal(pdt, f["pdt"])
+    assert np.array_equal(N, f["N"]) and np.array_equal(ndt, f["ndt"])
