@@ -1534,6 +1534,54 @@ int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphe
     return np;
 }
 
+/* ChemistryIonize::apply, ch4/Collisions.cpp:10-31: over the cells (i
+ * outer, then j, then k), n_a and n_e = rho / QE gathered at the cell centre,
+ * dni = rate n_a n_e dt, and (int)(dni dV / mpw0 + U) ions are added.  Their
+ * position is World::pos(i + U, j + U, k + U), which the overload taking
+ * three ints (ch4/World.h:109-112) truncates to node (i, j, k); each is added
+ * with addParticle(pos, 0, mpw0), whose third argument is the particle's
+ * time left (ch4/Species.h:65-67): time mpw0, weight mpw0, velocity rewound
+ * by q/m E dt/2 (ch4/Species.cpp:103-119).  Uniforms: one per cell, three per
+ * ion.  New ions go to Q [7][max_new] with their time left in qdt; returns
+ * their count, -1 when u runs out, -2 when Q is full. */
+int64_t eo_chemistry_ionize(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
+                            double charge, double mass, double mpw0, double rate, double dt, double *Q,
+                            int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used) {
+    const double QE_ = 1.602176565e-19;
+    const double dV = g->dh[0] * g->dh[1] * g->dh[2];
+    int64_t k = 0, m = 0;
+    for (int i = 0; i < g->ni - 1; i++)
+        for (int j = 0; j < g->nj - 1; j++)
+            for (int kk = 0; kk < g->nk - 1; kk++) {
+                const double lc[3] = {i + 0.5, j + 0.5, kk + 0.5};
+                const double na = gather1(g, den_n, lc);
+                const double ne = gather1(g, rho, lc) / QE_;
+                const double dni = rate * na * ne * dt;
+                if (k >= nu) return -1;
+                const int num_p = (int)(dni * dV / mpw0 + u[k++]);
+                for (int p = 0; p < num_p; p++) {
+                    if (k + 3 > nu) return -1;
+                    k += 3;
+                    const double x[3] = {g->x0[0] + g->dh[0] * (double)i, g->x0[1] + g->dh[1] * (double)j,
+                                         g->x0[2] + g->dh[2] * (double)kk};
+                    if (!eo_in_bounds(g, x)) continue;
+                    if (m >= max_new) return -2;
+                    double lc2[3], e[3];
+                    eo_xtol(g, x, lc2);
+                    eo_gather3(g, ef, lc2, e);
+                    for (int d = 0; d < 3; d++) {
+                        Q[d * max_new + m] = x[d];
+                        Q[(3 + d) * max_new + m] = 0.0 - charge / mass * e[d] * (0.5 * dt);
+                    }
+                    Q[6 * max_new + m] = mpw0;
+                    qdt[m] = mpw0;
+                    m++;
+                }
+            }
+    if (u_used) *u_used = k;
+    return m;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Threaded CPU baseline: the per-thread particle ranges and private deposit
  * buffers of ch9/MT (Species.cpp:9-110), for the sphere push + compaction +

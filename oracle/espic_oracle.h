@@ -147,6 +147,10 @@ int64_t eo_mcc_cex(const eo_grid *g, double *P, int64_t stride, int64_t n, const
 int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double mass, double dt, double *P,
                                int64_t stride, int64_t n, double *pdt, const double *u, int64_t nu,
                                int64_t *u_used, int64_t *p_off, int holes);
+/* ChemistryIonize::apply (ch4/Collisions.cpp:10-31) */
+int64_t eo_chemistry_ionize(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
+                            double charge, double mass, double mpw0, double rate, double dt, double *Q,
+                            int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used);
 /* ch4 Species::advance of a charged species: ions striking the sphere create
  * neutrals and sputtered particles (ch4/Species.cpp:8-91, 103-119) */
 int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphere[4], double charge, double mass,

@@ -78,6 +78,8 @@ def _sig(L):
     L.eo_compute_mpc.argtypes = [C.POINTER(Grid), PD, I64, I64, PD]
     L.eo_mcc_cex.restype = I64
     L.eo_mcc_cex.argtypes = [C.POINTER(Grid), PD, I64, I64, PD, PD, D, PD, I64, PI64, PI64]
+    L.eo_chemistry_ionize.restype = I64
+    L.eo_chemistry_ionize.argtypes = [C.POINTER(Grid), PD, PD, PD, D, D, D, D, D, PD, I64, PD, PD, I64, PI64]
     L.eo_advance_ch4_ion.restype = I64
     L.eo_advance_ch4_ion.argtypes = [C.POINTER(Grid), PD, PD, D, D, D, D, PD, I64, I64, PD, D, D, D, D, D, D, PD,
                                      I64, C.POINTER(C.c_int32), PD, PI64, PD, I64, PI64]
@@ -322,6 +324,18 @@ def advance_ch4_neutral(g, sphere, mass, dt, P, pdt, u, holes=False):
                                      u.size, C.byref(used), off.ctypes.data_as(PI64), 1 if holes else 0)
     assert m >= 0, "uniforms ran out"
     return np.ascontiguousarray(P[:, :m]), pdt[:m].copy(), used.value, off[:P.shape[1]]
+
+
+def chemistry_ionize(g, den_n, rho, ef, charge, mass, mpw0, rate, dt, u, max_new=200000):
+    """eo_chemistry_ionize: (new ions [7][m], their time left, uniforms used)"""
+    den_n, rho, ef = (np.ascontiguousarray(a, dtype=np.float64) for a in (den_n, rho, ef))
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    Q, qdt = np.zeros((7, max_new)), np.zeros(max_new)
+    used = C.c_int64(0)
+    m = lib().eo_chemistry_ionize(C.byref(g), pd(den_n), pd(rho), pd(ef), charge, mass, mpw0, rate, dt, pd(Q),
+                                  max_new, pd(qdt), pd(u), u.size, C.byref(used))
+    assert m >= 0, "uniforms ran out or the buffer of new particles is full"
+    return np.ascontiguousarray(Q[:, :m]), qdt[:m].copy(), used.value
 
 
 def advance_ch4_ion(g, ef, sphere, charge, mass, mpw0, dt, P, pdt, neutral, spherium, u, max_new=100000):

@@ -5,7 +5,7 @@
  * with the sphere's diffuse reflection through their public API for golden
  * vectors.
  * TEST INFRASTRUCTURE ONLY; compiled against the reference sources by
- * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc|advance|advance_ion <in.kv> <out.kv>
+ * oracle/build_ref.py.  Usage: ref_ch4 inject_warm|dsmc|moments|mcc|advance|advance_ion|ionize <in.kv> <out.kv>
  */
 #include <chrono>
 #include <cmath>
@@ -196,6 +196,34 @@ int main(int argc, char **argv) {
             out[q == &sp ? "sp0_dt" : "sp1_dt"] = dts;
         }
         out["u"] = us;
+        kv_write(argv[3], out);
+        return 0;
+    }
+    if (op == "ionize") {
+        /* ChemistryIonize(sp1 neutrals, sp0 ions, world, rate).apply(dt)
+         * with sp1's density and the world's rho given */
+        const std::vector<double> &mq1 = kv_get(in, "sp1_mq");
+        Species neu("sp1", mq1[0], mq1[1], mq1[2], world);
+        field_in(neu.den, kv_get(in, "sp1_den"), ni, nj, nk);
+        field_in(world.rho, kv_get(in, "rho"), ni, nj, nk);
+        ChemistryIonize chem(neu, sp, world, kv_s(in, "rate"));
+        Rnd before = rnd;
+        chem.apply(kv_s(in, "dt"));
+        std::vector<double> us;
+        for (long g = 0; g < 2000000000L && !(before.mt_gen == rnd.mt_gen); g++) us.push_back(before());
+        size_t m = sp.particles.size();
+        std::vector<double> v(7 * m), dts(m);
+        for (size_t p = 0; p < m; p++) {
+            for (int d = 0; d < 3; d++) {
+                v[d * m + p] = sp.particles[p].pos[d];
+                v[(3 + d) * m + p] = sp.particles[p].vel[d];
+            }
+            v[6 * m + p] = sp.particles[p].mpw;
+            dts[p] = sp.particles[p].dt;
+        }
+        out["u"] = us;
+        out["sp0_P"] = v;
+        out["sp0_dt"] = dts;
         kv_write(argv[3], out);
         return 0;
     }

@@ -3,7 +3,7 @@ CPU code (ch2, ch3/ver2, ch4, compiled from its sources by
 oracle/build_ref.py) on seeded inputs.
 
 Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral] [ch4push] [ch4ion]
+    python tests/golden/make_golden.py [base] [steady] [dsmc] [neutral] [ch4push] [ch4ion] [ionize]
 The .npz files it writes are committed; the GPU host never needs the
 reference.  Every fixture stores its inputs next to the reference outputs.
 """
@@ -320,6 +320,25 @@ def ch4_ion_push_cases():
          P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"], N=o["sp1_P"].reshape(7, -1), ndt=o["sp1_dt"])
 
 
+def ionize_cases():
+    """ChemistryIonize::apply (ch4/Collisions.cpp:10-31) on a 11x11x21 grid:
+    neutral density 1e16-1e17 m^-3, rho of a 1e13-1e14 m^-3 plasma, rate
+    5e-11 m^3/s (about one ion per cell), ion weight 1e8, an E field for the
+    velocity rewind."""
+    geo = dict(grid=[11, 11, 21], x0=[-0.1, -0.1, 0.0], xm=[0.1, 0.1, 0.4])
+    rng = np.random.default_rng(20261208)
+    nn = int(np.prod(geo["grid"]))
+    den = 1e16 * (1 + 9 * rng.random(nn))
+    rho = QE * 1e13 * (1 + 9 * rng.random(nn))
+    ef = 100 * rng.standard_normal((nn, 3))
+    mass, mpw0, rate, dt = 16 * AMU, 1e8, 5e-11, 1e-7
+    o = po.run_reference("ref_ch4", "ionize", base_inputs(geo, dt, seed=[19], sp0_mq=[mass, QE, mpw0],
+                                                          sp1_mq=[mass, 0.0, 1e12], sp1_den=den, rho=rho,
+                                                          ef=ef.ravel(), rate=[rate]))
+    save("ch4_ionize", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, charge=QE, mpw0=mpw0, rate=rate,
+         dt=dt, den=den, rho=rho, ef=ef.ravel(), u=o["u"], P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"])
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -356,8 +375,8 @@ def steady_cases():
 
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
-    # stream), "steady", "dsmc", "neutral", "ch4push", "ch4ion" (default: all)
-    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral", "ch4push", "ch4ion"]
+    # stream), "steady", "dsmc", "neutral", "ch4push", "ch4ion", "ionize" (default: all)
+    cases = sys.argv[1:] or ["base", "steady", "dsmc", "neutral", "ch4push", "ch4ion", "ionize"]
     build_ref.build_reference()
     if "base" in cases:
         rng = np.random.default_rng(20261203)
@@ -373,3 +392,5 @@ if __name__ == "__main__":
         ch4_push_cases()
     if "ch4ion" in cases:
         ch4_ion_push_cases()
+    if "ionize" in cases:
+        ionize_cases()

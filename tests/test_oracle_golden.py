@@ -339,3 +339,16 @@ def test_ch4_ion_push_bitexact(po):
     assert off == f["u"].size and N.shape[1] > 50 and sputtered > 0
     assert np.array_equal(P, f["P"]) and np.array_equal(pdt, f["pdt"])
     assert np.array_equal(N, f["N"]) and np.array_equal(ndt, f["ndt"])
+
+
+def test_chemistry_ionize_bitexact(po):
+    """ChemistryIonize::apply of the reference (ch4/Collisions.cpp:10-31):
+    the ions it adds (at the cell's corner node, as World::pos(int, int, int)
+    truncates their sampled positions), their rewound velocities, weights and
+    time left (mpw0), and the uniform count, bit for bit."""
+    f = golden("ch4_ionize")
+    g = po.grid(f["grid"], f["x0"], f["xm"])
+    Q, qdt, used = po.chemistry_ionize(g, f["den"], f["rho"], f["ef"], float(f["charge"]), float(f["mass"]),
+                                       float(f["mpw0"]), float(f["rate"]), float(f["dt"]), f["u"])
+    assert Q.shape[1] > 1000 and used == f["u"].size
+    assert np.array_equal(Q, f["P"]) and np.array_equal(qdt, f["pdt"])
