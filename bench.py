@@ -29,8 +29,8 @@ Other workloads (--config): sphere256 and sphere128 (the same step on
 larger grids), box21 (the ch2 box, FP64 form), ensemble512 (512 ch2 boxes
 stepped together), diff32 (forward + adjoint of the sphere run), dsmc41
 (one DSMC_MEX::apply over the 6.4M-atom ch4 neutral gas, with the ch4
-moment sampling and MCC timed beside it; its reference arm runs the
-oracle's DSMC_MEX on the host).
+moment sampling, MCC and neutral push timed beside it; its reference arm
+runs the oracle's DSMC_MEX on the host).
 """
 import argparse
 import json
@@ -741,6 +741,10 @@ def run_dsmc(args, E, torch):
     mcc = E.MCC_CEX(s, s, w)
     ms_mcc = timed(lambda: mcc.apply(dt))
     P = s.particles()
+    # the ch4 neutral push (no sphere here: atoms leave through the faces)
+    n_before = s.getNp()
+    ms_push = timed(s.advance_ch4)
+    n_after = s.getNp()
     w.close()
     # CPU: the oracle on the same atoms, starting from the warmed-up sigma_cr_max
     _, _, cpu_t = dsmc_cpu_calls(cfg, P, smax, 2)
@@ -770,7 +774,10 @@ def run_dsmc(args, E, torch):
                                "bytes_per_particle": 56,
                                "hbm_frac": 56.0 * n / (ms_mom * 1e-3) / 1e9 / hbm},
             "mcc_cex": {"ms_per_call": ms_mcc, "particles_per_s": n / (ms_mcc * 1e-3), "bytes_per_particle": 48,
-                        "hbm_frac": 48.0 * n / (ms_mcc * 1e-3) / 1e9 / hbm}}
+                        "hbm_frac": 48.0 * n / (ms_mcc * 1e-3) / 1e9 / hbm},
+            "ch4_push": {"ms_per_call": ms_push, "particles": [n_before, n_after],
+                         "particles_per_s": 0.5 * (n_before + n_after) / (ms_push * 1e-3), "bytes_per_particle": 96,
+                         "hbm_frac": 96.0 * 0.5 * (n_before + n_after) / (ms_push * 1e-3) / 1e9 / hbm}}
     print(json.dumps(line))
 
 
