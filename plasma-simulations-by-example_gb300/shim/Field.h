@@ -13,6 +13,7 @@
 #ifndef ESPIC_SHIM_FIELD_H
 #define ESPIC_SHIM_FIELD_H
 
+#include <cmath>
 #include <cstdint>
 #include <functional>
 #include <memory>
@@ -44,6 +45,24 @@ struct vec3 {
         d[1] -= o[1];
         d[2] -= o[2];
         return *this;
+    }
+    /* ch4/Field.h:17-34: division by a scalar, dot, mag, unit, cross */
+    vec3<T> operator/(double s) const { return vec3<T>(d[0] / s, d[1] / s, d[2] / s); }
+    vec3<T> &operator/=(double s) {
+        d[0] /= s;
+        d[1] /= s;
+        d[2] /= s;
+        return *this;
+    }
+    friend T dot(const vec3<T> &v1, const vec3<T> &v2) {
+        T s = 0;
+        for (int i = 0; i < 3; i++) s += v1(i) * v2(i);
+        return s;
+    }
+    friend T mag(const vec3<T> &v) { return std::sqrt(dot(v, v)); }
+    friend vec3<T> unit(const vec3<T> &v) { return vec3<T>(v) / mag(v); }
+    friend vec3<T> cross(const vec3<T> &a, const vec3<T> &b) {
+        return vec3<T>(a(1) * b(2) - a(2) * b(1), a(2) * b(0) - a(0) * b(2), a(0) * b(1) - a(1) * b(0));
     }
 
 protected:

@@ -87,6 +87,19 @@ public:
         return pos(x);
     }
     int U(int i, int j, int k) { return object_id.U(i, j, k); }
+    /* ch4/World.h:88-98: cell indices and the cell number of a position */
+    int3 XtoIJK(double3 x) const {
+        double3 lc = XtoL(x);
+        return int3((int)lc[0], (int)lc[1], (int)lc[2]);
+    }
+    int XtoC(double3 x) const {
+        int3 i = XtoIJK(x);
+        return i[2] * (nj - 1) * (ni - 1) + i[1] * (ni - 1) + i[0];
+    }
+    /* ch4/World.cpp:160-199 (host): the segment's sphere crossing and a
+     * diffuse direction off the sphere at x (two host rnd() draws) */
+    double lineSphereIntersect(const double3 &x1, const double3 &x2);
+    double3 sphereDiffuseVector(const double3 &x);
 
     void computeChargeDensity(std::vector<Species> &species);
     double getPE();

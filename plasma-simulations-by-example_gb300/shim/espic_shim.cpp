@@ -204,6 +204,41 @@ bool World::steadyState(std::vector<Species> &species) {
     return steady_state;
 }
 
+/* World::lineSphereIntersect, ch4/World.cpp:160-182 */
+double World::lineSphereIntersect(const double3 &x1, const double3 &x2) {
+    double3 B = x2 - x1;
+    double3 A = x1 - sphere_x0;
+    double a = dot(B, B);
+    double b = 2 * dot(A, B);
+    double c = dot(A, A) - sphere_rad2;
+    double det = b * b - 4 * a * c;
+    if (det < 0) return 0.5;
+    double tp = (-b + sqrt(det)) / (2 * a);
+    if (tp < 0 || tp > 1.0) {
+        tp = (-b - sqrt(det)) / (2 * a);
+        if (tp < 0 || tp > 1.0) {
+            std::cerr << "Failed to find a line-sphere intersection!" << std::endl;
+            tp = 0.5;
+        }
+    }
+    return tp;
+}
+
+/* World::sphereDiffuseVector, ch4/World.cpp:185-199 */
+double3 World::sphereDiffuseVector(const double3 &x) {
+    double sin_theta = rnd();
+    double cos_theta = sqrt(1 - sin_theta * sin_theta);
+    double psi = 2 * Const::PI * rnd();
+    double3 n = unit(x - sphere_x0);
+    double3 t1;
+    if (dot(n, double3(1, 0, 0)) != 0)
+        t1 = cross(n, double3(1, 0, 0));
+    else
+        t1 = cross(n, double3(0, 1, 0));
+    double3 t2 = cross(n, t1);
+    return sin_theta * cos(psi) * t1 + sin_theta * sin(psi) * t2 + cos_theta * n;
+}
+
 /* ---------------------------------------------------------------- Species */
 std::vector<Particle> &ParticleVector::host() {
     if (!host_valid) {

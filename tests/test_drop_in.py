@@ -131,3 +131,12 @@ def test_ch4_main_with_particle_output_compiles(tmp_path):
     E = _espic_module()
     r = E.compile_drop_in(str(edited), str(tmp_path / "main"), stdin_source=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_ch4_api_program_compiles(tmp_path):
+    """A program using the ch4 World helpers (XtoC, lineSphereIntersect,
+    sphereDiffuseVector), vec3 dot/mag/unit/cross, DSMC_MEX, MCC_CEX and the
+    ch4 Species calls builds against the drop-in headers."""
+    E = _espic_module()
+    r = E.compile_drop_in(os.path.join(DROP, "ch4_api_main.cpp"), str(tmp_path / "main"))
+    assert r.returncode == 0, r.stderr[-2000:]
