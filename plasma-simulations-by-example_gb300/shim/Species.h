@@ -79,6 +79,12 @@ public:
     void computeNumberDensity();
     void addParticle(double3 pos, double3 vel, double mpwt);
     void addParticle(double3 pos, double3 vel) { addParticle(pos, vel, mpw0); }
+    /* ch4/Species.h:67: the library keeps no per-particle time; a particle
+     * added here has one dt left at the next ch4 push, whatever dt says */
+    void addParticle(double3 pos, double3 vel, double dt, double mpw) {
+        (void)dt;
+        addParticle(pos, vel, mpw);
+    }
     void loadParticlesBox(double3 x1, double3 x2, double num_den, int num_mp);
     void loadParticlesBoxQS(double3 x1, double3 x2, double num_den, int3 num_mp);
     void updateAverages();
