@@ -339,6 +339,24 @@ def ionize_cases():
          dt=dt, den=den, rho=rho, ef=ef.ravel(), u=o["u"], P=o["sp0_P"].reshape(7, -1), pdt=o["sp0_dt"])
 
 
+def dsmc_sparse_cases():
+    """DSMC_MEX::apply on 300 atoms in 125 cells (0 to ~6 per cell): cells
+    too small to pair, and two-atom cells where the second pick is redrawn
+    until it differs from the first (ch4/Collisions.cpp:148-152), five calls
+    from the reference's starting sigma_cr_max."""
+    geo = dict(grid=[6, 6, 6], x0=[0.0, 0.0, 0.0], xm=[0.05, 0.05, 0.05])
+    rng = np.random.default_rng(20261209)
+    n, mass, mpw0, dt = 300, 16 * AMU, 1e15, 1e-6
+    P = np.zeros((7, n))
+    P[0:3] = rng.random((3, n)) * 0.05 * 0.999999
+    P[3:6] = 500 * rng.standard_normal((3, n))
+    P[6] = mpw0
+    o = po.run_reference("ref_ch4", "dsmc", base_inputs(geo, dt, seed=[78], sp0_mq=[mass, 0.0, mpw0],
+                                                        sp0_P=P.ravel(), steps=[5]))
+    save("dsmc_sparse", grid=geo["grid"], x0=geo["x0"], xm=geo["xm"], mass=mass, mpw0=mpw0, dt=dt, P0=P,
+         P=o["sp0_P"].reshape(7, -1), u=o["u"], sigma_cr_max=o["sigma_cr_max"], c=o["c"], steps=5)
+
+
 def steady_run(seed):
     """One 600-step run of the ch3/ver2 main loop at the reference's own
     macroparticle weight (ch3/ver2/Main.cpp:33), with batch means of den and
@@ -386,6 +404,7 @@ if __name__ == "__main__":
         steady_cases()
     if "dsmc" in cases:
         dsmc_cases()
+        dsmc_sparse_cases()
     if "neutral" in cases:
         neutral_cases()
     if "ch4push" in cases:

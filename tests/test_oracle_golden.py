@@ -1,6 +1,7 @@
 """Pins the CPU oracle to the reference: every restated function against the
 golden vectors produced by the reference's own code (tests/golden/)."""
 import numpy as np
+import pytest
 
 from conftest import golden
 
@@ -255,14 +256,17 @@ def test_sphere_main_loop_bitexact(po):
     assert np.array_equal(P, f["P"])
 
 
-def test_dsmc_bitexact(po):
-    """Three DSMC_MEX::apply calls of the reference (ch4/Collisions.cpp:
-    108-183), replayed with its recorded uniforms: velocities, sigma_cr_max
-    and the uniform count reproduced bit for bit."""
-    f = golden("dsmc_steps")
+@pytest.mark.parametrize("case", ["dsmc_steps", "dsmc_sparse"])
+def test_dsmc_bitexact(po, case):
+    """DSMC_MEX::apply calls of the reference (ch4/Collisions.cpp:108-183),
+    replayed with its recorded uniforms: velocities, sigma_cr_max and the
+    uniform count reproduced bit for bit.  dsmc_steps: 3000 atoms, three
+    calls; dsmc_sparse: 300 atoms in 125 cells (empty, single and two-atom
+    cells, whose second pick is redrawn), five calls."""
+    f = golden(case)
     g = po.grid(f["grid"], f["x0"], f["xm"])
     P, smax, off = f["P0"], 1e-14, 0
-    for st in range(3):
+    for st in range(int(f["steps"]) if "steps" in f else 3):
         P, smax, ncol, used, _ = po.dsmc_mex(g, float(f["mass"]), float(f["mpw0"]), float(f["dt"]), f["c"], smax,
                                              P, f["u"][off:])
         off += used
