@@ -321,31 +321,41 @@ int espic_profile_read(espic_world *w, double ms[ESPIC_NPHASES], int64_t count[E
 int espic_solver_totals(espic_world *w, int64_t *solves, int64_t *outer, int64_t *inner);
 
 /* ---- deposit without allocation --------------------------------------------- */
-/* No counterpart in the reference: an extra entry point for callers that may
- * not allocate device memory once they are running -- a host application or
- * plugin host that has already given all device memory to its own pool
- * allocator, a loop with real-time deadlines that forbids allocation after
- * start-up, or code that must not synchronise the device, which cudaMalloc
- * and cudaFree may do.  It computes the number density of
- * Species::computeNumberDensity (ch2/Species.cpp:41-52), with the same
- * fixed-point arithmetic as espic_deposit, from particles the caller already
- * holds on the device: d_P is [7][stride] float64 (x, y, z, vx, vy, vz, mpw;
- * only x, y, z and mpw are read), d_den receives ni*nj*nk values in U order.
- * The fixed-point scale is that of a species of capacity n whose weights do
- * not exceed weight_bound.  It allocates nothing: its int64 scratch is a
- * static device array of ESPIC_NOALLOC_MAX_NODES nodes (8 MiB, held by every
- * GPU that loads the library until the process exits), and a larger grid is
- * refused with ESPIC_ERR_ARG.  The first call on a device looks up that
+/* A library entry point with no counterpart in the reference.  It exists for
+ * callers that may not allocate device memory once they are running: a host
+ * application or plugin host that has already given all device memory to its
+ * own pool allocator, a loop with real-time deadlines that forbids allocation
+ * after start-up, or code that must not synchronise the device, which
+ * cudaMalloc and cudaFree may do.  It computes the CIC number density of
+ * espic_deposit (same corner order, same rounding of each corner weight to a
+ * count of 1/fx, same division by the node volume) from particles the caller
+ * already holds on the device: d_P is [7][stride] float64 (x, y, z, vx, vy,
+ * vz, mpw; only x, y, z and mpw are read), d_den receives ni*nj*nk values in
+ * U order.  The fixed-point scale fx is that of a species of capacity n whose
+ * weights do not exceed weight_bound, so the result equals espic_deposit's bit
+ * for bit when that species' capacity is n.
+ *
+ * It allocates nothing: its int64 scratch is a static device array of
+ * ESPIC_NOALLOC_MAX_NODES nodes (8 MiB, held by every GPU that loads the
+ * library until the process exits), and a larger grid is refused with
+ * ESPIC_ERR_ARG before any work.  The first call on a device looks up that
  * array's device address (no allocation, but make this first call before any
  * stream capture).  Work is queued on `stream` (a cudaStream_t; NULL for the
- * default stream) and the call returns without waiting.  Every call shares
- * the one scratch array and clears the part it uses before use; calls whose
- * work overlaps on the GPU (other streams, other threads) race on it and must
- * be serialised by the caller. */
+ * default stream) and the call returns without waiting.  Every call shares the
+ * one scratch array and clears the part it uses before use; calls whose work
+ * overlaps on the GPU (other streams, other threads) race on it and must be
+ * serialised by the caller.
+ *
+ * d_flags (optional, a caller-owned device int) is set to 0 on the stream and
+ * then receives ESPIC_NOALLOC_RANGE for a weight with |mpw| > weight_bound and
+ * ESPIC_NOALLOC_NONFINITE for a non-finite position; such particles deposit
+ * nothing.  Read it after the stream's work has finished. */
 #define ESPIC_NOALLOC_MAX_NODES (1 << 20)
+#define ESPIC_NOALLOC_RANGE 1
+#define ESPIC_NOALLOC_NONFINITE 2
 int espic_deposit_noalloc(const double *d_P, int64_t stride, int64_t n, int ni, int nj, int nk,
                           const double x0[3], const double xm[3], double weight_bound, double *d_den,
-                          void *stream);
+                          int *d_flags, void *stream);
 
 /* ---- output snapshots ------------------------------------------------------- */
 /* Output::fields (ch3/ver2/Output.cpp:12-79) without stalling the step: packs

@@ -1681,3 +1681,222 @@ double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sp
     if (n_out) *n_out = n;
     return el;
 }
+
+/* ======================================================================
+ * The mixed particle form (the chosen GPU form): an int32 cell key
+ * i | j<<10 | k<<20, a float in-cell offset and a float velocity, with the
+ * species weight mpw0.  These functions restate the GPU arithmetic
+ * operation by operation (float products, fused multiply-adds where the GPU
+ * code names them), so that the GPU's mixed state and its integer charge can
+ * be checked bit for bit; the float64 functions above then bound the
+ * distance of the mixed form from the reference.
+ *
+ * Reference behaviour restated in float: Species::advance
+ * (ch3/ver2/Species.cpp:7-48, ch2/Species.cpp:7-38) with Field_::gather
+ * (ch2/Field.h:186-208); Species::computeNumberDensity
+ * (ch2/Species.cpp:41-52) with Field_::scatter (ch2/Field.h:164-183).
+ * ====================================================================== */
+
+void eo_mix_args_set(eo_mix_args *a, const eo_grid *g, double charge, double mass, double dt,
+                     const double *sphere) {
+    a->ni = g->ni;
+    a->nj = g->nj;
+    a->nk = g->nk;
+    a->qmdt = (float)(charge / mass * dt);
+    for (int d = 0; d < 3; d++) {
+        a->dtdh[d] = (float)(dt / g->dh[d]);
+        a->dh[d] = (float)g->dh[d];
+        a->sx[d] = (float)(g->x0[d] - (sphere ? sphere[d] : 0.0));
+    }
+    a->r2 = sphere ? (float)sphere[3] : -1.f;
+}
+
+void eo_ef_to_f32(int64_t nn, const double *ef, float *ef4) {
+    for (int64_t u = 0; u < nn; u++) {
+        for (int d = 0; d < 3; d++) ef4[4 * u + d] = (float)ef[3 * u + d];
+        ef4[4 * u + 3] = 0.f;
+    }
+}
+
+/* float64 block -> mixed form: World::XtoL in float64 (ch2/World.h:72-78),
+ * truncation, clamp to [0, n-2], offset rounded to float */
+void eo_to_mixed(const eo_grid *g, const double *P, int64_t pstride, int64_t n, int32_t *cell, float *off,
+                 float *vel, int64_t stride) {
+    const int nmax[3] = {g->ni, g->nj, g->nk};
+    for (int64_t p = 0; p < n; p++) {
+        int c[3];
+        for (int d = 0; d < 3; d++) {
+            double lc = (P[d * pstride + p] - g->x0[d]) / g->dh[d];
+            int i = (int)lc;
+            if (i < 0) i = 0;
+            if (i > nmax[d] - 2) i = nmax[d] - 2;
+            c[d] = i;
+            off[d * stride + p] = (float)(lc - i);
+            vel[d * stride + p] = (float)P[(3 + d) * pstride + p];
+        }
+        cell[p] = c[0] | (c[1] << 10) | (c[2] << 20);
+    }
+}
+
+static inline void mix_unpack(int32_t key, int *i, int *j, int *k) {
+    *i = key & 1023;
+    *j = (key >> 10) & 1023;
+    *k = key >> 20;
+}
+
+/* the eight CIC corner weights in float, Field_::scatter's corner order */
+static inline void mix_cic(float fx, float fy, float fz, float w[8]) {
+    const float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
+    w[0] = gx * gy * gz;
+    w[1] = fx * gy * gz;
+    w[2] = fx * fy * gz;
+    w[3] = gx * fy * gz;
+    w[4] = gx * gy * fz;
+    w[5] = fx * gy * fz;
+    w[6] = fx * fy * fz;
+    w[7] = gx * fy * fz;
+}
+
+/* a coordinate moved by v*dtdh cells: new cell index, offset in [0,1) */
+static inline int mix_advance_axis(int i, float *f, float v, float dtdh) {
+    float x = fmaf(v, dtdh, *f);
+    float fl = floorf(x);
+    i += (int)fl;
+    x -= fl;
+    if (x >= 1.f) {
+        x -= 1.f;
+        i += 1;
+    }
+    *f = x;
+    return i;
+}
+
+/* one mirror bounce (ch2/Species.cpp:32-36) in cell units */
+static inline void mix_reflect_axis(int *i, float *f, float *v, int n) {
+    float p = (float)*i + *f;
+    const float top = (float)(n - 1);
+    if (p < 0.f) {
+        p = -p;
+        *v = -*v;
+    } else if (p >= top) {
+        p = 2.f * top - p;
+        *v = -*v;
+    }
+    int ii = (int)p;
+    if (ii > n - 2) ii = n - 2;
+    if (ii < 0) ii = 0;
+    *i = ii;
+    *f = p - (float)ii;
+}
+
+/* One push of n particles in the mixed form: E gathered from the float copy
+ * ef4 ([nn][4]) with a chain of fused multiply-adds in corner order,
+ * v = fma(E, q/m dt, v), x moved in cell units, then the walls: reflecting
+ * (walls 0) or absorbing with the sphere (walls 1).  dead[p] marks particles
+ * absorbed or made non-finite. */
+void eo_push_mixed(const eo_mix_args *a, const float *ef4, int walls, int32_t *cell, float *off, float *vel,
+                   int64_t stride, int64_t n, uint8_t *dead) {
+    const int64_t sy = a->ni, sz = (int64_t)a->ni * a->nj;
+    for (int64_t p = 0; p < n; p++) {
+        int i, j, k;
+        mix_unpack(cell[p], &i, &j, &k);
+        float fx = off[p], fy = off[stride + p], fz = off[2 * stride + p];
+        float vx = vel[p], vy = vel[stride + p], vz = vel[2 * stride + p];
+        float w[8];
+        mix_cic(fx, fy, fz, w);
+        const int64_t n0 = ((int64_t)k * a->nj + j) * a->ni + i;
+        const int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+        float e[3];
+        for (int d = 0; d < 3; d++) {
+            float s = w[0] * ef4[4 * idx[0] + d];
+            for (int c = 1; c < 8; c++) s = fmaf(w[c], ef4[4 * idx[c] + d], s);
+            e[d] = s;
+        }
+        vx = fmaf(e[0], a->qmdt, vx);
+        vy = fmaf(e[1], a->qmdt, vy);
+        vz = fmaf(e[2], a->qmdt, vz);
+        i = mix_advance_axis(i, &fx, vx, a->dtdh[0]);
+        j = mix_advance_axis(j, &fy, vy, a->dtdh[1]);
+        k = mix_advance_axis(k, &fz, vz, a->dtdh[2]);
+        int gone = 0;
+        if (walls == 0) {
+            mix_reflect_axis(&i, &fx, &vx, a->ni);
+            mix_reflect_axis(&j, &fy, &vy, a->nj);
+            mix_reflect_axis(&k, &fz, &vz, a->nk);
+        } else {
+            gone = i < 0 || i > a->ni - 2 || j < 0 || j > a->nj - 2 || k < 0 || k > a->nk - 2;
+            if (!gone && a->r2 >= 0.f) {
+                const float rx = fmaf((float)i + fx, a->dh[0], a->sx[0]);
+                const float ry = fmaf((float)j + fy, a->dh[1], a->sx[1]);
+                const float rz = fmaf((float)k + fz, a->dh[2], a->sx[2]);
+                gone = fmaf(rz, rz, fmaf(ry, ry, rx * rx)) <= a->r2;
+            }
+        }
+        if (!(isfinite(fx) && isfinite(fy) && isfinite(fz) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
+            gone = 1;
+            i = j = k = 0;
+            fx = fy = fz = 0.f;
+        }
+        cell[p] = (i & 1023) | ((j & 1023) << 10) | (k << 20);
+        off[p] = fx;
+        off[stride + p] = fy;
+        off[2 * stride + p] = fz;
+        vel[p] = vx;
+        vel[stride + p] = vy;
+        vel[2 * stride + p] = vz;
+        dead[p] = (uint8_t)gone;
+    }
+}
+
+/* The removal of the GPU path in the mixed form: the r-th dead slot below
+ * the new count receives the r-th live particle above it (the holes order
+ * of eo_compact_holes).  Returns the new count. */
+int64_t eo_compact_mixed(int32_t *cell, float *off, float *vel, int64_t stride, int64_t n, const uint8_t *dead) {
+    int64_t alive = 0;
+    for (int64_t p = 0; p < n; p++) alive += !dead[p];
+    int64_t hole = 0;
+    for (int64_t src = alive; src < n; src++) {
+        if (dead[src]) continue;
+        while (!dead[hole]) hole++;
+        cell[hole] = cell[src];
+        for (int d = 0; d < 3; d++) {
+            off[d * stride + hole] = off[d * stride + src];
+            vel[d * stride + hole] = vel[d * stride + src];
+        }
+        hole++;
+    }
+    return alive;
+}
+
+/* The mixed deposit: each corner weight w (float, in [0,1]) becomes
+ * round-half-even(w * 2^23) counts of mpw0 * 2^-23, added to the node's
+ * int64 sum (particles with skip[p] set deposit nothing; skip may be NULL). */
+void eo_deposit_mixed(const eo_grid *g, const int32_t *cell, const float *off, int64_t stride, int64_t n,
+                      const uint8_t *skip, int64_t *acc) {
+    const int64_t sy = g->ni, sz = (int64_t)g->ni * g->nj;
+    for (int64_t p = 0; p < n; p++) {
+        if (skip && skip[p]) continue;
+        int i, j, k;
+        mix_unpack(cell[p], &i, &j, &k);
+        float w[8];
+        mix_cic(off[p], off[stride + p], off[2 * stride + p], w);
+        const int64_t n0 = ((int64_t)k * g->nj + j) * g->ni + i;
+        const int64_t idx[8] = {n0, n0 + 1, n0 + 1 + sy, n0 + sy, n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+        for (int c = 0; c < 8; c++) acc[idx[c]] += (int64_t)(uint32_t)rintf(w[c] * 8388608.f);
+    }
+}
+
+/* mixed form -> float64: x = x0 + (i + f) dh, the GPU's one fused
+ * multiply-add; v widened */
+void eo_from_mixed(const eo_grid *g, const int32_t *cell, const float *off, const float *vel, int64_t stride,
+                   int64_t n, double mpw0, double *P, int64_t pstride) {
+    for (int64_t p = 0; p < n; p++) {
+        int c[3];
+        mix_unpack(cell[p], &c[0], &c[1], &c[2]);
+        for (int d = 0; d < 3; d++) {
+            P[d * pstride + p] = fma((double)c[d] + (double)off[d * stride + p], g->dh[d], g->x0[d]);
+            P[(3 + d) * pstride + p] = (double)vel[d * stride + p];
+        }
+        P[6 * pstride + p] = mpw0;
+    }
+}

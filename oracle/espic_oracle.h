@@ -159,6 +159,30 @@ int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphe
                            double sph_mass, double *Q, int64_t max_new, int32_t *tag, double *qdt, int64_t *n_new,
                            const double *u, int64_t nu, int64_t *u_used);
 
+/* ---- the mixed particle form (the chosen GPU form) -------------------------
+ * int32 cell key i | j<<10 | k<<20, float offsets and velocities [3][stride],
+ * weight mpw0; the GPU arithmetic restated operation by operation. */
+typedef struct {
+    int ni, nj, nk;
+    float qmdt;    /* (float)(q/m dt) */
+    float dtdh[3]; /* (float)(dt/dh) */
+    float dh[3];
+    float sx[3];   /* (float)(x0 - sphere centre) */
+    float r2;      /* (float)(radius^2), < 0 without a sphere */
+} eo_mix_args;
+void eo_mix_args_set(eo_mix_args *a, const eo_grid *g, double charge, double mass, double dt,
+                     const double *sphere);
+void eo_ef_to_f32(int64_t nn, const double *ef, float *ef4);
+void eo_to_mixed(const eo_grid *g, const double *P, int64_t pstride, int64_t n, int32_t *cell, float *off,
+                 float *vel, int64_t stride);
+void eo_from_mixed(const eo_grid *g, const int32_t *cell, const float *off, const float *vel, int64_t stride,
+                   int64_t n, double mpw0, double *P, int64_t pstride);
+void eo_push_mixed(const eo_mix_args *a, const float *ef4, int walls, int32_t *cell, float *off, float *vel,
+                   int64_t stride, int64_t n, uint8_t *dead);
+int64_t eo_compact_mixed(int32_t *cell, float *off, float *vel, int64_t stride, int64_t n, const uint8_t *dead);
+void eo_deposit_mixed(const eo_grid *g, const int32_t *cell, const float *off, int64_t stride, int64_t n,
+                      const uint8_t *skip, int64_t *acc);
+
 /* ---- CPU baseline (threaded like ch9/MT) ------------------------------ */
 double eo_bench_push_deposit(const eo_grid *g, const double *ef, const double sphere[4],
                              double charge, double mass, double dt, double fx, double *P,

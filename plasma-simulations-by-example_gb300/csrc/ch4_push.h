@@ -111,7 +111,11 @@ __host__ __device__ inline int ch4_advance_one(const Ch4Geo &G, double mass, dou
             const double v1 = v_th * (U(k) + U(k + 1) + U(k + 2) - 1.5);
             const double v2 = v_th * (U(k + 3) + U(k + 4) + U(k + 5) - 1.5);
             const double v3 = v_th * (U(k + 6) + U(k + 7) + U(k + 8) - 1.5);
-            const double vth = 3 / sqrt(2 + 2 + 2) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+            /* 3 / sqrt(2 + 2 + 2) in the reference: sqrt of the int 6 is
+             * sqrt(6.0) on the host; in device code sqrt must be given a
+             * double (an int argument made nvcc drop the rest of this
+             * branch) */
+            const double vth = 3.0 / sqrt(6.0) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
             const double a_th = 1;
             const double v_mag2 = v_mag1 + a_th * (vth - v_mag1);
             /* sphereDiffuseVector */

@@ -13,7 +13,10 @@
  * receive that address.  All calls share the one array and leave their sums
  * in it, so each call clears the part it uses first, and calls that overlap
  * on the GPU (different streams, or different host threads on one device)
- * race on it.
+ * race on it.  Particles the fixed-point sum cannot take (a weight beyond
+ * weight_bound, a non-finite position) are skipped and reported in the
+ * caller's flag word, the counterpart of the allocating path's
+ * ESPIC_ERR_FIXED and ESPIC_ERR_NONFINITE.
  *
  * The arithmetic is the float64 deposit of k_fp64.cu: corner weights
  * value*(1-di)*(1-dj)*(1-dk) in the reference's corner order (Field_::scatter,
@@ -39,18 +42,28 @@ struct NaGeo {
 
 __device__ __forceinline__ int na_clamp(int i, int n) { return i < 0 ? 0 : (i > n - 2 ? n - 2 : i); }
 
-__global__ void k_na_clear(unsigned long long *acc, int64_t nn) {
+__global__ void k_na_clear(unsigned long long *acc, int64_t nn, int *flags) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (u < nn) acc[u] = 0ull;
+    if (u == 0 && flags) *flags = 0;
 }
 
+/* A particle whose position is not finite, or whose weight is not within
+ * [-weight_bound, weight_bound] (so that its corner counts could wrap the
+ * int64 sums), deposits nothing and sets a bit of *flags. */
 __global__ void k_na_deposit(NaGeo g, const double *__restrict__ P, int64_t stride, int64_t n, double fx,
-                             unsigned long long *acc) {
+                             double weight_bound, unsigned long long *acc, int *flags) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     double lc[3];
     for (int d = 0; d < 3; d++) lc[d] = (P[d * stride + p] - g.x0[d]) / g.dh[d];
     double value = P[6 * stride + p];
+    const bool finite = isfinite(lc[0]) && isfinite(lc[1]) && isfinite(lc[2]);
+    const bool in_range = fabs(value) <= weight_bound; /* false for NaN */
+    if (!(finite && in_range)) {
+        if (flags) atomicOr(flags, (finite ? 0 : ESPIC_NOALLOC_NONFINITE) | (in_range ? 0 : ESPIC_NOALLOC_RANGE));
+        return;
+    }
     int i = na_clamp((int)lc[0], g.ni), j = na_clamp((int)lc[1], g.nj), k = na_clamp((int)lc[2], g.nk);
     double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
     int64_t n0 = ((int64_t)k * g.nj + j) * g.ni + i;
@@ -117,19 +130,22 @@ static int na_scratch(unsigned long long **out) {
 
 extern "C" int espic_deposit_noalloc(const double *d_P, int64_t stride, int64_t n, int ni, int nj, int nk,
                                      const double x0[3], const double xm[3], double weight_bound, double *d_den,
-                                     void *stream) {
+                                     int *d_flags, void *stream) {
     if (!x0 || !xm || !d_den || (n > 0 && !d_P))
         return espic_internal_fail(ESPIC_ERR_ARG, "espic_deposit_noalloc: null argument");
     if (ni < 3 || nj < 3 || nk < 3)
         return espic_internal_fail(ESPIC_ERR_ARG, "espic_deposit_noalloc: need at least 3 nodes per axis");
-    int64_t nn = (int64_t)ni * nj * nk;
-    if (nn > ESPIC_NOALLOC_MAX_NODES) {
-        char buf[200];
+    /* bound each factor before multiplying, so that no product can wrap */
+    if (ni > ESPIC_NOALLOC_MAX_NODES || nj > ESPIC_NOALLOC_MAX_NODES || nk > ESPIC_NOALLOC_MAX_NODES ||
+        (int64_t)ni * nj > ESPIC_NOALLOC_MAX_NODES / nk) {
+        char buf[240];
         snprintf(buf, sizeof buf,
-                 "espic_deposit_noalloc: %lld nodes exceed its fixed scratch of %d nodes; use espic_deposit",
-                 (long long)nn, ESPIC_NOALLOC_MAX_NODES);
+                 "espic_deposit_noalloc: a %d x %d x %d grid exceeds its fixed scratch of %d nodes; use "
+                 "espic_deposit",
+                 ni, nj, nk, ESPIC_NOALLOC_MAX_NODES);
         return espic_internal_fail(ESPIC_ERR_ARG, buf);
     }
+    const int64_t nn = (int64_t)ni * nj * nk;
     if (n < 0 || stride < n) return espic_internal_fail(ESPIC_ERR_ARG, "espic_deposit_noalloc: bad particle count");
     if (!(weight_bound > 0)) return espic_internal_fail(ESPIC_ERR_ARG, "espic_deposit_noalloc: weight_bound <= 0");
     for (int d = 0; d < 3; d++)
@@ -154,8 +170,9 @@ extern "C" int espic_deposit_noalloc(const double *d_P, int64_t stride, int64_t 
     int S = ex - 1 > 52 ? 52 : ex - 1;
     double fx = ldexp(1.0, S);
     cudaStream_t st = (cudaStream_t)stream;
-    k_na_clear<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(acc, nn);
-    if (n > 0) k_na_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, d_P, stride, n, fx, acc);
+    k_na_clear<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(acc, nn, d_flags);
+    if (n > 0)
+        k_na_deposit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, d_P, stride, n, fx, weight_bound, acc, d_flags);
     k_na_density<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(g, acc, 1.0 / fx, d_den);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

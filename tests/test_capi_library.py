@@ -71,3 +71,26 @@ def test_entry_points_refuse_a_null_world(libpath):
         buf = ctypes.create_string_buffer(256)
         L.espic_last_error(buf, 256)
         assert b"null world" in buf.value, (name, buf.value)
+
+
+def test_noalloc_refuses_oversized_grids_before_any_work(libpath):
+    """espic_deposit_noalloc bounds each axis before multiplying: grids whose
+    node count would wrap a 64-bit product (2^22 x 2^21 x 2^21 wraps to 0,
+    (2^21)^3 to a negative value) are refused like any grid beyond the
+    static scratch, without touching the GPU (so this runs on any host)."""
+    L = ctypes.CDLL(libpath)
+    L.espic_last_error.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    f = L.espic_deposit_noalloc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    x0 = (ctypes.c_double * 3)(0, 0, 0)
+    xm = (ctypes.c_double * 3)(1, 1, 1)
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: the call refuses first
+    for dims in [(1 << 22, 1 << 21, 1 << 21), (1 << 21, 1 << 21, 1 << 21), (1 << 20, 1 << 20, 4),
+                 (2**31 - 1, 3, 3), (102, 103, 101)]:
+        rc = f(None, 0, 0, *dims, x0, xm, 1.0, fake, None, None)
+        assert rc == -1, dims
+        buf = ctypes.create_string_buffer(256)
+        L.espic_last_error(buf, 256)
+        assert b"scratch" in buf.value, (dims, buf.value)
