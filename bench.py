@@ -270,45 +270,197 @@ def e2e_steps(E, torch, w, s, src, sol, cfg, steps):
 
 def phi_error(E, w, cfg):
     """phi of the chosen (FP32-inner) solve against a tight FP64 Newton-PCG
-    on the same charge density."""
+    on the same charge density (the GPU's float64 solver, which the parity
+    tests pin to the oracle's)."""
     phi_mixed = w.phi.copy()
     sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
     sol.setReferenceValues(PHI0, TE, N0)
     sol.setNewton(nr_max=50, nr_tol=1e-11, pcg_max=40000, pcg_tol=1e-12, fp32_inner=False)
     conv, _, _, _ = sol.solve()
     phi64 = w.phi
-    return float(np.max(np.abs(phi_mixed - phi64)) / np.max(np.abs(phi64))), bool(conv)
+    return float(np.max(np.abs(phi_mixed - phi64)) / np.max(np.abs(phi64))), bool(conv), phi64
 
 
-def cpu_baseline(cfg, P0, inner_per_step, threads, steps=2, it_cap=8):
-    """The oracle port on this host: threaded push + compaction + fixed-point
-    deposit on the full particle set (ch9/MT's scheme), and the serial
-    Newton-PCG timed per inner iteration, scaled to the GPU's count."""
+def _err(a, b):
+    d = np.asarray(a, dtype=np.float64) - np.asarray(b, dtype=np.float64)
+    ref = np.abs(np.asarray(b, dtype=np.float64))
+    return {"max_rel": float(np.max(np.abs(d)) / max(np.max(ref), 1e-300)),
+            "rms_rel": float(np.sqrt(np.mean(d * d)) / max(np.sqrt(np.mean(ref * ref)), 1e-300))}
+
+
+def oracle_errors(E, w, s, cfg, full, snap, phi64, conv64):
+    """Errors of the chosen (mixed) form against the float64 oracle
+    (oracle/espic_oracle.c) on the state of the last timed step:
+
+    * ion density: the GPU's mixed deposit against the oracle's float64
+      deposit (Field_::scatter, ch2/Field.h:164-183) of the same particles,
+      widened exactly to float64 -- on every node (full) or on the node planes
+      of a 33-plane slab through the sphere (cells outside the slab's
+      particles do not touch it);
+    * phi: the GPU's FP32-inner Newton-PCG result against the oracle's float64
+      Newton-PCG on the oracle's charge density (full), or against the GPU's
+      float64 Newton-PCG on the same density (phi64; the grid is too large
+      for the host solve);
+    * E: the GPU's computeEF of the mixed phi against the oracle's computeEF
+      (ch2/PotentialSolver.cpp:70-110) of the float64 phi."""
     from oracle import pyoracle as po
-    import ctypes as C
+    g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
+    vol = w.read(E.FIELD_NODE_VOL)
+    den_gpu, phi_gpu, ef_gpu = snap["den"], snap["phi"], snap["ef"]
+    obj = w.object_id
+    cell, off, vel = s.get_mixed()
+    ni, nj, nk = cfg["n"]
+    plane = ni * nj
+    if full:
+        sel = slice(None)
+        k0, k1 = 0, nk - 1
+    else:
+        kc = int(round((cfg["center"][2] - cfg["x0"][2]) / ((cfg["xm"][2] - cfg["x0"][2]) / (nk - 1))))
+        k0, k1 = kc - 16, kc + 16
+        kk = cell >> 20
+        sel = (kk >= k0 - 1) & (kk <= k1)
+    P64 = po.from_mixed(g, np.ascontiguousarray(cell[sel]), np.ascontiguousarray(off[:, sel]),
+                        np.ascontiguousarray(vel[:, sel]), cfg["mpw0"])
+    del cell, off, vel
+    den_o = po.divide_volume(po.deposit_fp64(g, P64), vol)
+    del P64
+    nodes = slice(k0 * plane, (k1 + 1) * plane)
+    out = {"den": _err(den_gpu[nodes], den_o[nodes]), "den_nodes": "all" if full else "planes %d-%d" % (k0, k1)}
+    if full:
+        phi_o, conv, _, _ = po.newton_pcg(g, phi_gpu, den_o * QE, obj, PHI0, TE, N0, nr_max=50, nr_tol=1e-11,
+                                          pcg_max=200000, pcg_tol=1e-12)
+        out["phi_reference"] = "oracle float64 Newton-PCG on the oracle's density (converged: %s)" % conv
+    else:
+        phi_o = phi64
+        out["phi_reference"] = "GPU float64 Newton-PCG on the same density (converged: %s)" % conv64
+    out["phi"] = _err(phi_gpu, phi_o)
+    ef_o = po.efield(g, phi_o)
+    out["E"] = _err(ef_gpu, ef_o)
+    out["E_reference"] = "oracle computeEF of that float64 phi"
+    return out
+
+
+def gpu_reference_algorithm_iterations(E, w, s, src, cfg):
+    """Newton and PCG iterations of the reference's algorithm (Newton with a
+    Jacobi-preconditioned CG in float64, no predictor) for one step of this
+    state, on the GPU: the count the host baseline's per-iteration cost is
+    multiplied by."""
+    src.sample()
+    s.advance(deposit=True)
+    w.computeChargeDensity()
+    sol = E.PotentialSolver(w, E.SOLVER_PCG, 1000, 1e-4)
+    sol.setReferenceValues(PHI0, TE, N0)
+    sol.setNewton(nr_max=20, nr_tol=NR_TOL, pcg_max=200000, pcg_tol=PCG_TOL, fp32_inner=False)
+    sol.setMultigrid(0)
+    sol.setPredictor(False)
+    conv, nr, inner, _ = sol.solve()
+    sol.setMultigrid(12)
+    sol.setPredictor(True)
+    return dict(newton=nr, pcg=inner, converged=bool(conv))
+
+
+def _oracle_sphere(cfg):
+    from oracle import pyoracle as po
     g = po.grid(cfg["n"], cfg["x0"], cfg["xm"])
     obj, phi = po.objects(g, cfg["center"], cfg["radius"], cfg["phi_s"])
-    ef = po.efield(g, phi)
-    P = np.ascontiguousarray(P0.copy())
-    n = P.shape[1]
     sph = np.array(list(cfg["center"]) + [cfg["radius"] ** 2])
+    return po, g, obj, phi, sph
+
+
+def cpu_sphere_steps(cfg, P0, threads, steps, warmup, seed=7):
+    """The sphere step of ch3/ver2/Main.cpp:50-80 on this host's cores with
+    the oracle port: warm-beam injection (ch4/Source.cpp:31-55), push with
+    absorption and removal, fixed-point deposit (threaded over particle
+    ranges like ch9/MT/Species.cpp:37-110), charge density, the serial
+    Newton-PCG (Jacobi preconditioner, ch3/ver2/PotentialSolver.cpp:225-331,
+    in its symmetric form) from the previous step's potential to the GPU
+    arm's tolerances, and computeEF.  An initial cold solve precedes the
+    steps, as in Main.cpp.  Every step is timed whole; returns the mean
+    seconds per step, the mean particle count and the measured iterations."""
+    import ctypes as C
+    po, g, obj, phi, sph = _oracle_sphere(cfg)
+    vol = po.node_volumes(g)
+    M = 16 * AMU
+    n = P0.shape[1]
+    cap = n + 200_000
+    P = np.zeros((7, cap))
+    P[:, :n] = P0
+    fx = 2.0 ** po.fixed_scale_exponent(cfg["mpw0"], cap)
     acc = np.zeros(g.nn, dtype=np.int64)
     nout = C.c_int64(0)
-    fx = 2.0 ** po.fixed_scale_exponent(cfg["mpw0"], n)
-    t_pd = po.lib().eo_bench_push_deposit(C.byref(g), po.pd(ef), po.pd(sph), QE, 16 * AMU, cfg["dt"], fx,
-                                          po.pd(P), n, n, threads, steps, C.byref(nout), po.pi64(acc))
-    vol = po.node_volumes(g)
-    rho = po.density_from_fixed(acc, fx, vol) * QE
+    L = po.lib()
+    rng = np.random.default_rng(seed)
+
+    def density(P, n):
+        acc[:] = po.deposit_fixed(g, np.ascontiguousarray(P[:, :n]), fx)
+        return po.density_from_fixed(acc, fx, vol)
+
     t0 = time.perf_counter()
-    _, _, nr, pcg = po.newton_pcg(g, phi, rho, obj, PHI0, TE, N0, nr_max=1, nr_tol=0.0, pcg_max=it_cap,
-                                  pcg_tol=0.0)
-    t_solve = time.perf_counter() - t0
-    per_iter = t_solve / max(pcg, 1)
-    step_s = t_pd / steps + per_iter * inner_per_step
-    return dict(value=n / step_s, push_deposit_s=t_pd / steps, pcg_iter_s=per_iter,
-                sample="%d steps of threaded push+compaction+deposit over all %d ions (%d threads); "
-                       "serial Newton-PCG timed over %d inner iterations and scaled to %.0f per step"
-                       % (steps, n, threads, pcg, inner_per_step))
+    phi, conv0, nr0, pcg0 = po.newton_pcg(g, phi, density(P, n) * QE, obj, PHI0, TE, N0, nr_max=50, nr_tol=NR_TOL,
+                                          pcg_max=200000, pcg_tol=PCG_TOL)
+    t_cold = time.perf_counter() - t0
+    ef = po.efield(g, phi)
+    times, counts, nrs, pcgs = [], [], [], []
+    for st in range(warmup + steps):
+        t0 = time.perf_counter()
+        # inject (the GPU arm's beam source: ch4 warm beam)
+        u = rng.random(1 + 13 * (int(N0 * V_DRIFT * 0.2 * 0.2 * cfg["dt"] / cfg["mpw0"]) + 2))
+        used = C.c_int64(0)
+        n = L.eo_inject_warm(C.byref(g), po.pd(ef), QE, M, cfg["dt"], cfg["mpw0"], V_DRIFT, N0, TI_EV * QE / K,
+                             po.pd(u), C.byref(used), po.pd(P), cap, n, cap)
+        assert n >= 0
+        # push + removal + deposit, threaded
+        L.eo_bench_push_deposit(C.byref(g), po.pd(ef), po.pd(sph), QE, M, cfg["dt"], fx, po.pd(P), cap, n, threads, 1,
+                                C.byref(nout), po.pi64(acc))
+        n = nout.value
+        rho = po.density_from_fixed(acc, fx, vol) * QE
+        phi, conv, nr, pcg = po.newton_pcg(g, phi, rho, obj, PHI0, TE, N0, nr_max=20, nr_tol=NR_TOL, pcg_max=200000,
+                                           pcg_tol=PCG_TOL)
+        ef = po.efield(g, phi)
+        el = time.perf_counter() - t0
+        if st >= warmup:
+            times.append(el)
+            counts.append(n)
+            nrs.append(nr)
+            pcgs.append(pcg)
+    return dict(seconds=float(np.mean(times)), n=float(np.mean(counts)), newton=float(np.mean(nrs)),
+                pcg=float(np.mean(pcgs)), cold_solve_s=t_cold, cold_pcg=pcg0, converged=bool(conv0))
+
+
+def cpu_sample_costs(cfg, n_sample, threads, seed=1):
+    """Per-particle cost of the threaded push + removal + deposit over a
+    contiguous sample of the synthetic state, and the serial Newton-PCG's
+    costs on the full grid: one residual evaluation (Newton iteration) and
+    one Jacobi-PCG iteration, separated by timing runs of 1 and 3 PCG
+    iterations."""
+    import ctypes as C
+    po, g, obj, phi, sph = _oracle_sphere(cfg)
+    P = np.ascontiguousarray(synthetic_state(cfg, n_sample, seed))
+    n = P.shape[1]
+    fx = 2.0 ** po.fixed_scale_exponent(cfg["mpw0"], n)
+    acc = np.zeros(g.nn, dtype=np.int64)
+    nout = C.c_int64(0)
+    ef = po.efield(g, phi)
+    t_pd = po.lib().eo_bench_push_deposit(C.byref(g), po.pd(ef), po.pd(sph), QE, 16 * AMU, cfg["dt"], fx, po.pd(P),
+                                          n, n, threads, 1, C.byref(nout), po.pi64(acc))
+    rho = po.density_from_fixed(acc, fx, po.node_volumes(g)) * QE
+    t = {}
+    for it in (1, 3):
+        t0 = time.perf_counter()
+        po.newton_pcg(g, phi, rho, obj, PHI0, TE, N0, nr_max=1, nr_tol=0.0, pcg_max=it, pcg_tol=0.0)
+        t[it] = time.perf_counter() - t0
+    per_iter = (t[3] - t[1]) / 2
+    return dict(pd_per_particle=t_pd / n, survive=nout.value / n, pcg_iter_s=per_iter,
+                newton_res_s=max(t[1] - per_iter, 0.0), sample=n)
+
+
+def c2_jacobi_iterations(threads, steps=3, warmup=1):
+    """Newton and Jacobi-PCG iterations per step of the oracle's serial solve
+    on the 64x64x128 sphere, measured on this host (cold solve, then steps
+    warm-started from the previous potential)."""
+    cfg = CONFIGS["sphere64"]
+    r = cpu_sphere_steps(cfg, synthetic_state(cfg, cfg["np"], 1), threads, steps, warmup)
+    return r
 
 
 def run_reference(args):
@@ -321,23 +473,61 @@ def run_reference(args):
         return
     cfg = CONFIGS[args.config]
     threads = os.cpu_count() or 1
-    P0 = synthetic_state(cfg, cfg["np"] if args.config == "sphere64" else 20_000_000, 1)
-    inner_per_step = float(os.environ.get("ESPIC_REF_INNER_PER_STEP", "800"))
-    vals = []
-    for i in range(args.warmup + args.steps):
-        b = cpu_baseline(cfg, P0, inner_per_step, threads, steps=1)
-        if i >= args.warmup:
-            vals.append(b)
-    v = float(np.mean([b["value"] for b in vals]))
+    if args.config == "sphere64":
+        # every step measured whole, on the GPU arm's initial state and ion count
+        P0 = synthetic_state(cfg, cfg["np"], 1)
+        # a host step takes seconds: at most 6 timed steps after 1 warm-up
+        ksteps, kwarm = min(args.steps, 6), min(args.warmup, 1)
+        r = cpu_sphere_steps(cfg, P0, threads, ksteps, kwarm)
+        v = r["n"] / r["seconds"]
+        sample = ("%d whole steps after %d warm-up steps (inject, threaded push+removal+deposit on %d threads, "
+                  "serial Newton-PCG with Jacobi preconditioner from the previous potential: %.2f Newton and %.1f "
+                  "PCG iterations per step measured, computeEF) over %.0f ions; cold initial solve %.1f s "
+                  "(%d PCG iterations)" % (ksteps, kwarm, threads, r["newton"], r["pcg"], r["n"],
+                                            r["cold_solve_s"], r["cold_pcg"]))
+        extra = {"newton_per_step": r["newton"], "pcg_iterations_per_step": r["pcg"],
+                 "poisson_ms_per_step": None}
+        ms = 1e3 * r["seconds"]
+        particles = r["n"]
+    else:
+        # the 256x256x512 case cannot run whole on the host (a single step's
+        # serial solve takes minutes): a bounded sample, stated
+        c2 = c2_jacobi_iterations(threads)
+        c2cfg = CONFIGS["sphere64"]
+        refine = max((c2cfg["xm"][d] - c2cfg["x0"][d]) / (c2cfg["n"][d] - 1) /
+                     ((cfg["xm"][d] - cfg["x0"][d]) / (cfg["n"][d] - 1)) for d in range(3))
+        vals = []
+        for i in range(args.warmup + args.steps):
+            c = cpu_sample_costs(cfg, 20_000_000, threads, seed=1 + i)
+            if i >= args.warmup:
+                vals.append(c)
+        pd_pp = float(np.mean([c["pd_per_particle"] for c in vals]))
+        it_s = float(np.mean([c["pcg_iter_s"] for c in vals]))
+        res_s = float(np.mean([c["newton_res_s"] for c in vals]))
+        particles = cfg["np"] * float(np.mean([c["survive"] for c in vals]))
+        pcg = c2["pcg"] * refine
+        solve_s = c2["newton"] * res_s + pcg * it_s
+        step_s = particles * pd_pp + solve_s
+        v = particles / step_s
+        ms = 1e3 * step_s
+        sample = ("per step: threaded push+removal+deposit of a 20M-ion sample (%d threads) scaled to %.0f ions; "
+                  "serial Newton-PCG costs on the full grid (residual %.3f s, Jacobi-PCG iteration %.3f s, "
+                  "measured) x the iterations per step measured on this host at 64x64x128 (%.2f Newton, %.1f PCG, "
+                  "warm-started steps after a cold solve) with the PCG count scaled by the grid refinement %.2f "
+                  "(Jacobi-PCG iterations grow as 1/h): %.0f PCG iterations per step"
+                  % (threads, particles, res_s, it_s, c2["newton"], c2["pcg"], refine, pcg))
+        extra = {"newton_per_step": c2["newton"], "pcg_iterations_per_step": pcg,
+                 "poisson_ms_per_step": 1e3 * solve_s, "c2_measured": {"newton": c2["newton"], "pcg": c2["pcg"]}}
     line = {"metric": METRIC, "value": v, "unit": "particle-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * P0.shape[1] / v, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.config, "grid": list(cfg["n"]), "particles": P0.shape[1]},
+            "config": {"workload": args.config, "grid": list(cfg["n"]), "particles": particles},
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                             "sample": vals[-1]["sample"]},
+                             "sample": sample},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line))
 
 
@@ -471,20 +661,36 @@ def ensemble_spec(cfg):
     return nodes, n_i, n_e, octant, mpw
 
 
-def make_ensemble(E, cfg):
+def make_ensemble(E, cfg, boxes=None):
+    """The ensemble of cfg's boxes, or of the subset `boxes` (their ids in
+    the whole ensemble key their random streams, so each box loads the same
+    particles whichever rank owns it)."""
     nodes, n_i, n_e, octant, mpw = ensemble_spec(cfg)
-    nb = cfg["nbox"]
+    ids = np.arange(cfg["nbox"]) if boxes is None else np.asarray(boxes, dtype=np.int64)
     x0, xm = np.array(cfg["x0"]), np.array(cfg["xm"])
-    ens = E.Ensemble(nodes, x0, xm, [16 * AMU, E.ME], [QE, -QE], mpw, np.stack([n_i, n_e], axis=1), cfg["dt"])
+    ens = E.Ensemble(nodes[ids], x0, xm, [16 * AMU, E.ME], [QE, -QE], mpw[ids],
+                     np.stack([n_i[ids], n_e[ids]], axis=1), cfg["dt"])
+    if boxes is not None:
+        ens.set_box_ids(ids)
     mid = (x0 + xm) / 2
-    for b in range(nb):
-        ens.load_box(b, 0, x0, xm, n_i[b])
+    for local, b in enumerate(ids):
+        ens.load_box(local, 0, x0, xm, n_i[b])
         lo = np.where((octant[b] >> np.arange(3)) & 1, mid, x0)
         hi = np.where((octant[b] >> np.arange(3)) & 1, xm, mid)
-        ens.load_box(b, 1, lo, hi, n_e[b])
+        ens.load_box(local, 1, lo, hi, n_e[b])
     ens.set_solver(10000, 1e-4, 0.0)
     ens.prepare()
-    return ens, int(n_i.sum() + n_e.sum()), nodes
+    return ens, int(n_i[ids].sum() + n_e[ids].sum()), nodes[ids]
+
+
+def ensemble_shard(E, cfg, rank, world_size):
+    """The boxes this rank steps: the whole ensemble split by work
+    (particles + nodes) with no exchange between ranks."""
+    if world_size <= 1:
+        return None
+    nodes, n_i, n_e, _, _ = ensemble_spec(cfg)
+    owner, _ = E.partition_boxes(E.ensemble_work(nodes, n_i + n_e), world_size)
+    return np.nonzero(owner == rank)[0]
 
 
 def ensemble_cpu_baseline(E, ens, nodes, cfg, nsample=3):
@@ -521,7 +727,8 @@ def run_ensemble(args, E, torch, dist, rank, world_size):
     over a work list, per-box SOR + E), FP32 particles under an FP64
     residual, tol 1e-4, the per-box optimal red-black factor."""
     cfg = CONFIGS["ensemble512"]
-    ens, npart, nodes = make_ensemble(E, cfg)
+    mine = ensemble_shard(E, cfg, rank, world_size)
+    ens, npart, nodes = make_ensemble(E, cfg, mine)
     tune = ens.autotune()
     stream = torch.cuda.ExternalStream(ens.stream_handle())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -552,13 +759,15 @@ def run_ensemble(args, E, torch, dist, rank, world_size):
         ens.step(1)
         ens.status()
     e2e_s = (time.perf_counter() - t0) / args.steps
+    _, e2e_value, _ = aggregate(1e3 * e2e_s, float(npart), dist, "cuda")
     hbm, kind = peaks()
     push_gbs = 56.0 * npart / (tune["push_ms"] * 1e-3) / 1e9
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "f32+i32 particles, f32 SOR sweeps under f64 residual",
             "data": "synthetic",
-            "config": {"workload": "ensemble512", "boxes": cfg["nbox"], "particles": npart,
+            "config": {"workload": "ensemble512", "boxes": cfg["nbox"], "boxes_rank0": int(len(nodes)),
+                       "particles_rank0": npart, "parallelism": "boxes split by work over %d ranks" % ws,
                        "nodes": int(np.prod(nodes, axis=1).sum()), "solver": "red-black SOR, per-box optimal "
                        "omega, tol 1e-4", "launch": {k: tune[k] for k in ("chunk", "push_threads",
                                                                         "solve_threads", "cluster")},
@@ -566,8 +775,8 @@ def run_ensemble(args, E, torch, dist, rank, world_size):
             "phase_ms_per_step": {"push": tune["push_ms"], "solve": tune["solve_ms"]},
             "sor_sweeps_per_step": {"mean": float(np.mean(sweeps)), "max": int(np.max(sweeps))},
             "converged_boxes": int(conv.sum()),
-            "e2e": {"value": npart * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": int(cfg["nbox"] * 16)},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(len(nodes) * 16)},
             "gpu_launches": launches,
             "roofline_push": {"bound": "hbm", "kernel": "k_ens_push", "achieved": push_gbs, "peak": hbm,
                               "unit": "GB/s", "frac": push_gbs / hbm, "bytes_per_particle": 56,
@@ -854,7 +1063,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="espic", choices=["espic", "reference"])
-    ap.add_argument("--config", default="sphere64", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="sphere256", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain form")
     ap.add_argument("--ncu-case", action="store_true",
@@ -916,7 +1125,10 @@ def main():
     ck = clocks.stop()
     ms_step, value, _ = aggregate(float(np.sum(t["ms"])) / args.steps, t["n"], dist, "cuda")
     phases, counts = profiled_steps(E, w, cfg, max(3, min(args.steps, 10)))
-    err, conv64 = phi_error(E, w, cfg)
+    snap = {"den": s.den, "phi": w.phi.copy(), "ef": w.ef}
+    err, conv64, phi64 = phi_error(E, w, cfg)
+    errs = oracle_errors(E, w, s, cfg, not big, snap, phi64, conv64)
+    ref_it = gpu_reference_algorithm_iterations(E, w, s, src, cfg)
     inner_per_step = t["inner"] / max(args.steps, 1)
     # e2e through the C-ABI (a fresh world, same state)
     w.close()
@@ -969,6 +1181,8 @@ def main():
         "phase_ms_per_step": phases,
         "newton_per_step": t["newton"] / args.steps, "pcg_iterations_per_step": inner_per_step,
         "phi_rel_err_vs_fp64": err, "fp64_reference_converged": conv64,
+        "errors_vs_fp64_oracle": errs,
+        "reference_algorithm_iterations_per_step": ref_it,
         "fp64": fp64,
         "speedup_mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
         "e2e": {"value": e["n"] * world_size / (e["seconds"] / e2e_n), "unit": "particle-steps/s",
@@ -985,10 +1199,24 @@ def main():
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         if big:
-            b = cpu_baseline(cfg, synthetic_state(cfg, 20_000_000, 1), inner_per_step, threads, steps=1,
-                             it_cap=2)
+            # a bounded sample: per-particle and per-iteration host costs,
+            # measured, times this state's ion count and the reference
+            # algorithm's iterations measured above
+            c = cpu_sample_costs(cfg, 20_000_000, threads)
+            step_s = t["n"] * c["pd_per_particle"] + ref_it["newton"] * c["newton_res_s"] + \
+                ref_it["pcg"] * c["pcg_iter_s"]
+            b = {"value": t["n"] / step_s,
+                 "sample": "threaded push+removal+deposit of a 20M-ion sample (%d threads) scaled to %d ions; serial "
+                           "Newton-PCG costs on the full grid (residual %.3f s, Jacobi-PCG iteration %.3f s) x the "
+                           "reference algorithm's iterations for this state (%d Newton, %d Jacobi-PCG, measured on "
+                           "the GPU above)" % (threads, int(t["n"]), c["newton_res_s"], c["pcg_iter_s"],
+                                               ref_it["newton"], ref_it["pcg"])}
         else:
-            b = cpu_baseline(cfg, P0, inner_per_step, threads)
+            r = cpu_sphere_steps(cfg, P0, threads, steps=2, warmup=1)
+            b = {"value": r["n"] / r["seconds"],
+                 "sample": "2 whole steps after 1 warm-up step on the host (%d threads for the particles, serial "
+                           "Newton-PCG: %.2f Newton and %.1f Jacobi-PCG iterations per step, measured)"
+                           % (threads, r["newton"], r["pcg"])}
         line["cpu_baseline"] = {"value": b["value"], "unit": "particle-steps/s", "cores": threads, "kind": "port",
                                 "sample": b["sample"]}
     if rank == 0:

@@ -111,6 +111,16 @@ int espic_species_add(espic_world *w, int sp, const double *pos3, const double *
  * (the mixed form is converted to float64). */
 int espic_species_set(espic_world *w, int sp, const double *P, int64_t stride, int64_t n);
 int espic_species_get(espic_world *w, int sp, double *P, int64_t stride, int64_t cap, int64_t *n);
+/* The same access to Species::particles (ch2/Species.h:60) for a species in
+ * the mixed form, without conversion: cell keys i | j<<10 | k<<20 ([n]),
+ * in-cell offsets and velocities ([3][stride] float).  The state round-trips
+ * bit for bit (checkpoints, parity checks of the mixed arithmetic).
+ * espic_species_set_mixed refuses keys outside the cells and offsets outside
+ * [0,1] with ESPIC_ERR_ARG before copying anything. */
+int espic_species_set_mixed(espic_world *w, int sp, const int32_t *cell, const float *off, const float *vel,
+                            int64_t stride, int64_t n);
+int espic_species_get_mixed(espic_world *w, int sp, int32_t *cell, float *off, float *vel, int64_t stride,
+                            int64_t cap, int64_t *n);
 /* Species::loadParticlesBox, ch2/Species.cpp:74-97.  u = 3*num_mp uniforms
  * (x, y, z per particle) or NULL to draw them from the world's Philox stream. */
 int espic_species_load_box(espic_world *w, int sp, const double x1[3], const double x2[3],
@@ -396,6 +406,17 @@ int espic_ensemble_create(int nbox, const int32_t *nodes, const double *x0, cons
                           const double *mass, const double *charge, const double *mpw0, const int64_t *capacity,
                           double dt, espic_ensemble **out);
 void espic_ensemble_destroy(espic_ensemble *e);
+/* Sharding an ensemble over GPUs (one process per GPU, no exchange: the
+ * boxes are independent).  espic_partition_boxes assigns nbox boxes of the
+ * given work to nparts parts (largest work first, each to the least loaded
+ * part; deterministic, so every rank computes the same owner[]); load
+ * (optional, [nparts]) receives each part's work.  espic_ensemble_set_box_ids
+ * gives the boxes of a part their ids in the whole ensemble, which key their
+ * random streams, so a box loads the same particles on whichever rank owns
+ * it (ids NULL: the box index).  The ch9/MPI decomposition
+ * (ch9/MPI/include/World.h:73-128) splits one domain; boxes need no split. */
+int espic_partition_boxes(int nbox, const double *work, int nparts, int32_t *owner, double *load);
+int espic_ensemble_set_box_ids(espic_ensemble *e, const int32_t *ids);
 int espic_ensemble_set_seed(espic_ensemble *e, uint64_t seed);
 /* particles of (box, species) from a host [7][stride] float64 block (replaces
  * the segment); the weight row is ignored (the segment's mpw0 is used) */

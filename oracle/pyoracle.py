@@ -527,3 +527,108 @@ def run_reference(binary, op, inputs):
         subprocess.run([exe, op, fi, fo], check=True, stdout=subprocess.DEVNULL,
                        stderr=subprocess.DEVNULL)
         return kv_read(fo)
+
+
+# ---- the mixed particle form (the chosen GPU form), restated -------------------
+class MixArgs(C.Structure):
+    _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("qmdt", C.c_float),
+                ("dtdh", C.c_float * 3), ("dh", C.c_float * 3), ("sx", C.c_float * 3), ("r2", C.c_float)]
+
+
+def _sig_mixed(L):
+    PF = C.POINTER(C.c_float)
+    P32 = C.POINTER(C.c_int32)
+    PU8 = C.POINTER(C.c_uint8)
+    L.eo_mix_args_set.argtypes = [C.POINTER(MixArgs), C.POINTER(Grid), D, D, D, PD]
+    L.eo_ef_to_f32.argtypes = [I64, PD, PF]
+    L.eo_to_mixed.argtypes = [C.POINTER(Grid), PD, I64, I64, P32, PF, PF, I64]
+    L.eo_from_mixed.argtypes = [C.POINTER(Grid), P32, PF, PF, I64, I64, D, PD, I64]
+    L.eo_push_mixed.argtypes = [C.POINTER(MixArgs), PF, C.c_int, P32, PF, PF, I64, I64, PU8]
+    L.eo_compact_mixed.restype = I64
+    L.eo_compact_mixed.argtypes = [P32, PF, PF, I64, I64, PU8]
+    L.eo_deposit_mixed.argtypes = [C.POINTER(Grid), P32, PF, I64, I64, PU8, PI64]
+
+
+def _mlib():
+    L = lib()
+    if not getattr(L, "_mixed_sig", False):
+        _sig_mixed(L)
+        L._mixed_sig = True
+    return L
+
+
+def _pf(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _p32(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _pu8(a):
+    assert a.dtype == np.uint8 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_uint8))
+
+
+def mix_args(g, charge, mass, dt, sphere4=None):
+    a = MixArgs()
+    sph = None if sphere4 is None else np.ascontiguousarray(sphere4, dtype=np.float64)
+    _mlib().eo_mix_args_set(C.byref(a), C.byref(g), charge, mass, dt, None if sph is None else pd(sph))
+    return a
+
+
+def ef_to_f32(ef):
+    ef = np.ascontiguousarray(ef, dtype=np.float64).reshape(-1)
+    nn = ef.size // 3
+    out = np.zeros(4 * nn, dtype=np.float32)
+    _mlib().eo_ef_to_f32(nn, pd(ef), _pf(out))
+    return out
+
+
+def to_mixed(g, P):
+    """float64 block [7][n] -> (cell [n] int32, off [3][n] f32, vel [3][n] f32)"""
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    n = P.shape[1]
+    cell = np.zeros(n, dtype=np.int32)
+    off = np.zeros((3, n), dtype=np.float32)
+    vel = np.zeros((3, n), dtype=np.float32)
+    _mlib().eo_to_mixed(C.byref(g), pd(P), n, n, _p32(cell), _pf(off), _pf(vel), n)
+    return cell, off, vel
+
+
+def from_mixed(g, cell, off, vel, mpw0):
+    n = cell.size
+    P = np.zeros((7, n))
+    _mlib().eo_from_mixed(C.byref(g), _p32(np.ascontiguousarray(cell)), _pf(np.ascontiguousarray(off)),
+                          _pf(np.ascontiguousarray(vel)), n, n, mpw0, pd(P), n)
+    return P
+
+
+def push_mixed(a, ef4, walls, cell, off, vel, compact=True):
+    """One mixed push (walls 0 reflect, 1 absorb); with compact the dead are
+    removed in the GPU's holes order.  Returns (cell, off, vel, dead)."""
+    cell = np.ascontiguousarray(cell, dtype=np.int32).copy()
+    off = np.ascontiguousarray(off, dtype=np.float32).copy()
+    vel = np.ascontiguousarray(vel, dtype=np.float32).copy()
+    n = cell.size
+    dead = np.zeros(n, dtype=np.uint8)
+    L = _mlib()
+    L.eo_push_mixed(C.byref(a), _pf(np.ascontiguousarray(ef4, dtype=np.float32)), walls, _p32(cell), _pf(off),
+                    _pf(vel), n, n, _pu8(dead))
+    if not compact:
+        return cell, off, vel, dead
+    m = L.eo_compact_mixed(_p32(cell), _pf(off), _pf(vel), n, n, _pu8(dead))
+    return cell[:m].copy(), np.ascontiguousarray(off[:, :m]), np.ascontiguousarray(vel[:, :m]), dead
+
+
+def deposit_mixed(g, cell, off, skip=None):
+    """int64 node sums of round(w * 2^23) per corner (counts of mpw0 * 2^-23)"""
+    cell = np.ascontiguousarray(cell, dtype=np.int32)
+    off = np.ascontiguousarray(off, dtype=np.float32)
+    n = cell.size
+    acc = np.zeros(g.nn, dtype=np.int64)
+    sk = None if skip is None else _pu8(np.ascontiguousarray(skip, dtype=np.uint8))
+    _mlib().eo_deposit_mixed(C.byref(g), _p32(cell), _pf(off), n, n, sk, pi64(acc))
+    return acc

@@ -93,6 +93,10 @@ def lib():
             "espic_species_add": [VP, C.c_int, PD, PD, PD, I64],
             "espic_species_set": [VP, C.c_int, PD, I64, I64],
             "espic_species_get": [VP, C.c_int, PD, I64, I64, C.POINTER(I64)],
+            "espic_species_set_mixed": [VP, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), I64, I64],
+            "espic_species_get_mixed": [VP, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), I64, I64, C.POINTER(I64)],
             "espic_species_load_box": [VP, C.c_int, PD, PD, C.c_double, I64, PD],
             "espic_species_load_box_qs": [VP, C.c_int, PD, PD, C.c_double, PI],
             "espic_species_load_box_thermal": [VP, C.c_int, PD, PD, C.c_double, I64, PD, C.c_double, PD],
@@ -140,6 +144,8 @@ def lib():
             "espic_ensemble_create": [C.c_int, PI, PD, PD, C.c_int, PD, PD, PD, C.POINTER(I64), C.c_double,
                                       C.POINTER(VP)],
             "espic_ensemble_set_seed": [VP, C.c_uint64],
+            "espic_ensemble_set_box_ids": [VP, PI],
+            "espic_partition_boxes": [C.c_int, PD, C.c_int, PI, PD],
             "espic_ensemble_set_particles": [VP, C.c_int, C.c_int, PD, I64, I64],
             "espic_ensemble_get_particles": [VP, C.c_int, C.c_int, PD, I64, I64, C.POINTER(I64)],
             "espic_ensemble_load_box": [VP, C.c_int, C.c_int, PD, PD, I64],
@@ -402,6 +408,31 @@ class Species:
                                       C.byref(m)))
         return np.ascontiguousarray(P[:, :m.value])
 
+    def set_mixed(self, cell, off, vel):
+        """the mixed form's own state: cell keys [n] int32, offsets and
+        velocities [3][n] float32 (no conversion)"""
+        cell = np.ascontiguousarray(cell, dtype=np.int32)
+        off = np.ascontiguousarray(off, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        n = cell.size
+        check(lib().espic_species_set_mixed(self.world.h, self.id, cell.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            off.ctypes.data_as(C.POINTER(C.c_float)),
+                                            vel.ctypes.data_as(C.POINTER(C.c_float)), n, n))
+
+    def get_mixed(self):
+        """(cell [n] int32, off [3][n] float32, vel [3][n] float32)"""
+        m = I64()
+        check(lib().espic_species_get_mixed(self.world.h, self.id, None, None, None, 0, 0, C.byref(m)))
+        n = max(m.value, 1)
+        cell = np.zeros(n, dtype=np.int32)
+        off = np.zeros((3, n), dtype=np.float32)
+        vel = np.zeros((3, n), dtype=np.float32)
+        check(lib().espic_species_get_mixed(self.world.h, self.id, cell.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            off.ctypes.data_as(C.POINTER(C.c_float)),
+                                            vel.ctypes.data_as(C.POINTER(C.c_float)), n, n, C.byref(m)))
+        k = m.value
+        return cell[:k].copy(), np.ascontiguousarray(off[:, :k]), np.ascontiguousarray(vel[:, :k])
+
     def loadParticlesBox(self, x1, x2, num_den, num_mp, u=None):
         u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
         check(lib().espic_species_load_box(self.world.h, self.id, _d3(x1), _d3(x2), num_den,
@@ -621,6 +652,23 @@ class PotentialSolver:
         check(lib().espic_efield(self.world.h))
 
 
+def partition_boxes(work, nparts):
+    """Owner part of every box (largest work first, each to the least loaded
+    part; the same on every rank) and the work of each part."""
+    work = np.ascontiguousarray(work, dtype=np.float64)
+    owner = np.zeros(max(work.size, 1), dtype=np.int32)
+    load = np.zeros(nparts)
+    check(lib().espic_partition_boxes(work.size, _pd(work), nparts, owner.ctypes.data_as(PI), _pd(load)))
+    return owner[:work.size].copy(), load
+
+
+def ensemble_work(nodes, particles, node_weight=14.0):
+    """Work of a box step: its particles plus node_weight per node (the SOR
+    sweeps cost about 14 particle pushes per node on a GB300)."""
+    nodes = np.asarray(nodes).reshape(-1, 3)
+    return np.asarray(particles, dtype=np.float64) + node_weight * np.prod(nodes, axis=1).astype(np.float64)
+
+
 class Ensemble:
     """A batched ensemble of independent ch2 grounded boxes (ch2/Main.cpp:14-75
     per member): per-box node counts and extents, per (box, species) weights
@@ -645,6 +693,16 @@ class Ensemble:
         self.nodes, self.x0, self.xm = nodes, x0, xm
         self.nbox, self.nsp = nbox, nsp
         self.mass, self.charge, self.mpw0 = mass, charge, mpw0
+
+    def set_box_ids(self, ids):
+        """ids of these boxes in a larger ensemble (they key the boxes' random
+        streams); None restores the box index"""
+        if ids is None:
+            check(lib().espic_ensemble_set_box_ids(self.h, None))
+            return
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        assert ids.size == self.nbox
+        check(lib().espic_ensemble_set_box_ids(self.h, ids.ctypes.data_as(PI)))
 
     def close(self):
         if self.h:

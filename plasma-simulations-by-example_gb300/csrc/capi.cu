@@ -569,6 +569,66 @@ extern "C" int espic_species_get(espic_world *h, int sp, double *P, int64_t stri
     return take_device_errors(w);
 }
 
+extern "C" int espic_species_set_mixed(espic_world *h, int sp, const int32_t *cell, const float *off,
+                                       const float *vel, int64_t stride, int64_t n) {
+    WORLD(h);
+    SPECIES(sp);
+    if (s.form != ESPIC_FORM_MIXED) return fail(ESPIC_ERR_ARG, "the species is not in the mixed form");
+    if (n < 0 || n > s.cap) return fail(ESPIC_ERR_CAPACITY, "%lld particles exceed the capacity", (long long)n);
+    if (n > 0 && (!cell || !off || !vel || stride < n)) return fail(ESPIC_ERR_ARG, "bad mixed particle block");
+    /* every key must name a cell and every offset lie in [0,1] (1 itself
+     * occurs when an offset just below 1 rounds up to float): the kernels
+     * index the node fields with them */
+    for (int64_t p = 0; p < n; p++) {
+        const int32_t key = cell[p];
+        const int i = key & 1023, j = (key >> 10) & 1023, k = key >> 20;
+        if (key < 0 || i > w.g.ni - 2 || j > w.g.nj - 2 || k > w.g.nk - 2)
+            return fail(ESPIC_ERR_ARG, "particle %lld: cell key %d names no cell of the grid", (long long)p, key);
+        for (int d = 0; d < 3; d++) {
+            const float f = off[d * stride + p];
+            if (!(f >= 0.f && f <= 1.f))
+                return fail(ESPIC_ERR_ARG, "particle %lld: in-cell offset outside [0,1]", (long long)p);
+        }
+    }
+    if (n > 0) {
+        CK(cudaMemcpyAsync(s.cell, cell, n * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream));
+        CK(cudaMemcpy2DAsync(s.off, s.ms * sizeof(float), off, stride * sizeof(float), n * sizeof(float), 3,
+                             cudaMemcpyHostToDevice, w.stream));
+        CK(cudaMemcpy2DAsync(s.vel, s.ms * sizeof(float), vel, stride * sizeof(float), n * sizeof(float), 3,
+                             cudaMemcpyHostToDevice, w.stream));
+    }
+    int64_t cnt[4] = {n, n, 0, 0};
+    CK(cudaMemcpyAsync(s.d_count, cnt, sizeof cnt, cudaMemcpyHostToDevice, w.stream));
+    CK(cudaStreamSynchronize(w.stream));
+    s.host_bound = n;
+    return take_device_errors(w);
+}
+
+extern "C" int espic_species_get_mixed(espic_world *h, int sp, int32_t *cell, float *off, float *vel, int64_t stride,
+                                       int64_t cap, int64_t *np) {
+    WORLD(h);
+    SPECIES(sp);
+    if (s.form != ESPIC_FORM_MIXED) return fail(ESPIC_ERR_ARG, "the species is not in the mixed form");
+    int64_t n = 0;
+    CK(cudaMemcpyAsync(&n, s.d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, w.stream));
+    CK(cudaStreamSynchronize(w.stream));
+    s.host_bound = n;
+    if (np) *np = n;
+    if (!cell) return take_device_errors(w);
+    if (!off || !vel) return fail(ESPIC_ERR_ARG, "null offset or velocity block");
+    if (n > cap || stride < n) return fail(ESPIC_ERR_CAPACITY, "output holds %lld of %lld particles", (long long)cap,
+                                         (long long)n);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(cell, s.cell, n * sizeof(int32_t), cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaMemcpy2DAsync(off, stride * sizeof(float), s.off, s.ms * sizeof(float), n * sizeof(float), 3,
+                             cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaMemcpy2DAsync(vel, stride * sizeof(float), s.vel, s.ms * sizeof(float), n * sizeof(float), 3,
+                             cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaStreamSynchronize(w.stream));
+    }
+    return take_device_errors(w);
+}
+
 extern "C" int espic_species_load_box(espic_world *h, int sp, const double x1[3], const double x2[3],
                                       double num_den, int64_t num_mp, const double *u) {
     WORLD(h);

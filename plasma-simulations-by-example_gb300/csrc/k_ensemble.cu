@@ -426,6 +426,7 @@ struct espic_ensemble {
     double dt = 0;
     uint64_t seed = 0x5eed;
     std::vector<EnsBox> boxes;
+    std::vector<int32_t> box_id; /* the id that keys each box's random streams (default: its index) */
     std::vector<EnsSeg> segs; /* [box][species] */
     std::vector<double> mass, charge, mpw0;
     int64_t total_nodes = 0, total_cap = 0;
@@ -762,7 +763,8 @@ extern "C" int espic_ensemble_load_box(espic_ensemble *h, int box, int sp, const
     for (int d = 0; d < 3; d++)
         if (x1[d] < BX.g.x0[d] || x2[d] > BX.g.xm[d] || !(x2[d] > x1[d]))
             return efail(ESPIC_ERR_ARG, "load region must lie inside the box");
-    uint64_t stream = ((uint64_t)(0x40000 + (uint64_t)box * E.nsp + sp)) << 32;
+    const uint64_t id = E.box_id.empty() ? (uint64_t)box : (uint64_t)E.box_id[box];
+    uint64_t stream = ((uint64_t)(0x40000 + id * E.nsp + sp)) << 32;
     if (num_mp > 0) {
         k_ens_load<<<blocks_for(num_mp, 256), 256, 0, E.stream>>>(BX.g, make_double3(x1[0], x1[1], x1[2]),
                                                                   make_double3(x2[0], x2[1], x2[2]), num_mp, E.seed,
@@ -774,6 +776,41 @@ extern "C" int espic_ensemble_load_box(espic_ensemble *h, int box, int sp, const
     E.work_valid = false;
     ens_drop_graph(E);
     return ens_upload_tables(E);
+}
+
+extern "C" int espic_ensemble_set_box_ids(espic_ensemble *h, const int32_t *ids) {
+    ENSEMBLE(h);
+    if (!ids) {
+        E.box_id.clear();
+        return ESPIC_OK;
+    }
+    for (int b = 0; b < E.nbox; b++)
+        if (ids[b] < 0 || ids[b] >= (1 << 24)) return efail(ESPIC_ERR_ARG, "box id %d out of range", ids[b]);
+    E.box_id.assign(ids, ids + E.nbox);
+    return ESPIC_OK;
+}
+
+extern "C" int espic_partition_boxes(int nbox, const double *work, int nparts, int32_t *owner, double *load) {
+    if (nbox < 0 || nparts < 1 || (nbox > 0 && (!work || !owner)))
+        return efail(ESPIC_ERR_ARG, "bad partition arguments");
+    for (int b = 0; b < nbox; b++)
+        if (!(work[b] >= 0)) return efail(ESPIC_ERR_ARG, "box %d: work must be finite and >= 0", b);
+    /* largest work first (ties by box index), each to the least loaded part
+     * (ties to the lowest part): deterministic on every rank */
+    std::vector<int> order(nbox);
+    for (int b = 0; b < nbox; b++) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+    std::vector<double> L(nparts, 0.0);
+    for (int b : order) {
+        int best = 0;
+        for (int r = 1; r < nparts; r++)
+            if (L[r] < L[best]) best = r;
+        owner[b] = best;
+        L[best] += work[b];
+    }
+    if (load)
+        for (int r = 0; r < nparts; r++) load[r] = L[r];
+    return ESPIC_OK;
 }
 
 extern "C" int espic_ensemble_set_seed(espic_ensemble *h, uint64_t seed) {

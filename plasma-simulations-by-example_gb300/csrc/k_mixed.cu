@@ -56,9 +56,10 @@ __device__ __forceinline__ void cic_w(float fx, float fy, float fz, float w[8]) 
     w[7] = gx * fy * fz;
 }
 
-/* move a coordinate in cell units: returns the new cell index */
-__device__ __forceinline__ int advance_axis(int i, float &f, float dv) {
-    f += dv;
+/* move a coordinate by v*dtdh cells (one fused multiply-add): returns the
+ * new cell index, f stays in [0,1) */
+__device__ __forceinline__ int advance_axis(int i, float &f, float v, float dtdh) {
+    f = __fmaf_rn(v, dtdh, f);
     float fl = floorf(f);
     i += (int)fl;
     f -= fl;
@@ -67,6 +68,19 @@ __device__ __forceinline__ int advance_axis(int i, float &f, float dv) {
         i += 1;
     }
     return i;
+}
+
+/* trilinear E at the particle: a chain of fused multiply-adds over the
+ * corners in Field_::gather's order (ch2/Field.h:186-208), from corner 0 */
+__device__ __forceinline__ float3 gather_corners(const float w[8], const float4 e[8]) {
+    float3 r = make_float3(__fmul_rn(w[0], e[0].x), __fmul_rn(w[0], e[0].y), __fmul_rn(w[0], e[0].z));
+#pragma unroll
+    for (int c = 1; c < 8; c++) {
+        r.x = __fmaf_rn(w[c], e[c].x, r.x);
+        r.y = __fmaf_rn(w[c], e[c].y, r.y);
+        r.z = __fmaf_rn(w[c], e[c].z, r.z);
+    }
+    return r;
 }
 
 __device__ __forceinline__ void reflect_axis(int &i, float &f, float &v, int n) {
@@ -169,21 +183,15 @@ __device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const floa
     int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
     float w[8];
     cic_w(fx, fy, fz, w);
-    float4 e0 = __ldg(ef4 + n0), e1 = __ldg(ef4 + n0 + 1), e2 = __ldg(ef4 + n0 + 1 + sy), e3 = __ldg(ef4 + n0 + sy),
-           e4 = __ldg(ef4 + n0 + sz), e5 = __ldg(ef4 + n0 + 1 + sz), e6 = __ldg(ef4 + n0 + 1 + sy + sz),
-           e7 = __ldg(ef4 + n0 + sy + sz);
-    float ex = w[0] * e0.x + w[1] * e1.x + w[2] * e2.x + w[3] * e3.x + w[4] * e4.x + w[5] * e5.x + w[6] * e6.x +
-               w[7] * e7.x;
-    float ey = w[0] * e0.y + w[1] * e1.y + w[2] * e2.y + w[3] * e3.y + w[4] * e4.y + w[5] * e5.y + w[6] * e6.y +
-               w[7] * e7.y;
-    float ez = w[0] * e0.z + w[1] * e1.z + w[2] * e2.z + w[3] * e3.z + w[4] * e4.z + w[5] * e5.z + w[6] * e6.z +
-               w[7] * e7.z;
-    vx += ex * a.qmdt;
-    vy += ey * a.qmdt;
-    vz += ez * a.qmdt;
-    i = advance_axis(i, fx, vx * a.dtdh[0]);
-    j = advance_axis(j, fy, vy * a.dtdh[1]);
-    k = advance_axis(k, fz, vz * a.dtdh[2]);
+    const float4 e[8] = {__ldg(ef4 + n0),      __ldg(ef4 + n0 + 1),      __ldg(ef4 + n0 + 1 + sy),      __ldg(ef4 + n0 + sy),
+                         __ldg(ef4 + n0 + sz), __ldg(ef4 + n0 + 1 + sz), __ldg(ef4 + n0 + 1 + sy + sz), __ldg(ef4 + n0 + sy + sz)};
+    const float3 E = gather_corners(w, e);
+    vx = __fmaf_rn(E.x, a.qmdt, vx);
+    vy = __fmaf_rn(E.y, a.qmdt, vy);
+    vz = __fmaf_rn(E.z, a.qmdt, vz);
+    i = advance_axis(i, fx, vx, a.dtdh[0]);
+    j = advance_axis(j, fy, vy, a.dtdh[1]);
+    k = advance_axis(k, fz, vz, a.dtdh[2]);
     bool dead = false;
     if (WALLS == M_REFLECT) {
         reflect_axis(i, fx, vx, a.ni);
@@ -192,10 +200,10 @@ __device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const floa
     } else {
         dead = i < 0 || i > a.ni - 2 || j < 0 || j > a.nj - 2 || k < 0 || k > a.nk - 2;
         if (!dead && a.r2 >= 0.f) {
-            float rx = ((float)i + fx) * a.dh[0] + a.sx[0];
-            float ry = ((float)j + fy) * a.dh[1] + a.sx[1];
-            float rz = ((float)k + fz) * a.dh[2] + a.sx[2];
-            dead = rx * rx + ry * ry + rz * rz <= a.r2;
+            const float rx = __fmaf_rn((float)i + fx, a.dh[0], a.sx[0]);
+            const float ry = __fmaf_rn((float)j + fy, a.dh[1], a.sx[1]);
+            const float rz = __fmaf_rn((float)k + fz, a.dh[2], a.sx[2]);
+            dead = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx))) <= a.r2;
         }
     }
     if (!(isfinite(fx) && isfinite(fy) && isfinite(fz) && isfinite(vx) && isfinite(vy) && isfinite(vz))) {
@@ -348,7 +356,7 @@ __global__ void k_from_mixed_n(Geo g, const int32_t *__restrict__ cell, const fl
     int i[3];
     unpack(cell[p], i[0], i[1], i[2]);
     for (int d = 0; d < 3; d++) {
-        P[d * pstride + t] = g.x0[d] + ((double)i[d] + (double)off[d * stride + p]) * g.dh[d];
+        P[d * pstride + t] = __fma_rn((double)i[d] + (double)off[d * stride + p], g.dh[d], g.x0[d]);
         P[(3 + d) * pstride + t] = (double)vel[d * stride + p];
     }
     P[6 * pstride + t] = w0;
@@ -383,7 +391,7 @@ __global__ void k_from_mixed(Geo g, const int32_t *__restrict__ cell, const floa
     int i[3];
     unpack(cell[p], i[0], i[1], i[2]);
     for (int d = 0; d < 3; d++) {
-        P[d * pstride + p] = g.x0[d] + ((double)i[d] + (double)off[d * stride + p]) * g.dh[d];
+        P[d * pstride + p] = __fma_rn((double)i[d] + (double)off[d * stride + p], g.dh[d], g.x0[d]);
         P[(3 + d) * pstride + p] = (double)vel[d * stride + p];
     }
     P[6 * pstride + p] = w0;

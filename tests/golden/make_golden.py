@@ -391,6 +391,46 @@ def steady_cases():
     save("sphere_steady", steps=ss.STEPS, dt=ss.DT, mpw0=ss.MPW0, avg=np.array(ss.AVG), **arrays)
 
 
+LONG_STEPS, LONG_BATCH, LONG_SEEDS = 10000, 500, (1, 2, 3, 4, 5, 6)
+
+
+def box_longrun(seed):
+    """One 10,000-step run of the ch2 main loop at the reference's
+    configuration 1 (80,000 O+ over the box and 10,000 electrons in the
+    octant [-0.1,0]^2 x [0,0.1] at n = 1e11, ch2/snippets/step4/Main.cpp:31-34;
+    dt 2e-10; SOR to 1e-4, ch2/Main.cpp:38): the energy history
+    (ch2/Output.cpp:82-118 columns) reduced to batch means."""
+    g = po.grid(BOX["grid"], BOX["x0"], BOX["xm"])
+    dt = 2e-10
+    li = po.run_reference("ref_ch2", "load_box", base_inputs(
+        BOX, dt, ns=[1], sp0_mq=[16 * AMU, QE], seed=[1000 + seed], x1=BOX["x0"], x2=BOX["xm"],
+        num_den=[1e11], num_mp=[80000], ef=np.zeros(3 * g.nn)))
+    le = po.run_reference("ref_ch2", "load_box", base_inputs(
+        BOX, dt, ns=[1], sp0_mq=[ME, -QE], seed=[2000 + seed], x1=BOX["x0"], x2=[0.0, 0.0, 0.1],
+        num_den=[1e11], num_mp=[10000], ef=np.zeros(3 * g.nn)))
+    st = base_inputs(BOX, dt, steps=[LONG_STEPS], ns=[2], sp0_mq=[16 * AMU, QE], sp1_mq=[ME, -QE],
+                     sp0_P=li["sp0_P"], sp1_P=le["sp0_P"], max_it=[10000], tol=[1e-4], initial_solve=[1])
+    # one row per time step (the loop runs while ts <= num_ts: steps + 1 rows);
+    # columns: ts, then per species np, real count, px, py, pz, KE; then PE
+    h = po.run_reference("ref_ch2", "steps", st)["hist"].reshape(-1, 14)[:LONG_STEPS]
+    return np.stack([h[:, 6], h[:, 12], h[:, 13], h[:, 6] + h[:, 12] + h[:, 13]], axis=1)
+
+
+def box_longrun_cases():
+    """Energy history of configuration 1 from several seeds of the
+    reference's own loop (run concurrently): batch means of KE (ions,
+    electrons), PE and their sum over 500-step batches, and the full
+    history of the first 200 steps."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(len(LONG_SEEDS)) as ex:
+        runs = list(ex.map(box_longrun, LONG_SEEDS))
+    E = np.stack(runs)  # [seed][step][KE_i, KE_e, PE, total]
+    nb = LONG_STEPS // LONG_BATCH
+    batches = E.reshape(len(LONG_SEEDS), nb, LONG_BATCH, 4).mean(axis=2)
+    save("box_longrun", steps=LONG_STEPS, batch=LONG_BATCH, seeds=np.array(LONG_SEEDS), batches=batches,
+         early=E[:, :200, :])
+
+
 if __name__ == "__main__":
     # optional arguments select cases: "base" (box and sphere, one random
     # stream), "steady", "dsmc", "neutral", "ch4push", "ch4ion", "ionize" (default: all)
@@ -413,3 +453,5 @@ if __name__ == "__main__":
         ch4_ion_push_cases()
     if "ionize" in cases:
         ionize_cases()
+    if "longrun" in cases:
+        box_longrun_cases()

@@ -175,3 +175,47 @@ def test_ensemble_reference_box_energy_history(espic):
             e_ref = ref[6] + ref[12] + ref[13]
             worst = max(worst, abs(e_ens - e_ref) / abs(e_ref))
         assert worst <= 1e-4, worst
+
+
+def test_sharded_ensemble_matches_whole(espic):
+    """The ensemble split by work into two parts (the per-rank shards of a
+    2-GPU run, stepped here one after the other on one GPU: no part waits on
+    the other) evolves every box bit for bit like the whole ensemble: boxes
+    load from streams keyed by their ids in the whole ensemble, and nothing
+    is exchanged between parts."""
+    nb = 10
+    rng = np.random.default_rng(4)
+    nodes = rng.integers(9, 20, size=(nb, 3))
+    n_i = rng.integers(2000, 20000, size=nb)
+    n_e = n_i // 4
+    x0, xm = np.array(X0), np.array(XM)
+    mpw = np.stack([1e11 * 0.008 / n_i, 1e11 * 0.001 / n_e], axis=1)
+
+    def make(ids):
+        E = espic.Ensemble(nodes[ids], x0, xm, MASS, CHARGE, mpw[ids], np.stack([n_i[ids], n_e[ids]], axis=1), 2e-10)
+        if len(ids) < nb:
+            E.set_box_ids(ids)
+        E.set_seed(99)
+        for loc, b in enumerate(ids):
+            E.load_box(loc, 0, x0, xm, int(n_i[b]))
+            E.load_box(loc, 1, x0, (x0 + xm) / 2, int(n_e[b]))
+        E.set_solver(10000, 1e-4, 0.0)
+        E.prepare()
+        E.step(3)
+        E.sync()
+        return {b: (E.particles(loc, 0), E.particles(loc, 1), E.read(loc, espic.FIELD_PHI)) for loc, b in
+                enumerate(ids)}, E
+
+    owner, load = espic.partition_boxes(espic.ensemble_work(nodes, n_i + n_e), 2)
+    assert set(owner) == {0, 1} and max(load) <= 1.5 * min(load)
+    whole, Ew = make(np.arange(nb))
+    with Ew:
+        parts = {}
+        for r in (0, 1):
+            res, Er = make(np.nonzero(owner == r)[0])
+            with Er:
+                parts.update(res)
+    assert sorted(parts) == list(range(nb))
+    for b in range(nb):
+        for a, c in zip(whole[b], parts[b]):
+            assert np.array_equal(a, c), b

@@ -125,3 +125,110 @@ def test_mixed_push_box_reflect_against_oracle(espic, po):
     assert got.shape == want.shape
     assert np.max(np.abs(got[0:3] - want[0:3]) / dh[:, None]) <= 1e-5
     assert np.max(np.abs(got[3:6] - want[3:6])) <= 1e-5 * np.max(np.abs(want[3:6]))
+
+
+# ---- bit-exact parity of the mixed form with its oracle restatement ------------
+# (oracle/espic_oracle.c restates the mixed arithmetic operation by operation:
+# float CIC weights, the gather's fused multiply-add chain, the push, the walls,
+# the removal order and the 2^-23 fixed-point deposit)
+
+def _ef4(w, po):
+    return po.ef_to_f32(w.ef)
+
+
+def test_to_mixed_matches_oracle(espic, po):
+    P = state(SPH, 50_000, 21)
+    g = po.grid(*SPH)
+    w, s = make(espic, SPH, P, espic.WALLS_ABSORB, False)
+    with w:
+        cell, off, vel = s.get_mixed()
+        back = s.particles()
+    c2, o2, v2 = po.to_mixed(g, P)
+    assert np.array_equal(cell, c2) and np.array_equal(off, o2) and np.array_equal(vel, v2)
+    # and back to float64: x = x0 + (i + f) dh with one fused multiply-add
+    assert np.array_equal(back, po.from_mixed(g, c2, o2, v2, 40.0))
+    assert np.max(np.abs(back[0:3] - P[0:3]) / np.array(g.dh)[:, None]) <= 2.0 ** -23
+
+
+@pytest.mark.parametrize("walls", ["reflect", "absorb"])
+@pytest.mark.parametrize("n", [1, 777, 300_000])
+def test_mixed_push_and_deposit_bitexact(espic, po, walls, n):
+    """One fused push + deposit on the GPU against the oracle's mixed
+    restatement from the same mixed state: cell keys, offsets, velocities,
+    the survivors and their order, and the integer charge (through the
+    density) agree bit for bit."""
+    wk = espic.WALLS_REFLECT if walls == "reflect" else espic.WALLS_ABSORB
+    geo = BOX if walls == "reflect" else SPH
+    P = state(geo, n, 40 + n, sphere=walls == "absorb", vd=0.0 if walls == "reflect" else 7000.0,
+              vth=8e5 if walls == "reflect" else 800.0)
+    if walls == "absorb" and n > 1000:
+        c, r = np.array(SPHERE[0]), SPHERE[1]
+        d = np.random.default_rng(3).standard_normal((3, 5000))
+        d /= np.linalg.norm(d, axis=0)
+        P[0:3, :5000] = c[:, None] + (r + 2e-4) * d
+        P[3:6, :5000] = -5e3 * d
+    g = po.grid(*geo)
+    dt = 1e-7 if walls == "absorb" else 2e-10
+    w, s = make(espic, geo, P, wk, False)
+    with w:
+        cell0, off0, vel0 = s.get_mixed()
+        ef4 = _ef4(w, po)
+        s.advance(deposit=True)
+        cell, off, vel = s.get_mixed()
+        den = s.den
+        vol = w.read(espic.FIELD_NODE_VOL)
+    a = po.mix_args(g, QE, M, dt, SPHERE4 if walls == "absorb" else None)
+    c2, o2, v2, dead = po.push_mixed(a, ef4, 0 if walls == "reflect" else 1, cell0, off0, vel0)
+    assert np.array_equal(cell, c2)
+    assert np.array_equal(off, o2) and np.array_equal(vel, v2)
+    acc = po.deposit_mixed(g, c2, o2)
+    want = po.density_from_fixed(acc, 8388608.0 / 40.0, vol)
+    assert np.array_equal(den, want)
+    if walls == "absorb" and n > 1000:
+        assert dead.sum() > 0
+
+
+def test_mixed_density_and_potential_against_fp64_oracle(espic, po):
+    """The chosen (mixed) form against the float64 oracle on the same
+    particles: the ion density within the deposit's quantisation and float
+    weight bound (each corner count is off by at most 1/2 of 2^-23 mpw0,
+    and the float weight by at most 4 ulps), then phi from the FP32-inner
+    Newton-PCG against the oracle's FP64 Newton-PCG on the oracle's density
+    (relative 1e-6 of max|phi|, the stated target) and E against the
+    oracle's computeEF of that phi (relative 1e-6 of max|E|)."""
+    P = state(SPH, 400_000, 77)
+    g = po.grid(*SPH)
+    w, s = make(espic, SPH, P, espic.WALLS_ABSORB, True)
+    with w:
+        w.addInlet()
+        sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 1000, 1e-4)
+        sol.setReferenceValues(0.0, 3.0, 1e10)
+        sol.setNewton(nr_max=20, nr_tol=1e-6, pcg_max=20000, pcg_tol=1e-4, fp32_inner=True)
+        s.advance(deposit=True)
+        den = s.den
+        cell, off, vel = s.get_mixed()
+        w.computeChargeDensity()
+        phi_start = w.phi
+        conv = sol.solve()[0]
+        phi = w.phi
+        sol.computeEF()
+        ef = w.ef
+        obj = w.object_id
+        vol = w.read(espic.FIELD_NODE_VOL)
+    assert conv
+    # density: the same particles in float64 through the oracle's deposit
+    P64 = po.from_mixed(g, cell, off, vel, 40.0)
+    den64 = po.divide_volume(po.deposit_fp64(g, P64), vol)
+    count = po.deposit_fp64(g, np.vstack([P64[:6], np.ones((1, P64.shape[1]))]))
+    contrib = np.ceil(count * 8 + 8)  # corner contributions per node, generous
+    bound = contrib * 40.0 * 5 * 2.0 ** -24 / np.where(vol > 0, vol, 1)
+    assert np.all(np.abs(den - den64) <= bound)
+    rel = np.abs(den - den64)[den64 > 0] / den64[den64 > 0]
+    assert np.sqrt(np.mean(rel ** 2)) < 1e-6
+    # phi: the oracle's float64 Newton-PCG on the oracle's charge density
+    rho64 = den64 * QE
+    phi64, conv64, _, _ = po.newton_pcg(g, phi_start, rho64, obj, 0.0, 3.0, 1e10, 30, 1e-10, 20000, 1e-12)
+    assert conv64
+    assert np.max(np.abs(phi - phi64)) <= 1e-6 * np.max(np.abs(phi64))
+    ef64 = po.efield(g, phi64)
+    assert np.max(np.abs(ef - ef64)) <= 1e-6 * np.max(np.abs(ef64))
