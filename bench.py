@@ -373,8 +373,8 @@ def cpu_sphere_steps(cfg, P0, threads, steps, warmup, seed=7):
     absorption and removal, fixed-point deposit (threaded over particle
     ranges like ch9/MT/Species.cpp:37-110), charge density, the serial
     Newton-PCG (Jacobi preconditioner, ch3/ver2/PotentialSolver.cpp:225-331,
-    in its symmetric form) from the previous step's potential to the GPU
-    arm's tolerances, and computeEF.  An initial cold solve precedes the
+    in its symmetric form, with the GPU path's inner stop rule) from the
+    previous step's potential to the GPU arm's tolerances, and computeEF.  An initial cold solve precedes the
     steps, as in Main.cpp.  Every step is timed whole; returns the mean
     seconds per step, the mean particle count and the measured iterations."""
     import ctypes as C
@@ -396,8 +396,8 @@ def cpu_sphere_steps(cfg, P0, threads, steps, warmup, seed=7):
         return po.density_from_fixed(acc, fx, vol)
 
     t0 = time.perf_counter()
-    phi, conv0, nr0, pcg0 = po.newton_pcg(g, phi, density(P, n) * QE, obj, PHI0, TE, N0, nr_max=50, nr_tol=NR_TOL,
-                                          pcg_max=200000, pcg_tol=PCG_TOL)
+    phi, conv0, nr0, pcg0, _ = po.newton_pcg_fallback(g, phi, density(P, n) * QE, obj, PHI0, TE, N0, 50, NR_TOL,
+                                                      200000, PCG_TOL, 0, 0.0, early_stop=True)
     t_cold = time.perf_counter() - t0
     ef = po.efield(g, phi)
     times, counts, nrs, pcgs = [], [], [], []
@@ -414,8 +414,8 @@ def cpu_sphere_steps(cfg, P0, threads, steps, warmup, seed=7):
                                 C.byref(nout), po.pi64(acc))
         n = nout.value
         rho = po.density_from_fixed(acc, fx, vol) * QE
-        phi, conv, nr, pcg = po.newton_pcg(g, phi, rho, obj, PHI0, TE, N0, nr_max=20, nr_tol=NR_TOL, pcg_max=200000,
-                                           pcg_tol=PCG_TOL)
+        phi, conv, nr, pcg, _ = po.newton_pcg_fallback(g, phi, rho, obj, PHI0, TE, N0, 20, NR_TOL, 200000, PCG_TOL,
+                                                       0, 0.0, early_stop=True)
         ef = po.efield(g, phi)
         el = time.perf_counter() - t0
         if st >= warmup:
@@ -1066,6 +1066,8 @@ def main():
     ap.add_argument("--config", default="sphere256", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain form")
+    ap.add_argument("--sort-every", type=int, default=0,
+                    help="steps between counting sorts of the mixed particles (default: the workload's)")
     ap.add_argument("--ncu-case", action="store_true",
                     help="one push + one solve of the workload (mixed form), for an ncu capture")
     ap.add_argument("--ncu-particles", type=int, default=0,
@@ -1109,7 +1111,9 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.sort_every:
+        cfg["sort_every"] = args.sort_every
     big = cfg["np"] > 50_000_000
     # large cases are loaded on the GPU; the CPU baseline then uses a sample
     P0 = None if big else synthetic_state(cfg, cfg["np"], 1 + rank)
@@ -1124,7 +1128,8 @@ def main():
     t = timed_steps(E, torch, w, cfg, args.steps, args.warmup, flush)
     ck = clocks.stop()
     ms_step, value, _ = aggregate(float(np.sum(t["ms"])) / args.steps, t["n"], dist, "cuda")
-    phases, counts = profiled_steps(E, w, cfg, max(3, min(args.steps, 10)))
+    # one whole sort period, so the sort's share of a step is in the table
+    phases, counts = profiled_steps(E, w, cfg, cfg["sort_every"] or max(3, min(args.steps, 10)))
     snap = {"den": s.den, "phi": w.phi.copy(), "ef": w.ef}
     err, conv64, phi64 = phi_error(E, w, cfg)
     errs = oracle_errors(E, w, s, cfg, not big, snap, phi64, conv64)

@@ -209,6 +209,17 @@ int espic_solver_set_launch(espic_world *w, int max_blocks);
  * converged solution and its test are unchanged.  No reference counterpart
  * (the reference starts from phi^n). */
 int espic_solver_set_predictor(espic_world *w, int enable);
+/* The reference's fallback when the inner linear PCG fails
+ * (ch3/ver2/PotentialSolver.cpp:270-271): Gauss-Seidel with omega 1
+ * (solveGSLinear, :433-461) on the same linear system from the PCG's last
+ * iterate, up to the solver's max_it sweeps, residual RMS checked every 25
+ * sweeps against its tolerance.  On (1) by default; 0 turns it off. */
+int espic_solver_set_fallback(espic_world *w, int enable);
+/* The last solve's outcome (waits for the world's stream): converged flag,
+ * Newton (or SOR/GS) iterations, inner PCG iterations, fallback Gauss-Seidel
+ * sweeps and the final norm. */
+int espic_solver_status(espic_world *w, int *converged, int *iterations, int *inner_iterations,
+                        int *fallback_sweeps, double *residual);
 /* Multigrid levels with fewer than block_nodes nodes run on one thread block
  * between two grid barriers (default 4096); larger levels run on the whole
  * grid.  A tuning knob with no reference counterpart. */

@@ -1001,6 +1001,23 @@ static void apply_L(const nk_ctx *K, const double *x, double *y, double *diag) {
 int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *obj,
                   const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
                   int pcg_max, double pcg_tol, int *nr_it_out, int *pcg_it_out) {
+    return eo_newton_pcg_fb(g, phi, rho, obj, target, phi0, te0, n0, nr_max, nr_tol, pcg_max, pcg_tol, 0, 0.0, 0,
+                            nr_it_out, pcg_it_out, NULL);
+}
+
+/* Newton-PCG as above, with the reference's fallback when the linear PCG
+ * fails (ch3/ver2/PotentialSolver.cpp:270-271): Gauss-Seidel with omega 1
+ * (solveGSLinear, :433-461) on J y = F from the PCG's last iterate, in node
+ * order, its residual's RMS over all nodes checked at sweeps 0, 25, 50, ...
+ * against gs_tol, at most gs_max sweeps (0: no fallback).  With early_stop
+ * the inner PCG also stops, as the CUDA path's does, once the RMS of the
+ * preconditioned residual z (over all nodes) is below nr_tol / 3, and z
+ * itself is the update when the first z already is. */
+int eo_newton_pcg_fb(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                     const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
+                     int pcg_max, double pcg_tol, int gs_max, double gs_tol, int early_stop, int *nr_it_out,
+                     int *pcg_it_out, int *gs_it_out) {
+    int gs_total = 0;
     int64_t nn = (int64_t)g->ni * g->nj * g->nk;
     nk_ctx K = {g, obj, {1.0 / (g->dh[0] * g->dh[0]), 1.0 / (g->dh[1] * g->dh[1]),
                          1.0 / (g->dh[2] * g->dh[2])}};
@@ -1049,8 +1066,18 @@ int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *o
             rz += r[u] * z[u];
         }
         double stop2 = pcg_tol * pcg_tol * fn;
-        int it = 0;
-        if (fn > 0) {
+        const double zz_stop = nr_tol * nr_tol / 9.0 * (double)nn;
+        int it = 0, pcg_ok = 0, take_z = 0;
+        if (early_stop && fn > 0) {
+            double zz = 0;
+            for (int64_t u = 0; u < nn; u++) zz += z[u] * z[u];
+            if (zz < zz_stop) {
+                take_z = 1;
+                pcg_ok = 1;
+                for (int64_t u = 0; u < nn; u++) y[u] = z[u];
+            }
+        }
+        if (fn > 0 && !take_z) {
             for (it = 0; it < pcg_max; it++) {
                 apply_L(&K, p, q, NULL);
                 double pq = 0;
@@ -1067,13 +1094,20 @@ int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *o
                 }
                 if (rr <= stop2) {
                     it++;
+                    pcg_ok = 1;
                     break;
                 }
-                double rz_new = 0;
+                double rz_new = 0, zz = 0;
                 for (int64_t u = 0; u < nn; u++) {
                     double dg = diagL[u] + Pd[u];
                     z[u] = (dg != 0) ? r[u] / dg : 0;
                     rz_new += r[u] * z[u];
+                    zz += z[u] * z[u];
+                }
+                if (early_stop && zz < zz_stop) {
+                    it++;
+                    pcg_ok = 1;
+                    break;
                 }
                 double beta = rz_new / rz;
                 rz = rz_new;
@@ -1081,6 +1115,34 @@ int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *o
             }
         }
         pcg_total += it;
+        if (fn > 0 && !pcg_ok && gs_max > 0) {
+            /* Gauss-Seidel on J y = F from the PCG's y, in node order */
+            for (int sw = 0; sw < gs_max; sw++) {
+                for (int k = 1; k < g->nk - 1; k++)
+                    for (int j = 1; j < g->nj - 1; j++)
+                        for (int i = 1; i < g->ni - 1; i++) {
+                            int64_t u = NODE(g, i, j, k);
+                            if (obj[u] != 0) continue;
+                            double s = F[u];
+                            for (int m = 0; m < 6; m++) {
+                                int a = i + NB_OFF[m][0], b = j + NB_OFF[m][1], c = k + NB_OFF[m][2];
+                                if (nb_kind(&K, a, b, c) == 0) s += K.c[m >> 1] * y[NODE(g, a, b, c)];
+                            }
+                            y[u] = s / (diagL[u] + Pd[u]);
+                        }
+                gs_total++;
+                if (sw % 25 == 0) {
+                    apply_L(&K, y, q, NULL);
+                    double R2 = 0;
+                    for (int64_t u = 0; u < nn; u++) {
+                        if (obj[u] != 0) continue;
+                        double R = q[u] + Pd[u] * y[u] - F[u];
+                        R2 += R * R;
+                    }
+                    if (sqrt(R2 / nn) < gs_tol) break;
+                }
+            }
+        }
         double yn = 0;
         for (int64_t u = 0; u < nn; u++) {
             if (obj[u] != 0) continue;
@@ -1108,6 +1170,7 @@ int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *o
     free(xu);
     if (nr_it_out) *nr_it_out = nr;
     if (pcg_it_out) *pcg_it_out = pcg_total;
+    if (gs_it_out) *gs_it_out = gs_total;
     return conv;
 }
 

@@ -130,6 +130,10 @@ void eo_qn(const eo_grid *g, double *phi, const double *rho, const int *obj, dou
 int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *obj,
                   const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
                   int pcg_max, double pcg_tol, int *nr_it_out, int *pcg_it_out);
+int eo_newton_pcg_fb(const eo_grid *g, double *phi, const double *rho, const int *obj,
+                     const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
+                     int pcg_max, double pcg_tol, int gs_max, double gs_tol, int early_stop, int *nr_it_out,
+                     int *pcg_it_out, int *gs_it_out);
 void eo_efield(const eo_grid *g, const double *phi, double *ef);
 
 /* ---- diagnostics ----------------------------------------------------- */

@@ -465,6 +465,25 @@ def newton_pcg(g, phi, rho, obj, phi0, te0, n0, nr_max=20, nr_tol=1e-6, pcg_max=
     return phi, bool(conv), a.value, b.value
 
 
+def newton_pcg_fallback(g, phi, rho, obj, phi0, te0, n0, nr_max, nr_tol, pcg_max, pcg_tol, gs_max, gs_tol,
+                        early_stop=False):
+    """Newton-PCG with the reference's Gauss-Seidel fallback after a failed
+    inner PCG (and, with early_stop, the CUDA path's inner stop on the RMS of
+    the preconditioned residual); returns (phi, converged, newton, pcg, gs
+    sweeps)"""
+    L = lib()
+    f = L.eo_newton_pcg_fb
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(Grid), PD, PD, PI, PI, D, D, D, C.c_int, D, C.c_int, D, C.c_int, D, C.c_int, PI, PI,
+                  PI]
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    t = neumann_targets(g, obj)
+    a, b, c = C.c_int(0), C.c_int(0), C.c_int(0)
+    conv = f(C.byref(g), pd(phi), pd(rho), pi(obj), pi(t), phi0, te0, n0, nr_max, nr_tol, pcg_max, pcg_tol, gs_max,
+             gs_tol, 1 if early_stop else 0, C.byref(a), C.byref(b), C.byref(c))
+    return phi, bool(conv), a.value, b.value, c.value
+
+
 def efield(g, phi):
     ef = np.zeros((g.nn, 3))
     lib().eo_efield(C.byref(g), pd(np.ascontiguousarray(phi, dtype=np.float64)), pd(ef))

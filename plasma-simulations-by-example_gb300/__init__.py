@@ -116,6 +116,8 @@ def lib():
             "espic_solver_set_coarse": [VP, I64],
             "espic_solver_set_dense": [VP, I64],
             "espic_solver_set_predictor": [VP, C.c_int],
+            "espic_solver_set_fallback": [VP, C.c_int],
+            "espic_solver_status": [VP, PI, PI, PI, PI, PD],
             "espic_solve": [VP, PI, PI, PD],
             "espic_efield": [VP],
             "espic_species_diag": [VP, C.c_int, PD],
@@ -624,6 +626,19 @@ class PotentialSolver:
 
     def setLaunch(self, max_blocks=0):
         check(lib().espic_solver_set_launch(self.world.h, max_blocks))
+
+    def setFallback(self, enable=True):
+        """Gauss-Seidel after an inner PCG that fails (the reference's
+        fallback, ch3/ver2/PotentialSolver.cpp:270-271); on by default."""
+        check(lib().espic_solver_set_fallback(self.world.h, 1 if enable else 0))
+
+    def status(self):
+        """(converged, iterations, inner iterations, fallback sweeps, norm) of
+        the last solve"""
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        r = C.c_double()
+        check(lib().espic_solver_status(self.world.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d), C.byref(r)))
+        return bool(a.value), b.value, c.value, d.value, r.value
 
     def setPredictor(self, enable=True):
         """Start Newton solves of consecutive steps from 2 phi^n - phi^(n-1)."""

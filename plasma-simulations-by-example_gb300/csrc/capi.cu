@@ -904,6 +904,26 @@ extern "C" int espic_solver_set_multigrid(espic_world *h, int levels, double sca
     return ESPIC_OK;
 }
 
+extern "C" int espic_solver_set_fallback(espic_world *h, int enable) {
+    WORLD(h);
+    w.gs_fallback = enable != 0;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_solver_status(espic_world *h, int *converged, int *iterations, int *inner_iterations,
+                                   int *fallback_sweeps, double *residual) {
+    WORLD(h);
+    SolveStatus st;
+    CK(cudaMemcpyAsync(&st, w.d_status, sizeof st, cudaMemcpyDeviceToHost, w.stream));
+    CK(cudaStreamSynchronize(w.stream));
+    if (converged) *converged = st.converged;
+    if (iterations) *iterations = st.iterations;
+    if (inner_iterations) *inner_iterations = st.inner_iterations;
+    if (fallback_sweeps) *fallback_sweeps = st.fallback_sweeps;
+    if (residual) *residual = st.residual;
+    return take_device_errors(w);
+}
+
 extern "C" int espic_solver_set_coarse(espic_world *h, int64_t block_nodes) {
     WORLD(h);
     if (block_nodes < 0) return fail(ESPIC_ERR_ARG, "bad coarse-level size");

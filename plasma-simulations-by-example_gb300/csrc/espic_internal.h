@@ -49,7 +49,7 @@ struct SolveStatus {
     int converged;
     int iterations;
     int inner_iterations;
-    int pad;
+    int fallback_sweeps; /* Gauss-Seidel sweeps after a failed inner PCG (Newton-PCG) */
     double residual;
     long long solves;       /* running totals, added by every solve */
     long long outer_total;

@@ -108,6 +108,7 @@ struct World {
     int solver_kind = 0, max_it = 10000;
     double tol = 1e-4, phi0 = 0, te0 = 1.5, n0 = 1e12;
     int nr_max = 20, pcg_max = 10000, fp32_inner = 0;
+    bool gs_fallback = true; /* Gauss-Seidel after an inner PCG that fails (the reference's fallback) */
     double nr_tol = 1e-3, pcg_tol = 1e-6;
     void *pcg_buf = nullptr;
     bool pcg_codes_valid = false;

@@ -815,7 +815,8 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         int pcg_max, double pcg_tol, T *y, T *r, T *z, T *p0,
                                                         T *p1, T *q, T *dg, MgArgs<T> mg, const int32_t *lists,
                                                         double *partials, SolveStatus *st, int *err,
-                                                        double *lin_y, const double *__restrict__ lin_b) {
+                                                        double *lin_y, const double *__restrict__ lin_b,
+                                                        int gs_max, double gs_tol) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char pcg_smem[];
     __shared__ T bc_alpha, bc_beta;
@@ -850,7 +851,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     F.pk[0] = lists + F.nlist;
     F.list[1] = lists + 2 * (int64_t)F.nlist;
     F.pk[1] = lists + 3 * (int64_t)F.nlist;
-    int round = 0, nr, conv = 0, inner = 0;
+    int round = 0, nr, conv = 0, inner = 0, fallback = 0;
     double norm = 0;
     /* linear mode (lin_y != null): Newton on F(y) = J y - b with J frozen at
      * phi solves J y = b; the stopping test is relative to the first update */
@@ -960,6 +961,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             /* the first preconditioned residual already estimates an update
              * below the inner stop: it is the update */
             take_z = ZZ < zz_stop;
+            bool inner_ok = take_z;
             T beta = 0;
             T *pold = p0, *pnew = p1;
             for (int it = 0; it < pcg_max && !take_z; it++) {
@@ -1054,7 +1056,10 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                 inner++;
                 if (threadIdx.x == 0) bc_stop = !(s4[0] > stop2); /* also leaves on NaN */
                 __syncthreads();
-                if (bc_stop) break;
+                if (bc_stop) {
+                    inner_ok = true;
+                    break;
+                }
                 double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
                 /* z = M r estimates the remaining error of y: once its RMS is
                  * below a third of the Newton tolerance, further inner
@@ -1064,12 +1069,63 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                     bc_beta = (T)(RZn / RZ);
                 }
                 __syncthreads();
-                if (bc_stop) break;
+                if (bc_stop) {
+                    inner_ok = true;
+                    break;
+                }
                 beta = bc_beta;
                 RZ = RZn;
                 T *tp = pold;
                 pold = pnew;
                 pnew = tp;
+            }
+            /* The reference's fallback when the linear PCG fails
+             * (ch3/ver2/PotentialSolver.cpp:270-271, solveGSLinear :433-461):
+             * Gauss-Seidel (omega 1) on the same linear system from the
+             * inner solve's last iterate, the residual's RMS checked every
+             * 25 sweeps (from the first) against the solver tolerance, at
+             * most gs_max sweeps.  Here the sweeps are red-black and act on
+             * the correction, J e = r from e = 0 (r = F - J y is the PCG's
+             * residual), then y += e. */
+            if (!inner_ok && gs_max > 0) {
+                for (int64_t u = gtid; u < nn; u += gsize) z[u] = (T)0;
+                grid.sync();
+                for (int sw = 0; sw < gs_max; sw++) {
+                    for (int col = 0; col < 2; col++) {
+                        for (int64_t u = gtid; u < nn; u += gsize) {
+                            const uint16_t cc = code[u];
+                            if (!(cc & SELF) || ((cc & BLACK) ? 1 : 0) != col) continue;
+                            T acc = r[u];
+#pragma unroll
+                            for (int m = 0; m < 6; m++)
+                                if (cc & (1u << m)) acc += ct[m >> 1] * z[u + off[m]];
+                            z[u] = acc / full_diag(cc, dg[u], ct);
+                        }
+                        grid.sync();
+                    }
+                    fallback++;
+                    if (sw % 25 == 0) {
+                        T rr2 = 0;
+                        for (int64_t u = gtid; u < nn; u += gsize) {
+                            const uint16_t cc = code[u];
+                            if (!(cc & SELF)) continue;
+                            T xn[6];
+#pragma unroll
+                            for (int m = 0; m < 6; m++) xn[m] = (cc & (1u << m)) ? z[u + off[m]] : (T)0;
+                            const T R = r[u] - jacobian_apply(cc, dg[u], ct, z[u], xn);
+                            rr2 += R * R;
+                        }
+                        const T t5[1] = {rr2};
+                        double s5[1];
+                        grid_sum_t<1, T>(grid, t5, s5, partials, round);
+                        if (threadIdx.x == 0) bc_stop = sqrt(s5[0] / (double)nn) < gs_tol;
+                        __syncthreads();
+                        if (bc_stop) break;
+                    }
+                }
+                for (int64_t u = gtid; u < nn; u += gsize)
+                    if (code[u] & SELF) y[u] += z[u];
+                grid.sync();
             }
         }
         /* Newton update */
@@ -1123,6 +1179,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         st->converged = conv;
         st->iterations = nr;
         st->inner_iterations = inner;
+        st->fallback_sweeps = fallback;
         st->residual = norm;
         st->solves += 1;
         st->outer_total += nr;
@@ -1427,9 +1484,11 @@ static int run_pcg(World &w) {
     const int32_t *lst = lists;
     double *ly = w.lin_y;
     const double *lb = w.lin_b;
+    int gs_max = w.gs_fallback ? w.max_it : 0;
+    double gs_tol = w.tol;
     void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
                     &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
-                    &ly,   &lb};
+                    &ly,   &lb,   &gs_max, &gs_tol};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, dyn, w.stream);
 }

@@ -323,6 +323,41 @@ def test_newton_pcg(espic, po, fp32, levels):
             assert inner < 40 * nr, (nr, inner)
 
 
+@pytest.mark.parametrize("fp32", [False, True])
+def test_newton_pcg_gauss_seidel_fallback(espic, po, fp32):
+    """An inner PCG that fails (capped at 2 iterations) is followed, as in the
+    reference (ch3/ver2/PotentialSolver.cpp:270-271), by Gauss-Seidel sweeps
+    on the same linear system (solveGSLinear :433-461) up to the solver's
+    max_it, its residual checked every 25 sweeps against the solver
+    tolerance: the Newton solve still converges, to the reference's
+    converged solveGS (relative 1e-8, 1e-6 with float inner iterations), as
+    the oracle's restatement of the fallback does.  With the fallback off the
+    capped solve does not converge."""
+    f = golden("sphere_solve")
+    phi0, te0, n0 = f["ref"]
+    g = po.grid(*SPH)
+    for fallback in (True, False):
+        with world(espic, SPH) as w:
+            _sphere_solver_setup(espic, f, w)
+            sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 20000, 1e-6)
+            sol.setReferenceValues(phi0, te0, n0)
+            sol.setNewton(nr_max=50 if fallback else 6, nr_tol=1e-9, pcg_max=2, pcg_tol=1e-12, fp32_inner=fp32)
+            sol.setMultigrid(0)
+            sol.setFallback(fallback)
+            conv, nr, inner, norm = sol.solve()
+            st = sol.status()
+            if fallback:
+                assert conv and st[3] > 0, (nr, inner, st)
+                assert rel(w.phi, f["phi_tight"]) <= (1e-6 if fp32 else 1e-8)
+                obj = w.object_id
+                phi_o, conv_o, _, _, gs_o = po.newton_pcg_fallback(g, f["phi_init"], f["rho"], obj, phi0, te0,
+                                                                   n0, 50, 1e-9, 2, 1e-12, 20000, 1e-6)
+                assert conv_o and gs_o > 0
+                assert rel(w.phi, phi_o) <= (1e-6 if fp32 else 1e-8)
+            else:
+                assert not conv and st[3] == 0 and nr == 6
+
+
 def test_newton_pcg_dense_coarsest_level(espic, po):
     """The coarsest multigrid level (here 6x6x11) solved by its dense inverse,
     the default, or by smoothing sweeps on one block: the same converged phi,
