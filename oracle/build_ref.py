@@ -15,7 +15,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get("ESPIC_REFERENCE", "/root/reference")
+# the reference checkout: ESPIC_REFERENCE, else a sibling "reference" folder of
+# the repository's parent (absent on hosts without it: build_reference skips)
+REFERENCE = os.environ.get("ESPIC_REFERENCE",
+                           os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 ORACLE_SO = os.path.join(HERE, "_build", "libespic_oracle.so")
 
 REF_TARGETS = {
@@ -23,7 +26,11 @@ REF_TARGETS = {
     "ref_ch3": ("ch3/ver2", ["World.cpp", "Species.cpp", "PotentialSolver.cpp", "Source.cpp"],
                 "ch3_harness.cpp"),
     "ref_ch4": ("ch4", ["World.cpp", "Species.cpp", "Source.cpp", "Collisions.cpp"], "ch4_harness.cpp"),
+    # the particle source of the MPI variant; its headers name MPI, which is
+    # not installed, so a stand-in mpi.h (ref_harness/mpi_stub) satisfies them
+    "ref_ch9mpi": ("ch9/MPI", ["src/Source.cpp", "src/World.cpp"], "ch9mpi_harness.cpp"),
 }
+EXTRA_INCLUDES = {"ref_ch9mpi": ["include", "@mpi_stub"]}
 
 
 def _stale(out, deps):
@@ -67,9 +74,11 @@ def build_reference(force=False):
         out = os.path.join(outdir, name)
         built[name] = out
         deps = srcs + [os.path.join(hdir, "harness_io.h"), __file__]
+        incs = ["-I", hdir, "-I", cdir]
+        for d in EXTRA_INCLUDES.get(name, []):
+            incs += ["-I", os.path.join(hdir, d[1:]) if d.startswith("@") else os.path.join(cdir, d)]
         if force or _stale(out, deps):
-            cmd = ["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-w", "-I", hdir, "-I", cdir,
-                   "-o", out] + srcs
+            cmd = ["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-w"] + incs + ["-o", out] + srcs
             procs.append((name, subprocess.Popen(cmd)))
     for name, p in procs:
         if p.wait() != 0:

@@ -528,8 +528,10 @@ int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double
     double Ly = g->dh[1] * (g->nj - 1);
     int num_sim;
     if (rem) {
-        double A = Lx * Ly;
-        double num_real = den * v_drift * A * dt;
+        /* the remainder count of ch9/MPI/src/Source.cpp:10-27, in its order */
+        double area = (g->ni - 1) * g->dh[0] * (g->nj - 1) * g->dh[1];
+        double num_per_sec = den * v_drift * area;
+        double num_real = num_per_sec * dt;
         double f = num_real / mpw0 + *rem;
         num_sim = (int)f;
         *rem = f - num_sim;
@@ -541,6 +543,10 @@ int64_t eo_inject_beam(const eo_grid *g, const double *ef, double charge, double
     for (int i = 0; i < num_sim; i++) {
         const double *ui = u + 1 + upp * (int64_t)i;
         double pos[3] = {g->x0[0] + ui[0] * Lx, g->x0[1] + ui[1] * Ly, g->x0[2]};
+        if (mode == 2) { /* x0 + U (ni-1) dh, ch9/MPI/src/Source.cpp:33-35 */
+            pos[0] = g->x0[0] + ui[0] * (g->ni - 1) * g->dh[0];
+            pos[1] = g->x0[1] + ui[1] * (g->nj - 1) * g->dh[1];
+        }
         double vel[3];
         if (mode == 2) {
             double v_th = sqrt(2 * 1.3806488e-23 * temp / mass);

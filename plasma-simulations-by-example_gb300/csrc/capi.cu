@@ -152,7 +152,7 @@ static void free_species(Species *s) {
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
                     s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum,
                     s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol,
-                    s->ch4_settled, s->ch4_bounces};
+                    s->ch4_settled, s->ch4_bounces, s->seg};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -384,7 +384,10 @@ extern "C" int espic_species_create(espic_world *h, double mass, double charge, 
     if (form == ESPIC_FORM_FP64) {
         TRY(dalloc(&s->P, 7 * (size_t)capacity));
     } else {
-        int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+        const int64_t ntiles =
+            (int64_t)tile_count(w.g.ni - 1) * tile_count(w.g.nj - 1) * tile_count(w.g.nk - 1);
+        const int64_t ncells = ntiles * TILE_CELLS * TILE_CELLS * TILE_CELLS; /* tile-major sort slots */
+        TRY(dalloc(&s->seg, ntiles + 1));
         TRY(dalloc(&s->cell, s->ms));
         TRY(dalloc(&s->cell2, s->ms));
         TRY(dalloc(&s->off, 3 * (size_t)s->ms));
@@ -530,6 +533,7 @@ extern "C" int espic_species_set(espic_world *h, int sp, const double *P, int64_
     }
     int64_t cnt[4] = {n, n, 0, 0};
     CK(cudaMemcpyAsync(s.d_count, cnt, sizeof cnt, cudaMemcpyHostToDevice, w.stream));
+    s.tiled = false; /* new particle order: no tile segments until the next sort */
     /* for the ch4 push, particles set here have a step's time left */
     if (s.ch4_settled) CK(cudaMemsetAsync(s.ch4_settled, 0, sizeof(int64_t), w.stream));
     CK(cudaStreamSynchronize(w.stream));
@@ -601,6 +605,7 @@ extern "C" int espic_species_set_mixed(espic_world *h, int sp, const int32_t *ce
     CK(cudaMemcpyAsync(s.d_count, cnt, sizeof cnt, cudaMemcpyHostToDevice, w.stream));
     CK(cudaStreamSynchronize(w.stream));
     s.host_bound = n;
+    s.tiled = false;
     return take_device_errors(w);
 }
 
@@ -795,16 +800,20 @@ extern "C" int espic_source_create(espic_world *h, int sp, double v_drift, doubl
  * 18) or, with the remainder count, (int)(N_real / mpw0 + remainder) with the
  * fraction carried to the next call (ch9/MPI/src/Source.cpp:20-27) */
 static int inject_count(const World &w, Source &src, double mpw0, double u0) {
-    double Lx = w.g.dh[0] * (w.g.ni - 1);
-    double Ly = w.g.dh[1] * (w.g.nj - 1);
-    double A = Lx * Ly;
-    double num_real = src.den * src.v_drift * A * w.dt;
     if (src.count_mode == ESPIC_COUNT_REMAINDER) {
+        /* ch9/MPI/src/Source.cpp:10-27, in its own operand order */
+        const double area = (w.g.ni - 1) * w.g.dh[0] * (w.g.nj - 1) * w.g.dh[1];
+        const double num_per_sec = src.den * src.v_drift * area;
+        const double num_real = num_per_sec * w.dt;
         double f = num_real / mpw0 + src.remainder;
         int n = (int)f;
         src.remainder = f - n;
         return n;
     }
+    double Lx = w.g.dh[0] * (w.g.ni - 1);
+    double Ly = w.g.dh[1] * (w.g.nj - 1);
+    double A = Lx * Ly;
+    double num_real = src.den * src.v_drift * A * w.dt;
     return (int)(num_real / mpw0 + u0);
 }
 

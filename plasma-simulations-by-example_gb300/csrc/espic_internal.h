@@ -42,6 +42,10 @@ struct Geo {
 /* particles per dead-count tile of the compaction */
 constexpr int TILE_PARTICLES = 32768;
 
+/* cells per edge of a tile of the mixed form's sort order */
+constexpr int TILE_CELLS = 8;
+__host__ __device__ inline int tile_count(int ncell) { return (ncell + TILE_CELLS - 1) / TILE_CELLS; }
+
 /* sampled velocity moments of a ch4 species: n, n u, n v, n w, n u u, n v v, n w w */
 constexpr int NMOM = 7;
 

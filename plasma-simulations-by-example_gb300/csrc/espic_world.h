@@ -26,7 +26,9 @@ struct Species {
     int32_t *cell = nullptr, *cell2 = nullptr;
     float *off = nullptr, *off2 = nullptr; /* [3][ms] */
     float *vel = nullptr, *vel2 = nullptr; /* [3][ms] */
-    int32_t *sort_count = nullptr;         /* [ncells + 1] */
+    int32_t *sort_count = nullptr;         /* [tile-major cell slots + 1], then the scan's block sums */
+    int32_t *seg = nullptr;                /* [ntiles + 1] first particle of each tile after the last sort */
+    bool tiled = false;                    /* seg describes the particle order (a sort and no reorder since) */
     /* compaction */
     uint32_t *deadmask = nullptr; /* [cap/32 + 1] */
     int32_t *tiledead = nullptr;  /* [ntiles + 1] */

@@ -427,6 +427,7 @@ struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27),
                     Source::sample of ch9/MPI (ch9/MPI/src/Source.cpp:5-72)
                     and a drifting-Maxwellian beam */
     double x0[3], Lx, Ly, v_drift, mpw0, v_th;
+    double ncx, ncy, dhx, dhy; /* cells and spacing across the face (ch9/MPI's position formula) */
     int mode; /* 0 cold, 1 ch4 warm, 2 ch9 isotropic, 3 Maxwellian */
     const double *u; /* count draw at 0, then beam_uniforms(mode) per particle */
     uint64_t seed, stream;
@@ -434,8 +435,13 @@ struct GenBeam { /* ColdBeamSource::sample (ch3/ver2/Source.cpp:4-27),
     __device__ int64_t base(int64_t i) const { return 1 + (int64_t)beam_uniforms(mode) * i; }
     __device__ void pos(int64_t i, double x[3]) const {
         int64_t b = base(i);
-        x[0] = x0[0] + U(b) * Lx;
-        x[1] = x0[1] + U(b + 1) * Ly;
+        if (mode == 2) { /* x0 + U (ni-1) dh, ch9/MPI/src/Source.cpp:33-35 */
+            x[0] = x0[0] + U(b) * ncx * dhx;
+            x[1] = x0[1] + U(b + 1) * ncy * dhy;
+        } else {
+            x[0] = x0[0] + U(b) * Lx;
+            x[1] = x0[1] + U(b + 1) * Ly;
+        }
         x[2] = x0[2];
     }
     __device__ void make(int64_t i, double x[3], double v[3], double &w_) const {
@@ -1346,6 +1352,10 @@ void launch_inject(World &w, Species &s, int num_sim, double v_drift, double tem
     for (int d = 0; d < 3; d++) b.x0[d] = w.g.x0[d];
     b.Lx = w.g.dh[0] * (w.g.ni - 1);
     b.Ly = w.g.dh[1] * (w.g.nj - 1);
+    b.ncx = (double)(w.g.ni - 1);
+    b.ncy = (double)(w.g.nj - 1);
+    b.dhx = w.g.dh[0];
+    b.dhy = w.g.dh[1];
     b.v_drift = v_drift;
     b.mpw0 = s.mpw0;
     b.mode = vmode;

@@ -168,24 +168,15 @@ __device__ __forceinline__ void deposit_block(bool me, int32_t key, int ni, int 
     }
 }
 
-/* One particle of Species::advance in the mixed form: gather E at the cell
- * corners from ef4 (one 16-byte load per corner), v += (q/m) E dt, move in
- * cell units, then the walls (REFLECT: one mirror bounce per axis; ABSORB:
- * out of the domain or inside the sphere).  A non-finite state is flagged and
- * the particle killed.  Returns true when the particle is dead. */
+/* The move of one particle once E at its position is known: v += (q/m) E dt,
+ * move in cell units, then the walls (REFLECT: one mirror bounce per axis;
+ * ABSORB: out of the domain or inside the sphere).  A non-finite state is
+ * flagged and the particle killed.  Returns true when the particle is dead;
+ * key receives the new cell. */
 template <int WALLS>
-__device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const float4 *__restrict__ ef4, int32_t &key,
-                                                    float &fx, float &fy, float &fz, float &vx, float &vy,
-                                                    float &vz, int *err) {
-    int i, j, k;
-    unpack(key, i, j, k);
-    int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
-    int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
-    float w[8];
-    cic_w(fx, fy, fz, w);
-    const float4 e[8] = {__ldg(ef4 + n0),      __ldg(ef4 + n0 + 1),      __ldg(ef4 + n0 + 1 + sy),      __ldg(ef4 + n0 + sy),
-                         __ldg(ef4 + n0 + sz), __ldg(ef4 + n0 + 1 + sz), __ldg(ef4 + n0 + 1 + sy + sz), __ldg(ef4 + n0 + sy + sz)};
-    const float3 E = gather_corners(w, e);
+__device__ __forceinline__ bool move_particle_mixed(const MixArgs &a, const float3 E, int i, int j, int k,
+                                                    int32_t &key, float &fx, float &fy, float &fz, float &vx,
+                                                    float &vy, float &vz, int *err) {
     vx = __fmaf_rn(E.x, a.qmdt, vx);
     vy = __fmaf_rn(E.y, a.qmdt, vy);
     vz = __fmaf_rn(E.z, a.qmdt, vz);
@@ -214,6 +205,24 @@ __device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const floa
     }
     key = (i & 1023) | ((j & 1023) << 10) | (k << 20);
     return dead;
+}
+
+/* One particle of Species::advance in the mixed form: gather E at the cell
+ * corners from ef4 (one 16-byte load per corner), then the move. */
+template <int WALLS>
+__device__ __forceinline__ bool push_particle_mixed(const MixArgs &a, const float4 *__restrict__ ef4, int32_t &key,
+                                                    float &fx, float &fy, float &fz, float &vx, float &vy,
+                                                    float &vz, int *err) {
+    int i, j, k;
+    unpack(key, i, j, k);
+    int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+    float w[8];
+    cic_w(fx, fy, fz, w);
+    const float4 e[8] = {__ldg(ef4 + n0),      __ldg(ef4 + n0 + 1),      __ldg(ef4 + n0 + 1 + sy),      __ldg(ef4 + n0 + sy),
+                         __ldg(ef4 + n0 + sz), __ldg(ef4 + n0 + 1 + sz), __ldg(ef4 + n0 + 1 + sy + sz), __ldg(ef4 + n0 + sy + sz)};
+    const float3 E = gather_corners(w, e);
+    return move_particle_mixed<WALLS>(a, E, i, j, k, key, fx, fy, fz, vx, vy, vz, err);
 }
 
 template <int WALLS, bool DEPOSIT>
@@ -248,6 +257,217 @@ __global__ void __launch_bounds__(256, 5) k_push_mixed(MixArgs a, const float4 *
         if ((threadIdx.x & 31) == 0 && live) {
             deadmask[p >> 5] = m;
             if (m) atomicAdd(tiledead + (p / TILE_PARTICLES), __popc(m));
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* The push over tile segments.  After a counting sort the particles lie in
+ * tile-major cell order (tiles of TILE_CELLS^3 cells, cells row-major within
+ * a tile), and seg[t] is the first particle of tile t.  One thread block
+ * takes one tile's segment: it stages the float E of a TBW^3-node box
+ * around the segment's particles in shared memory, pushes the particles
+ * 256 at a time with the E gather read from that box, and deposits their
+ * 2^-23 fixed-point corner weights into a shared TBW^3-node integer box,
+ * which it adds to the grid once at the end (one global atomic per touched
+ * node).  The box is centred on the per-axis median cell of 32 keys spread
+ * over the segment, so it follows the drift of the segment's particles
+ * between sorts; particles outside it (the few that moved more than three
+ * cells from their tile, and particles the removal moved into the segment)
+ * gather from global memory and deposit with global atomics.  The arithmetic
+ * per particle is push_particle_mixed's; the integer sums do not depend on
+ * where they are accumulated, so the charge equals that of k_push_mixed bit
+ * for bit.  Particles appended since the sort (after seg[ntiles]) are pushed
+ * by k_push_tail. */
+constexpr int TBW = 15; /* nodes per edge of a block's E and deposit box */
+
+/* the median over the warp of one int per lane (the 16th smallest) */
+__device__ __forceinline__ int warp_median(int v) {
+    int below = 0, same = 0;
+#pragma unroll 8
+    for (int l = 0; l < 32; l++) {
+        const int x = __shfl_sync(0xffffffffu, v, l);
+        below += x < v;
+        same += x == v;
+    }
+    const unsigned pick = __ballot_sync(0xffffffffu, below <= 15 && below + same > 15);
+    return __shfl_sync(0xffffffffu, v, __ffs(pick) - 1);
+}
+
+template <int WALLS, bool DEPOSIT>
+__global__ void __launch_bounds__(256) k_push_tiles(MixArgs a, const float4 *__restrict__ ef4, int32_t *cell,
+                                                    float *off, float *vel, int64_t stride,
+                                                    const int32_t *__restrict__ seg,
+                                                    const int64_t *__restrict__ d_count, uint32_t *deadmask,
+                                                    int32_t *tiledead, unsigned long long *acc, int *err) {
+    constexpr int BV = TBW * TBW * TBW;
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    float4 *sE = (float4 *)tile_smem;
+    unsigned int *sD = (unsigned int *)(tile_smem + BV * sizeof(float4));
+    __shared__ int s_lo[3];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int64_t n = d_count[0];
+    const int p0 = seg[blockIdx.x];
+    const int p1 = (int)min((int64_t)seg[blockIdx.x + 1], n);
+    if (p1 <= p0) return; /* block-uniform */
+    if (warp == 0) {
+        const int q = p0 + (int)(((int64_t)(p1 - p0) * lane) >> 5);
+        int i, j, k;
+        unpack(cell[q], i, j, k);
+        const int c[3] = {warp_median(i), warp_median(j), warp_median(k)};
+        const int ncell[3] = {a.ni - 1, a.nj - 1, a.nk - 1};
+        if (lane < 3) {
+            int lo = c[lane] - (TBW - 1) / 2;
+            if (lo > ncell[lane] - (TBW - 1)) lo = ncell[lane] - (TBW - 1);
+            if (lo < 0) lo = 0;
+            s_lo[lane] = lo; /* box nodes lo .. lo + TBW - 1, cells lo .. lo + TBW - 2 */
+        }
+    }
+    if (DEPOSIT)
+        for (int t = threadIdx.x; t < BV; t += blockDim.x) sD[t] = 0u;
+    __syncthreads();
+    const int li = s_lo[0], lj = s_lo[1], lk = s_lo[2];
+    const int sy = a.ni, sz = a.ni * a.nj;
+    for (int r = warp; r < TBW * TBW; r += nwarps) {
+        const int tk = r / TBW, tj = r - tk * TBW;
+        const float4 *src = ef4 + ((int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + li);
+        for (int ti = lane; ti < TBW; ti += 32) sE[r * TBW + ti] = __ldg(src + ti);
+    }
+    __syncthreads();
+    float *off1 = off + stride, *off2 = off + 2 * stride, *vel1 = vel + stride, *vel2 = vel + 2 * stride;
+    for (int base = p0; base < p1; base += blockDim.x) {
+        const int p = base + threadIdx.x;
+        const bool live = p < p1;
+        bool dead = false;
+        int32_t key = -1;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        if (live) {
+            key = cell[p];
+            fx = off[p];
+            fy = off1[p];
+            fz = off2[p];
+            float vx = vel[p], vy = vel1[p], vz = vel2[p];
+            int i, j, k;
+            unpack(key, i, j, k);
+            float w[8];
+            cic_w(fx, fy, fz, w);
+            float4 e[8];
+            const int bi = i - li, bj = j - lj, bk = k - lk;
+            if ((unsigned)bi < TBW - 1 && (unsigned)bj < TBW - 1 && (unsigned)bk < TBW - 1) {
+                const int L = (bk * TBW + bj) * TBW + bi;
+                e[0] = sE[L];
+                e[1] = sE[L + 1];
+                e[2] = sE[L + 1 + TBW];
+                e[3] = sE[L + TBW];
+                e[4] = sE[L + TBW * TBW];
+                e[5] = sE[L + 1 + TBW * TBW];
+                e[6] = sE[L + 1 + TBW + TBW * TBW];
+                e[7] = sE[L + TBW + TBW * TBW];
+            } else {
+                const float4 *E0 = ef4 + (((int64_t)k * a.nj + j) * a.ni + i);
+                e[0] = __ldg(E0);
+                e[1] = __ldg(E0 + 1);
+                e[2] = __ldg(E0 + 1 + sy);
+                e[3] = __ldg(E0 + sy);
+                e[4] = __ldg(E0 + sz);
+                e[5] = __ldg(E0 + 1 + sz);
+                e[6] = __ldg(E0 + 1 + sy + sz);
+                e[7] = __ldg(E0 + sy + sz);
+            }
+            const float3 E = gather_corners(w, e);
+            dead = move_particle_mixed<WALLS>(a, E, i, j, k, key, fx, fy, fz, vx, vy, vz, err);
+            cell[p] = key;
+            off[p] = fx;
+            off1[p] = fy;
+            off2[p] = fz;
+            vel[p] = vx;
+            vel1[p] = vy;
+            vel2[p] = vz;
+            if (WALLS == M_ABSORB && dead) {
+                atomicOr(deadmask + (p >> 5), 1u << (p & 31));
+                atomicAdd(tiledead + (p / TILE_PARTICLES), 1);
+            }
+        }
+        if (DEPOSIT && live && !dead) {
+            float w[8];
+            cic_w(fx, fy, fz, w);
+            int i, j, k;
+            unpack(key, i, j, k);
+            const int bi = i - li, bj = j - lj, bk = k - lk;
+            if ((unsigned)bi < TBW - 1 && (unsigned)bj < TBW - 1 && (unsigned)bk < TBW - 1) {
+                const int L = (bk * TBW + bj) * TBW + bi;
+                const int idx[8] = {L,           L + 1,           L + 1 + TBW,           L + TBW,
+                                    L + TBW * TBW, L + 1 + TBW * TBW, L + 1 + TBW + TBW * TBW, L + TBW + TBW * TBW};
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                    if (q) atomicAdd(&sD[idx[c]], q);
+                }
+            } else {
+                const int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+                const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                        n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                    if (q) atomicAdd(acc + idx[c], (unsigned long long)q);
+                }
+            }
+        }
+    }
+    if (!DEPOSIT) return;
+    __syncthreads();
+    for (int r = warp; r < TBW * TBW; r += nwarps) {
+        const int tk = r / TBW, tj = r - tk * TBW;
+        unsigned long long *dst = acc + ((int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + li);
+        for (int ti = lane; ti < TBW; ti += 32) {
+            const unsigned v = sD[r * TBW + ti];
+            if (v) atomicAdd(dst + ti, (unsigned long long)v);
+        }
+    }
+}
+
+/* particles appended since the sort: [seg[ntiles], n), grid-stride, the
+ * particle step of push_particle_mixed and global-atomic deposits */
+template <int WALLS, bool DEPOSIT>
+__global__ void __launch_bounds__(256) k_push_tail(MixArgs a, const float4 *__restrict__ ef4, int32_t *cell,
+                                                   float *off, float *vel, int64_t stride,
+                                                   const int32_t *__restrict__ first,
+                                                   const int64_t *__restrict__ d_count, uint32_t *deadmask,
+                                                   int32_t *tiledead, unsigned long long *acc, int *err) {
+    const int64_t n = d_count[0];
+    const int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    for (int64_t p = first[0] + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        int32_t key = cell[p];
+        float fx = off[p], fy = off[stride + p], fz = off[2 * stride + p];
+        float vx = vel[p], vy = vel[stride + p], vz = vel[2 * stride + p];
+        const bool dead = push_particle_mixed<WALLS>(a, ef4, key, fx, fy, fz, vx, vy, vz, err);
+        cell[p] = key;
+        off[p] = fx;
+        off[stride + p] = fy;
+        off[2 * stride + p] = fz;
+        vel[p] = vx;
+        vel[stride + p] = vy;
+        vel[2 * stride + p] = vz;
+        if (WALLS == M_ABSORB && dead) {
+            atomicOr(deadmask + (p >> 5), 1u << (p & 31));
+            atomicAdd(tiledead + (p / TILE_PARTICLES), 1);
+        }
+        if (DEPOSIT && !dead) {
+            int i, j, k;
+            unpack(key, i, j, k);
+            float w[8];
+            cic_w(fx, fy, fz, w);
+            const int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+            const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                    n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                if (q) atomicAdd(acc + idx[c], (unsigned long long)q);
+            }
         }
     }
 }
@@ -399,10 +619,24 @@ __global__ void k_from_mixed(Geo g, const int32_t *__restrict__ cell, const floa
 
 /* ---------------------------------------------------------------------- */
 /* counting sort by cell: histogram, exclusive scan, scatter               */
-__device__ __forceinline__ int32_t linear_cell(int32_t key, int ni, int nj) {
+/* the sort order: tile-major (tiles of TILE_CELLS^3 cells, ntx x nty tiles
+ * per plane of tiles), cells row-major within a tile; partial tiles at the
+ * far faces leave unused slots */
+__device__ __forceinline__ int32_t linear_cell(int32_t key, int ntx, int nty) {
     int i, j, k;
     unpack(key, i, j, k);
-    return (k * (nj - 1) + j) * (ni - 1) + i;
+    const int tile = ((k / TILE_CELLS) * nty + (j / TILE_CELLS)) * ntx + (i / TILE_CELLS);
+    return (tile * TILE_CELLS + (k % TILE_CELLS)) * TILE_CELLS * TILE_CELLS + (j % TILE_CELLS) * TILE_CELLS +
+           (i % TILE_CELLS);
+}
+
+/* seg[t] = first particle of tile t (from the exclusive scan of the cell
+ * counts), seg[ntiles] = the count */
+__global__ void k_tile_seg(const int32_t *__restrict__ counts, int64_t ntiles, const int64_t *__restrict__ d_count,
+                           int32_t *seg) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ntiles) seg[t] = counts[t * TILE_CELLS * TILE_CELLS * TILE_CELLS];
+    if (t == ntiles) seg[t] = (int32_t)d_count[0];
 }
 
 /* Runs of equal cells in lane order (the particles are nearly sorted, so a
@@ -422,11 +656,11 @@ __device__ __forceinline__ void cell_runs(int32_t lc, int &head, int &len) {
 }
 
 __global__ void __launch_bounds__(256) k_sort_hist(const int32_t *__restrict__ cell,
-                                                   const int64_t *__restrict__ d_count, int ni, int nj,
+                                                   const int64_t *__restrict__ d_count, int ntx, int nty,
                                                    int32_t *counts) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool me = p < d_count[0];
-    int32_t lc = me ? linear_cell(cell[p], ni, nj) : -1;
+    int32_t lc = me ? linear_cell(cell[p], ntx, nty) : -1;
     int head, len;
     cell_runs(lc, head, len);
     if (me && (int)(threadIdx.x & 31) == head) atomicAdd(counts + lc, len);
@@ -511,11 +745,11 @@ __global__ void __launch_bounds__(1024) k_scan_down(int32_t *x, int64_t n, const
  * took 71 ms, gathering all seven in one pass 22 ms, one array per pass
  * 18 ms (plus 7 ms of histogram, scan and index scatter). */
 __global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict__ cell,
-                                                      const int64_t *__restrict__ d_count, int ni, int nj,
+                                                      const int64_t *__restrict__ d_count, int ntx, int nty,
                                                       int32_t *cursor, int32_t *perm) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool me = p < d_count[0];
-    int32_t lc = me ? linear_cell(cell[p], ni, nj) : -1;
+    int32_t lc = me ? linear_cell(cell[p], ntx, nty) : -1;
     int head, len;
     cell_runs(lc, head, len);
     const int lane = threadIdx.x & 31;
@@ -630,9 +864,31 @@ static MixArgs mix_args(World &w, Species &s) {
     return a;
 }
 
+/* the tile-segment push needs a whole box inside the grid */
+static bool tiles_usable(const World &w, const Species &s) {
+    return s.tiled && w.g.ni >= TBW && w.g.nj >= TBW && w.g.nk >= TBW;
+}
+
 template <int WALLS, bool DEP>
 static void push_mixed_as(World &w, Species &s, int64_t n) {
     MixArgs a = mix_args(w, s);
+    if (tiles_usable(w, s)) {
+        const int64_t ntiles = (int64_t)tile_count(w.g.ni - 1) * tile_count(w.g.nj - 1) * tile_count(w.g.nk - 1);
+        constexpr int BV = TBW * TBW * TBW;
+        const int smem = BV * (int)sizeof(float4) + BV * (int)sizeof(unsigned int);
+        /* the boxes take 67.5 KB of shared memory (set for the current device) */
+        cudaFuncSetAttribute(k_push_tiles<WALLS, DEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (WALLS == M_ABSORB) /* the tile kernels OR their dead bits into the mask */
+            cudaMemsetAsync(s.deadmask, 0, ((n + 31) / 32) * sizeof(uint32_t), w.stream);
+        k_push_tiles<WALLS, DEP><<<(unsigned)ntiles, 256, smem, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
+                                                                            s.seg, s.d_count, s.deadmask,
+                                                                            s.tiledead, s.acc, w.d_err);
+        k_push_tail<WALLS, DEP><<<2 * w.sm_count, 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
+                                                                       s.seg + ntiles, s.d_count, s.deadmask,
+                                                                       s.tiledead, s.acc, w.d_err);
+        w.nlaunch += 2;
+        return;
+    }
     k_push_mixed<WALLS, DEP><<<blocks_for(n, 256), 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
                                                                       s.d_count, s.deadmask, s.tiledead, s.acc,
                                                                       w.d_err);
@@ -692,16 +948,19 @@ void launch_from_mixed(World &w, Species &s, double *P, int64_t stride, int64_t 
 void launch_sort_mixed(World &w, Species &s) {
     int64_t n = s.host_bound;
     if (n <= 0) return;
-    int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    const int ntx = tile_count(w.g.ni - 1), nty = tile_count(w.g.nj - 1), ntz = tile_count(w.g.nk - 1);
+    const int64_t ntiles = (int64_t)ntx * nty * ntz;
+    const int64_t ncells = ntiles * TILE_CELLS * TILE_CELLS * TILE_CELLS; /* slots of the tile-major order */
     int32_t *counts = s.sort_count;
     int32_t *bsum = counts + ncells + 1;
     int64_t nb = (ncells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
     cudaMemsetAsync(counts, 0, (ncells + 1) * sizeof(int32_t), w.stream);
-    k_sort_hist<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, w.g.ni, w.g.nj, counts);
+    k_sort_hist<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, ntx, nty, counts);
     k_scan_reduce<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
     k_scan_bsum<<<1, 1024, 0, w.stream>>>(bsum, nb);
     k_scan_down<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
-    k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, w.g.ni, w.g.nj, counts, s.cell2);
+    k_tile_seg<<<blocks_for(ntiles + 1, 256), 256, 0, w.stream>>>(counts, ntiles, s.d_count, s.seg);
+    k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, ntx, nty, counts, s.cell2);
     for (int d = 0; d < 3; d++) {
         k_sort_gather<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.off + d * s.ms, s.cell2, s.d_count,
                                                                 s.off2 + d * s.ms, w.d_err);
@@ -709,7 +968,8 @@ void launch_sort_mixed(World &w, Species &s) {
                                                                 s.vel2 + d * s.ms, w.d_err);
     }
     k_sort_gather_keys<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, s.cell2, w.d_err);
-    w.nlaunch += 12;
+    w.nlaunch += 13;
+    s.tiled = true;
     int32_t *tc = s.cell;
     s.cell = s.cell2;
     s.cell2 = tc;

@@ -391,6 +391,23 @@ def steady_cases():
     save("sphere_steady", steps=ss.STEPS, dt=ss.DT, mpw0=ss.MPW0, avg=np.array(ss.AVG), **arrays)
 
 
+def ch9mpi_source_cases(rng):
+    """Five calls of the particle source of the ch9/MPI variant
+    (ch9/MPI/src/Source.cpp:5-72, compiled with a stand-in mpi.h): fixed-
+    speed isotropic velocities, v_z < 0 reflected, the macroparticle count's
+    fraction carried between calls, velocities rewound in a smooth E."""
+    g = po.grid(SPH["grid"], SPH["x0"], SPH["xm"])
+    phi = smooth_phi(SPH, rng, 40.0)
+    ef = po.efield(g, phi)
+    dt, spwt, den0, v_drift, T = 1e-7, 3.1e3, 1e10, 7000.0, 0.1 * QE / K
+    inp = dict(grid=SPH["grid"], x0=SPH["x0"], dh=list(g.dh), dt=[dt], ef=ef.ravel(), seed=[4242],
+               species=[16 * AMU, QE, spwt, 5000], source=[den0, v_drift, T], calls=[5])
+    o = po.run_reference("ref_ch9mpi", "sample", inp)
+    n = int(o["counts"].sum())
+    save("inject_ch9mpi", phi=phi, dt=dt, spwt=spwt, den0=den0, v_drift=v_drift, T=T, P=o["P"].reshape(7, n),
+         counts=o["counts"], rem=o["rem"], used=o["used"], u=o["u"], v_th=o["v_th"])
+
+
 LONG_STEPS, LONG_BATCH, LONG_SEEDS = 10000, 500, (1, 2, 3, 4, 5, 6)
 
 
@@ -455,3 +472,5 @@ if __name__ == "__main__":
         ionize_cases()
     if "longrun" in cases:
         box_longrun_cases()
+    if "ch9mpi" in cases:
+        ch9mpi_source_cases(np.random.default_rng(909))

@@ -233,3 +233,46 @@ def test_mixed_density_and_potential_against_fp64_oracle(espic, po):
     assert np.max(np.abs(phi - phi64)) <= 1e-6 * np.max(np.abs(phi64))
     ef64 = po.efield(g, phi64)
     assert np.max(np.abs(ef - ef64)) <= 1e-6 * np.max(np.abs(ef64))
+
+
+@pytest.mark.parametrize("walls", ["reflect", "absorb"])
+def test_tile_segment_push_matches_oracle_over_steps(espic, po, walls):
+    """After a sort the push runs over tile segments (one block per 8^3-cell
+    tile, E and the deposit staged in shared-memory boxes), particles
+    appended since the sort by a tail kernel, and particles that the removal
+    moved into a segment through the global fallback.  Six steps with
+    particles appended before each: every step's cell keys, offsets,
+    velocities, survivors and integer charge equal the oracle's mixed
+    restatement run on the GPU's state, bit for bit."""
+    wk = espic.WALLS_REFLECT if walls == "reflect" else espic.WALLS_ABSORB
+    geo = BOX if walls == "reflect" else SPH
+    dt = 1e-7 if walls == "absorb" else 2e-10
+    P = state(geo, 200_000, 61, sphere=walls == "absorb", vd=0.0 if walls == "reflect" else 7000.0,
+              vth=8e5 if walls == "reflect" else 800.0)
+    g = po.grid(*geo)
+    rng = np.random.default_rng(62)
+    w, s = make(espic, geo, P, wk, True)
+    with w:
+        ef4 = _ef4(w, po)
+        vol = w.read(espic.FIELD_NODE_VOL)
+        a = po.mix_args(g, QE, M, dt, SPHERE4 if walls == "absorb" else None)
+        dead_total = 0
+        for st in range(6):
+            x0, xm = np.array(geo[1]), np.array(geo[2])
+            pos = x0 + (0.05 + 0.9 * rng.random((500, 3))) * (xm - x0)
+            if walls == "absorb":
+                pos = pos[np.sum((pos - np.array(SPHERE[0])) ** 2, axis=1) > SPHERE[1] ** 2]
+            vel = rng.standard_normal(pos.shape) * (8e5 if walls == "reflect" else 800.0)
+            s.addParticles(pos, vel)
+            cell0, off0, vel0 = s.get_mixed()
+            s.advance(deposit=True)
+            cell, off, vv = s.get_mixed()
+            den = s.den
+            c2, o2, v2, dead = po.push_mixed(a, ef4, 0 if walls == "reflect" else 1, cell0, off0, vel0)
+            assert np.array_equal(cell, c2), st
+            assert np.array_equal(off, o2) and np.array_equal(vv, v2), st
+            want = po.density_from_fixed(po.deposit_mixed(g, c2, o2), 8388608.0 / 40.0, vol)
+            assert np.array_equal(den, want), st
+            dead_total += int(dead.sum())
+        if walls == "absorb":
+            assert dead_total > 0

@@ -626,6 +626,33 @@ def test_output_snapshot_is_taken_at_begin(espic, po):
         assert not np.array_equal(w.phi, want["phi"])
 
 
+
+def test_ch9mpi_source_replays_the_reference(espic, po):
+    """The ch9/MPI particle source on the GPU (isotropic beam, remainder
+    count) replaying the uniforms the reference's own Source::sample drew
+    (tests/golden/inject_ch9mpi.npz, ch9/MPI/src/Source.cpp:5-72 compiled with
+    a stand-in mpi.h): counts and positions bit-exact against the reference,
+    velocities within 1e-13 (CUDA's cos, sin and sqrt against glibc's)."""
+    f = golden("inject_ch9mpi")
+    with world(espic, SPH) as w:
+        w.setTime(float(f["dt"]), 1)
+        w.write(espic.FIELD_PHI, f["phi"])
+        espic.PotentialSolver(w).computeEF()
+        s = espic.Species(w, "O+", 16 * AMU, QE, mpw0=float(f["spwt"]), capacity=4096, walls=espic.WALLS_ABSORB)
+        src = espic.BeamSource(s, float(f["v_drift"]), float(f["den0"]), float(f["T"]))
+        src.set_mode(espic.BEAM_ISOTROPIC, espic.COUNT_REMAINDER)
+        off = 0
+        for c in range(len(f["counts"])):
+            k = int(f["used"][c])
+            used = src.sample(u=np.concatenate([[0.0], f["u"][off:off + k]]))
+            assert used == k + 1
+            off += k
+        P = s.particles()
+    assert P.shape == f["P"].shape
+    assert np.array_equal(P[0:3], f["P"][0:3]) and np.array_equal(P[6], f["P"][6])
+    assert rel(P[3:6], f["P"][3:6]) <= 1e-13
+
+
 @pytest.mark.parametrize("mode", ["isotropic", "maxwellian"])
 def test_injection_modes_and_remainder_count(espic, po, mode):
     """The ch9/MPI beam (ch9/MPI/src/Source.cpp:5-72: isotropic direction at

@@ -356,3 +356,27 @@ def test_chemistry_ionize_bitexact(po):
                                        float(f["mpw0"]), float(f["rate"]), float(f["dt"]), f["u"])
     assert Q.shape[1] > 1000 and used == f["u"].size
     assert np.array_equal(Q, f["P"]) and np.array_equal(qdt, f["pdt"])
+
+
+def test_ch9mpi_source_bitexact(po):
+    """The particle source of the ch9/MPI variant (ch9/MPI/src/Source.cpp:5-72),
+    compiled from the reference's sources with a stand-in mpi.h: five calls
+    with the remainder carry.  The oracle's restatement (eo_inject_beam, mode
+    2 with the remainder count) reproduces counts, remainders, positions and
+    rewound velocities bit for bit when fed the same uniforms (the oracle's
+    layout reserves a count slot first, unused by the remainder count)."""
+    f = golden("inject_ch9mpi")
+    g = po.grid([21, 21, 41], [-0.1, -0.1, 0.0], [0.1, 0.1, 0.4])
+    ef = po.efield(g, f["phi"])
+    rem = np.zeros(1)
+    off, out = 0, []
+    for c in range(len(f["counts"])):
+        k = int(f["used"][c])
+        u = np.concatenate([[0.0], f["u"][off:off + k]])
+        off += k
+        B, used = po.inject_beam(g, ef, QE, 16 * AMU, float(f["dt"]), float(f["spwt"]), float(f["v_drift"]),
+                                 float(f["den0"]), float(f["T"]), 2, u, rem=rem)
+        assert B.shape[1] == int(f["counts"][c]) and used == k + 1
+        assert rem[0] == f["rem"][c]
+        out.append(B)
+    assert np.array_equal(np.concatenate(out, axis=1), f["P"])
