@@ -1522,8 +1522,22 @@ int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphe
                            double neu_mpw0, double neu_charge, double neu_mass, double sph_mpw0, double sph_charge,
                            double sph_mass, double *Q, int64_t max_new, int32_t *tag, double *qdt, int64_t *n_new,
                            const double *u, int64_t nu, int64_t *u_used) {
+    return eo_advance_ch4_ion_ex(g, ef, sphere, charge, mass, mpw0, dt, P, stride, n, pdt, neu_mpw0, neu_charge,
+                                 neu_mass, sph_mpw0, sph_charge, sph_mass, Q, max_new, tag, qdt, n_new, u, nu, u_used,
+                                 NULL, 0);
+}
+
+/* as eo_advance_ch4_ion; p_off (optional, [n]) receives the index of each
+ * particle's first uniform, and with holes the dead are removed in the CUDA
+ * path's order (eo_compact_holes) instead of the reference's swap-with-last */
+int64_t eo_advance_ch4_ion_ex(const eo_grid *g, const double *ef, const double sphere[4], double charge, double mass,
+                              double mpw0, double dt, double *P, int64_t stride, int64_t n, double *pdt,
+                              double neu_mpw0, double neu_charge, double neu_mass, double sph_mpw0, double sph_charge,
+                              double sph_mass, double *Q, int64_t max_new, int32_t *tag, double *qdt, int64_t *n_new,
+                              const double *u, int64_t nu, int64_t *u_used, int64_t *p_off, int holes) {
     int64_t k = 0, m = 0;
     for (int64_t p = 0; p < n; p++) {
+        if (p_off) p_off[p] = k;
         pdt[p] += dt;
         double x[3] = {P[p], P[stride + p], P[2 * stride + p]}, lc[3], e[3];
         eo_xtol(g, x, lc);
@@ -1591,12 +1605,18 @@ int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphe
         }
     }
     int64_t np = n;
-    for (int64_t p = 0; p < np; p++) {
-        if (P[6 * stride + p] > 0) continue;
-        copy_particle(P, stride, p, np - 1);
-        pdt[p] = pdt[np - 1];
-        np--;
-        p--;
+    if (holes) {
+        /* every survivor has used its time: pdt is 0 for all of them */
+        np = eo_compact_holes(P, stride, n);
+        for (int64_t p = 0; p < np; p++) pdt[p] = 0;
+    } else {
+        for (int64_t p = 0; p < np; p++) {
+            if (P[6 * stride + p] > 0) continue;
+            copy_particle(P, stride, p, np - 1);
+            pdt[p] = pdt[np - 1];
+            np--;
+            p--;
+        }
     }
     if (u_used) *u_used = k;
     if (n_new) *n_new = m;
@@ -1616,7 +1636,19 @@ int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphe
 int64_t eo_chemistry_ionize(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
                             double charge, double mass, double mpw0, double rate, double dt, double *Q,
                             int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used) {
+    return eo_chemistry_ionize_ex(g, den_n, rho, ef, charge, mass, mpw0, rate, dt, Q, max_new, qdt, u, nu, u_used,
+                                  NULL);
+}
+
+/* as eo_chemistry_ionize; cell_off (optional, one entry per cell in the
+ * reference's loop order, i outer, k inner) receives the index of each
+ * cell's first uniform */
+int64_t eo_chemistry_ionize_ex(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
+                               double charge, double mass, double mpw0, double rate, double dt, double *Q,
+                               int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used,
+                               int64_t *cell_off) {
     const double QE_ = 1.602176565e-19;
+    int64_t cidx = 0;
     const double dV = g->dh[0] * g->dh[1] * g->dh[2];
     int64_t k = 0, m = 0;
     for (int i = 0; i < g->ni - 1; i++)
@@ -1626,6 +1658,8 @@ int64_t eo_chemistry_ionize(const eo_grid *g, const double *den_n, const double 
                 const double na = gather1(g, den_n, lc);
                 const double ne = gather1(g, rho, lc) / QE_;
                 const double dni = rate * na * ne * dt;
+                if (cell_off) cell_off[cidx] = k;
+                cidx++;
                 if (k >= nu) return -1;
                 const int num_p = (int)(dni * dV / mpw0 + u[k++]);
                 for (int p = 0; p < num_p; p++) {

@@ -155,6 +155,15 @@ int64_t eo_advance_ch4_neutral(const eo_grid *g, const double sphere[4], double 
 int64_t eo_chemistry_ionize(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
                             double charge, double mass, double mpw0, double rate, double dt, double *Q,
                             int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used);
+int64_t eo_chemistry_ionize_ex(const eo_grid *g, const double *den_n, const double *rho, const double *ef,
+                               double charge, double mass, double mpw0, double rate, double dt, double *Q,
+                               int64_t max_new, double *qdt, const double *u, int64_t nu, int64_t *u_used,
+                               int64_t *cell_off);
+int64_t eo_advance_ch4_ion_ex(const eo_grid *g, const double *ef, const double sphere[4], double charge, double mass,
+                              double mpw0, double dt, double *P, int64_t stride, int64_t n, double *pdt,
+                              double neu_mpw0, double neu_charge, double neu_mass, double sph_mpw0, double sph_charge,
+                              double sph_mass, double *Q, int64_t max_new, int32_t *tag, double *qdt, int64_t *n_new,
+                              const double *u, int64_t nu, int64_t *u_used, int64_t *p_off, int holes);
 /* ch4 Species::advance of a charged species: ions striking the sphere create
  * neutrals and sputtered particles (ch4/Species.cpp:8-91, 103-119) */
 int64_t eo_advance_ch4_ion(const eo_grid *g, const double *ef, const double sphere[4], double charge, double mass,

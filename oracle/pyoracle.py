@@ -651,3 +651,52 @@ def deposit_mixed(g, cell, off, skip=None):
     sk = None if skip is None else _pu8(np.ascontiguousarray(skip, dtype=np.uint8))
     _mlib().eo_deposit_mixed(C.byref(g), _p32(cell), _pf(off), n, n, sk, pi64(acc))
     return acc
+
+
+def chemistry_ionize_offsets(g, den_n, rho, ef, charge, mass, mpw0, rate, dt, u, max_new=200000):
+    """eo_chemistry_ionize_ex: (new ions [7][m], their time left, uniforms
+    used, each cell's first uniform in the reference's cell order)"""
+    L = lib()
+    f = L.eo_chemistry_ionize_ex
+    f.restype = I64
+    f.argtypes = [C.POINTER(Grid), PD, PD, PD, D, D, D, D, D, PD, I64, PD, PD, I64, PI64, PI64]
+    den_n, rho, ef = (np.ascontiguousarray(a, dtype=np.float64) for a in (den_n, rho, ef))
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    Q, qdt = np.zeros((7, max_new)), np.zeros(max_new)
+    ncell = (g.ni - 1) * (g.nj - 1) * (g.nk - 1)
+    off = np.zeros(ncell, dtype=np.int64)
+    used = C.c_int64(0)
+    m = f(C.byref(g), pd(den_n), pd(rho), pd(ef), charge, mass, mpw0, rate, dt, pd(Q), max_new, pd(qdt), pd(u),
+          u.size, C.byref(used), pi64(off))
+    assert m >= 0, "uniforms ran out or the buffer of new particles is full"
+    return np.ascontiguousarray(Q[:, :m]), qdt[:m].copy(), used.value, off
+
+
+def advance_ch4_ion_holes(g, ef, sphere, charge, mass, mpw0, dt, P, pdt, neutral, spherium, u, max_new=100000):
+    """eo_advance_ch4_ion_ex with the CUDA path's removal order: (P, pdt,
+    created [7][m], tags, their time left, uniforms used, each particle's
+    first uniform)"""
+    L = lib()
+    f = L.eo_advance_ch4_ion_ex
+    f.restype = I64
+    f.argtypes = [C.POINTER(Grid), PD, PD, D, D, D, D, PD, I64, I64, PD, D, D, D, D, D, D, PD, I64,
+                  C.POINTER(C.c_int32), PD, PI64, PD, I64, PI64, PI64, C.c_int]
+    P = np.array(P, dtype=np.float64, order="C", copy=True)
+    pdt = np.array(pdt, dtype=np.float64, copy=True)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    ef = np.ascontiguousarray(ef, dtype=np.float64)
+    sph = np.array(list(sphere[:3]) + [sphere[3] ** 2], dtype=np.float64)
+    n = P.shape[1]
+    Q = np.zeros((7, max_new))
+    tag = np.zeros(max_new, dtype=np.int32)
+    qdt = np.zeros(max_new)
+    off = np.zeros(max(n, 1), dtype=np.int64)
+    m, used = C.c_int64(0), C.c_int64(0)
+    npart = f(C.byref(g), pd(ef), pd(sph), charge, mass, mpw0, dt, pd(P), n, n, pd(pdt), neutral[0], neutral[1],
+              neutral[2], spherium[0], spherium[1], spherium[2], pd(Q), max_new,
+              tag.ctypes.data_as(C.POINTER(C.c_int32)), pd(qdt), C.byref(m), pd(u), u.size, C.byref(used), pi64(off),
+              1)
+    assert npart >= 0, "uniforms ran out or the buffer of new particles is full"
+    k = m.value
+    return (np.ascontiguousarray(P[:, :npart]), pdt[:npart].copy(), np.ascontiguousarray(Q[:, :k]), tag[:k].copy(),
+            qdt[:k].copy(), used.value, off[:n].copy())
