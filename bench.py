@@ -532,9 +532,9 @@ def run_reference(args):
 
 
 def ncu_case(args):
-    """The workload's state, then exactly one k_push_mixed (push + deposit)
-    and one k_newton_pcg<float> launch: the case profiled with
-    ncu -k regex:"k_push_mixed|k_newton_pcg" -c 2."""
+    """The workload's state, then exactly one push with the fused deposit
+    (k_push_tiles after the tile sort) and one k_newton_pcg<float> launch:
+    the case profiled with ncu -k regex:"k_push_tiles|k_newton_pcg" -c 2."""
     E = espic_module()
     if not os.path.exists(E.LIB_PATH):
         E.build()
@@ -1161,6 +1161,9 @@ def main():
     ni, nj, nk = cfg["n"]
     n_unknown = (ni - 2) * (nj - 2) * (nk - 2)
     dom = max(phases, key=lambda k: phases[k])
+    # after a sort the push runs one block per tile segment (k_push_tiles);
+    # grids narrower than a tile box keep the per-particle k_push_mixed
+    push_kernel = "k_push_tiles" if min(cfg["n"]) >= 13 and cfg["sort_every"] else "k_push_mixed"
     push_bytes = 56.0 * t["n"]
     push_gbs = push_bytes / (phases["push"] * 1e-3) / 1e9
     if dom == "solve":
@@ -1170,9 +1173,9 @@ def main():
     else:
         alg = push_bytes
         achieved = push_gbs
-        kname = "k_push_mixed"
+        kname = push_kernel
     traffic = measured_traffic(args.config, kname, inner_per_step if dom == "solve" else t["n"])
-    push_traffic = measured_traffic(args.config, "k_push_mixed", t["n"])
+    push_traffic = measured_traffic(args.config, push_kernel, t["n"])
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -1196,7 +1199,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg},
-        "roofline_push": {"bound": "hbm", "kernel": "k_push_mixed", "achieved": push_gbs, "peak": hbm,
+        "roofline_push": {"bound": "hbm", "kernel": push_kernel, "achieved": push_gbs, "peak": hbm,
                           "unit": "GB/s", "frac": push_gbs / hbm, "bytes_per_particle": 56,
                           "traffic": push_traffic},
         "clocks": ck,
