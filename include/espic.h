@@ -296,9 +296,40 @@ int espic_mcc_cex(espic_world *w, int src, int tgt, double dt, const double *u, 
  * checks): particle p's k-th uniform is u[p_off[p] + k], 11 per bounce.  The
  * removal keeps this library's compaction order (the survivors of the
  * reference's swap-with-last).  bounces (may be NULL; non-NULL waits): sphere
- * strikes of the call.  Charged species (ch4's ion branch) are refused. */
+ * strikes of the call.  Charged species move with espic_advance_ch4_ions. */
 int espic_advance_ch4(espic_world *w, int sp, const double *pdt, const double *u, int64_t nu, const int64_t *p_off,
                       int64_t *bounces);
+/* Species::advance(neutrals, spherium) of a charged species (ch4's ion
+ * branch, ch4/Species.cpp:8-91) with the world's dt: each ion's velocity is
+ * kicked by E (t q / m) over its time left t (plus dt), then it moves for t;
+ * leaving the domain removes it; striking the sphere removes it and adds,
+ * at 0.999 of the way to the surface, (int)(mpw0 / neutrals' mpw0 + U)
+ * particles to species `neutrals` and, above 5000 m/s, (int)(0.1 mpw0 /
+ * spherium's mpw0 + U) to species `spherium` (which may be `neutrals`), each
+ * with a diffusely reflected velocity at the speed of a 1000 K wall for the
+ * ion's mass, rewound by the target's q/m E dt/2, the target's mpw0 and one
+ * dt of time left (Species::addParticle, ch4/Species.cpp:103-119).  Each
+ * target receives the particles in ion order (an ion's neutrals before its
+ * sputtered particles).  pdt, u, p_off as espic_advance_ch4, u holding per
+ * strike the neutral count's uniform, 11 per neutral, the sputter count's,
+ * 11 per sputtered particle.  The targets must be other float64-form
+ * species.  The call waits.  strikes (may be NULL): ions that struck the
+ * sphere. */
+int espic_advance_ch4_ions(espic_world *w, int sp, int neutrals, int spherium, const double *pdt, const double *u,
+                           int64_t nu, const int64_t *p_off, int64_t *strikes);
+/* ChemistryIonize(neutrals, ions, rate).apply(dt), ch4/Collisions.cpp:10-31:
+ * for each cell (the reference's order: i outer, k inner), n_a (neutrals'
+ * den) and n_e = rho / QE at the cell centre, and (int)(rate n_a n_e dt dV /
+ * ions' mpw0 + U) ions added at the cell's corner node (i, j, k) (World::pos
+ * of the truncated coordinates, ch4/World.h:107-111) with velocity 0 rewound
+ * by q/m E dt/2 and weight mpw0.  They join the species as appended
+ * particles (one dt of time left at its next ch4 push; the reference passes
+ * mpw0 as addParticle's time-left argument).  u NULL: cell c draws index c of
+ * the call's counter-based stream; u non-NULL (parity checks): cell c draws
+ * u[cell_off[c]] (cell_off: one entry per cell).  The ion species must be
+ * in the float64 form.  The call waits.  created (may be NULL): ions added. */
+int espic_chemistry_ionize(espic_world *w, int neutrals, int ions, double rate, double dt, const double *u,
+                           int64_t nu, const int64_t *cell_off, int64_t *created);
 /* World::getPE, ch2/World.cpp:72-84 */
 int espic_potential_energy(espic_world *w, double *pe);
 /* The per-step columns of Output::diagOutput, ch3/ver2/Output.cpp:96-132, with

@@ -131,6 +131,10 @@ def lib():
             "espic_mcc_cex": [VP, C.c_int, C.c_int, C.c_double, PD, I64, C.POINTER(C.c_int64),
                               C.POINTER(C.c_int64)],
             "espic_advance_ch4": [VP, C.c_int, PD, PD, I64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+            "espic_advance_ch4_ions": [VP, C.c_int, C.c_int, C.c_int, PD, PD, I64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)],
+            "espic_chemistry_ionize": [VP, C.c_int, C.c_int, C.c_double, C.c_double, PD, I64,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
             "espic_potential_energy": [VP, PD],
             "espic_diag_row": [VP, PD, C.c_int],
             "espic_update_average": [VP, C.c_int],
@@ -509,6 +513,28 @@ class Species:
                                           off.ctypes.data_as(C.POINTER(C.c_int64)), pb))
         return b.value if pb is not None else None
 
+    def advance_ch4_ions(self, neutrals, spherium=None, pdt=None, u=None, p_off=None):
+        """Species::advance(neutrals, spherium) of a charged species (ch4's
+        ion branch, ch4/Species.cpp:8-91): ions striking the sphere are
+        removed and create particles in `neutrals` and `spherium` (default:
+        `neutrals`, as ch4/Main.cpp:81 calls it).  pdt, u, p_off as
+        advance_ch4.  Waits; returns the number of strikes."""
+        spherium = neutrals if spherium is None else spherium
+        b = C.c_int64(0)
+        pp = None
+        if pdt is not None:
+            pdt = np.ascontiguousarray(pdt, dtype=np.float64)
+            pp = _pd(pdt)
+        if u is None:
+            check(lib().espic_advance_ch4_ions(self.world.h, self.id, neutrals.id, spherium.id, pp, None, 0,
+                                               None, C.byref(b)))
+        else:
+            uu = np.ascontiguousarray(u, dtype=np.float64)
+            off = np.ascontiguousarray(p_off, dtype=np.int64)
+            check(lib().espic_advance_ch4_ions(self.world.h, self.id, neutrals.id, spherium.id, pp, _pd(uu),
+                                               uu.size, off.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(b)))
+        return b.value
+
     # ch4 species moments (ch4/Species.cpp:191-240, float64 form)
     def sampleMoments(self):
         check(lib().espic_sample_moments(self.world.h, self.id))
@@ -575,6 +601,34 @@ class MCC_CEX:
             check(lib().espic_mcc_cex(self.world.h, self.source.id, self.target.id, dt, _pd(uu), uu.size,
                                       off.ctypes.data_as(C.POINTER(C.c_int64)), pn))
         self.last = n.value if pn is not None else None
+        return self.last
+
+
+class ChemistryIonize:
+    """ChemistryIonize(neutrals, ions, world, rate) (ch4/Collisions.h:76-86):
+    ions created at rate n_a n_e per cell (ch4/Collisions.cpp:10-31)."""
+
+    def __init__(self, neutrals, ions, world=None, rate=0.0):
+        self.neutrals, self.ions = neutrals, ions
+        self.world = world or ions.world
+        self.rate = float(rate)
+        self.last = None
+
+    def apply(self, dt, u=None, cell_off=None):
+        """ChemistryIonize::apply(dt); with u and cell_off the uniforms are
+        replayed (cell c, in the reference's loop order, draws
+        u[cell_off[c]]).  Waits; returns the number of ions added."""
+        n = C.c_int64(0)
+        if u is None:
+            check(lib().espic_chemistry_ionize(self.world.h, self.neutrals.id, self.ions.id, self.rate, dt, None, 0,
+                                               None, C.byref(n)))
+        else:
+            uu = np.ascontiguousarray(u, dtype=np.float64)
+            off = np.ascontiguousarray(cell_off, dtype=np.int64)
+            check(lib().espic_chemistry_ionize(self.world.h, self.neutrals.id, self.ions.id, self.rate, dt,
+                                               _pd(uu), uu.size, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                               C.byref(n)))
+        self.last = n.value
         return self.last
 
 

@@ -152,7 +152,7 @@ static void free_species(Species *s) {
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
                     s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum,
                     s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol,
-                    s->ch4_settled, s->ch4_bounces, s->seg};
+                    s->ch4_settled, s->ch4_bounces, s->seg, s->ch4_cnt, s->ionize_cnt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -1210,7 +1210,7 @@ extern "C" int espic_advance_ch4(espic_world *h, int sp, const double *pdt, cons
     SPECIES(sp);
     if (s.form != ESPIC_FORM_FP64) return fail(ESPIC_ERR_ARG, "the ch4 push works on a species in the float64 form");
     if (s.charge != 0)
-        return fail(ESPIC_ERR_ARG, "the ch4 push of a charged species (ions striking the sphere) is not built");
+        return fail(ESPIC_ERR_ARG, "a charged species moves with espic_advance_ch4_ions");
     if (!(w.dt > 0)) return fail(ESPIC_ERR_ARG, "set the time step first");
     if (u && (!p_off || nu < 0)) return fail(ESPIC_ERR_ARG, "replayed uniforms need their particle offsets");
     if (!s.ch4_settled) {
@@ -1257,6 +1257,130 @@ extern "C" int espic_advance_ch4(espic_world *h, int sp, const double *pdt, cons
     }
     if (staged || bounces) return take_device_errors(w);
     return ESPIC_OK;
+}
+
+/* copies n values to a new device buffer (nothing when host is NULL) */
+template <class T>
+static int stage(T **d, const T *host, int64_t n, cudaStream_t st) {
+    *d = nullptr;
+    if (!host) return ESPIC_OK;
+    if (dalloc(d, n > 0 ? n : 1) != ESPIC_OK) return ESPIC_ERR_CUDA;
+    if (n > 0 && cudaMemcpyAsync(*d, host, n * sizeof(T), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return ESPIC_ERR_CUDA;
+    return ESPIC_OK;
+}
+
+static int refresh_bound(World &w, Species &t) {
+    int64_t c = 0;
+    CK(cudaMemcpy(&c, t.d_count, sizeof c, cudaMemcpyDeviceToHost));
+    t.host_bound = c;
+    return ESPIC_OK;
+}
+
+extern "C" int espic_advance_ch4_ions(espic_world *h, int sp, int neutrals, int spherium, const double *pdt,
+                                      const double *u, int64_t nu, const int64_t *p_off, int64_t *strikes) {
+    WORLD(h);
+    SPECIES(sp);
+    if (s.form != ESPIC_FORM_FP64) return fail(ESPIC_ERR_ARG, "the ch4 push works on a species in the float64 form");
+    if (s.charge == 0) return fail(ESPIC_ERR_ARG, "a neutral species moves with espic_advance_ch4");
+    if (neutrals < 0 || neutrals >= (int)w.species.size() || spherium < 0 || spherium >= (int)w.species.size())
+        return fail(ESPIC_ERR_ARG, "target species id out of range");
+    if (neutrals == sp || spherium == sp)
+        return fail(ESPIC_ERR_ARG, "an ion species cannot receive the particles its own strikes create");
+    Species &neu = *w.species[neutrals], &sph = *w.species[spherium];
+    if (neu.form != ESPIC_FORM_FP64 || sph.form != ESPIC_FORM_FP64)
+        return fail(ESPIC_ERR_ARG, "the target species must be in the float64 form");
+    if (!(neu.mpw0 > 0) || !(sph.mpw0 > 0) || !(s.mpw0 > 0))
+        return fail(ESPIC_ERR_ARG, "the ion and target species need mpw0 > 0");
+    if (!(w.dt > 0)) return fail(ESPIC_ERR_ARG, "set the time step first");
+    if (u && (!p_off || nu < 0)) return fail(ESPIC_ERR_ARG, "replayed uniforms need their particle offsets");
+    /* most particles one strike creates: the uniforms of one ion must fit
+     * its 2^20 indices of the counter-based stream, and the counts of one
+     * call an int32 scan */
+    const double most = floor(s.mpw0 / neu.mpw0 + 1) + floor(0.1 * s.mpw0 / sph.mpw0 + 1);
+    if (!(2 + 11 * most < (double)(1 << 20)) || !(most * (double)(s.cap + 1) < 2147483647.0))
+        return fail(ESPIC_ERR_ARG, "mpw0 ratios of %g particles per strike are beyond this push", most);
+    if (!s.ch4_settled) {
+        if (dalloc(&s.ch4_settled, 1) != ESPIC_OK || dalloc(&s.ch4_bounces, 1) != ESPIC_OK) return ESPIC_ERR_CUDA;
+        CK(cudaMemsetAsync(s.ch4_settled, 0, sizeof(int64_t), w.stream));
+    }
+    if (!s.ch4_cnt && dalloc(&s.ch4_cnt, 2 * (s.cap + 1) + int_scan_blocks(s.cap + 1) + 1) != ESPIC_OK)
+        return ESPIC_ERR_CUDA;
+    double *dpdt = nullptr, *du = nullptr;
+    int64_t *doff = nullptr;
+    if (pdt || u) {
+        int64_t np = 0; /* pdt and p_off hold one entry per particle: the exact count */
+        CK(cudaMemcpyAsync(&np, s.d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, w.stream));
+        CK(cudaStreamSynchronize(w.stream));
+        s.host_bound = np;
+        int rc = stage(&dpdt, pdt, np, w.stream);
+        if (rc == ESPIC_OK) rc = stage(&du, u, nu, w.stream);
+        if (rc == ESPIC_OK) rc = stage(&doff, u ? p_off : (const int64_t *)nullptr, np, w.stream);
+        if (rc != ESPIC_OK) {
+            cudaFree(dpdt);
+            cudaFree(du);
+            cudaFree(doff);
+            return fail(ESPIC_ERR_CUDA, "staging the replayed inputs failed");
+        }
+    }
+    {
+        PhaseScope ph(w, ESPIC_PHASE_PUSH);
+        launch_advance_ch4_ions(w, s, neu, sph, w.dt, dpdt, du, nu, doff);
+    }
+    const cudaError_t e = cudaStreamSynchronize(w.stream);
+    cudaFree(dpdt);
+    cudaFree(du);
+    cudaFree(doff);
+    if (e != cudaSuccess) return fail(ESPIC_ERR_CUDA, "%s", cudaGetErrorString(e));
+    CHECK_LAUNCH();
+    /* the targets grew by counts known only on the device */
+    if (refresh_bound(w, neu) != ESPIC_OK || refresh_bound(w, sph) != ESPIC_OK) return ESPIC_ERR_CUDA;
+    if (strikes) {
+        unsigned long long c = 0;
+        CK(cudaMemcpy(&c, s.ch4_bounces, sizeof c, cudaMemcpyDeviceToHost));
+        *strikes = (int64_t)c;
+    }
+    return take_device_errors(w);
+}
+
+extern "C" int espic_chemistry_ionize(espic_world *h, int neutrals, int ions, double rate, double dt,
+                                      const double *u, int64_t nu, const int64_t *cell_off, int64_t *created) {
+    WORLD(h);
+    if (neutrals < 0 || neutrals >= (int)w.species.size() || ions < 0 || ions >= (int)w.species.size())
+        return fail(ESPIC_ERR_ARG, "species id out of range");
+    Species &neu = *w.species[neutrals], &ion = *w.species[ions];
+    if (ion.form != ESPIC_FORM_FP64) return fail(ESPIC_ERR_ARG, "the ion species must be in the float64 form");
+    if (!(ion.mpw0 > 0)) return fail(ESPIC_ERR_ARG, "the ion species needs mpw0 > 0");
+    if (u && (!cell_off || nu < 0)) return fail(ESPIC_ERR_ARG, "replayed uniforms need their cell offsets");
+    const int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    if (!ion.ionize_cnt && dalloc(&ion.ionize_cnt, ncells + 1 + int_scan_blocks(ncells + 1) + 1) != ESPIC_OK)
+        return ESPIC_ERR_CUDA;
+    double *du = nullptr;
+    int64_t *doff = nullptr;
+    int rc = stage(&du, u, nu, w.stream);
+    if (rc == ESPIC_OK) rc = stage(&doff, u ? cell_off : (const int64_t *)nullptr, ncells, w.stream);
+    if (rc != ESPIC_OK) {
+        cudaFree(du);
+        cudaFree(doff);
+        return fail(ESPIC_ERR_CUDA, "staging the replayed inputs failed");
+    }
+    const uint64_t stream = (0xC6ull << 56) | ((uint64_t)(ion.id & 0xff) << 48) |
+                            (ion.ionize_calls & 0xffffffffffffull);
+    {
+        PhaseScope ph(w, ESPIC_PHASE_INJECT);
+        launch_ionize(w, neu, ion, rate, dt, du, nu, doff, ion.ionize_cnt, stream);
+    }
+    ion.ionize_calls++;
+    const cudaError_t e = cudaStreamSynchronize(w.stream);
+    cudaFree(du);
+    cudaFree(doff);
+    if (e != cudaSuccess) return fail(ESPIC_ERR_CUDA, "%s", cudaGetErrorString(e));
+    CHECK_LAUNCH();
+    int64_t c[2] = {0, 0};
+    CK(cudaMemcpy(c, ion.d_count, sizeof c, cudaMemcpyDeviceToHost));
+    ion.host_bound = c[0];
+    if (created) *created = c[0] - c[1];
+    return take_device_errors(w);
 }
 
 extern "C" int espic_species_diag(espic_world *h, int sp, double out[5]) {

@@ -80,6 +80,41 @@ __host__ __device__ inline double c4_line_sphere(const Ch4Geo &G, const double x
     return tp;
 }
 
+/* Species::sampleReflectedVelocity (ch4/Species.cpp:94-100): speed
+ * v_mag1 + a_th (v_th - v_mag1) with a_th = 1 and v_th of sampleVth(1000)
+ * for the striking particle's mass, direction World::sphereDiffuseVector
+ * (ch4/World.cpp:185-199) at x.  Uniforms U(k) .. U(k + 10): 9 for
+ * sampleVth (three sums of three, ch4/Species.cpp:149-158), then sin_theta
+ * and psi. */
+template <class UF>
+__host__ __device__ inline void c4_reflect(const Ch4Geo &G, double mass, const double x[3], double v_mag1, UF &U,
+                                           int k, double vel[3]) {
+    const double v_th = sqrt(2 * CH4_K * 1000 / mass);
+    const double v1 = v_th * (U(k) + U(k + 1) + U(k + 2) - 1.5);
+    const double v2 = v_th * (U(k + 3) + U(k + 4) + U(k + 5) - 1.5);
+    const double v3 = v_th * (U(k + 6) + U(k + 7) + U(k + 8) - 1.5);
+    /* 3 / sqrt(2 + 2 + 2) in the reference: sqrt of the int 6 is sqrt(6.0)
+     * on the host; in device code sqrt must be given a double (an int
+     * argument made nvcc drop the rest of the caller's branch) */
+    const double vth = 3.0 / sqrt(6.0) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    const double a_th = 1;
+    const double v_mag2 = v_mag1 + a_th * (vth - v_mag1);
+    const double sin_theta = U(k + 9);
+    const double cos_theta = sqrt(1 - sin_theta * sin_theta);
+    const double psi = 2 * CH4_PI * U(k + 10);
+    double r[3] = {x[0] - G.sph[0], x[1] - G.sph[1], x[2] - G.sph[2]}, n[3], t1[3], t2[3];
+    const double m = sqrt(c4_dot(r, r));
+    for (int i = 0; i < 3; i++) n[i] = r[i] / m;
+    const double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0};
+    if (c4_dot(n, ex) != 0)
+        c4_cross(n, ex, t1);
+    else
+        c4_cross(n, ey, t1);
+    c4_cross(n, t1, t2);
+    const double cp = cos(psi), sp = sin(psi);
+    for (int i = 0; i < 3; i++) vel[i] = v_mag2 * (sin_theta * cp * t1[i] + sin_theta * sp * t2[i] + cos_theta * n[i]);
+}
+
 /* The step of one particle: t its time for this step, x and v updated in
  * place.  U(k) returns the particle's k-th uniform of the step.  Returns
  * the number of bounces; alive becomes false when the particle leaves the
@@ -105,34 +140,7 @@ __host__ __device__ inline int ch4_advance_one(const Ch4Geo &G, double mass, dou
             const double s = 0.999 * tp;
             for (int i = 0; i < 3; i++) x[i] = old[i] + s * (x[i] - old[i]);
             const double v_mag1 = sqrt(c4_dot(v, v));
-            const int k = 11 * bounces;
-            /* sampleVth(1000), ch4/Species.cpp:149-158 */
-            const double v_th = sqrt(2 * CH4_K * 1000 / mass);
-            const double v1 = v_th * (U(k) + U(k + 1) + U(k + 2) - 1.5);
-            const double v2 = v_th * (U(k + 3) + U(k + 4) + U(k + 5) - 1.5);
-            const double v3 = v_th * (U(k + 6) + U(k + 7) + U(k + 8) - 1.5);
-            /* 3 / sqrt(2 + 2 + 2) in the reference: sqrt of the int 6 is
-             * sqrt(6.0) on the host; in device code sqrt must be given a
-             * double (an int argument made nvcc drop the rest of this
-             * branch) */
-            const double vth = 3.0 / sqrt(6.0) * sqrt(v1 * v1 + v2 * v2 + v3 * v3);
-            const double a_th = 1;
-            const double v_mag2 = v_mag1 + a_th * (vth - v_mag1);
-            /* sphereDiffuseVector */
-            const double sin_theta = U(k + 9);
-            const double cos_theta = sqrt(1 - sin_theta * sin_theta);
-            const double psi = 2 * CH4_PI * U(k + 10);
-            double r[3] = {x[0] - G.sph[0], x[1] - G.sph[1], x[2] - G.sph[2]}, n[3], t1[3], t2[3];
-            const double m = sqrt(c4_dot(r, r));
-            for (int i = 0; i < 3; i++) n[i] = r[i] / m;
-            const double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0};
-            if (c4_dot(n, ex) != 0)
-                c4_cross(n, ex, t1);
-            else
-                c4_cross(n, ey, t1);
-            c4_cross(n, t1, t2);
-            const double cp = cos(psi), sp = sin(psi);
-            for (int i = 0; i < 3; i++) v[i] = v_mag2 * (sin_theta * cp * t1[i] + sin_theta * sp * t2[i] + cos_theta * n[i]);
+            c4_reflect(G, mass, x, v_mag1, U, 11 * bounces, v);
             if (++bounces > max_bounces) alive = false;
             continue;
         }
@@ -140,6 +148,33 @@ __host__ __device__ inline int ch4_advance_one(const Ch4Geo &G, double mass, dou
         if (++n_steps > 20) alive = false;
     }
     return bounces;
+}
+
+/* The move of one ion of ch4's ion branch (Species::advance of a charged
+ * species, ch4/Species.cpp:26-85) after its E kick: it moves for its whole
+ * time t; leaving the domain kills it (returns 1); landing in the sphere
+ * puts it 0.999 of the way to the intersection, sets v_mag1 to its speed
+ * and kills it (returns 2: the caller creates the neutrals and sputtered
+ * particles); else it survives (returns 0).  The reference's loop ends after
+ * one pass in every case: a surviving ion has no time left and a killed one
+ * no weight. */
+__host__ __device__ inline int ch4_ion_move(const Ch4Geo &G, double t, double x[3], const double v[3],
+                                            double &v_mag1) {
+    if (!(t > 0)) return 0;
+    double old[3];
+    for (int i = 0; i < 3; i++) {
+        old[i] = x[i];
+        x[i] = old[i] + v[i] * t;
+    }
+    if (!c4_in_bounds(G, x)) return 1;
+    if (c4_in_sphere(G, x)) {
+        const double tp = c4_line_sphere(G, old, x);
+        const double s = 0.999 * tp;
+        for (int i = 0; i < 3; i++) x[i] = old[i] + s * (x[i] - old[i]);
+        v_mag1 = sqrt(c4_dot(v, v));
+        return 2;
+    }
+    return 0;
 }
 
 }  // namespace espic

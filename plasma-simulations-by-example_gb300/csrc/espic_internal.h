@@ -144,6 +144,13 @@ void launch_mcc(World &w, Species &src, const Species &tgt, double dt, const dou
 /* ch4 Species::advance of a neutral species (sphere diffuse reflection) */
 void launch_advance_ch4(World &w, Species &s, double dt, const double *d_pdt, const double *d_u, int64_t nu,
                         const int64_t *d_off);
+/* ch4 Species::advance of a charged species: struck ions create particles
+ * in neu and sph (which may be one species) */
+void launch_advance_ch4_ions(World &w, Species &s, Species &neu, Species &sph, double dt, const double *d_pdt,
+                             const double *d_u, int64_t nu, const int64_t *d_off);
+/* ChemistryIonize::apply; cnt: ncells + 1 + int_scan_blocks(ncells + 1) entries */
+void launch_ionize(World &w, const Species &neu, Species &ion, double rate, double dt, const double *d_u,
+                   int64_t nu, const int64_t *d_off, int32_t *cnt, uint64_t stream);
 void launch_inv_vol(World &w);
 void launch_charge(World &w);
 void launch_add_fp64(World &w, Species &s, const double *d_pos3, const double *d_vel3,

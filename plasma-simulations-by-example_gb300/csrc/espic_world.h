@@ -63,8 +63,13 @@ struct Species {
     /* ch4 neutral push: particles below *ch4_settled have used their time
      * (those above were appended since the last push), bounces of the call */
     int64_t *ch4_settled = nullptr;
-    unsigned long long *ch4_bounces = nullptr;
+    unsigned long long *ch4_bounces = nullptr; /* bounces (neutrals) or sphere strikes (ions) of the call */
     uint64_t ch4_calls = 0;
+    /* ch4 ion push: per-ion counts of new particles for each target and
+     * their scans' block sums; ChemistryIonize into this species: per-cell
+     * counts and block sums (both allocated on first use) */
+    int32_t *ch4_cnt = nullptr, *ionize_cnt = nullptr;
+    uint64_t ionize_calls = 0;
 };
 
 struct Source {

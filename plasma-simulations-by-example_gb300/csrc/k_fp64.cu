@@ -2173,3 +2173,335 @@ void launch_advance_ch4(World &w, Species &s, double dt, const double *d_pdt, co
 }
 
 }  // namespace espic
+
+namespace espic {
+
+/* ------------------------------------------------------------------------ */
+/* ch4 ion push: Species::advance(neutrals, spherium) of a charged species
+ * (ch4/Species.cpp:8-91).  Pass 1, one thread per ion: the E kick over the
+ * ion's whole time left (v += E (t q / m)), one move (ch4_ion_move); an ion
+ * leaving the domain is dead; one striking the sphere is dead and draws its
+ * neutral count (int)(mpw0 / neutral mpw0 + U(0)) and its sputter count
+ * (int)(yield mpw0 / spherium mpw0 + U(1 + 11 n0)), yield 0.1 above
+ * 5000 m/s.  The strike point replaces the ion's position and its speed its
+ * vx (pass 2 reads them before the compaction).  cnt0 / cnt1 receive the
+ * particles each ion adds to each target (0 when the strike point is
+ * outside [x0, xm), which addParticle rejects, ch4/Species.cpp:103-119);
+ * when both targets are one species cnt0 holds both.  Threads n .. nb write
+ * the zeros that close the scans. */
+struct Ch4IonArgs {
+    Geo g;
+    Ch4Geo G;
+    double charge, mass, mpw0, dt;
+    double ratio0;   /* mpw0 / neutral mpw0 */
+    double sph_mpw0; /* spherium mpw0 */
+    double tq[2], tm[2], tw[2]; /* target charge, mass, mpw0 */
+    int same;        /* both targets are one species */
+    int write_w[2];  /* the target keeps a weight row */
+};
+
+__global__ void __launch_bounds__(256) k_ch4_ion_push(Ch4IonArgs a, const double *__restrict__ ef, double *P,
+                                                      int64_t stride, int64_t nb, const int64_t *__restrict__ d_count,
+                                                      const int64_t *__restrict__ d_settled,
+                                                      const double *__restrict__ pdt, const double *__restrict__ u,
+                                                      int64_t nu, const int64_t *__restrict__ p_off, uint64_t seed,
+                                                      uint64_t stream, int32_t *cnt0, int32_t *cnt1,
+                                                      uint32_t *deadmask, int32_t *tiledead,
+                                                      unsigned long long *nstrike, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = d_count[0];
+    bool dead = false, struck = false;
+    int32_t c0 = 0, c1 = 0;
+    if (p < n) {
+        double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+        double v[3] = {P[3 * stride + p], P[4 * stride + p], P[5 * stride + p]};
+        const double t = (pdt ? pdt[p] : (p >= d_settled[0] ? a.dt : 0.0)) + a.dt;
+        double lc[3], e[3];
+        xtol(a.g, x, lc);
+        gather3(a.g, ef, lc, e);
+        const double s = t * a.charge / a.mass;
+        for (int d = 0; d < 3; d++) v[d] += e[d] * s;
+        double v_mag1 = 0;
+        const int res = ch4_ion_move(a.G, t, x, v, v_mag1);
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+            atomicOr(err, DERR_NONFINITE);
+            dead = true;
+        } else if (res == 2) {
+            dead = struck = true;
+            Ch4Uniforms U{u, nu, u ? p_off[p] : 0, seed, stream, (uint64_t)p << 20, false};
+            const int n0 = (int)(a.ratio0 + U(0));
+            const double sput_yield = (v_mag1 > 5000) ? 0.1 : 0;
+            const int n1 = (int)(sput_yield * a.mpw0 / a.sph_mpw0 + U(1 + 11 * n0));
+            if (U.bad) atomicOr(err, DERR_NEUTRAL);
+            if (in_bounds(a.g, x)) {
+                c0 = a.same ? n0 + n1 : n0;
+                c1 = a.same ? 0 : n1;
+            }
+            v[0] = v_mag1;
+        } else {
+            dead = res != 0;
+        }
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + p] = x[d];
+            P[(3 + d) * stride + p] = v[d];
+        }
+    }
+    if (p <= nb) {
+        cnt0[p] = c0;
+        if (cnt1) cnt1[p] = c1;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, dead);
+    const unsigned ms = __ballot_sync(0xffffffffu, struck);
+    if ((threadIdx.x & 31) == 0 && p < n) {
+        deadmask[p >> 5] = m;
+        if (m) atomicAdd(tiledead + (p / TILE_PARTICLES), __popc(m));
+        if (ms) atomicAdd(nstrike, (unsigned long long)__popc(ms));
+    }
+}
+
+/* The scanned counts' total (entry nb) grows the target: the count before
+ * goes to d_count[1], the new count (at most the capacity) to d_count[0]. */
+__global__ void k_ch4_ion_reserve(const int32_t *__restrict__ pre, int64_t nb, int64_t *d_count, int64_t cap,
+                                  int *err) {
+    const int64_t n_old = d_count[0];
+    int64_t n_new = n_old + pre[nb];
+    if (n_new > cap) {
+        atomicOr(err, DERR_CAPACITY);
+        n_new = cap;
+    }
+    d_count[1] = n_old;
+    d_count[0] = n_new;
+}
+
+struct Ch4Target {
+    double *P;
+    int64_t stride, cap;
+    const int64_t *d_count;
+};
+
+__device__ inline void ch4_ion_put(const Ch4IonArgs &a, const Ch4Target &T, int kind, int64_t dst, const double x[3],
+                                   const double vel[3], const double e2[3]) {
+    if (dst >= T.cap) return;
+    for (int i = 0; i < 3; i++) {
+        T.P[i * T.stride + dst] = x[i];
+        T.P[(3 + i) * T.stride + dst] = vel[i] - a.tq[kind] / a.tm[kind] * e2[i] * (0.5 * a.dt);
+    }
+    if (a.write_w[kind]) T.P[6 * T.stride + dst] = a.tw[kind];
+}
+
+/* Pass 2, one thread per ion: a struck ion's particles in the reference's
+ * order (its neutrals, then its sputtered particles), each with a diffusely
+ * reflected velocity (the ion's mass in sampleVth) rewound by the target's
+ * q/m E dt/2 at the strike point; ion p's particles go to its target at
+ * the count before the call plus the exclusive prefix of the counts, so each
+ * target receives them in ion order, as the reference's emplace_back. */
+__global__ void __launch_bounds__(256) k_ch4_ion_create(Ch4IonArgs a, const double *__restrict__ ef,
+                                                        const double *__restrict__ P, int64_t stride, int64_t nb,
+                                                        const int32_t *__restrict__ pre0,
+                                                        const int32_t *__restrict__ pre1, Ch4Target T0, Ch4Target T1,
+                                                        const double *__restrict__ u, int64_t nu,
+                                                        const int64_t *__restrict__ p_off, uint64_t seed,
+                                                        uint64_t stream, int *err) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nb) return;
+    const int32_t b0 = pre0[p], c0 = pre0[p + 1] - b0;
+    const int32_t b1 = a.same ? 0 : pre1[p], c1 = a.same ? 0 : pre1[p + 1] - b1;
+    if (c0 + c1 == 0) return;
+    const double x[3] = {P[p], P[stride + p], P[2 * stride + p]};
+    const double v_mag1 = P[3 * stride + p];
+    Ch4Uniforms U{u, nu, u ? p_off[p] : 0, seed, stream, (uint64_t)p << 20, false};
+    const int n0 = (int)(a.ratio0 + U(0));
+    const int n1 = a.same ? c0 - n0 : c1;
+    double lc[3], e2[3];
+    xtol(a.g, x, lc);
+    gather3(a.g, ef, lc, e2);
+    const int64_t base0 = T0.d_count[1] + b0;
+    for (int c = 0; c < n0; c++) {
+        double vel[3];
+        c4_reflect(a.G, a.mass, x, v_mag1, U, 1 + 11 * c, vel);
+        ch4_ion_put(a, T0, 0, base0 + c, x, vel, e2);
+    }
+    const Ch4Target &Ts = a.same ? T0 : T1;
+    const int64_t base1 = a.same ? base0 + n0 : T1.d_count[1] + b1;
+    for (int c = 0; c < n1; c++) {
+        double vel[3];
+        c4_reflect(a.G, a.mass, x, v_mag1, U, 2 + 11 * n0 + 11 * c, vel);
+        ch4_ion_put(a, Ts, 1, base1 + c, x, vel, e2);
+    }
+    if (U.bad) atomicOr(err, DERR_NEUTRAL);
+}
+
+static Ch4Geo ch4_geo(const World &w) {
+    Ch4Geo G;
+    for (int d = 0; d < 3; d++) {
+        G.x0[d] = w.g.x0[d];
+        G.xm[d] = w.g.xm[d];
+        G.sph[d] = w.sphere[d];
+    }
+    G.sph[3] = w.has_sphere ? w.sphere[3] : -1.0;
+    return G;
+}
+
+void launch_advance_ch4_ions(World &w, Species &s, Species &neu, Species &sph, double dt, const double *d_pdt,
+                             const double *d_u, int64_t nu, const int64_t *d_off) {
+    cudaMemsetAsync(s.ch4_bounces, 0, sizeof(unsigned long long), w.stream);
+    const int64_t nb = s.host_bound;
+    if (nb > 0) {
+        Ch4IonArgs a;
+        a.g = w.g;
+        a.G = ch4_geo(w);
+        a.charge = s.charge;
+        a.mass = s.mass;
+        a.mpw0 = s.mpw0;
+        a.dt = dt;
+        a.ratio0 = s.mpw0 / neu.mpw0;
+        a.sph_mpw0 = sph.mpw0;
+        a.tq[0] = neu.charge;
+        a.tm[0] = neu.mass;
+        a.tw[0] = neu.mpw0;
+        a.tq[1] = sph.charge;
+        a.tm[1] = sph.mass;
+        a.tw[1] = sph.mpw0;
+        a.same = &neu == &sph;
+        a.write_w[0] = !neu.uniform_w;
+        a.write_w[1] = !sph.uniform_w;
+        const uint64_t stream = (0xC5ull << 56) | ((uint64_t)(s.id & 0xff) << 48) |
+                                (s.ch4_calls & 0xffffffffffffull);
+        int32_t *cnt0 = s.ch4_cnt, *cnt1 = a.same ? nullptr : s.ch4_cnt + (nb + 1);
+        int32_t *bsum = s.ch4_cnt + 2 * (nb + 1);
+        k_ch4_ion_push<<<blocks_for(nb + 1, 256), 256, 0, w.stream>>>(
+            a, w.ef, s.P, s.cap, nb, s.d_count, s.ch4_settled, d_pdt, d_u, nu, d_off, w.seed, stream, cnt0, cnt1,
+            s.deadmask, s.tiledead, s.ch4_bounces, w.d_err);
+        launch_int_excl_scan(w.stream, cnt0, nb + 1, bsum);
+        k_ch4_ion_reserve<<<1, 1, 0, w.stream>>>(cnt0, nb, neu.d_count, neu.cap, w.d_err);
+        if (cnt1) {
+            launch_int_excl_scan(w.stream, cnt1, nb + 1, bsum);
+            k_ch4_ion_reserve<<<1, 1, 0, w.stream>>>(cnt1, nb, sph.d_count, sph.cap, w.d_err);
+        }
+        Ch4Target T0{neu.P, neu.cap, neu.cap, neu.d_count}, T1{sph.P, sph.cap, sph.cap, sph.d_count};
+        k_ch4_ion_create<<<blocks_for(nb, 256), 256, 0, w.stream>>>(a, w.ef, s.P, s.cap, nb, cnt0, cnt1, T0, T1, d_u,
+                                                                     nu, d_off, w.seed, stream, w.d_err);
+        w.nlaunch += 4 + (cnt1 ? 4 : 0) + 3;
+        launch_compact(w, s);
+    }
+    k_ch4_settle<<<1, 1, 0, w.stream>>>(s.d_count, s.ch4_settled);
+    w.nlaunch++;
+    s.ch4_calls++;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ChemistryIonize::apply (ch4/Collisions.cpp:10-31), one thread per cell
+ * c = (i (nj-1) + j) (nk-1) + k, the reference's loop order: n_a and
+ * n_e = rho / QE gathered at the cell centre (Field_::gather's 8 terms in its
+ * corner order), dni = rate n_a n_e dt, and (int)(dni dV / mpw0 + U) ions
+ * (none when that is below 1 or not a number).  Uniform: u[cell_off[c]] when
+ * replaying, else index c of the call's counter-based stream (the three the
+ * reference draws per ion only feed World::pos(int, int, int), which
+ * truncates them away, ch4/World.h:107-111).  Entry ncells .. closes the
+ * scan with 0. */
+__device__ __forceinline__ double gather1(const Geo &g, const double *__restrict__ f, const double lc[3]) {
+    const int i = clamp_cell((int)lc[0], g.ni), j = clamp_cell((int)lc[1], g.nj), k = clamp_cell((int)lc[2], g.nk);
+    const double di = lc[0] - i, dj = lc[1] - j, dk = lc[2] - k;
+    const int64_t n0 = node_of(g, i, j, k), sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    return f[n0] * (1 - di) * (1 - dj) * (1 - dk) + f[n0 + 1] * (di) * (1 - dj) * (1 - dk) +
+           f[n0 + 1 + sy] * (di) * (dj) * (1 - dk) + f[n0 + sy] * (1 - di) * (dj) * (1 - dk) +
+           f[n0 + sz] * (1 - di) * (1 - dj) * (dk) + f[n0 + 1 + sz] * (di) * (1 - dj) * (dk) +
+           f[n0 + 1 + sy + sz] * (di) * (dj) * (dk) + f[n0 + sy + sz] * (1 - di) * (dj) * (dk);
+}
+
+__device__ __forceinline__ void cell_ijk(const Geo &g, int64_t c, int &i, int &j, int &k) {
+    const int64_t ck = g.nk - 1, cj = g.nj - 1;
+    k = (int)(c % ck);
+    const int64_t r = c / ck;
+    j = (int)(r % cj);
+    i = (int)(r / cj);
+}
+
+__global__ void __launch_bounds__(256) k_ionize_count(Geo g, const double *__restrict__ den_n,
+                                                      const double *__restrict__ rho, double rate, double dt,
+                                                      double dV, double mpw0, int64_t ncells,
+                                                      const double *__restrict__ u, int64_t nu,
+                                                      const int64_t *__restrict__ cell_off, uint64_t seed,
+                                                      uint64_t stream, int32_t *cnt, int *err) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ncells) return;
+    int32_t num = 0;
+    if (c < ncells) {
+        int i, j, k;
+        cell_ijk(g, c, i, j, k);
+        const double lc[3] = {i + 0.5, j + 0.5, k + 0.5};
+        const double na = gather1(g, den_n, lc);
+        const double ne = gather1(g, rho, lc) / QE;
+        const double dni = rate * na * ne * dt;
+        double U;
+        if (u) {
+            const int64_t o = cell_off[c];
+            if (o < 0 || o >= nu) {
+                atomicOr(err, DERR_NEUTRAL);
+                U = 0.0;
+            } else {
+                U = u[o];
+            }
+        } else {
+            U = philox_uniform(seed, stream, (uint64_t)c);
+        }
+        const double y = dni * dV / mpw0 + U;
+        if (y >= 2147483647.0) {
+            atomicOr(err, DERR_CAPACITY);
+        } else if (y >= 1) {
+            num = (int32_t)y;
+        }
+    }
+    cnt[c] = num;
+}
+
+/* Each new ion of cell (i, j, k) sits at node (i, j, k) (World::pos of the
+ * truncated coordinates) with velocity 0 rewound by q/m E dt/2 (dt: the
+ * world's time step, as addParticle) and weight mpw0, written after the
+ * species' particles in cell order. */
+__global__ void __launch_bounds__(256) k_ionize_create(Geo g, const double *__restrict__ ef, double qm,
+                                                       double dt, double mpw0, int write_w, int64_t ncells,
+                                                       const int32_t *__restrict__ pre, double *P, int64_t stride,
+                                                       int64_t cap, const int64_t *__restrict__ d_count) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int32_t b = pre[c], num = pre[c + 1] - b;
+    if (num <= 0) return;
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
+    const double x[3] = {g.x0[0] + g.dh[0] * (double)i, g.x0[1] + g.dh[1] * (double)j,
+                         g.x0[2] + g.dh[2] * (double)k};
+    double lc[3], e[3];
+    xtol(g, x, lc);
+    gather3(g, ef, lc, e);
+    double v[3];
+    for (int d = 0; d < 3; d++) v[d] = 0.0 - qm * e[d] * (0.5 * dt);
+    const int64_t base = d_count[1] + b;
+    for (int q = 0; q < num; q++) {
+        const int64_t dst = base + q;
+        if (dst >= cap) return;
+        for (int d = 0; d < 3; d++) {
+            P[d * stride + dst] = x[d];
+            P[(3 + d) * stride + dst] = v[d];
+        }
+        if (write_w) P[6 * stride + dst] = mpw0;
+    }
+}
+
+void launch_ionize(World &w, const Species &neu, Species &ion, double rate, double dt, const double *d_u,
+                   int64_t nu, const int64_t *d_off, int32_t *cnt, uint64_t stream) {
+    const int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
+    const double dV = w.g.dh[0] * w.g.dh[1] * w.g.dh[2];
+    int32_t *bsum = cnt + ncells + 1;
+    k_ionize_count<<<blocks_for(ncells + 1, 256), 256, 0, w.stream>>>(w.g, neu.den, w.rho, rate, dt, dV, ion.mpw0,
+                                                                       ncells, d_u, nu, d_off, w.seed, stream, cnt,
+                                                                       w.d_err);
+    launch_int_excl_scan(w.stream, cnt, ncells + 1, bsum);
+    k_ch4_ion_reserve<<<1, 1, 0, w.stream>>>(cnt, ncells, ion.d_count, ion.cap, w.d_err);
+    k_ionize_create<<<blocks_for(ncells, 256), 256, 0, w.stream>>>(w.g, w.ef, ion.charge / ion.mass, w.dt, ion.mpw0,
+                                                                    !ion.uniform_w, ncells, cnt, ion.P, ion.cap,
+                                                                    ion.cap, ion.d_count);
+    w.nlaunch += 6;
+}
+
+}  // namespace espic

@@ -1,8 +1,8 @@
 /*
  * Collisions.h (drop-in) -- the material interactions of the reference
  * (ch4/Collisions.h:33-89) on libespic: DSMC_MEX (neutral-neutral
- * collisions) and MCC_CEX (charge exchange) run on the GPU;
- * ChemistryIonize is not built (its apply() throws).
+ * collisions), MCC_CEX (charge exchange) and ChemistryIonize (ions created
+ * from the neutral density and rho) run on the GPU.
  */
 #ifndef ESPIC_SHIM_COLLISIONS_H
 #define ESPIC_SHIM_COLLISIONS_H
@@ -41,7 +41,7 @@ protected:
     World &world;
 };
 
-/* ChemistryIonize (ch4/Collisions.cpp:10-31): not built */
+/* ChemistryIonize::apply, ch4/Collisions.cpp:10-31 */
 class ChemistryIonize : public Interaction {
 public:
     ChemistryIonize(Species &neutrals, Species &ions, World &world, double rate)

@@ -442,15 +442,25 @@ void Species::updateAverages() {
     den_ave.device_written();
 }
 
-/* ch4 Species::advance(neutrals, spherium), ch4/Species.cpp:8-100: the
- * neutral branch runs on the GPU; the ion branch (ions striking the sphere
- * become neutrals and sputter) is not built */
-void Species::advance(Species &, Species &) {
-    if (charge != 0) throw std::runtime_error("Species::advance(neutrals, spherium) of a charged species is not built");
+/* ch4 Species::advance(neutrals, spherium), ch4/Species.cpp:8-100, on the
+ * GPU: the neutral branch (diffuse reflection at the sphere) and the ion
+ * branch (ions striking the sphere are removed and add neutrals and
+ * sputtered particles to the two targets) */
+void Species::advance(Species &neutrals, Species &spherium) {
     g_ch4_layout = true;
     settle();
     world.push_host_edits();
-    ck(espic_advance_ch4(world.handle(), sid, nullptr, nullptr, 0, nullptr, nullptr), "espic_advance_ch4");
+    if (charge == 0) {
+        ck(espic_advance_ch4(world.handle(), sid, nullptr, nullptr, 0, nullptr, nullptr), "espic_advance_ch4");
+    } else {
+        neutrals.settle();
+        spherium.settle();
+        ck(espic_advance_ch4_ions(world.handle(), sid, neutrals.id(), spherium.id(), nullptr, nullptr, 0, nullptr,
+                                  nullptr),
+           "espic_advance_ch4_ions");
+        neutrals.particles_changed();
+        spherium.particles_changed();
+    }
     particles_changed();
 }
 
@@ -510,8 +520,16 @@ double DSMC_MEX::sigmaCrMax() {
     return s;
 }
 
-void ChemistryIonize::apply(double) {
-    throw std::runtime_error("ChemistryIonize is not built in libespic");
+/* ChemistryIonize::apply, ch4/Collisions.cpp:10-31: the neutrals' den and
+ * the world's rho (host edits pushed first) at each cell centre */
+void ChemistryIonize::apply(double dt) {
+    g_ch4_layout = true;
+    ions.settle();
+    neutrals.den.push();
+    world.push_host_edits();
+    ck(espic_chemistry_ionize(world.handle(), neutrals.id(), ions.id(), rate, dt, nullptr, 0, nullptr, nullptr),
+       "espic_chemistry_ionize");
+    ions.particles_changed();
 }
 
 /* Species::sampleVth / sampleIsotropicVel, ch4/Species.cpp:149-175 (host) */

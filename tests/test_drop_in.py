@@ -133,6 +133,43 @@ def test_ch4_main_with_particle_output_compiles(tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
 
 
+@pytest.mark.gpu
+def test_drop_in_ch4_ions_runs(tmp_path, espic):
+    """Ions of a beam strike the sphere and add neutrals and sputtered atoms
+    (the ion branch of Species::advance(neutrals, spherium)); sputtered atoms
+    are ionized (ChemistryIonize); MCC_CEX stops ions.  Same seed, same
+    counts."""
+    lines = _run(tmp_path, "ch4_ions_main", 30, 5)
+    rows = np.array([[int(x) for x in l.split()] for l in lines])
+    assert rows.shape == (30, 5) and list(rows[:, 0]) == list(range(1, 31))
+    n_o, n_ion, n_sph, n_sphi = rows[-1, 1:]
+    assert n_o > 0 and n_ion > 0
+    assert n_sph > 0  # ions at 7 km/s reached the sphere and sputtered
+    assert _run(tmp_path, "ch4_ions_main", 30, 5) == lines
+
+
+def test_ch4_main_with_ions_compiles(tmp_path):
+    """ch4/Main.cpp with its commented-out ion species, ion sources and
+    ChemistryIonize / MCC_CEX interactions restored (ch4/Main.cpp:36-57)
+    compiles against the drop-in headers."""
+    src = os.path.join(REF, "ch4", "Main.cpp")
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present")
+    out = []
+    for line in open(src).read().splitlines():
+        t = line.lstrip()
+        if t.startswith("//") and any(k in t for k in ("species.push_back", "Species &", "ColdBeamSource",
+                                                       "ChemistryIonize", "MCC_CEX")):
+            line = line.replace("//", "", 1)
+        out.append(line)
+    edited = tmp_path / "main_ions.cpp"
+    edited.write_text("\n".join(out) + "\n")
+    assert "emplace_back(newChemistryIonize(sph,sph_ions" in edited.read_text().replace(" ", "")
+    E = _espic_module()
+    r = E.compile_drop_in(str(edited), str(tmp_path / "main"), stdin_source=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
 def test_ch4_api_program_compiles(tmp_path):
     """A program using the ch4 World helpers (XtoC, lineSphereIntersect,
     sphereDiffuseVector), vec3 dot/mag/unit/cross, DSMC_MEX, MCC_CEX and the
