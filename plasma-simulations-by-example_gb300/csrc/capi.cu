@@ -161,7 +161,7 @@ static void free_species(Species *s) {
 static void free_world(World &w) {
     for (Species *s : w.species) free_species(s);
     w.species.clear();
-    void *ptrs[] = {w.phi, w.rho, w.vol, w.ivol, w.ef, w.ef4, w.obj, w.target, w.d_err, w.d_status, w.d_partials,
+    void *ptrs[] = {w.phi, w.rho, w.vol, w.ivol, w.ef, w.ef4, w.pe_part, w.phi_ef, w.obj, w.target, w.d_err, w.d_status, w.d_partials,
                     w.d_small, w.d_u, w.d_stage, w.d_blockcnt, w.pcg_buf, w.phi_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1034,7 +1034,7 @@ extern "C" int espic_solve(espic_world *h, int *iterations, int *inner_iteration
 extern "C" int espic_efield(espic_world *h) {
     WORLD(h);
     PhaseScope ph(w, ESPIC_PHASE_EFIELD);
-    launch_efield(w);
+    launch_efield(w, false);
     CHECK_LAUNCH();
     return ESPIC_OK;
 }
@@ -1506,7 +1506,11 @@ static int field_ptr(World &w, int field, int sp, double **p, int64_t *count) {
         case ESPIC_FIELD_PHI: *p = w.phi; *count = w.nn; return ESPIC_OK;
         case ESPIC_FIELD_RHO: *p = w.rho; *count = w.nn; return ESPIC_OK;
         case ESPIC_FIELD_NODE_VOL: *p = w.vol; *count = w.nn; return ESPIC_OK;
-        case ESPIC_FIELD_EF: *p = w.ef; *count = 3 * w.nn; return ESPIC_OK;
+        case ESPIC_FIELD_EF:
+            ensure_ef64(w); /* the float64 field of a mixed-form world is completed on demand */
+            *p = w.ef;
+            *count = 3 * w.nn;
+            return ESPIC_OK;
         case ESPIC_FIELD_DEN:
         case ESPIC_FIELD_DEN_AVE:
             if (sp < 0 || sp >= (int)w.species.size()) return fail(ESPIC_ERR_ARG, "bad species id");
@@ -1575,7 +1579,12 @@ extern "C" int espic_field_write(espic_world *h, int field, int sp, const double
     if (rc != ESPIC_OK) return rc;
     if (n < cnt) return fail(ESPIC_ERR_ARG, "buffer holds %lld of %lld values", (long long)n, (long long)cnt);
     CK(cudaMemcpyAsync(p, host, cnt * sizeof(double), cudaMemcpyHostToDevice, w.stream));
-    if (field == ESPIC_FIELD_EF) launch_ef4(w);
+    if (field == ESPIC_FIELD_EF) {
+        launch_ef4(w);
+        w.ef64_valid = true;
+    }
+    /* a written field or volume: the cached energy sum no longer applies */
+    if (field == ESPIC_FIELD_EF || field == ESPIC_FIELD_NODE_VOL) w.pe_parts = 0;
     if (field == ESPIC_FIELD_NODE_VOL) launch_inv_vol(w);
     if (field == ESPIC_FIELD_PHI) w.phi_prev_valid = false;
     if (field == ESPIC_FIELD_RHO) w.rho_version++;
@@ -1654,7 +1663,7 @@ extern "C" int espic_step(espic_world *h, int sort_every, double *row, int len) 
     if ((rc = enqueue_solve(w)) != ESPIC_OK) return rc;
     {
         PhaseScope ph(w, ESPIC_PHASE_EFIELD);
-        launch_efield(w);
+        launch_efield(w, false);
     }
     CHECK_LAUNCH();
     w.step_count++;

@@ -127,7 +127,11 @@ struct World;
 void launch_objects_sphere(World &w, const double c[3], double radius, double phi_s);
 void launch_objects_inlet(World &w);
 void launch_targets(World &w);
-void launch_efield(World &w);
+/* computeEF.  full = false lets a world whose species are all in the mixed
+ * form write ef4 and the inlet planes of ef only; ensure_ef64 completes ef
+ * before a float64 consumer reads it */
+void launch_efield(World &w, bool full = true);
+void ensure_ef64(World &w);
 void launch_push_fp64(World &w, Species &s, bool deposit);
 void launch_deposit_fp64(World &w, Species &s);
 void launch_compact(World &w, Species &s);

@@ -95,6 +95,10 @@ struct World {
     double *ivol = nullptr; /* RN(1 / node_vol), 0 where the volume is 0: the density's divisor */
     float4 *ef4 = nullptr;
     bool ef4_valid = false;
+    bool ef64_valid = true; /* false after a computeEF that wrote ef4 and only the planes k < 2 of ef */
+    double *pe_part = nullptr; /* k_efield4's per-block sums of |E|^2 vol */
+    int64_t pe_parts = 0;      /* > 0: those sums describe the current field */
+    double *phi_ef = nullptr;  /* the potential k_efield4 read (ef is completed from it) */
     int32_t *obj = nullptr, *target = nullptr;
     bool targets_valid = false;
     double sphere[4] = {0, 0, 0, 0}; /* centre, radius^2 */

@@ -20,6 +20,8 @@
 #include <limits.h>
 #include <stdio.h>
 
+#include <type_traits>
+
 #include "ch4_push.h"
 #include "espic_world.h"
 
@@ -636,8 +638,20 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
  * central inside.  Also writes the float32 copy used by the mixed push. */
+/* The numerator of one component at node u with stride st along an axis of
+ * n nodes at index i: one-sided on the faces, central inside, each in the
+ * reference's arithmetic (ch2/PotentialSolver.cpp:70-110). */
+__device__ __forceinline__ double ef_num(const double *__restrict__ phi, int64_t u, int64_t st, int i, int n) {
+    if (i == 0) return -(-3 * phi[u] + 4 * phi[u + st] - phi[u + 2 * st]);
+    if (i == n - 1) return -(phi[u - 2 * st] - 4 * phi[u - st] + 3 * phi[u]);
+    return -(phi[u + st] - phi[u - st]);
+}
+
 /* grid: x over the nodes of a k-plane, y over the planes (no 64-bit index
- * division per node) */
+ * division per node).  Interior nodes take the central differences alone:
+ * the face formulas sit behind a branch the whole warp skips, so their
+ * float64 operations are not issued for every node (this GPU's float64 rate
+ * bounds the kernel). */
 __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double *__restrict__ phi, double *ef,
                                                 float4 *ef4) {
     const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
@@ -646,28 +660,19 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double 
     const int k = blockIdx.y;
     const uint32_t jj = div_small(pl, (uint32_t)g.ni, 1.f / (float)g.ni);
     const int j = (int)jj, i = (int)(pl - jj * (uint32_t)g.ni);
-    int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+    const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
     const int64_t u = (int64_t)k * sz + pl;
     const double d2x = 2 * g.dh[0], d2y = 2 * g.dh[1], d2z = 2 * g.dh[2];
     double n0, n1, n2;
-    if (i == 0)
-        n0 = -(-3 * phi[u] + 4 * phi[u + 1] - phi[u + 2]);
-    else if (i == g.ni - 1)
-        n0 = -(phi[u - 2] - 4 * phi[u - 1] + 3 * phi[u]);
-    else
+    if (i > 0 && i < g.ni - 1 && j > 0 && j < g.nj - 1 && k > 0 && k < g.nk - 1) {
         n0 = -(phi[u + 1] - phi[u - 1]);
-    if (j == 0)
-        n1 = -(-3 * phi[u] + 4 * phi[u + sy] - phi[u + 2 * sy]);
-    else if (j == g.nj - 1)
-        n1 = -(phi[u - 2 * sy] - 4 * phi[u - sy] + 3 * phi[u]);
-    else
         n1 = -(phi[u + sy] - phi[u - sy]);
-    if (k == 0)
-        n2 = -(-3 * phi[u] + 4 * phi[u + sz] - phi[u + 2 * sz]);
-    else if (k == g.nk - 1)
-        n2 = -(phi[u - 2 * sz] - 4 * phi[u - sz] + 3 * phi[u]);
-    else
         n2 = -(phi[u + sz] - phi[u - sz]);
+    } else {
+        n0 = ef_num(phi, u, 1, i, g.ni);
+        n1 = ef_num(phi, u, sy, j, g.nj);
+        n2 = ef_num(phi, u, sz, k, g.nk);
+    }
     const double e0 = div_rcp(n0, d2x, y2.x);
     const double e1 = div_rcp(n1, d2y, y2.y);
     const double e2 = div_rcp(n2, d2z, y2.z);
@@ -675,6 +680,110 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double 
     ef[3 * u + 1] = e1;
     ef[3 * u + 2] = e2;
     if (ef4) ef4[u] = make_float4((float)e0, (float)e1, (float)e2, 0.f);
+}
+
+/* ------------------------------------------------------------------------ */
+/* RN_f(x) for a float64 x that lies within 3 ulps of the quotient whose
+ * float64 rounding is wanted, computed on the integer pipes: false when x is
+ * within 4 ulps of a float rounding midpoint (the float rounding of the
+ * float64 quotient could then differ) or outside the normal float range, in
+ * which case the caller rounds the exact quotient itself.  A float rounding
+ * boundary is the midpoint between two floats: the low 29 of the 52
+ * fraction bits equal to 2^28. */
+__device__ __forceinline__ bool f32_of_near(double x, float &out) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const unsigned long long mag = b & 0x7fffffffffffffffull;
+    if (mag == 0) {
+        out = __uint_as_float(sign);
+        return true;
+    }
+    const int e = (int)(mag >> 52);
+    if (e < 1023 - 125 || e > 1023 + 127) return false;
+    const unsigned long long m = mag & 0xfffffffffffffull;
+    const long long low = (long long)(m & 0x1fffffffull);
+    const long long dist = low - (1ll << 28);
+    if (dist >= -4 && dist <= 4) return false;
+    unsigned int fb = ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29);
+    fb += dist > 0 ? 1u : 0u;
+    if (fb >= 0x7f800000u) return false;
+    out = __uint_as_float(fb | sign);
+    return true;
+}
+
+/* computeEF for worlds whose particles all live in the mixed form: the
+ * float copy ef4 = RN_f(RN_d(n / 2dh)) of every node, bit for bit that of
+ * k_efield, from q = n RN(1 / 2dh) (within 3 ulps of the float64 quotient)
+ * rounded on the integer pipes, and the exact quotient only where q lies
+ * near a float rounding boundary: two float64 operations per component
+ * instead of five (this GPU's float64 rate bounds k_efield).  The float64
+ * field is written on the planes k < 2 alone, the ones a beam source's
+ * addParticle gathers at (its particles start at z = x0); the rest of it is
+ * completed on demand by k_efield from phi_ef, the copy of phi this
+ * kernel reads (the solver changes phi before the field is next computed,
+ * and the reference's ef stays that of the last computeEF).
+ * World::getPE's sum of |E|^2 vol over the nodes rides along from the same
+ * q (each within 6 ulps of the float64 |E|^2 term, far inside the 1e-13 to
+ * which the sum's order already defines it).  Each thread takes EF_KPT
+ * planes of its (i, j) column, so the block sum is paid once per EF_KPT
+ * nodes: one partial per block, [plane group][block of the plane]. */
+constexpr int EF_KPT = 4; /* planes per thread of k_efield4 */
+
+__global__ void __launch_bounds__(256) k_efield4(Geo g, double3 y2, const double *__restrict__ phi, double *ef,
+                                                 float4 *ef4, const double *__restrict__ vol, double *pe_part,
+                                                 double *phi_ef) {
+    const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nplane = (uint32_t)g.ni * (uint32_t)g.nj;
+    double pe = 0;
+    if (pl < nplane) {
+        const uint32_t jj = div_small(pl, (uint32_t)g.ni, 1.f / (float)g.ni);
+        const int j = (int)jj, i = (int)(pl - jj * (uint32_t)g.ni);
+        const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+        const bool in_ij = i > 0 && i < g.ni - 1 && j > 0 && j < g.nj - 1;
+        const double d2[3] = {2 * g.dh[0], 2 * g.dh[1], 2 * g.dh[2]}, yy[3] = {y2.x, y2.y, y2.z};
+        /* -RN(1 / 2dh): (phi_+ - phi_-) (-y) is -(phi_+ - phi_-) y to the
+         * bit, signed zero included */
+        const double ny[3] = {-y2.x, -y2.y, -y2.z};
+        const int k0 = blockIdx.y * EF_KPT;
+        for (int kk = 0; kk < EF_KPT; kk++) {
+            const int k = k0 + kk;
+            if (k >= g.nk) break;
+            const int64_t u = (int64_t)k * sz + pl;
+            phi_ef[u] = phi[u];
+            float f[3];
+            double q[3];
+            if (in_ij && k >= 2 && k < g.nk - 1) {
+                const double dd[3] = {phi[u + 1] - phi[u - 1], phi[u + sy] - phi[u - sy], phi[u + sz] - phi[u - sz]};
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    q[c] = dd[c] * ny[c];
+                    if (!f32_of_near(q[c], f[c])) f[c] = (float)div_rcp(-dd[c], d2[c], yy[c]);
+                }
+            } else {
+                const double n[3] = {ef_num(phi, u, 1, i, g.ni), ef_num(phi, u, sy, j, g.nj),
+                                     ef_num(phi, u, sz, k, g.nk)};
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const double e = div_rcp(n[c], d2[c], yy[c]);
+                    if (k < 2) ef[3 * u + c] = e;
+                    f[c] = (float)e;
+                    q[c] = e;
+                }
+            }
+            ef4[u] = make_float4(f[0], f[1], f[2], 0.f);
+            pe = __fma_rn(__fma_rn(q[2], q[2], __fma_rn(q[1], q[1], q[0] * q[0])), vol[u], pe);
+        }
+    }
+    /* deterministic block sum: warp butterflies, then the 8 warps in order */
+    __shared__ double ws[8];
+    for (int o = 16; o > 0; o >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = pe;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w8 = 0; w8 < (int)(blockDim.x >> 5); w8++) t += ws[w8];
+        pe_part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -849,6 +958,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_pe_partials(int64_t nn, const d
         acc[0] += ef2 * vol[u];
     }
     block_sum_store<1>(acc, partials + blockIdx.x);
+}
+
+/* 0.5 eps0 times the sum of k_efield4's block partials, in a fixed order */
+__global__ void __launch_bounds__(1024) k_pe_sum(const double *__restrict__ part, int64_t n, double *out) {
+    __shared__ double ws[32];
+    double s = 0;
+    for (int64_t b = threadIdx.x; b < n; b += blockDim.x) s += part[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w32 = 0; w32 < 32; w32++) t += ws[w32];
+        out[0] = 0.5 * EPS_0 * t;
+    }
 }
 
 __global__ void k_pe_final(const double *__restrict__ partials, double *out) {
@@ -1118,6 +1242,7 @@ void launch_snapshot(World &w, double *out) {
         a.den[s] = w.species[s]->den;
         a.ave[s] = w.species[s]->den_ave;
     }
+    ensure_ef64(w);
     k_snapshot<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.obj, w.vol, w.phi, w.rho, w.ef, a, out);
     w.nlaunch++;
 }
@@ -1165,16 +1290,49 @@ void launch_targets(World &w) {
     w.nlaunch++;
 }
 
-void launch_efield(World &w) {
-    bool mixed = false;
-    for (Species *s : w.species) mixed |= (s->form == 1);
+void launch_efield(World &w, bool full) {
+    bool mixed = false, fp64 = false;
+    for (Species *s : w.species) {
+        mixed |= (s->form == 1);
+        fp64 |= (s->form == 0);
+    }
     /* RN(1 / (2 dh)) per axis, for div_rcp */
     double3 y2 = make_double3(1.0 / (2 * w.g.dh[0]), 1.0 / (2 * w.g.dh[1]), 1.0 / (2 * w.g.dh[2]));
     dim3 grid((unsigned)blocks_for((int64_t)w.g.ni * w.g.nj, 256), (unsigned)w.g.nk);
+    dim3 grid4(grid.x, (unsigned)((w.g.nk + EF_KPT - 1) / EF_KPT));
+    const int64_t nparts = (int64_t)grid4.x * grid4.y;
+    if (!full && mixed && !fp64 && !w.phi_ef) {
+        /* allocated once per world on the first such call */
+        if (cudaMalloc(&w.pe_part, nparts * sizeof(double)) != cudaSuccess) w.pe_part = nullptr;
+        if (w.pe_part && cudaMalloc(&w.phi_ef, w.nn * sizeof(double)) != cudaSuccess) w.phi_ef = nullptr;
+        if (!w.phi_ef && w.pe_part) {
+            cudaFree(w.pe_part);
+            w.pe_part = nullptr;
+        }
+    }
+    if (!full && mixed && !fp64 && w.phi_ef) {
+        k_efield4<<<grid4, 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, w.ef4, w.vol, w.pe_part, w.phi_ef);
+        w.nlaunch++;
+        w.ef4_valid = true;
+        w.ef64_valid = false;
+        w.pe_parts = nparts;
+        return;
+    }
     k_efield<<<grid, 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, mixed ? w.ef4 : nullptr);
     w.nlaunch++;
-    if (mixed) w.ef4_valid = true;
-    else w.ef4_valid = false;
+    w.ef4_valid = mixed;
+    w.ef64_valid = true;
+    w.pe_parts = 0;
+}
+
+void ensure_ef64(World &w) {
+    if (w.ef64_valid) return;
+    double3 y2 = make_double3(1.0 / (2 * w.g.dh[0]), 1.0 / (2 * w.g.dh[1]), 1.0 / (2 * w.g.dh[2]));
+    dim3 grid((unsigned)blocks_for((int64_t)w.g.ni * w.g.nj, 256), (unsigned)w.g.nk);
+    /* from the potential of the last computeEF */
+    k_efield<<<grid, 256, 0, w.stream>>>(w.g, y2, w.phi_ef, w.ef, nullptr);
+    w.nlaunch++;
+    w.ef64_valid = true;
 }
 
 template <int WALLS, bool DEP, bool UNI>
@@ -1189,6 +1347,7 @@ static void push_fp64_as(World &w, Species &s, int blocks) {
 void launch_push_fp64(World &w, Species &s, bool deposit) {
     int64_t n = s.host_bound;
     if (n <= 0) return;
+    ensure_ef64(w);
     int blocks = blocks_for(n, 256);
     if (s.walls == 0) {
         if (!deposit)
@@ -1277,6 +1436,9 @@ static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int writ
         }
     }
     double qm = s.charge / s.mass;
+    /* a beam's particles start at z = x0, where the float64 field is always
+     * current; any other generator needs all of it */
+    if (!std::is_same<Gen, GenBeam>::value) ensure_ef64(w);
     k_append_count<Gen><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(w.g, gen, ncand, w.d_blockcnt);
     k_append_scan<<<1, 1024, 0, w.stream>>>(w.d_blockcnt, blocks, s.d_count, s.cap, w.d_err);
     if (s.form == 0)
@@ -1698,6 +1860,12 @@ void launch_dsmc(World &w, Species &s, double dt, const double *d_u, int64_t nu,
 }
 
 void launch_pe(World &w, double *d_out1) {
+    if (w.pe_parts > 0) { /* the sum k_efield4 left behind */
+        k_pe_sum<<<1, 1024, 0, w.stream>>>(w.pe_part, w.pe_parts, d_out1);
+        w.nlaunch++;
+        return;
+    }
+    ensure_ef64(w);
     k_pe_partials<<<RED_BLOCKS, RED_THREADS, 0, w.stream>>>(w.nn, w.ef, w.vol, w.d_partials);
     k_pe_final<<<1, 32, 0, w.stream>>>(w.d_partials, d_out1);
     w.nlaunch += 2;
@@ -1758,6 +1926,7 @@ void launch_node_vol(World &w) {
 }
 
 void launch_ef4(World &w) {
+    ensure_ef64(w);
     k_ef_to_ef4<<<blocks_for(w.nn, 256), 256, 0, w.stream>>>(w.nn, w.ef, w.ef4);
     w.nlaunch++;
     w.ef4_valid = true;
@@ -2344,6 +2513,7 @@ static Ch4Geo ch4_geo(const World &w) {
 
 void launch_advance_ch4_ions(World &w, Species &s, Species &neu, Species &sph, double dt, const double *d_pdt,
                              const double *d_u, int64_t nu, const int64_t *d_off) {
+    ensure_ef64(w);
     cudaMemsetAsync(s.ch4_bounces, 0, sizeof(unsigned long long), w.stream);
     const int64_t nb = s.host_bound;
     if (nb > 0) {
@@ -2493,6 +2663,7 @@ void launch_ionize(World &w, const Species &neu, Species &ion, double rate, doub
     const int64_t ncells = (int64_t)(w.g.ni - 1) * (w.g.nj - 1) * (w.g.nk - 1);
     const double dV = w.g.dh[0] * w.g.dh[1] * w.g.dh[2];
     int32_t *bsum = cnt + ncells + 1;
+    ensure_ef64(w);
     k_ionize_count<<<blocks_for(ncells + 1, 256), 256, 0, w.stream>>>(w.g, neu.den, w.rho, rate, dt, dV, ion.mpw0,
                                                                        ncells, d_u, nu, d_off, w.seed, stream, cnt,
                                                                        w.d_err);

@@ -41,7 +41,7 @@ int main(int argc, char **argv) {
     sources.emplace_back(new ColdBeamSource(ions, world, 7000, 1e12));
 
     std::vector<std::unique_ptr<Interaction>> interactions;
-    interactions.emplace_back(new ChemistryIonize(sph, sph_ions, world, 1e-4));
+    interactions.emplace_back(new ChemistryIonize(sph, sph_ions, world, 1e-11));
     interactions.emplace_back(new MCC_CEX(ions, neutrals, world));
 
     PotentialSolver solver(world, SolverType::GS, 2000, 1e-4);
@@ -57,7 +57,7 @@ int main(int argc, char **argv) {
             sp.computeNumberDensity();
         }
         world.computeChargeDensity(species);
-        solver.solve();
+        /* as ch4/Main.cpp: the potential of the initial solve, E each step */
         solver.computeEF();
         printf("%d", world.getTs());
         for (Species &sp : species) printf(" %zu", sp.getNp());

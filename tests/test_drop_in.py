@@ -141,7 +141,8 @@ def test_drop_in_ch4_ions_runs(tmp_path, espic):
     counts."""
     lines = _run(tmp_path, "ch4_ions_main", 30, 5)
     rows = np.array([[int(x) for x in l.split()] for l in lines])
-    assert rows.shape == (30, 5) and list(rows[:, 0]) == list(range(1, 31))
+    # World::advanceTime runs time steps 0 .. num_ts (ch4/World.h:70, ts from -1)
+    assert rows.shape == (31, 5) and list(rows[:, 0]) == list(range(0, 31))
     n_o, n_ion, n_sph, n_sphi = rows[-1, 1:]
     assert n_o > 0 and n_ion > 0
     assert n_sph > 0  # ions at 7 km/s reached the sphere and sputtered
