@@ -322,7 +322,8 @@ __device__ __forceinline__ int64_t clamp_node(int64_t v, int64_t nn) { return v 
  * (j, k), with i2 = t mod hx; below 2^24 entries the coordinates come from
  * float-estimated divisions, above from the precomputed lists. */
 template <typename T>
-__device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale, T &rz, T &zz) {
+__device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale, T &rz_out, T &zz_out) {
+    T rz = 0, zz = 0;
     int64_t t0, ts;
     span(true, t0, ts);
     const int32_t *list = F.list[c], *pk = F.pk[c];
@@ -409,6 +410,8 @@ __device__ void fine_half(const Fine<T> &F, int c, const MgLevel<T> *C, T scale,
             zz += zu * zu;
         }
     }
+    rz_out += rz;
+    zz_out += zz;
 }
 
 /* one half sweep of colour c on a coarse level; with C != null the
@@ -807,6 +810,138 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
     return v[0];
 }
 
+/* Double-float arithmetic: a value as an unevaluated sum hi + lo of two
+ * floats (|lo| <= ulp(hi) / 2), ~48 significant bits, on the float pipes.
+ * TwoSum (Knuth) and Fast2Sum (Dekker) give the exact rounding error of a
+ * sum; a product's error comes from one FMA.  (D. E. Knuth, TAOCP vol. 2,
+ * 4.2.2; T. J. Dekker, Numer. Math. 18, 1971.) */
+struct dfl {
+    float h, l;
+};
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dfl df_fast2(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
+    const dfl s = df_two_sum(x.h, y.h);
+    return df_fast2(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ dfl df_neg(dfl x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
+    const float p = x.h * y.h;
+    const float e = __fmaf_rn(x.h, y.h, -p);
+    return df_fast2(p, __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, e)));
+}
+__device__ __forceinline__ dfl df_of(double v) {
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+/* df_of on the integer pipes: hi = RN_f(v) from the 53-bit significand
+ * rounded to 24 bits (ties to even), lo = RN_f(v - hi) from the exact
+ * remainder (|r| <= 2^28).  Magnitudes outside [2^-60, 2^60] (zero included)
+ * take the float64 conversion. */
+__device__ __forceinline__ dfl df_split(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 60 || e > 1023 + 60) return df_of(v);
+    const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+    unsigned long long mh = m >> 29;
+    const unsigned long long rem = m & 0x1fffffffull;
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (mh & 1))) mh++;
+    const int r = (int)((long long)m - (long long)(mh << 29));
+    int eh = e - 1023 + 127;
+    if (mh == (1ull << 24)) {
+        mh >>= 1;
+        eh++;
+    }
+    const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
+    const float hi = __uint_as_float(sgn | ((unsigned int)eh << 23) | ((unsigned int)mh & 0x7fffffu));
+    /* r 2^(e - 1075), the power of two built from its exponent bits */
+    const float scale = __uint_as_float((unsigned int)(e - 1075 + 127) << 23);
+    const float lo = __int2float_rn(r) * scale;
+    return {hi, sgn ? -lo : lo};
+}
+__device__ __forceinline__ float2 df_pack(dfl x) { return make_float2(x.h, x.l); }
+__device__ __forceinline__ dfl df_unpack(float2 v) { return {v.x, v.y}; }
+
+/* The pairs of phi and rho / eps0 at every node, once per solve */
+__device__ __noinline__ void df_prepass(const double *__restrict__ phi, const double *__restrict__ rho, float2 *phf,
+                                        float2 *rhf, dfl d_inv_eps0, int64_t nn, int64_t gtid, int64_t gsize) {
+    for (int64_t u = gtid; u < nn; u += gsize) {
+        phf[u] = df_pack(df_split(phi[u]));
+        rhf[u] = df_pack(df_mul(df_split(rho[u]), d_inv_eps0));
+    }
+}
+
+/* The Newton update phi -= y on the pairs of the unknowns; returns the
+ * thread's sum of y^2 */
+template <typename T>
+__device__ __noinline__ float df_update(const uint16_t *__restrict__ code, const T *__restrict__ yv, float2 *phf,
+                                        int64_t nn, int64_t gtid, int64_t gsize) {
+    float yys = 0.f;
+    for (int64_t u = gtid; u < nn; u += gsize) {
+        const uint16_t cu = code[u];
+        if (!(cu & SELF)) continue;
+        const float yu = (float)yv[u];
+        phf[u] = df_pack(df_add(df_unpack(phf[u]), {-yu, 0.f}));
+        yys = __fmaf_rn(yu, yu, yys);
+    }
+    return yys;
+}
+
+/* The Newton residual pass of the float-inner nonlinear solve in
+ * double-float arithmetic (per axis c (2 x_u - x_w - x_e), a missing link
+ * reading x_u; the Boltzmann factor as expf of the leading part times a
+ * first-order factor for the rest; rho / eps0 from its pair), with the
+ * Jacobian's Boltzmann diagonal and the first red smoothing half sweep.
+ * Returns the thread's sum of r^2.  Not inlined: the call spills the
+ * solver's live state once, and the loop gets the registers (inlined, the
+ * loop ran 4x slower).  An unknown is an interior node, so its neighbours
+ * need no clamp (s1, s2: the y and z strides). */
+template <typename T>
+__device__ __noinline__ float df_residual(const uint16_t *__restrict__ code, const float2 *__restrict__ phf,
+                                          const float2 *__restrict__ rhf, T *z, T *dg, T *r, T *y, int64_t nn,
+                                          int64_t gtid, int64_t gsize, int32_t s1, int32_t s2, const T ct[3],
+                                          const float cl[3], dfl d_phi0, dfl d_inv_te0, dfl d_A0, float A0_te0,
+                                          bool jacobi) {
+    float ffs = 0.f;
+    for (int64_t u = gtid; u < nn; u += gsize) {
+        const uint16_t c = code[u];
+        if (!(c & SELF)) continue;
+        const float2 *pu = phf + u;
+        const float2 xu = pu[0];
+        const float2 pn[6] = {pu[-1], pu[1], pu[-s1], pu[s1], pu[-s2], pu[s2]};
+        const float2 bv = rhf[u];
+        const dfl x = df_unpack(xu);
+        dfl L = {0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const unsigned mw = (1u << (2 * a)) | (1u << (6 + 2 * a));
+            const unsigned me = (1u << (2 * a + 1)) | (1u << (7 + 2 * a));
+            const dfl pw = df_unpack((c & mw) ? pn[2 * a] : xu);
+            const dfl pe = df_unpack((c & me) ? pn[2 * a + 1] : xu);
+            const dfl d = df_add(df_add({2.f * x.h, 2.f * x.l}, df_neg(pw)), df_neg(pe));
+            L = df_add(L, df_mul(d, {(float)ct[a], cl[a]}));
+        }
+        const dfl xa = df_mul(df_add(x, df_neg(d_phi0)), d_inv_te0);
+        const float ef = expf(xa.h);
+        const dfl e = df_fast2(ef, ef * xa.l);
+        const dfl Fd = df_add(df_add(L, df_mul(d_A0, e)), df_neg(df_unpack(bv)));
+        const float rv = Fd.h + Fd.l;
+        const float dBt = A0_te0 * ef;
+        if (jacobi || !(c & BLACK)) z[u] = (T)(rv / full_diag(c, (T)dBt, ct));
+        dg[u] = (T)dBt;
+        r[u] = (T)rv;
+        y[u] = 0;
+        ffs = __fmaf_rn(rv, rv, ffs);
+    }
+    return ffs;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, const double *__restrict__ rho,
                                                         const uint16_t *__restrict__ code,
@@ -816,7 +951,7 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
                                                         T *p1, T *q, T *dg, MgArgs<T> mg, const int32_t *lists,
                                                         double *partials, SolveStatus *st, int *err,
                                                         double *lin_y, const double *__restrict__ lin_b,
-                                                        int gs_max, double gs_tol) {
+                                                        int gs_max, double gs_tol, float2 *dfbuf) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char pcg_smem[];
     __shared__ T bc_alpha, bc_beta;
@@ -856,6 +991,20 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
     /* linear mode (lin_y != null): Newton on F(y) = J y - b with J frozen at
      * phi solves J y = b; the stopping test is relative to the first update */
     const bool linear = lin_y != nullptr;
+    /* float inner solve of the nonlinear problem: the Newton residual and
+     * update run in double-float arithmetic on the float pipes (the float64
+     * pipe of this GPU is narrow) from phi and rho / eps0 split once into
+     * (hi, lo) pairs here; phi is rebuilt from its pairs after the last
+     * update */
+    const bool dfm = sizeof(T) == sizeof(float) && !linear && dfbuf != nullptr;
+    float2 *phf = dfbuf, *rhf = dfbuf ? dfbuf + nn : nullptr;
+    const dfl d_phi0 = df_of(phi0), d_inv_te0 = df_of(inv_te0), d_A0 = df_of(A0), d_inv_eps0 = df_of(inv_eps0);
+    if (dfm) {
+        df_prepass(phi, rho, phf, rhf, d_inv_eps0, nn, gtid, gsize);
+        grid.sync();
+    }
+    const float cl[3] = {(float)(cd[0] - (double)ct[0]), (float)(cd[1] - (double)ct[1]),
+                         (float)(cd[2] - (double)ct[2])};
     double nr_scale = linear ? 0.0 : 1.0;
     double zz_stop = nr_tol * nr_tol / 9.0 * (double)nn * nr_scale;
     for (nr = 0; nr < nr_max; nr++) {
@@ -864,6 +1013,15 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
          * preconditioner rides along */
         double ff = 0;
         const double *XR = linear ? lin_y : phi;
+        if (dfm) {
+            /* the residual of the float-inner form below, in double-float:
+             * per axis c (2 x_u - x_w - x_e) (a missing link reads x_u), the
+             * Boltzmann factor as expf of the leading part times a
+             * first-order factor for the rest, rho / eps0 from its pair */
+            const float ffs = df_residual<T>(code, phf, rhf, z, dg, r, y, nn, gtid, gsize, (int32_t)sy, (int32_t)sz,
+                                             ct, cl, d_phi0, d_inv_te0, d_A0, (float)A0_te0, jacobi);
+            ff = (double)ffs;
+        } else
         /* two nodes per pass, every load before any store; the loads do not
          * wait for the code word (neighbour indices are clamped into the
          * grid, a node past the end reads the interior node (1,1,1)), and
@@ -1131,6 +1289,9 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
         /* Newton update */
         double yy = 0;
         double *X = linear ? lin_y : phi;
+        if (dfm) {
+            yy = (double)df_update<T>(code, take_z ? z : y, phf, nn, gtid, gsize);
+        } else
         /* two nodes per pass, loads ahead of the code test and the stores */
         for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
             const int64_t uq[2] = {u0, u0 + gsize};
@@ -1169,6 +1330,15 @@ __global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, cons
             nr++;
             break;
         }
+    }
+    if (dfm) {
+        /* phi of the unknowns from their pairs (hi + lo rounded once) */
+        for (int64_t u = gtid; u < nn; u += gsize)
+            if (code[u] & SELF) {
+                const float2 v = phf[u];
+                phi[u] = (double)v.x + (double)v.y;
+            }
+        grid.sync();
     }
     /* Neumann boundary nodes take the value at the end of their chain */
     for (int64_t u = gtid; u < nn && !linear; u += gsize) {
@@ -1401,7 +1571,9 @@ static int run_pcg(World &w) {
      * nodes arithmetically (2^24 entries or more, see fine_half) */
     const bool need_lists = nlist >= (1 << 24);
     size_t listb = need_lists ? ((4 * nlist * sizeof(int32_t) + 255) / 256) * 256 : 0;
-    size_t need = 7 * vec + codeb + mgb + listb;
+    /* float inner solves: the (hi, lo) pairs of phi and rho / eps0 */
+    size_t dfb = sizeof(T) == sizeof(float) ? 2 * (((size_t)w.nn * sizeof(float2) + 255) / 256) * 256 : 0;
+    size_t need = 7 * vec + codeb + mgb + listb + dfb;
     if (w.pcg_bytes < need || w.pcg_elem != (int)es) {
         if (w.pcg_buf) {
             cudaStreamSynchronize(w.stream);
@@ -1486,9 +1658,11 @@ static int run_pcg(World &w) {
     const double *lb = w.lin_b;
     int gs_max = w.gs_fallback ? w.max_it : 0;
     double gs_tol = w.tol;
+    /* the pairs hold nn float2 each, the second array 256-byte aligned */
+    float2 *dfp = dfb ? (float2 *)(base + 7 * vec + codeb + mgb + listb) : nullptr;
     void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
                     &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
-                    &ly,   &lb,   &gs_max, &gs_tol};
+                    &ly,   &lb,   &gs_max, &gs_tol, &dfp};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, dyn, w.stream);
 }
