@@ -241,7 +241,9 @@ def profiled_steps(E, w, cfg, steps):
 
 def e2e_steps(E, torch, w, s, src, sol, cfg, steps):
     """The Main-loop body through the C-ABI: injection uniforms H2D from pinned
-    memory, the phases, the diag row D2H every step."""
+    memory, the phases, the diag row D2H every step.  The uniforms of at most
+    four steps are drawn (a 256x256x512 step takes 91 MB of them) and reused
+    in turn: every step still copies its whole set from host memory."""
     import ctypes as C
     lib = E.lib()
     rng = np.random.default_rng(5)
@@ -249,15 +251,16 @@ def e2e_steps(E, torch, w, s, src, sol, cfg, steps):
     Ly = w.dh[1] * (w.nj - 1)
     per = N0 * V_DRIFT * Lx * Ly * cfg["dt"] / cfg["mpw0"]
     nu = 1 + 13 * (int(per) + 2)
-    pinned = torch.empty((steps, nu), dtype=torch.float64, pin_memory=True)
-    pinned.copy_(torch.from_numpy(rng.random((steps, nu))))
+    slots = min(steps, 4)
+    pinned = torch.empty((slots, nu), dtype=torch.float64, pin_memory=True)
+    pinned.copy_(torch.from_numpy(rng.random((slots, nu))))
     row = torch.empty(7, dtype=torch.float64, pin_memory=True)
     used = E.I64()
     h2d = 0
     w.sync()
     t0 = time.perf_counter()
     for i in range(steps):
-        ptr = C.cast(pinned[i].data_ptr(), E.PD)
+        ptr = C.cast(pinned[i % slots].data_ptr(), E.PD)
         E.check(lib.espic_source_sample_uniforms(w.h, src.id, ptr, nu, C.byref(used)))
         h2d += used.value * 8
         if cfg["sort_every"] and i % cfg["sort_every"] == 0:
@@ -1143,7 +1146,8 @@ def main():
     w, s, src, sol = make_world(E, cfg, E.FORM_MIXED, P0)
     for _ in range(args.warmup):
         w.step(cfg["sort_every"])
-    e2e_n = min(args.steps, 5) if big else args.steps
+    # one whole sort period, as the timed steps amortise the sort
+    e2e_n = (cfg["sort_every"] or args.steps) if big else args.steps
     e = e2e_steps(E, torch, w, s, src, sol, cfg, e2e_n)
     w.close()
 

@@ -797,21 +797,38 @@ __global__ void __launch_bounds__(256) k_sort_gather_keys(const int32_t *__restr
 
 /* per block: {count, mx, my, mz, sum w v^2} for the mixed form: float sums
  * over runs of 32 particles folded into float64 */
+/* Per block: count, sum v and sum |v|^2 of a mixed species.  Each thread
+ * takes four particles a pass (all twelve loads issued before the sums, so
+ * the pass is bound by bandwidth, not by the loads' latency); the float sums
+ * of every 32 particles are added into float64. */
 __global__ void __launch_bounds__(256) k_diag_mixed(const float *__restrict__ vel, int64_t stride,
                                                     const int64_t *__restrict__ d_count, double *partials,
                                                     int nblocks) {
-    int64_t n = d_count[0];
+    const int64_t n = d_count[0];
+    const int64_t S = (int64_t)nblocks * 256;
     double acc[5] = {0, 0, 0, 0, 0};
     float f[5] = {0, 0, 0, 0, 0};
     int run = 0;
-    for (int64_t p = (int64_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (int64_t)nblocks * 256) {
-        float v0 = vel[p], v1 = vel[stride + p], v2 = vel[2 * stride + p];
-        f[0] += 1.f;
-        f[1] += v0;
-        f[2] += v1;
-        f[3] += v2;
-        f[4] += v0 * v0 + v1 * v1 + v2 * v2;
-        if (++run == 32) {
+    for (int64_t p0 = (int64_t)blockIdx.x * 256 + threadIdx.x; p0 < n; p0 += 4 * S) {
+        float v[4][3];
+        bool ok[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int64_t p = p0 + h * S;
+            ok[h] = p < n;
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[h][c] = ok[h] ? vel[c * stride + p] : 0.f;
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            if (!ok[h]) continue;
+            f[0] += 1.f;
+            f[1] += v[h][0];
+            f[2] += v[h][1];
+            f[3] += v[h][2];
+            f[4] += v[h][0] * v[h][0] + v[h][1] * v[h][1] + v[h][2] * v[h][2];
+        }
+        if (++run == 8) {
             for (int q = 0; q < 5; q++) {
                 acc[q] += (double)f[q];
                 f[q] = 0.f;
@@ -997,7 +1014,9 @@ void launch_int_excl_scan(cudaStream_t st, int32_t *x, int64_t n, int32_t *bsum)
 }
 
 void launch_diag_mixed(World &w, Species &s, double *d_out5) {
-    const int nb = 592;
+    /* eight blocks of 256 per SM, within the partials buffer (5 per block) */
+    int nb = 8 * w.sm_count;
+    if (nb > w.partial_slots / 5) nb = w.partial_slots / 5;
     k_diag_mixed<<<nb, 256, 0, w.stream>>>(s.vel, s.ms, s.d_count, w.d_partials, nb);
     k_diag_mixed_final<<<1, 32, 0, w.stream>>>(w.d_partials, nb, s.mass, s.mpw0, d_out5);
     w.nlaunch += 2;
