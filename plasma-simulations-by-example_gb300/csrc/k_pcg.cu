@@ -178,6 +178,8 @@ __device__ __forceinline__ void grid_sum_t(cg::grid_group &grid, const T (&v)[NV
 }
 
 constexpr int MG_MAX = 12;
+/* threads per block of the cooperative solve (one block per SM) */
+constexpr int PCG_THREADS = 1024;
 constexpr size_t PCG_SMEM_MAX = 160 * 1024; /* shared memory for block 0's coarse levels */
 
 template <typename T>
@@ -652,12 +654,13 @@ __device__ void restrict_coarse(const MgLevel<T> &L, const MgLevel<T> &C, bool w
  * block b takes a contiguous range of rows, eight at a time, four warps per
  * row, each warp a quarter of the columns (lanes in a fixed order, a fixed
  * shuffle tree); the four quarter sums are added in order.  Every thread of
- * every block calls it (blocks of 1024 threads). */
+ * every block calls it (blocks of 128 threads or a multiple). */
 template <typename T>
 __device__ void dense_apply(const MgLevel<T> &L, const T *__restrict__ Ainv, int n) {
     __shared__ T part[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    constexpr int WPR = 4, RPP = 8; /* warps per row, rows per pass */
+    constexpr int WPR = 4; /* warps per row */
+    const int RPP = (int)(blockDim.x >> 5) / WPR; /* rows per pass */
     const int64_t rpb = ((int64_t)n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * rpb;
     const int64_t r1 = r0 + rpb < n ? r0 + rpb : n;
@@ -943,7 +946,7 @@ __device__ __noinline__ float df_residual(const uint16_t *__restrict__ code, con
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024, 1) k_newton_pcg(Geo g, double *phi, const double *__restrict__ rho,
+__global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *phi, const double *__restrict__ rho,
                                                         const uint16_t *__restrict__ code,
                                                         const int32_t *__restrict__ target, double phi0,
                                                         double te0, double n0, int nr_max, double nr_tol,
@@ -1628,7 +1631,7 @@ static int run_pcg(World &w) {
         w.pcg_codes_valid = true;
     }
     const void *fn = (const void *)k_newton_pcg<T>;
-    const int threads = 1024;
+    const int threads = PCG_THREADS;
     size_t dyn = 0;
     if (A.smem_from >= 0)
         for (int i = A.smem_from; i < A.nlev; i++) dyn += level_smem_bytes<T>(A.L[i].n);
