@@ -1017,7 +1017,7 @@ int eo_newton_pcg(const eo_grid *g, double *phi, const double *rho, const int *o
  * order, its residual's RMS over all nodes checked at sweeps 0, 25, 50, ...
  * against gs_tol, at most gs_max sweeps (0: no fallback).  With early_stop
  * the inner PCG also stops, as the CUDA path's does, once the RMS of the
- * preconditioned residual z (over all nodes) is below nr_tol / 3, and z
+ * preconditioned residual z (over all nodes) is below nr_tol / 2, and z
  * itself is the update when the first z already is. */
 int eo_newton_pcg_fb(const eo_grid *g, double *phi, const double *rho, const int *obj,
                      const int *target, double phi0, double te0, double n0, int nr_max, double nr_tol,
@@ -1072,7 +1072,7 @@ int eo_newton_pcg_fb(const eo_grid *g, double *phi, const double *rho, const int
             rz += r[u] * z[u];
         }
         double stop2 = pcg_tol * pcg_tol * fn;
-        const double zz_stop = nr_tol * nr_tol / 9.0 * (double)nn;
+        const double zz_stop = nr_tol * nr_tol / 4.0 * (double)nn;
         int it = 0, pcg_ok = 0, take_z = 0;
         if (early_stop && fn > 0) {
             double zz = 0;

@@ -21,7 +21,7 @@
  * order, so every block takes the same branch.  The inner PCG stops when
  * |r| <= pcg_tol |F|, or earlier once the RMS of the preconditioned residual
  * z = M r (an estimate of the error left in the Newton update y) is below
- * nr_tol / 3 (nr_tol / 10 in linear mode): the Newton test RMS(y) < nr_tol
+ * nr_tol / 2 (nr_tol / 10 in linear mode): the Newton test RMS(y) < nr_tol
  * cannot then depend on more inner accuracy, and the last Newton step stops
  * needing a full solve; when the first V-cycle's z is already that small,
  * z itself is the update.
@@ -1009,7 +1009,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
     const float cl[3] = {(float)(cd[0] - (double)ct[0]), (float)(cd[1] - (double)ct[1]),
                          (float)(cd[2] - (double)ct[2])};
     double nr_scale = linear ? 0.0 : 1.0;
-    double zz_stop = nr_tol * nr_tol / 9.0 * (double)nn * nr_scale;
+    double zz_stop = nr_tol * nr_tol / 4.0 * (double)nn * nr_scale;
     for (nr = 0; nr < nr_max; nr++) {
         /* Newton residual (float64) and the Boltzmann part of the Jacobian
          * diagonal; the first red smoothing half sweep (or Jacobi) of the
@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
                 }
                 double RZn = vcycle_rest(grid, F, mg, partials, round, ZZ, SB);
                 /* z = M r estimates the remaining error of y: once its RMS is
-                 * below a third of the Newton tolerance, further inner
+                 * below half the Newton tolerance, further inner
                  * iterations cannot change the outcome of the Newton test */
                 if (threadIdx.x == 0) {
                     bc_stop = ZZ < zz_stop;
