@@ -764,26 +764,17 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict_
     perm[base + (lane - head)] = (int32_t)p;
 }
 
-/* out[q] = in[perm[q]] for one float array (an index outside the species,
- * which the histogram and scatter cannot produce, is flagged, not read) */
-__global__ void __launch_bounds__(256) k_sort_gather(const float *__restrict__ in, const int32_t *__restrict__ perm,
-                                                     const int64_t *__restrict__ d_count, float *out, int *err) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t n = d_count[0];
-    if (q >= n) return;
-    const int64_t p = perm[q];
-    if (p < 0 || p >= n) {
-        atomicOr(err, DERR_SORT);
-        return;
-    }
-    out[q] = in[p];
-}
-
-/* the keys last: perm is overwritten in place (each thread reads its slot
- * before writing it) */
-__global__ void __launch_bounds__(256) k_sort_gather_keys(const int32_t *__restrict__ cell,
-                                                          const int64_t *__restrict__ d_count, int32_t *perm_key,
-                                                          int *err) {
+/* The whole particle in one pass: q's source index p = perm[q] is read
+ * once, then the key and the six float rows are gathered from p and written
+ * at q (offsets and velocities to the second set of arrays, the key over
+ * perm in place: each thread reads its slot before writing it).  An index
+ * outside the species, which the histogram and scatter cannot produce, is
+ * flagged, not read. */
+__global__ void __launch_bounds__(256) k_sort_gather_all(const int32_t *__restrict__ cell,
+                                                         const float *__restrict__ off,
+                                                         const float *__restrict__ vel, int64_t stride,
+                                                         const int64_t *__restrict__ d_count, int32_t *perm_key,
+                                                         float *off2, float *vel2, int *err) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = d_count[0];
     if (q >= n) return;
@@ -792,11 +783,21 @@ __global__ void __launch_bounds__(256) k_sort_gather_keys(const int32_t *__restr
         atomicOr(err, DERR_SORT);
         return;
     }
-    perm_key[q] = cell[p];
+    const int32_t key = cell[p];
+    float v[6];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        v[d] = off[d * stride + p];
+        v[3 + d] = vel[d * stride + p];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        off2[d * stride + q] = v[d];
+        vel2[d * stride + q] = v[3 + d];
+    }
+    perm_key[q] = key;
 }
 
-/* per block: {count, mx, my, mz, sum w v^2} for the mixed form: float sums
- * over runs of 32 particles folded into float64 */
 /* Per block: count, sum v and sum |v|^2 of a mixed species.  Each thread
  * takes four particles a pass (all twelve loads issued before the sums, so
  * the pass is bound by bandwidth, not by the loads' latency); the float sums
@@ -982,14 +983,9 @@ void launch_sort_mixed(World &w, Species &s) {
     k_scan_down<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
     k_tile_seg<<<blocks_for(ntiles + 1, 256), 256, 0, w.stream>>>(counts, ntiles, s.d_count, s.seg);
     k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, ntx, nty, counts, s.cell2);
-    for (int d = 0; d < 3; d++) {
-        k_sort_gather<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.off + d * s.ms, s.cell2, s.d_count,
-                                                                s.off2 + d * s.ms, w.d_err);
-        k_sort_gather<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.vel + d * s.ms, s.cell2, s.d_count,
-                                                                s.vel2 + d * s.ms, w.d_err);
-    }
-    k_sort_gather_keys<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, s.cell2, w.d_err);
-    w.nlaunch += 13;
+    k_sort_gather_all<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.off, s.vel, s.ms, s.d_count, s.cell2,
+                                                                 s.off2, s.vel2, w.d_err);
+    w.nlaunch += 7;
     s.tiled = true;
     int32_t *tc = s.cell;
     s.cell = s.cell2;

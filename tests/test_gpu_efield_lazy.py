@@ -90,3 +90,60 @@ def test_near_midpoint_quotients_occur(po):
     bits = ef.view(np.uint64) & np.uint64((1 << 29) - 1)
     near = np.abs(bits.astype(np.int64) - (1 << 28)) <= 4
     assert near.sum() > 1000
+
+
+def run_solved(espic, with_fp64):
+    """a sphere world, ions loaded and a float-inner Newton-PCG solve, then
+    computeEF (k_efield4 in a mixed-form world, k_efield with the float64
+    species)"""
+    n = (41, 37, 61)
+    x0, xm = (-0.1, -0.1, 0.0), (0.1, 0.1, 0.4)
+    with espic.World(*n, x0, xm) as w:
+        w.set_seed(5)
+        w.setTime(1e-7, 10)
+        w.addSphere((0.0, 0.0, 0.15), 0.05, -100.0)
+        w.addInlet()
+        ions = espic.Species(w, "O+", 16 * AMU, QE, mpw0=2e3, capacity=1 << 19, form=espic.FORM_MIXED,
+                             walls=espic.WALLS_ABSORB)
+        probe = espic.Species(w, "P+", 16 * AMU, QE, mpw0=1.0, capacity=8192, form=espic.FORM_MIXED)
+        if with_fp64:
+            espic.Species(w, "e", 9.1e-31, -QE, capacity=64)
+        ions.loadParticlesBoxThermal(x0, xm, 0.0, 300000, (0.0, 0.0, 7000.0), 1160.0)
+        sol = espic.PotentialSolver(w, espic.SOLVER_PCG, 1000, 1e-4)
+        sol.setReferenceValues(0.0, 3.0, 1e10)
+        sol.setNewton(nr_max=20, nr_tol=1e-6, pcg_max=2000, pcg_tol=1e-4, fp32_inner=True)
+        ions.computeNumberDensity()
+        w.computeChargeDensity()
+        conv = sol.solve()[0]
+        sol.computeEF()
+        rng = np.random.default_rng(11)
+        m = 4000
+        ii, jj, kk = rng.integers(2, n[0] - 3, m), rng.integers(2, n[1] - 3, m), rng.integers(2, n[2] - 3, m)
+        probe.set_mixed((ii | (jj << 10) | (kk << 20)).astype(np.int32), np.zeros((3, m), np.float32),
+                        np.zeros((3, m), np.float32))
+        probe.advance()
+        v = probe.get_mixed()[2]
+        pe = w.getPE()
+        phi = w.phi.copy()
+        ef = w.read(espic.FIELD_EF).copy()
+        return conv, v, pe, ef, phi, n, x0, xm
+
+
+@pytest.mark.gpu
+def test_efield_after_a_solve_matches_float64(espic, po):
+    """after a float-inner solve: the mixed world's float copy equals the
+    rounded float64 field of a world where k_efield writes both, the float64
+    field equals the oracle's computeEF of the solved phi, and getPE agrees
+    within 1e-13"""
+    c1, v_pairs, pe_pairs, ef_pairs, phi1, n, x0, xm = run_solved(espic, with_fp64=False)
+    c2, v_full, pe_full, ef_full, phi2, _, _, _ = run_solved(espic, with_fp64=True)
+    assert c1 and c2
+    assert np.array_equal(phi1, phi2)  # the empty float64 species changes nothing in the solve
+    assert np.array_equal(v_pairs, v_full)
+    assert np.count_nonzero(v_pairs) > 3 * 3500
+    g = po.grid(list(n), list(x0), list(xm))
+    ef_o = po.efield(g, phi1).reshape(-1, 3)
+    assert np.array_equal(ef_pairs.reshape(-1, 3), ef_o)
+    pe_o = po.potential_energy(g, ef_o, po.node_volumes(g))
+    assert abs(pe_pairs - pe_o) <= 1e-13 * abs(pe_o)
+    assert abs(pe_full - pe_o) <= 1e-13 * abs(pe_o)
