@@ -987,13 +987,17 @@ static int enqueue_solve(World &w) {
                 }
                 if (w.phi_prev) {
                     bool extrapolate = w.phi_prev_valid && w.rho_version == w.solve_rho_version + 1;
-                    launch_predict(w, extrapolate);
+                    if (w.fp32_inner) /* the float-inner solve does it in its first pass */
+                        w.predict_mode = extrapolate ? 2 : 1;
+                    else
+                        launch_predict(w, extrapolate);
                     w.phi_prev_valid = true;
                     w.solve_rho_version = w.rho_version;
                 }
             }
             e = w.solver_kind == ESPIC_SOLVER_GS ? launch_gs_sphere(w, w.max_it, w.tol)
                                                  : launch_newton_pcg(w, w.fp32_inner != 0);
+            w.predict_mode = 0;
             break;
         case ESPIC_SOLVER_QN: {
             launch_qn(w);

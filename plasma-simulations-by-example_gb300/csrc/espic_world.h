@@ -133,6 +133,7 @@ struct World {
     double *phi_prev = nullptr;    /* the potential before the last Newton solve (predictor) */
     bool phi_prev_valid = false;
     bool predictor = true;         /* start the Newton solve from 2 phi^n - phi^(n-1) */
+    int predict_mode = 0;          /* for the next float-inner solve: 1 copy phi to phi_prev, 2 also extrapolate */
     int64_t rho_version = 0;       /* charge densities computed so far */
     int64_t solve_rho_version = -1;
     double *lin_y = nullptr;       /* linear (adjoint) mode of the Newton-PCG kernel: solution */

@@ -871,12 +871,40 @@ __device__ __forceinline__ dfl df_split(double v) {
 __device__ __forceinline__ float2 df_pack(dfl x) { return make_float2(x.h, x.l); }
 __device__ __forceinline__ dfl df_unpack(float2 v) { return {v.x, v.y}; }
 
-/* The pairs of phi and rho / eps0 at every node, once per solve */
+/* The pairs of phi and rho / eps0 at every node, once per solve, with the
+ * predictor folded in (predict 1: phi_prev = phi; 2: also start each
+ * unknown from 2 phi - phi_prev, in double-float) */
 __device__ __noinline__ void df_prepass(const double *__restrict__ phi, const double *__restrict__ rho, float2 *phf,
-                                        float2 *rhf, dfl d_inv_eps0, int64_t nn, int64_t gtid, int64_t gsize) {
-    for (int64_t u = gtid; u < nn; u += gsize) {
-        phf[u] = df_pack(df_split(phi[u]));
-        rhf[u] = df_pack(df_mul(df_split(rho[u]), d_inv_eps0));
+                                        float2 *rhf, const uint16_t *__restrict__ code, double *phi_prev,
+                                        int predict, dfl d_inv_eps0, int64_t nn, int64_t gtid, int64_t gsize) {
+    /* four nodes a pass, every load before any store (the pass is bound by
+     * the loads in flight) */
+    for (int64_t u0 = gtid; u0 < nn; u0 += 4 * gsize) {
+        double cur[4], prev[4], rh[4];
+        uint16_t c[4];
+        bool on[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int64_t u = u0 + h * gsize;
+            on[h] = u < nn;
+            const int64_t v = on[h] ? u : 0;
+            cur[h] = phi[v];
+            rh[h] = rho[v];
+            c[h] = predict == 2 ? code[v] : (uint16_t)0;
+            prev[h] = predict == 2 ? phi_prev[v] : 0.0;
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            if (!on[h]) continue;
+            const int64_t u = u0 + h * gsize;
+            dfl x = df_split(cur[h]);
+            if (predict) {
+                if (predict == 2 && (c[h] & SELF)) x = df_add({2.f * x.h, 2.f * x.l}, df_neg(df_split(prev[h])));
+                phi_prev[u] = cur[h];
+            }
+            phf[u] = df_pack(x);
+            rhf[u] = df_pack(df_mul(df_split(rh[h]), d_inv_eps0));
+        }
     }
 }
 
@@ -886,12 +914,25 @@ template <typename T>
 __device__ __noinline__ float df_update(const uint16_t *__restrict__ code, const T *__restrict__ yv, float2 *phf,
                                         int64_t nn, int64_t gtid, int64_t gsize) {
     float yys = 0.f;
-    for (int64_t u = gtid; u < nn; u += gsize) {
-        const uint16_t cu = code[u];
-        if (!(cu & SELF)) continue;
-        const float yu = (float)yv[u];
-        phf[u] = df_pack(df_add(df_unpack(phf[u]), {-yu, 0.f}));
-        yys = __fmaf_rn(yu, yu, yys);
+    /* four nodes a pass, every load before any store */
+    for (int64_t u0 = gtid; u0 < nn; u0 += 4 * gsize) {
+        uint16_t c[4];
+        float yu[4];
+        float2 x[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int64_t u = u0 + h * gsize;
+            const int64_t v = u < nn ? u : 0;
+            c[h] = u < nn ? code[v] : (uint16_t)0;
+            yu[h] = (float)yv[v];
+            x[h] = phf[v];
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            if (!(c[h] & SELF)) continue;
+            phf[u0 + h * gsize] = df_pack(df_add(df_unpack(x[h]), {-yu[h], 0.f}));
+            yys = __fmaf_rn(yu[h], yu[h], yys);
+        }
     }
     return yys;
 }
@@ -912,35 +953,60 @@ __device__ __noinline__ float df_residual(const uint16_t *__restrict__ code, con
                                           const float cl[3], dfl d_phi0, dfl d_inv_te0, dfl d_A0, float A0_te0,
                                           bool jacobi) {
     float ffs = 0.f;
-    for (int64_t u = gtid; u < nn; u += gsize) {
-        const uint16_t c = code[u];
-        if (!(c & SELF)) continue;
-        const float2 *pu = phf + u;
-        const float2 xu = pu[0];
-        const float2 pn[6] = {pu[-1], pu[1], pu[-s1], pu[s1], pu[-s2], pu[s2]};
-        const float2 bv = rhf[u];
-        const dfl x = df_unpack(xu);
-        dfl L = {0.f, 0.f};
+    /* two nodes a pass, every load before the arithmetic; a node that is
+     * not an unknown reads the interior node safe_u and stores nothing */
+    const int64_t safe_u = (int64_t)s2 + s1 + 1;
+    for (int64_t u0 = gtid; u0 < nn; u0 += 2 * gsize) {
+        uint16_t cq[2];
+        int64_t uq[2];
+        float2 xq[2], pq[2][6], bq[2];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const unsigned mw = (1u << (2 * a)) | (1u << (6 + 2 * a));
-            const unsigned me = (1u << (2 * a + 1)) | (1u << (7 + 2 * a));
-            const dfl pw = df_unpack((c & mw) ? pn[2 * a] : xu);
-            const dfl pe = df_unpack((c & me) ? pn[2 * a + 1] : xu);
-            const dfl d = df_add(df_add({2.f * x.h, 2.f * x.l}, df_neg(pw)), df_neg(pe));
-            L = df_add(L, df_mul(d, {(float)ct[a], cl[a]}));
+        for (int h = 0; h < 2; h++) {
+            const int64_t u = u0 + h * gsize;
+            cq[h] = u < nn ? code[u] : (uint16_t)0;
+            uq[h] = (cq[h] & SELF) ? u : safe_u;
         }
-        const dfl xa = df_mul(df_add(x, df_neg(d_phi0)), d_inv_te0);
-        const float ef = expf(xa.h);
-        const dfl e = df_fast2(ef, ef * xa.l);
-        const dfl Fd = df_add(df_add(L, df_mul(d_A0, e)), df_neg(df_unpack(bv)));
-        const float rv = Fd.h + Fd.l;
-        const float dBt = A0_te0 * ef;
-        if (jacobi || !(c & BLACK)) z[u] = (T)(rv / full_diag(c, (T)dBt, ct));
-        dg[u] = (T)dBt;
-        r[u] = (T)rv;
-        y[u] = 0;
-        ffs = __fmaf_rn(rv, rv, ffs);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 *pu = phf + uq[h];
+            xq[h] = pu[0];
+            pq[h][0] = pu[-1];
+            pq[h][1] = pu[1];
+            pq[h][2] = pu[-s1];
+            pq[h][3] = pu[s1];
+            pq[h][4] = pu[-s2];
+            pq[h][5] = pu[s2];
+            bq[h] = rhf[uq[h]];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint16_t c = cq[h];
+            if (!(c & SELF)) continue;
+            const int64_t u = uq[h];
+            const float2 xu = xq[h];
+            const dfl x = df_unpack(xu);
+            dfl L = {0.f, 0.f};
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const unsigned mw = (1u << (2 * a)) | (1u << (6 + 2 * a));
+                const unsigned me = (1u << (2 * a + 1)) | (1u << (7 + 2 * a));
+                const dfl pw = df_unpack((c & mw) ? pq[h][2 * a] : xu);
+                const dfl pe = df_unpack((c & me) ? pq[h][2 * a + 1] : xu);
+                const dfl d = df_add(df_add({2.f * x.h, 2.f * x.l}, df_neg(pw)), df_neg(pe));
+                L = df_add(L, df_mul(d, {(float)ct[a], cl[a]}));
+            }
+            const dfl xa = df_mul(df_add(x, df_neg(d_phi0)), d_inv_te0);
+            const float ef = expf(xa.h);
+            const dfl e = df_fast2(ef, ef * xa.l);
+            const dfl Fd = df_add(df_add(L, df_mul(d_A0, e)), df_neg(df_unpack(bq[h])));
+            const float rv = Fd.h + Fd.l;
+            const float dBt = A0_te0 * ef;
+            if (jacobi || !(c & BLACK)) z[u] = (T)(rv / full_diag(c, (T)dBt, ct));
+            dg[u] = (T)dBt;
+            r[u] = (T)rv;
+            y[u] = 0;
+            ffs = __fmaf_rn(rv, rv, ffs);
+        }
     }
     return ffs;
 }
@@ -954,7 +1020,8 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
                                                         T *p1, T *q, T *dg, MgArgs<T> mg, const int32_t *lists,
                                                         double *partials, SolveStatus *st, int *err,
                                                         double *lin_y, const double *__restrict__ lin_b,
-                                                        int gs_max, double gs_tol, float2 *dfbuf) {
+                                                        int gs_max, double gs_tol, float2 *dfbuf, double *phi_prev,
+                                                        int predict) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char pcg_smem[];
     __shared__ T bc_alpha, bc_beta;
@@ -1003,7 +1070,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
     float2 *phf = dfbuf, *rhf = dfbuf ? dfbuf + nn : nullptr;
     const dfl d_phi0 = df_of(phi0), d_inv_te0 = df_of(inv_te0), d_A0 = df_of(A0), d_inv_eps0 = df_of(inv_eps0);
     if (dfm) {
-        df_prepass(phi, rho, phf, rhf, d_inv_eps0, nn, gtid, gsize);
+        df_prepass(phi, rho, phf, rhf, code, phi_prev, predict, d_inv_eps0, nn, gtid, gsize);
         grid.sync();
     }
     const float cl[3] = {(float)(cd[0] - (double)ct[0]), (float)(cd[1] - (double)ct[1]),
@@ -1663,9 +1730,13 @@ static int run_pcg(World &w) {
     double gs_tol = w.tol;
     /* the pairs hold nn float2 each, the second array 256-byte aligned */
     float2 *dfp = dfb ? (float2 *)(base + 7 * vec + codeb + mgb + listb) : nullptr;
+    /* the predictor rides on the pairs' pass (the caller skipped k_predict) */
+    double *pp = w.phi_prev;
+    int predict = dfp && !ly ? w.predict_mode : 0;
+    w.predict_mode = 0;
     void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
                     &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
-                    &ly,   &lb,   &gs_max, &gs_tol, &dfp};
+                    &ly,   &lb,   &gs_max, &gs_tol, &dfp,  &pp,   &predict};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, dyn, w.stream);
 }
