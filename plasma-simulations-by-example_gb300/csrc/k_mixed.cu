@@ -333,10 +333,23 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
     __syncthreads();
     const int li = s_lo[0], lj = s_lo[1], lk = s_lo[2];
     const int sy = a.ni, sz = a.ni * a.nj;
-    for (int r = warp; r < TBW * TBW; r += nwarps) {
-        const int tk = r / TBW, tj = r - tk * TBW;
-        const float4 *src = ef4 + ((int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + li);
-        for (int ti = lane; ti < TBW; ti += 32) sE[r * TBW + ti] = __ldg(src + ti);
+    /* the box's 2197 nodes, nine per thread with every load issued before
+     * the stores (one memory latency for the whole box, not one per row) */
+    {
+        constexpr int PER = (BV + 255) / 256;
+        float4 ev[PER];
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int t = threadIdx.x + q * 256;
+            const int tt = t < BV ? t : 0;
+            const int tk = tt / (TBW * TBW), rem = tt - tk * TBW * TBW, tj = rem / TBW, ti = rem - tj * TBW;
+            ev[q] = __ldg(ef4 + ((int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + li + ti));
+        }
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int t = threadIdx.x + q * 256;
+            if (t < BV) sE[t] = ev[q];
+        }
     }
     __syncthreads();
     float *off1 = off + stride, *off2 = off + 2 * stride, *vel1 = vel + stride, *vel2 = vel + 2 * stride;
