@@ -937,6 +937,43 @@ __device__ __noinline__ float df_update(const uint16_t *__restrict__ code, const
     return yys;
 }
 
+/* phi of the unknowns from their pairs (hi + lo rounded once), four nodes
+ * a pass with every load before any store */
+__device__ __noinline__ void df_rebuild(const uint16_t *__restrict__ code, const float2 *__restrict__ phf,
+                                        double *phi, int64_t nn, int64_t gtid, int64_t gsize) {
+    for (int64_t u0 = gtid; u0 < nn; u0 += 4 * gsize) {
+        uint16_t c[4];
+        float2 x[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int64_t u = u0 + h * gsize;
+            c[h] = u < nn ? code[u] : (uint16_t)0;
+            x[h] = phf[u < nn ? u : 0];
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++)
+            if (c[h] & SELF) phi[u0 + h * gsize] = (double)x[h].x + (double)x[h].y;
+    }
+}
+
+/* Neumann boundary nodes take the value at the end of their chain (the
+ * chains end at unknowns or Dirichlet nodes, which this pass does not
+ * write), four nodes a pass */
+__device__ __noinline__ void neumann_copies(const int32_t *__restrict__ target, double *phi, int64_t nn,
+                                            int64_t gtid, int64_t gsize) {
+    for (int64_t u0 = gtid; u0 < nn; u0 += 4 * gsize) {
+        int32_t t[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int64_t u = u0 + h * gsize;
+            t[h] = u < nn ? target[u] : -1;
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++)
+            if (t[h] >= 0) phi[u0 + h * gsize] = phi[t[h]];
+    }
+}
+
 /* The Newton residual pass of the float-inner nonlinear solve in
  * double-float arithmetic (per axis c (2 x_u - x_w - x_e), a missing link
  * reading x_u; the Boltzmann factor as expf of the leading part times a
@@ -1402,19 +1439,10 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
         }
     }
     if (dfm) {
-        /* phi of the unknowns from their pairs (hi + lo rounded once) */
-        for (int64_t u = gtid; u < nn; u += gsize)
-            if (code[u] & SELF) {
-                const float2 v = phf[u];
-                phi[u] = (double)v.x + (double)v.y;
-            }
+        df_rebuild(code, phf, phi, nn, gtid, gsize);
         grid.sync();
     }
-    /* Neumann boundary nodes take the value at the end of their chain */
-    for (int64_t u = gtid; u < nn && !linear; u += gsize) {
-        int32_t t = target[u];
-        if (t >= 0) phi[u] = phi[t];
-    }
+    if (!linear) neumann_copies(target, phi, nn, gtid, gsize);
     if (gtid == 0) {
         st->converged = conv;
         st->iterations = nr;
