@@ -152,7 +152,7 @@ static void free_species(Species *s) {
                     s->tiledead, s->tilepre, s->holes, s->d_count, s->acc, s->den, s->den_ave, s->d_dsmc,
                     s->dsmc_cell, s->dsmc_rank, s->dsmc_perm, s->dsmc_count, s->dsmc_start, s->dsmc_bsum,
                     s->mom, s->mom_scale, s->gvel, s->gtemp, s->mpc, s->mom_acc, s->mom_bound, s->mcc_ncol,
-                    s->ch4_settled, s->ch4_bounces, s->seg, s->ch4_cnt, s->ionize_cnt};
+                    s->ch4_settled, s->ch4_bounces, s->seg, s->ch4_cnt, s->ionize_cnt, s->dsum};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -534,6 +534,7 @@ extern "C" int espic_species_set(espic_world *h, int sp, const double *P, int64_
     int64_t cnt[4] = {n, n, 0, 0};
     CK(cudaMemcpyAsync(s.d_count, cnt, sizeof cnt, cudaMemcpyHostToDevice, w.stream));
     s.tiled = false; /* new particle order: no tile segments until the next sort */
+    s.dsum_valid = false;
     /* for the ch4 push, particles set here have a step's time left */
     if (s.ch4_settled) CK(cudaMemsetAsync(s.ch4_settled, 0, sizeof(int64_t), w.stream));
     CK(cudaStreamSynchronize(w.stream));
@@ -594,6 +595,7 @@ extern "C" int espic_species_set_mixed(espic_world *h, int sp, const int32_t *ce
                 return fail(ESPIC_ERR_ARG, "particle %lld: in-cell offset outside [0,1]", (long long)p);
         }
     }
+    s.dsum_valid = false;
     if (n > 0) {
         CK(cudaMemcpyAsync(s.cell, cell, n * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream));
         CK(cudaMemcpy2DAsync(s.off, s.ms * sizeof(float), off, stride * sizeof(float), n * sizeof(float), 3,

@@ -29,6 +29,11 @@ struct Species {
     int32_t *sort_count = nullptr;         /* [tile-major cell slots + 1], then the scan's block sums */
     int32_t *seg = nullptr;                /* [ntiles + 1] first particle of each tile after the last sort */
     bool tiled = false;                    /* seg describes the particle order (a sort and no reorder since) */
+    /* mixed form: per-block sums (count, v, |v|^2) of the particles the last
+     * tile push left, valid until the particles next change */
+    double *dsum = nullptr;
+    int64_t dsum_cap = 0, dsum_n = 0;
+    bool dsum_valid = false;
     /* compaction */
     uint32_t *deadmask = nullptr; /* [cap/32 + 1] */
     int32_t *tiledead = nullptr;  /* [ntiles + 1] */

@@ -1422,6 +1422,7 @@ void launch_update_average(World &w, Species &s) {
 template <class Gen>
 static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int write_w) {
     if (ncand <= 0) return;
+    s.dsum_valid = false; /* the push's diagnostics sums miss the new particles */
     int64_t blocks = (ncand + APPEND_THREADS - 1) / APPEND_THREADS;
     if (blocks > w.blockcnt_cap) {
         if (w.d_blockcnt) {

@@ -285,6 +285,25 @@ __global__ void __launch_bounds__(256, 5) k_push_mixed(MixArgs a, const float4 *
  * between sorts, 7% faster than 15 at three blocks per SM */
 constexpr int TBW = 13;
 
+/* The block's sums of four per-thread floats as float64 (warp butterflies
+ * in float, then the warps in order), written by thread 0..3.  Every thread
+ * of the block calls it. */
+__device__ __forceinline__ void block_dsum(float f1, float f2, float f3, float f4, double *out) {
+    __shared__ double wsum[8][4];
+    float v[4] = {f1, f2, f3, f4};
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 4; q++) wsum[threadIdx.x >> 5][q] = (double)v[q];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0;
+        for (int w8 = 0; w8 < (int)(blockDim.x >> 5); w8++) t += wsum[w8][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+}
+
 /* the median over the warp of one int per lane (the 16th smallest) */
 __device__ __forceinline__ int warp_median(int v) {
     int below = 0, same = 0;
@@ -303,7 +322,8 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
                                                     float *off, float *vel, int64_t stride,
                                                     const int32_t *__restrict__ seg,
                                                     const int64_t *__restrict__ d_count, uint32_t *deadmask,
-                                                    int32_t *tiledead, unsigned long long *acc, int *err) {
+                                                    int32_t *tiledead, unsigned long long *acc, int *err,
+                                                    double *dsum) {
     constexpr int BV = TBW * TBW * TBW;
     extern __shared__ __align__(16) unsigned char tile_smem[];
     float4 *sE = (float4 *)tile_smem;
@@ -314,7 +334,10 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
     const int64_t n = d_count[0];
     const int p0 = seg[blockIdx.x];
     const int p1 = (int)min((int64_t)seg[blockIdx.x + 1], n);
-    if (p1 <= p0) return; /* block-uniform */
+    if (p1 <= p0) { /* block-uniform */
+        if (dsum && threadIdx.x < 4) dsum[4 * (int64_t)blockIdx.x + threadIdx.x] = 0.0;
+        return;
+    }
     if (warp == 0) {
         const int q = p0 + (int)(((int64_t)(p1 - p0) * lane) >> 5);
         int i, j, k;
@@ -353,6 +376,8 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
     }
     __syncthreads();
     float *off1 = off + stride, *off2 = off + 2 * stride, *vel1 = vel + stride, *vel2 = vel + 2 * stride;
+    /* the diagnostics' sums over the pushed particles (count, v, |v|^2) */
+    float f1 = 0.f, f2 = 0.f, f3 = 0.f, f4 = 0.f;
     for (int base = p0; base < p1; base += blockDim.x) {
         const int p = base + threadIdx.x;
         const bool live = p < p1;
@@ -401,6 +426,12 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
             vel[p] = vx;
             vel1[p] = vy;
             vel2[p] = vz;
+            if (!dead) {
+                f1 += vx;
+                f2 += vy;
+                f3 += vz;
+                f4 += vx * vx + vy * vy + vz * vz;
+            }
             if (WALLS == M_ABSORB && dead) {
                 atomicOr(deadmask + (p >> 5), 1u << (p & 31));
                 atomicAdd(tiledead + (p / TILE_PARTICLES), 1);
@@ -433,6 +464,7 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
             }
         }
     }
+    if (dsum) block_dsum(f1, f2, f3, f4, dsum + 4 * (int64_t)blockIdx.x);
     if (!DEPOSIT) return;
     __syncthreads();
     for (int r = warp; r < TBW * TBW; r += nwarps) {
@@ -452,9 +484,11 @@ __global__ void __launch_bounds__(256) k_push_tail(MixArgs a, const float4 *__re
                                                    float *off, float *vel, int64_t stride,
                                                    const int32_t *__restrict__ first,
                                                    const int64_t *__restrict__ d_count, uint32_t *deadmask,
-                                                   int32_t *tiledead, unsigned long long *acc, int *err) {
+                                                   int32_t *tiledead, unsigned long long *acc, int *err,
+                                                   double *dsum) {
     const int64_t n = d_count[0];
     const int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    float f1 = 0.f, f2 = 0.f, f3 = 0.f, f4 = 0.f;
     for (int64_t p = first[0] + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
         int32_t key = cell[p];
@@ -468,6 +502,12 @@ __global__ void __launch_bounds__(256) k_push_tail(MixArgs a, const float4 *__re
         vel[p] = vx;
         vel[stride + p] = vy;
         vel[2 * stride + p] = vz;
+        if (!dead) {
+            f1 += vx;
+            f2 += vy;
+            f3 += vz;
+            f4 += vx * vx + vy * vy + vz * vz;
+        }
         if (WALLS == M_ABSORB && dead) {
             atomicOr(deadmask + (p >> 5), 1u << (p & 31));
             atomicAdd(tiledead + (p / TILE_PARTICLES), 1);
@@ -487,6 +527,7 @@ __global__ void __launch_bounds__(256) k_push_tail(MixArgs a, const float4 *__re
             }
         }
     }
+    if (dsum) block_dsum(f1, f2, f3, f4, dsum + 4 * (int64_t)blockIdx.x);
 }
 
 __global__ void __launch_bounds__(256) k_deposit_mixed(MixArgs a, const int32_t *__restrict__ cell,
@@ -915,15 +956,29 @@ static void push_mixed_as(World &w, Species &s, int64_t n) {
         cudaFuncSetAttribute(k_push_tiles<WALLS, DEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (WALLS == M_ABSORB) /* the tile kernels OR their dead bits into the mask */
             cudaMemsetAsync(s.deadmask, 0, ((n + 31) / 32) * sizeof(uint32_t), w.stream);
+        /* per-block sums of the pushed particles for the diagnostics row */
+        const int64_t nsum = ntiles + 2 * (int64_t)w.sm_count;
+        if (s.dsum_cap < nsum) {
+            if (s.dsum) {
+                cudaStreamSynchronize(w.stream);
+                cudaFree(s.dsum);
+            }
+            s.dsum_cap = cudaMalloc(&s.dsum, 4 * nsum * sizeof(double)) == cudaSuccess ? nsum : 0;
+            if (!s.dsum_cap) s.dsum = nullptr;
+        }
         k_push_tiles<WALLS, DEP><<<(unsigned)ntiles, 256, smem, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
                                                                             s.seg, s.d_count, s.deadmask,
-                                                                            s.tiledead, s.acc, w.d_err);
+                                                                            s.tiledead, s.acc, w.d_err, s.dsum);
         k_push_tail<WALLS, DEP><<<2 * w.sm_count, 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
                                                                        s.seg + ntiles, s.d_count, s.deadmask,
-                                                                       s.tiledead, s.acc, w.d_err);
+                                                                       s.tiledead, s.acc, w.d_err,
+                                                                       s.dsum ? s.dsum + 4 * ntiles : nullptr);
         w.nlaunch += 2;
+        s.dsum_n = s.dsum ? nsum : 0;
+        s.dsum_valid = s.dsum != nullptr;
         return;
     }
+    s.dsum_valid = false;
     k_push_mixed<WALLS, DEP><<<blocks_for(n, 256), 256, 0, w.stream>>>(a, w.ef4, s.cell, s.off, s.vel, s.ms,
                                                                       s.d_count, s.deadmask, s.tiledead, s.acc,
                                                                       w.d_err);
@@ -955,6 +1010,7 @@ void launch_deposit_mixed(World &w, Species &s) {
 }
 
 void launch_to_mixed(World &w, Species &s, const double *P, int64_t stride, int64_t first, int64_t n) {
+    s.dsum_valid = false;
     if (n <= 0) return;
     k_to_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(w.g, P, stride, n, first, s.cell, s.off, s.vel,
                                                           s.ms);
@@ -1022,7 +1078,37 @@ void launch_int_excl_scan(cudaStream_t st, int32_t *x, int64_t n, int32_t *bsum)
     k_scan_down<<<(unsigned)nb, 1024, 0, st>>>(x, n, bsum);
 }
 
+/* the diagnostics row from the push's per-block sums (sum v, sum |v|^2), in
+ * block order, and the live count */
+__global__ void k_dsum_final(const double *__restrict__ dsum, int64_t nb, const int64_t *__restrict__ d_count,
+                             double mass, double w0, double *out) {
+    __shared__ double ws[32][4];
+    double t[4] = {0, 0, 0, 0};
+    for (int64_t b = threadIdx.x; b < nb; b += blockDim.x)
+        for (int q = 0; q < 4; q++) t[q] += dsum[4 * b + q];
+    for (int q = 0; q < 4; q++)
+        for (int o = 16; o > 0; o >>= 1) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 4; q++) ws[threadIdx.x >> 5][q] = t[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s[4] = {0, 0, 0, 0};
+        for (int w32 = 0; w32 < (int)(blockDim.x >> 5); w32++)
+            for (int q = 0; q < 4; q++) s[q] += ws[w32][q];
+        out[0] = (double)d_count[0] * w0;
+        out[1] = s[0] * w0 * mass;
+        out[2] = s[1] * w0 * mass;
+        out[3] = s[2] * w0 * mass;
+        out[4] = 0.5 * mass * (w0 * s[3]);
+    }
+}
+
 void launch_diag_mixed(World &w, Species &s, double *d_out5) {
+    if (s.dsum_valid) { /* the sums the last push left (no particle has changed since) */
+        k_dsum_final<<<1, 1024, 0, w.stream>>>(s.dsum, s.dsum_n, s.d_count, s.mass, s.mpw0, d_out5);
+        w.nlaunch++;
+        return;
+    }
     /* eight blocks of 256 per SM, within the partials buffer (5 per block) */
     int nb = 8 * w.sm_count;
     if (nb > w.partial_slots / 5) nb = w.partial_slots / 5;
