@@ -179,6 +179,13 @@ struct World {
 /* n / d for n < 2^24 without an integer division: the float estimate is
  * within one of the quotient (n is exact in float and 1/d is rounded once),
  * and one remainder test corrects it */
+/* x == +-0, tested on the 32-bit halves of its bits: written as a 64-bit
+ * test of the bits it compiles to a float64 compare, which issues on this
+ * GPU's narrow float64 pipe */
+__device__ __forceinline__ bool zero_bits(double x) {
+    return (((unsigned int)__double2hiint(x) << 1) | (unsigned int)__double2loint(x)) == 0u;
+}
+
 __device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float inv_d) {
     uint32_t q = __float2uint_rz((float)n * inv_d);
     const int32_t r = (int32_t)(n - q * d);

@@ -68,7 +68,7 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
     const double q2 = __fma_rn(r, y, q);
     /* a == +-0 tested on the bits: an integer compare keeps the narrow
      * float64 pipe for the arithmetic */
-    return (__double_as_longlong(a) << 1) == 0 ? q : q2;
+    return zero_bits(a) ? q : q2;
 }
 
 /* sum of part[0..ENS_VW) in a fixed tree; every thread gets the total */

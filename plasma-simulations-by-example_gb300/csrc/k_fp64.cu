@@ -23,6 +23,7 @@
 #include <type_traits>
 
 #include "ch4_push.h"
+#include "dfloat.h"
 #include "espic_world.h"
 
 namespace cg = cooperative_groups;
@@ -633,7 +634,7 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
     const double q2 = __fma_rn(r, y, q);
     /* a == +-0 tested on the bits: an integer compare keeps the narrow
      * float64 pipe for the arithmetic */
-    return (__double_as_longlong(a) << 1) == 0 ? q : q2;
+    return zero_bits(a) ? q : q2;
 }
 
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
@@ -683,97 +684,128 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double 
 }
 
 /* ------------------------------------------------------------------------ */
-/* RN_f(x) for a float64 x that lies within 3 ulps of the quotient whose
- * float64 rounding is wanted, computed on the integer pipes: false when x is
- * within 4 ulps of a float rounding midpoint (the float rounding of the
- * float64 quotient could then differ) or outside the normal float range, in
- * which case the caller rounds the exact quotient itself.  A float rounding
- * boundary is the midpoint between two floats: the low 29 of the 52
- * fraction bits equal to 2^28. */
-__device__ __forceinline__ bool f32_of_near(double x, float &out) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-    const unsigned long long mag = b & 0x7fffffffffffffffull;
-    if (mag == 0) {
-        out = __uint_as_float(sign);
-        return true;
-    }
-    const int e = (int)(mag >> 52);
-    if (e < 1023 - 125 || e > 1023 + 127) return false;
-    const unsigned long long m = mag & 0xfffffffffffffull;
-    const long long low = (long long)(m & 0x1fffffffull);
-    const long long dist = low - (1ll << 28);
-    if (dist >= -4 && dist <= 4) return false;
-    unsigned int fb = ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29);
-    fb += dist > 0 ? 1u : 0u;
-    if (fb >= 0x7f800000u) return false;
-    out = __uint_as_float(fb | sign);
-    return true;
-}
-
 /* computeEF for worlds whose particles all live in the mixed form: the
  * float copy ef4 = RN_f(RN_d(n / 2dh)) of every node, bit for bit that of
- * k_efield, from q = n RN(1 / 2dh) (within 3 ulps of the float64 quotient)
- * rounded on the integer pipes, and the exact quotient only where q lies
- * near a float rounding boundary: two float64 operations per component
- * instead of five (this GPU's float64 rate bounds k_efield).  The float64
- * field is written on the planes k < 2 alone, the ones a beam source's
- * addParticle gathers at (its particles start at z = x0); the rest of it is
- * completed on demand by k_efield from phi_ef, the copy of phi this
- * kernel reads (the solver changes phi before the field is next computed,
- * and the reference's ef stays that of the last computeEF).
- * World::getPE's sum of |E|^2 vol over the nodes rides along from the same
- * q (each within 6 ulps of the float64 |E|^2 term, far inside the 1e-13 to
- * which the sum's order already defines it).  Each thread takes EF_KPT
- * planes of its (i, j) column, so the block sum is paid once per EF_KPT
- * nodes: one partial per block, [plane group][block of the plane]. */
+ * k_efield.  Interior nodes take the float64 differences n (the reference's
+ * numerators: three float64 operations) and the rest on the float and
+ * integer pipes: q = n (-1 / 2dh) in double-float (within 2^-45 |q| of the
+ * float64 quotient), rounded to float where it lies farther than 2^-40 |q|
+ * from a float rounding boundary.  The faces, and the rare interior node
+ * with a component near a boundary or outside the double-float range, take
+ * ef_node_exact.  The float64 field is written on the planes k < 2 alone,
+ * the ones a beam source's addParticle gathers at (its particles start at
+ * z = x0); the rest of it is completed on demand by k_efield from phi_ef,
+ * the copy of phi this kernel reads (the solver changes phi before the
+ * field is next computed, and the reference's ef stays that of the last
+ * computeEF).  World::getPE's sum of |E|^2 vol over the nodes rides along
+ * from the same q, in double-float (each term within 2^-44 of the float64
+ * term, far inside the 1e-13 to which the sum's order already defines it).
+ * Each thread takes EF_KPT planes of its (i, j) column, so the block sum is
+ * paid once per EF_KPT nodes: one partial per block, [plane group][block of
+ * the plane]. */
 constexpr int EF_KPT = 4; /* planes per thread of k_efield4 */
 
-__global__ void __launch_bounds__(256) k_efield4(Geo g, double3 y2, const double *__restrict__ phi, double *ef,
+struct EfConst {
+    double3 y2, d2; /* RN(1 / 2dh) and 2 dh per axis */
+    float2 ny[3];   /* -RN(1 / 2dh) as a float pair (hi, lo) */
+};
+
+/* one node of k_efield4 in float64: the numerators of ef_num, div_rcp, ef4
+ * (and ef on the planes k < 2); returns pe + |E|^2 vol.  Not inlined, so
+ * that it is a real branch: inlined, its float64 operations were
+ * if-converted and issued for every node. */
+__device__ __noinline__ double ef_node_exact(const double *__restrict__ phi, double *ef, float4 *ef4,
+                                             const double *__restrict__ vol, int64_t u, int i, int j, int k, int ni,
+                                             int nj, int nk, double3 d2, double3 y2, double pe) {
+    const int64_t sy = ni, sz = (int64_t)ni * nj;
+    const double e0 = div_rcp(ef_num(phi, u, 1, i, ni), d2.x, y2.x);
+    const double e1 = div_rcp(ef_num(phi, u, sy, j, nj), d2.y, y2.y);
+    const double e2 = div_rcp(ef_num(phi, u, sz, k, nk), d2.z, y2.z);
+    if (k < 2) {
+        ef[3 * u] = e0;
+        ef[3 * u + 1] = e1;
+        ef[3 * u + 2] = e2;
+    }
+    ef4[u] = make_float4((float)e0, (float)e1, (float)e2, 0.f);
+    return __fma_rn(__fma_rn(e2, e2, __fma_rn(e1, e1, e0 * e0)), vol[u], pe);
+}
+
+__global__ void __launch_bounds__(256) k_efield4(Geo g, EfConst ec, const double *__restrict__ phi, double *ef,
                                                  float4 *ef4, const double *__restrict__ vol, double *pe_part,
                                                  double *phi_ef) {
-    const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nplane = (uint32_t)g.ni * (uint32_t)g.nj;
-    double pe = 0;
-    if (pl < nplane) {
-        const uint32_t jj = div_small(pl, (uint32_t)g.ni, 1.f / (float)g.ni);
-        const int j = (int)jj, i = (int)(pl - jj * (uint32_t)g.ni);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ni = (uint32_t)g.ni, nj = (uint32_t)g.nj, nplane = ni * nj;
+    double pe = 0;         /* the nodes of ef_node_exact */
+    dfl pe_d = {0.f, 0.f}; /* the rest, in double-float */
+    if (t < nplane) {
+        /* threads [0, (ni-2)(nj-2)) take the columns off the i and j faces,
+         * i fastest; the rest take the face columns (the rows j = 0 and
+         * j = nj-1, then the columns i = 0 and i = ni-1), so that a warp's
+         * face nodes, which take ef_node_exact, share that call */
+        const uint32_t nin = (ni > 2 && nj > 2) ? (ni - 2) * (nj - 2) : 0u;
+        uint32_t i, j;
+        if (t < nin) {
+            const uint32_t jj = div_small(t, ni - 2, 1.f / (float)(ni - 2));
+            j = 1 + jj;
+            i = 1 + (t - jj * (ni - 2));
+        } else {
+            const uint32_t f = t - nin;
+            if (f < 2 * ni) {
+                j = f < ni ? 0u : nj - 1;
+                i = f < ni ? f : f - ni;
+            } else {
+                const uint32_t f2 = f - 2 * ni;
+                i = f2 < nj - 2 ? 0u : ni - 1;
+                j = 1 + (f2 < nj - 2 ? f2 : f2 - (nj - 2));
+            }
+        }
+        const uint32_t pl = j * ni + i;
         const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
-        const bool in_ij = i > 0 && i < g.ni - 1 && j > 0 && j < g.nj - 1;
-        const double d2[3] = {2 * g.dh[0], 2 * g.dh[1], 2 * g.dh[2]}, yy[3] = {y2.x, y2.y, y2.z};
-        /* -RN(1 / 2dh): (phi_+ - phi_-) (-y) is -(phi_+ - phi_-) y to the
-         * bit, signed zero included */
-        const double ny[3] = {-y2.x, -y2.y, -y2.z};
+        const bool in_ij = t < nin;
         const int k0 = blockIdx.y * EF_KPT;
         for (int kk = 0; kk < EF_KPT; kk++) {
             const int k = k0 + kk;
             if (k >= g.nk) break;
             const int64_t u = (int64_t)k * sz + pl;
             phi_ef[u] = phi[u];
-            float f[3];
-            double q[3];
-            if (in_ij && k >= 2 && k < g.nk - 1) {
+            bool exact = !(in_ij && k >= 2 && k < g.nk - 1);
+            if (!exact) {
                 const double dd[3] = {phi[u + 1] - phi[u - 1], phi[u + sy] - phi[u - sy], phi[u + sz] - phi[u - sz]};
+                float f[3];
+                dfl e2 = {0.f, 0.f};
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    q[c] = dd[c] * ny[c];
-                    if (!f32_of_near(q[c], f[c])) f[c] = (float)div_rcp(-dd[c], d2[c], yy[c]);
+                    dfl qd = {0.f, 0.f}, dv;
+                    if (df_split_int(dd[c], dv)) {
+                        qd = df_mul(dv, df_unpack(ec.ny[c]));
+                        if (!f32_of_df(qd, 9.1e-13f * fabsf(qd.h), f[c])) exact = true;
+                    } else {
+                        if (zero_bits(dd[c])) /* -dd / 2dh: the zero of the opposite sign */
+                            f[c] = __uint_as_float(((unsigned int)__double2hiint(dd[c]) & 0x80000000u) ^ 0x80000000u);
+                        else
+                            exact = true;
+                    }
+                    e2 = df_add(e2, df_mul(qd, qd));
                 }
-            } else {
-                const double n[3] = {ef_num(phi, u, 1, i, g.ni), ef_num(phi, u, sy, j, g.nj),
-                                     ef_num(phi, u, sz, k, g.nk)};
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    const double e = div_rcp(n[c], d2[c], yy[c]);
-                    if (k < 2) ef[3 * u + c] = e;
-                    f[c] = (float)e;
-                    q[c] = e;
+                dfl vd = {0.f, 0.f};
+                if (!df_split_int(vol[u], vd)) exact = true;
+                const dfl t = df_mul(e2, vd);
+                /* terms of magnitude in [2^-100, 2^100] keep ~48 bits in
+                 * double-float (a zero e2 is all three components zero) */
+                const unsigned int te = __float_as_uint(t.h) & 0x7f800000u,
+                                   ee = __float_as_uint(e2.h) & 0x7f800000u;
+                if (!((te >= (27u << 23) && te <= (227u << 23) && ee >= (27u << 23) && ee <= (227u << 23)) ||
+                      (__float_as_uint(e2.h) << 1) == 0u))
+                    exact = true;
+                if (!exact) {
+                    ef4[u] = make_float4(f[0], f[1], f[2], 0.f);
+                    pe_d = df_add(pe_d, t);
                 }
             }
-            ef4[u] = make_float4(f[0], f[1], f[2], 0.f);
-            pe = __fma_rn(__fma_rn(q[2], q[2], __fma_rn(q[1], q[1], q[0] * q[0])), vol[u], pe);
+            if (exact) pe = ef_node_exact(phi, ef, ef4, vol, u, (int)i, (int)j, k, g.ni, g.nj, g.nk, ec.d2, ec.y2, pe);
         }
     }
+    pe += (double)pe_d.h + (double)pe_d.l;
     /* deterministic block sum: warp butterflies, then the 8 warps in order */
     __shared__ double ws[8];
     for (int o = 16; o > 0; o >>= 1) pe += __shfl_xor_sync(0xffffffffu, pe, o);
@@ -852,7 +884,7 @@ __global__ void k_density(int64_t nn, const unsigned long long *__restrict__ acc
     double d = __ll2double_rn((long long)acc[u]) * unit;
     double v = vol[u];
     /* d / v, correctly rounded, from RN(1/v) (the float64 pipe is narrow) */
-    den[u] = (__double_as_longlong(v) << 1) != 0 ? div_rcp(d, v, ivol[u]) : 0.0;
+    den[u] = !zero_bits(v) ? div_rcp(d, v, ivol[u]) : 0.0;
 }
 
 struct ChargeArgs {
@@ -1311,7 +1343,15 @@ void launch_efield(World &w, bool full) {
         }
     }
     if (!full && mixed && !fp64 && w.phi_ef) {
-        k_efield4<<<grid4, 256, 0, w.stream>>>(w.g, y2, w.phi, w.ef, w.ef4, w.vol, w.pe_part, w.phi_ef);
+        EfConst ec;
+        ec.y2 = y2;
+        ec.d2 = make_double3(2 * w.g.dh[0], 2 * w.g.dh[1], 2 * w.g.dh[2]);
+        const double ny[3] = {-y2.x, -y2.y, -y2.z};
+        for (int c = 0; c < 3; c++) {
+            const float h = (float)ny[c];
+            ec.ny[c] = make_float2(h, (float)(ny[c] - (double)h));
+        }
+        k_efield4<<<grid4, 256, 0, w.stream>>>(w.g, ec, w.phi, w.ef, w.ef4, w.vol, w.pe_part, w.phi_ef);
         w.nlaunch++;
         w.ef4_valid = true;
         w.ef64_valid = false;

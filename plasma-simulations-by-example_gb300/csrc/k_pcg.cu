@@ -43,6 +43,7 @@
  */
 #include <cooperative_groups.h>
 
+#include "dfloat.h"
 #include "espic_world.h"
 
 namespace cg = cooperative_groups;
@@ -813,63 +814,7 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
     return v[0];
 }
 
-/* Double-float arithmetic: a value as an unevaluated sum hi + lo of two
- * floats (|lo| <= ulp(hi) / 2), ~48 significant bits, on the float pipes.
- * TwoSum (Knuth) and Fast2Sum (Dekker) give the exact rounding error of a
- * sum; a product's error comes from one FMA.  (D. E. Knuth, TAOCP vol. 2,
- * 4.2.2; T. J. Dekker, Numer. Math. 18, 1971.) */
-struct dfl {
-    float h, l;
-};
-__device__ __forceinline__ dfl df_two_sum(float a, float b) {
-    const float s = a + b, bb = s - a;
-    return {s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ dfl df_fast2(float a, float b) {
-    const float s = a + b;
-    return {s, b - (s - a)};
-}
-__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
-    const dfl s = df_two_sum(x.h, y.h);
-    return df_fast2(s.h, s.l + (x.l + y.l));
-}
-__device__ __forceinline__ dfl df_neg(dfl x) { return {-x.h, -x.l}; }
-__device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
-    const float p = x.h * y.h;
-    const float e = __fmaf_rn(x.h, y.h, -p);
-    return df_fast2(p, __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, e)));
-}
-__device__ __forceinline__ dfl df_of(double v) {
-    const float h = (float)v;
-    return {h, (float)(v - (double)h)};
-}
-/* df_of on the integer pipes: hi = RN_f(v) from the 53-bit significand
- * rounded to 24 bits (ties to even), lo = RN_f(v - hi) from the exact
- * remainder (|r| <= 2^28).  Magnitudes outside [2^-60, 2^60] (zero included)
- * take the float64 conversion. */
-__device__ __forceinline__ dfl df_split(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const int e = (int)((b >> 52) & 0x7ff);
-    if (e < 1023 - 60 || e > 1023 + 60) return df_of(v);
-    const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
-    unsigned long long mh = m >> 29;
-    const unsigned long long rem = m & 0x1fffffffull;
-    if (rem > (1ull << 28) || (rem == (1ull << 28) && (mh & 1))) mh++;
-    const int r = (int)((long long)m - (long long)(mh << 29));
-    int eh = e - 1023 + 127;
-    if (mh == (1ull << 24)) {
-        mh >>= 1;
-        eh++;
-    }
-    const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
-    const float hi = __uint_as_float(sgn | ((unsigned int)eh << 23) | ((unsigned int)mh & 0x7fffffu));
-    /* r 2^(e - 1075), the power of two built from its exponent bits */
-    const float scale = __uint_as_float((unsigned int)(e - 1075 + 127) << 23);
-    const float lo = __int2float_rn(r) * scale;
-    return {hi, sgn ? -lo : lo};
-}
-__device__ __forceinline__ float2 df_pack(dfl x) { return make_float2(x.h, x.l); }
-__device__ __forceinline__ dfl df_unpack(float2 v) { return {v.x, v.y}; }
+
 
 /* The pairs of phi and rho / eps0 at every node, once per solve, with the
  * predictor folded in (predict 1: phi_prev = phi; 2: also start each
