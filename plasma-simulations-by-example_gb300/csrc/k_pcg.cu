@@ -238,6 +238,11 @@ __device__ void smem_levels_init(const MgArgs<T> &A, MgArgs<T> &S, unsigned char
 
 /* everything the level-0 (node grid) operations need */
 template <typename T>
+struct Coef3 {
+    T c[3];
+};
+
+template <typename T>
 struct Fine {
     Geo g;
     const uint16_t *code;
@@ -1003,7 +1008,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
                                                         double *partials, SolveStatus *st, int *err,
                                                         double *lin_y, const double *__restrict__ lin_b,
                                                         int gs_max, double gs_tol, float2 *dfbuf, double *phi_prev,
-                                                        int predict) {
+                                                        int predict, Coef3<T> ctp) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char pcg_smem[];
     __shared__ T bc_alpha, bc_beta;
@@ -1019,7 +1024,11 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) k_newton_pcg(Geo g, double *ph
     const int64_t off[6] = {-1, 1, -sy, sy, -sz, sz};
     const int64_t safe = sz + sy + 1; /* the interior node (1,1,1) */
     const double cd[3] = {1.0 / (g.dh[0] * g.dh[0]), 1.0 / (g.dh[1] * g.dh[1]), 1.0 / (g.dh[2] * g.dh[2])};
-    const T ct[3] = {(T)cd[0], (T)cd[1], (T)cd[2]};
+    /* (T)cd from the host: derived here from cd, the compiler re-derived it
+     * inside the node loops (a float64-to-float conversion each time, on the
+     * narrow float64 pipe) instead of holding it */
+    const bool tf = sizeof(T) == sizeof(float);
+    const T ct[3] = {tf ? ctp.c[0] : (T)cd[0], tf ? ctp.c[1] : (T)cd[1], tf ? ctp.c[2] : (T)cd[2]};
     const double A0 = PCG_QE * n0 / PCG_EPS_0;
     const double inv_te0 = 1.0 / te0, A0_te0 = A0 / te0, inv_eps0 = 1.0 / PCG_EPS_0;
     const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1707,9 +1716,12 @@ static int run_pcg(World &w) {
     double *pp = w.phi_prev;
     int predict = dfp && !ly ? w.predict_mode : 0;
     w.predict_mode = 0;
+    /* the axis coefficients 1 / dh^2 rounded to T, as the kernel's cd */
+    Coef3<T> ctp;
+    for (int a = 0; a < 3; a++) ctp.c[a] = (T)(1.0 / (g.dh[a] * g.dh[a]));
     void *args[] = {&g,    &phi,  &rho,  &cc,   &tg,   &phi0, &te0, &n0,  &nr_max, &nr_tol, &pcg_max, &pcg_tol,
                     &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &A,  &lst,   &part,   &st,      &err,
-                    &ly,   &lb,   &gs_max, &gs_tol, &dfp,  &pp,   &predict};
+                    &ly,   &lb,   &gs_max, &gs_tol, &dfp,  &pp,   &predict, &ctp};
     w.nlaunch++;
     return (int)cudaLaunchCooperativeKernel(fn, grid, threads, args, dyn, w.stream);
 }
