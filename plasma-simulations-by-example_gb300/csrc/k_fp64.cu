@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double 
  * Each thread takes EF_KPT planes of its (i, j) column, so the block sum is
  * paid once per EF_KPT nodes: one partial per block, [plane group][block of
  * the plane]. */
-constexpr int EF_KPT = 4; /* planes per thread of k_efield4 */
+constexpr int EF_KPT = 8; /* planes per thread of k_efield4 */
 
 struct EfConst {
     double3 y2, d2; /* RN(1 / 2dh) and 2 dh per axis */
