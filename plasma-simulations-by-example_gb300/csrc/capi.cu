@@ -983,16 +983,21 @@ static int enqueue_solve(World &w) {
                 /* predictor: between consecutive steps (one new charge
                  * density since the last solve) the Newton solve starts
                  * from 2 phi^n - phi^(n-1); otherwise from phi^n */
-                if (!w.phi_prev && cudaMalloc(&w.phi_prev, w.nn * sizeof(double)) != cudaSuccess) {
+                /* two rows: the float-inner solve's quadratic predictor keeps
+                 * the last two potentials */
+                if (!w.phi_prev && cudaMalloc(&w.phi_prev, 2 * w.nn * sizeof(double)) != cudaSuccess) {
                     w.phi_prev = nullptr;
                     w.predictor = false;
                 }
                 if (w.phi_prev) {
                     bool extrapolate = w.phi_prev_valid && w.rho_version == w.solve_rho_version + 1;
-                    if (w.fp32_inner) /* the float-inner solve does it in its first pass */
-                        w.predict_mode = extrapolate ? 2 : 1;
-                    else
+                    if (w.fp32_inner) { /* the float-inner solve does it in its first pass */
+                        w.predict_mode = !extrapolate ? 1 : (w.phi_prev2_valid ? 3 : 2);
+                        w.phi_prev2_valid = extrapolate;
+                    } else {
                         launch_predict(w, extrapolate);
+                        w.phi_prev2_valid = false;
+                    }
                     w.phi_prev_valid = true;
                     w.solve_rho_version = w.rho_version;
                 }

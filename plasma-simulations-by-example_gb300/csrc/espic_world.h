@@ -137,6 +137,7 @@ struct World {
     int solver_blocks = 0;  /* cap on cooperative solver blocks (0: occupancy limit) */
     double *phi_prev = nullptr;    /* the potential before the last Newton solve (predictor) */
     bool phi_prev_valid = false;
+    bool phi_prev2_valid = false;  /* the second row of phi_prev: the solve before phi_prev's, consecutive */
     bool predictor = true;         /* start the Newton solve from 2 phi^n - phi^(n-1) */
     int predict_mode = 0;          /* for the next float-inner solve: 1 copy phi to phi_prev, 2 also extrapolate */
     int64_t rho_version = 0;       /* charge densities computed so far */

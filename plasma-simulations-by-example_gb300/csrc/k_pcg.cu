@@ -822,15 +822,18 @@ __device__ double vcycle_rest(cg::grid_group &grid, const Fine<T> &F, const MgAr
 
 
 /* The pairs of phi and rho / eps0 at every node, once per solve, with the
- * predictor folded in (predict 1: phi_prev = phi; 2: also start each
- * unknown from 2 phi - phi_prev, in double-float) */
+ * predictor folded in.  phi_prev holds two rows, the potentials of the last
+ * two solves before this one (p1 = phi_prev, p2 = phi_prev + nn); phi is
+ * the last solve's.  predict 1: p1 = phi; 2: also start each unknown from
+ * 2 phi - p1 (linear extrapolation in time), and p2 = p1; 3: start from
+ * 3 phi - 3 p1 + p2 (quadratic), and p2 = p1.  In double-float. */
 __device__ __noinline__ void df_prepass(const double *__restrict__ phi, const double *__restrict__ rho, float2 *phf,
                                         float2 *rhf, const uint16_t *__restrict__ code, double *phi_prev,
                                         int predict, dfl d_inv_eps0, int64_t nn, int64_t gtid, int64_t gsize) {
     /* four nodes a pass, every load before any store (the pass is bound by
      * the loads in flight) */
     for (int64_t u0 = gtid; u0 < nn; u0 += 4 * gsize) {
-        double cur[4], prev[4], rh[4];
+        double cur[4], prev[4], prev2[4], rh[4];
         uint16_t c[4];
         bool on[4];
 #pragma unroll
@@ -840,8 +843,9 @@ __device__ __noinline__ void df_prepass(const double *__restrict__ phi, const do
             const int64_t v = on[h] ? u : 0;
             cur[h] = phi[v];
             rh[h] = rho[v];
-            c[h] = predict == 2 ? code[v] : (uint16_t)0;
-            prev[h] = predict == 2 ? phi_prev[v] : 0.0;
+            c[h] = predict >= 2 ? code[v] : (uint16_t)0;
+            prev[h] = predict >= 2 ? phi_prev[v] : 0.0;
+            prev2[h] = predict == 3 ? phi_prev[nn + v] : 0.0;
         }
 #pragma unroll
         for (int h = 0; h < 4; h++) {
@@ -849,7 +853,16 @@ __device__ __noinline__ void df_prepass(const double *__restrict__ phi, const do
             const int64_t u = u0 + h * gsize;
             dfl x = df_split(cur[h]);
             if (predict) {
-                if (predict == 2 && (c[h] & SELF)) x = df_add({2.f * x.h, 2.f * x.l}, df_neg(df_split(prev[h])));
+                if (predict >= 2 && (c[h] & SELF)) {
+                    const dfl p1 = df_split(prev[h]);
+                    if (predict == 2) {
+                        x = df_add({2.f * x.h, 2.f * x.l}, df_neg(p1));
+                    } else {
+                        const dfl d = df_add(x, df_neg(p1));
+                        x = df_add({3.f * d.h, 3.f * d.l}, df_split(prev2[h]));
+                    }
+                }
+                if (predict >= 2) phi_prev[nn + u] = prev[h];
                 phi_prev[u] = cur[h];
             }
             phf[u] = df_pack(x);
