@@ -195,6 +195,33 @@ __device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float inv_
     return q;
 }
 
+/* the eight cloud-in-cell corner weights of a particle at offsets (fx, fy,
+ * fz) in its cell, corners in Field_::gather's order (ch2/Field.h:186-208) */
+__device__ __forceinline__ void cic_w(float fx, float fy, float fz, float w[8]) {
+    float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
+    w[0] = gx * gy * gz;
+    w[1] = fx * gy * gz;
+    w[2] = fx * fy * gz;
+    w[3] = gx * fy * gz;
+    w[4] = gx * gy * fz;
+    w[5] = fx * gy * fz;
+    w[6] = fx * fy * fz;
+    w[7] = gx * fy * fz;
+}
+
+/* trilinear E at the particle: a chain of fused multiply-adds over the
+ * corners in Field_::gather's order (ch2/Field.h:186-208), from corner 0 */
+__device__ __forceinline__ float3 gather_corners(const float w[8], const float4 e[8]) {
+    float3 r = make_float3(__fmul_rn(w[0], e[0].x), __fmul_rn(w[0], e[0].y), __fmul_rn(w[0], e[0].z));
+#pragma unroll
+    for (int c = 1; c < 8; c++) {
+        r.x = __fmaf_rn(w[c], e[c].x, r.x);
+        r.y = __fmaf_rn(w[c], e[c].y, r.y);
+        r.z = __fmaf_rn(w[c], e[c].z, r.z);
+    }
+    return r;
+}
+
 inline int blocks_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;

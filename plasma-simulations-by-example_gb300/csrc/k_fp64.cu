@@ -82,6 +82,30 @@ __device__ __forceinline__ bool in_bounds(const Geo &g, const double x[3]) {
     return true;
 }
 
+/* a / b correctly rounded, given y = RN(1/b) for b > 0: q = a y, the exact
+ * remainder r = a - b q (one FMA), then q + r y rounded -- Markstein's
+ * correction (P. Markstein, IBM J. Res. Develop. 34(1), 1990), which yields
+ * the correctly rounded quotient for normal operands, so results equal the
+ * division's bit for bit; a = +-0 returns a y, the zero of the right sign.
+ * Three float64 operations instead of a division: the GB300's float64 rate
+ * makes the division dominate the kernels below. */
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+    const double q = a * y;
+    const double r = __fma_rn(-q, b, a);
+    const double q2 = __fma_rn(r, y, q);
+    /* a == +-0 tested on the bits: an integer compare keeps the narrow
+     * float64 pipe for the arithmetic */
+    return zero_bits(a) ? q : q2;
+}
+
+/* x to logical coordinates with the correctly rounded reciprocal of dh:
+ * equal to World::XtoL's division bit for bit (div_rcp) */
+__device__ __forceinline__ void xtol_rcp(const Geo &g, double3 rdh, const double x[3], double lc[3]) {
+    lc[0] = div_rcp(x[0] - g.x0[0], g.dh[0], rdh.x);
+    lc[1] = div_rcp(x[1] - g.x0[1], g.dh[1], rdh.y);
+    lc[2] = div_rcp(x[2] - g.x0[2], g.dh[2], rdh.z);
+}
+
 __device__ __forceinline__ bool in_sphere(const double s[4], const double x[3]) {
     double r0 = x[0] - s[0], r1 = x[1] - s[1], r2 = x[2] - s[2];
     double rm2 = r0 * r0 + r1 * r1 + r2 * r2;
@@ -569,14 +593,20 @@ __global__ void __launch_bounds__(1024) k_append_scan(int32_t *blockcnt, int64_t
 
 /* Pass 3: each accepted candidate is rewound by (q/m)E dt/2 and written at
  * n_old + (number of accepted candidates before it), so the order is the
- * candidates' order, as the reference's emplace_back. */
+ * candidates' order, as the reference's emplace_back.  The float64 form
+ * gathers E from the float64 field in the reference's arithmetic; the mixed
+ * form from the float copy ef4 with the mixed push's float weights (its
+ * velocities are floats: the float64 gather cost ~100 float64 operations a
+ * particle for a change below their last bit but one), with qmdt2 =
+ * RN_f(q/m dt/2). */
 template <class Gen, int FORM>
-__global__ void __launch_bounds__(APPEND_THREADS) k_append_write(Geo g, Gen gen, int64_t ncand,
+__global__ void __launch_bounds__(APPEND_THREADS) k_append_write(Geo g, double3 rdh, Gen gen, int64_t ncand,
                                                       const int32_t *__restrict__ blockpre,
                                                       const int64_t *__restrict__ d_count,
-                                                      const double *__restrict__ ef, double qm, double dt,
-                                                      double *P, int32_t *cell, float *off, float *vel,
-                                                      int64_t stride, int64_t cap, int write_w) {
+                                                      const double *__restrict__ ef, const float4 *__restrict__ ef4,
+                                                      double qm, double dt, float qmdt2, double *P, int32_t *cell,
+                                                      float *off, float *vel, int64_t stride, int64_t cap,
+                                                      int write_w) {
     __shared__ int32_t sh[APPEND_THREADS / 32];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t s_base = d_count[1] + blockpre[blockIdx.x];
@@ -597,11 +627,12 @@ __global__ void __launch_bounds__(APPEND_THREADS) k_append_write(Geo g, Gen gen,
     if (ok) {
         int64_t dst = s_base + pre;
         if (dst < cap) {
-            double lc[3], e[3];
-            xtol(g, x, lc);
-            gather3(g, ef, lc, e);
-            for (int d = 0; d < 3; d++) v[d] = v[d] - e[d] * qm * (0.5 * dt);
+            double lc[3];
+            xtol_rcp(g, rdh, x, lc);
             if (FORM == 0) {
+                double e[3];
+                gather3(g, ef, lc, e);
+                for (int d = 0; d < 3; d++) v[d] = v[d] - e[d] * qm * (0.5 * dt);
                 for (int d = 0; d < 3; d++) {
                     P[d * stride + dst] = x[d];
                     P[(3 + d) * stride + dst] = v[d];
@@ -610,32 +641,27 @@ __global__ void __launch_bounds__(APPEND_THREADS) k_append_write(Geo g, Gen gen,
             } else {
                 int ci = clamp_cell((int)lc[0], g.ni), cj = clamp_cell((int)lc[1], g.nj),
                     ck = clamp_cell((int)lc[2], g.nk);
+                const float fx = (float)(lc[0] - ci), fy = (float)(lc[1] - cj), fz = (float)(lc[2] - ck);
+                float wc[8];
+                cic_w(fx, fy, fz, wc);
+                const int64_t sy = g.ni, sz = (int64_t)g.ni * g.nj;
+                const float4 *E0 = ef4 + node_of(g, ci, cj, ck);
+                const float4 e[8] = {__ldg(E0),      __ldg(E0 + 1),      __ldg(E0 + 1 + sy),      __ldg(E0 + sy),
+                                     __ldg(E0 + sz), __ldg(E0 + 1 + sz), __ldg(E0 + 1 + sy + sz), __ldg(E0 + sy + sz)};
+                const float3 E = gather_corners(wc, e);
                 cell[dst] = ci | (cj << 10) | (ck << 20);
-                off[dst] = (float)(lc[0] - ci);
-                off[stride + dst] = (float)(lc[1] - cj);
-                off[2 * stride + dst] = (float)(lc[2] - ck);
-                for (int d = 0; d < 3; d++) vel[d * stride + dst] = (float)v[d];
+                off[dst] = fx;
+                off[stride + dst] = fy;
+                off[2 * stride + dst] = fz;
+                vel[dst] = __fmaf_rn(-E.x, qmdt2, (float)v[0]);
+                vel[stride + dst] = __fmaf_rn(-E.y, qmdt2, (float)v[1]);
+                vel[2 * stride + dst] = __fmaf_rn(-E.z, qmdt2, (float)v[2]);
             }
         }
     }
 }
 
 /* ------------------------------------------------------------------------ */
-/* a / b correctly rounded, given y = RN(1/b) for b > 0: q = a y, the exact
- * remainder r = a - b q (one FMA), then q + r y rounded -- Markstein's
- * correction (P. Markstein, IBM J. Res. Develop. 34(1), 1990), which yields
- * the correctly rounded quotient for normal operands, so results equal the
- * division's bit for bit; a = +-0 returns a y, the zero of the right sign.
- * Three float64 operations instead of a division: the GB300's float64 rate
- * makes the division dominate the kernels below. */
-__device__ __forceinline__ double div_rcp(double a, double b, double y) {
-    const double q = a * y;
-    const double r = __fma_rn(-q, b, a);
-    const double q2 = __fma_rn(r, y, q);
-    /* a == +-0 tested on the bits: an integer compare keeps the narrow
-     * float64 pipe for the arithmetic */
-    return zero_bits(a) ? q : q2;
-}
 
 /* PotentialSolver::computeEF: 2nd-order one-sided differences on the faces,
  * central inside.  Also writes the float32 copy used by the mixed push. */
@@ -1477,19 +1503,26 @@ static void append(World &w, Species &s, const Gen &gen, int64_t ncand, int writ
         }
     }
     double qm = s.charge / s.mass;
-    /* a beam's particles start at z = x0, where the float64 field is always
-     * current; any other generator needs all of it */
-    if (!std::is_same<Gen, GenBeam>::value) ensure_ef64(w);
+    const double3 rdh = make_double3(1.0 / w.g.dh[0], 1.0 / w.g.dh[1], 1.0 / w.g.dh[2]);
+    const float qmdt2 = (float)(qm * (0.5 * w.dt));
+    /* the mixed form rewinds with the float copy of E; in the float64 form a
+     * beam's particles start at z = x0, where the float64 field is always
+     * current, and any other generator needs all of it */
+    if (s.form != 0) {
+        if (!w.ef4_valid) launch_ef4(w);
+    } else if (!std::is_same<Gen, GenBeam>::value) {
+        ensure_ef64(w);
+    }
     k_append_count<Gen><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(w.g, gen, ncand, w.d_blockcnt);
     k_append_scan<<<1, 1024, 0, w.stream>>>(w.d_blockcnt, blocks, s.d_count, s.cap, w.d_err);
     if (s.form == 0)
         k_append_write<Gen, 0><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(
-            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, s.P, nullptr, nullptr, nullptr, s.cap, s.cap,
-            write_w);
+            w.g, rdh, gen, ncand, w.d_blockcnt, s.d_count, w.ef, nullptr, qm, w.dt, qmdt2, s.P, nullptr, nullptr,
+            nullptr, s.cap, s.cap, write_w);
     else
         k_append_write<Gen, 1><<<(unsigned)blocks, APPEND_THREADS, 0, w.stream>>>(
-            w.g, gen, ncand, w.d_blockcnt, s.d_count, w.ef, qm, w.dt, nullptr, s.cell, s.off, s.vel, s.ms, s.cap,
-            0);
+            w.g, rdh, gen, ncand, w.d_blockcnt, s.d_count, w.ef, w.ef4, qm, w.dt, qmdt2, nullptr, s.cell, s.off,
+            s.vel, s.ms, s.cap, 0);
     w.nlaunch += 3;
     s.host_bound += ncand;
     if (s.host_bound > s.cap) s.host_bound = s.cap;
@@ -2073,14 +2106,6 @@ __device__ __forceinline__ void corner_weights(double di, double dj, double dk, 
     W[5] = a1 * dk;
     W[6] = a2 * dk;
     W[7] = a3 * dk;
-}
-
-/* x to logical coordinates with the correctly rounded reciprocal of dh:
- * equal to World::XtoL's division bit for bit (div_rcp) */
-__device__ __forceinline__ void xtol_rcp(const Geo &g, double3 rdh, const double x[3], double lc[3]) {
-    lc[0] = div_rcp(x[0] - g.x0[0], g.dh[0], rdh.x);
-    lc[1] = div_rcp(x[1] - g.x0[1], g.dh[1], rdh.y);
-    lc[2] = div_rcp(x[2] - g.x0[2], g.dh[2], rdh.z);
 }
 
 /* each sum's 8 corner contributions value * W_m, rounded once (from the exact

@@ -44,18 +44,6 @@ __device__ __forceinline__ void unpack(int32_t key, int &i, int &j, int &k) {
     k = key >> 20;
 }
 
-__device__ __forceinline__ void cic_w(float fx, float fy, float fz, float w[8]) {
-    float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
-    w[0] = gx * gy * gz;
-    w[1] = fx * gy * gz;
-    w[2] = fx * fy * gz;
-    w[3] = gx * fy * gz;
-    w[4] = gx * gy * fz;
-    w[5] = fx * gy * fz;
-    w[6] = fx * fy * fz;
-    w[7] = gx * fy * fz;
-}
-
 /* move a coordinate by v*dtdh cells (one fused multiply-add): returns the
  * new cell index, f stays in [0,1) */
 __device__ __forceinline__ int advance_axis(int i, float &f, float v, float dtdh) {
@@ -68,19 +56,6 @@ __device__ __forceinline__ int advance_axis(int i, float &f, float v, float dtdh
         i += 1;
     }
     return i;
-}
-
-/* trilinear E at the particle: a chain of fused multiply-adds over the
- * corners in Field_::gather's order (ch2/Field.h:186-208), from corner 0 */
-__device__ __forceinline__ float3 gather_corners(const float w[8], const float4 e[8]) {
-    float3 r = make_float3(__fmul_rn(w[0], e[0].x), __fmul_rn(w[0], e[0].y), __fmul_rn(w[0], e[0].z));
-#pragma unroll
-    for (int c = 1; c < 8; c++) {
-        r.x = __fmaf_rn(w[c], e[c].x, r.x);
-        r.y = __fmaf_rn(w[c], e[c].y, r.y);
-        r.z = __fmaf_rn(w[c], e[c].z, r.z);
-    }
-    return r;
 }
 
 __device__ __forceinline__ void reflect_axis(int &i, float &f, float &v, int n) {
