@@ -6,14 +6,14 @@ Workload (default, configuration 5): flow past a sphere on a
 warm beam (7 km/s drift, T_i = 0.1 eV, n0 = 1e10 m^-3) with mpw0 = 0.32 so
 that about 480M macroparticles fill the domain (~14.5 per cell); Boltzmann
 electrons (n0 = 1e10, Te = 3 eV, phi0 = 0); dt = 1e-7 s; Newton-PCG to RMS
-update 1e-6 V; tile sort every 20 steps.  The reference has no published
+update 1e-6 V; tile sort every 10 steps.  The reference has no published
 dataset: the run starts from a synthetic steady-state stand-in, 500M ions
 loaded on the GPU uniformly over the domain with the beam's drifting
 thermal velocities (seeded; those inside the sphere are absorbed by the
 first push), followed by an initial solve.  --config sphere64 is the
 reference's configuration 2 (64x64x128 nodes, ~4M ions, mpw0 = 40).
 
-A step = inject + push/deposit (+ sort every 20) + charge density + Newton-PCG
+A step = inject + push/deposit (+ the sort every 10) + charge density + Newton-PCG
 + computeEF.  value = particle-steps/s of the mixed form (int32 cell + f32
 offset + f32 velocity; float PCG under a Newton residual in double-float,
 pairs of floats with ~48 significant bits), timed with
@@ -55,7 +55,7 @@ CONFIGS = {
     "sphere64": dict(n=(64, 64, 128), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
                      radius=0.05, phi_s=-100.0, np=4_000_000, mpw0=40.0, dt=1e-7, sort_every=20),
     "sphere256": dict(n=(256, 256, 512), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
-                      radius=0.04, phi_s=-100.0, np=500_000_000, mpw0=0.32, dt=1e-7, sort_every=20),
+                      radius=0.04, phi_s=-100.0, np=500_000_000, mpw0=0.32, dt=1e-7, sort_every=10),
     # the 256x256x512 plasma on an eighth of the cells (the same ions per
     # cell): small enough for a full ncu capture of the push at that density
     "sphere128": dict(n=(128, 128, 256), x0=(-0.1, -0.1, 0.0), xm=(0.1, 0.1, 0.4), center=(0, 0, 0.15),
