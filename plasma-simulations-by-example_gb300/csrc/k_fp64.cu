@@ -719,8 +719,9 @@ __global__ void __launch_bounds__(256) k_efield(Geo g, double3 y2, const double 
  * from a float rounding boundary.  The faces, and the rare interior node
  * with a component near a boundary or outside the double-float range, take
  * ef_node_exact.  The float64 field is written on the planes k < 2 alone,
- * the ones a beam source's addParticle gathers at (its particles start at
- * z = x0); the rest of it is completed on demand by k_efield from phi_ef,
+ * the ones a float64-form beam source's addParticle gathers at (its
+ * particles start at z = x0; the mixed form's gathers from ef4); the rest
+ * of it is completed on demand by k_efield from phi_ef,
  * the copy of phi this kernel reads (the solver changes phi before the
  * field is next computed, and the reference's ef stays that of the last
  * computeEF).  World::getPE's sum of |E|^2 vol over the nodes rides along
