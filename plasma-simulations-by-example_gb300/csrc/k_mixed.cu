@@ -796,35 +796,55 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const int32_t *__restrict_
 /* The whole particle in one pass: q's source index p = perm[q] is read
  * once, then the key and the six float rows are gathered from p and written
  * at q (offsets and velocities to the second set of arrays, the key over
- * perm in place: each thread reads its slot before writing it).  An index
+ * perm in place: each thread reads its slots before writing them).  An index
  * outside the species, which the histogram and scatter cannot produce, is
- * flagged, not read. */
-__global__ void __launch_bounds__(256) k_sort_gather_all(const int32_t *__restrict__ cell,
-                                                         const float *__restrict__ off,
-                                                         const float *__restrict__ vel, int64_t stride,
-                                                         const int64_t *__restrict__ d_count, int32_t *perm_key,
-                                                         float *off2, float *vel2, int *err) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+ * flagged, not read.  A block takes 4096 consecutive slots (four per
+ * thread, one block per SM): the thermal spread sends the ions of a source
+ * sector to cells a few slots apart, so a block that holds a long run of
+ * slots finds most sector-mates of its sources still in the SM's L1. */
+constexpr int GATHER_THREADS = 1024, GATHER_PER = 4; /* one block of 4096 slots per SM at a time */
+
+__global__ void __launch_bounds__(GATHER_THREADS, 1) k_sort_gather_all(const int32_t *__restrict__ cell,
+                                                                       const float *__restrict__ off,
+                                                                       const float *__restrict__ vel, int64_t stride,
+                                                                       const int64_t *__restrict__ d_count,
+                                                                       int32_t *perm_key, float *off2, float *vel2,
+                                                                       int *err) {
     const int64_t n = d_count[0];
-    if (q >= n) return;
-    const int64_t p = perm_key[q];
-    if (p < 0 || p >= n) {
-        atomicOr(err, DERR_SORT);
-        return;
-    }
-    const int32_t key = cell[p];
-    float v[6];
+    const int64_t q0 = (int64_t)blockIdx.x * (GATHER_THREADS * GATHER_PER) + threadIdx.x;
+    int64_t p[GATHER_PER];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        v[d] = off[d * stride + p];
-        v[3 + d] = vel[d * stride + p];
+    for (int h = 0; h < GATHER_PER; h++) {
+        const int64_t q = q0 + h * GATHER_THREADS;
+        p[h] = q < n ? perm_key[q] : -1;
+        if (q < n && (p[h] < 0 || p[h] >= n)) {
+            atomicOr(err, DERR_SORT);
+            p[h] = -1;
+        }
+    }
+    int32_t key[GATHER_PER];
+    float v[GATHER_PER][6];
+#pragma unroll
+    for (int h = 0; h < GATHER_PER; h++) {
+        if (p[h] < 0) continue;
+        key[h] = cell[p[h]];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            v[h][d] = off[d * stride + p[h]];
+            v[h][3 + d] = vel[d * stride + p[h]];
+        }
     }
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        off2[d * stride + q] = v[d];
-        vel2[d * stride + q] = v[3 + d];
+    for (int h = 0; h < GATHER_PER; h++) {
+        if (p[h] < 0) continue;
+        const int64_t q = q0 + h * GATHER_THREADS;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            off2[d * stride + q] = v[h][d];
+            vel2[d * stride + q] = v[h][3 + d];
+        }
+        perm_key[q] = key[h];
     }
-    perm_key[q] = key;
 }
 
 /* Per block: count, sum v and sum |v|^2 of a mixed species.  Each thread
@@ -1027,8 +1047,13 @@ void launch_sort_mixed(World &w, Species &s) {
     k_scan_down<<<(unsigned)nb, 1024, 0, w.stream>>>(counts, ncells, bsum);
     k_tile_seg<<<blocks_for(ntiles + 1, 256), 256, 0, w.stream>>>(counts, ntiles, s.d_count, s.seg);
     k_sort_scatter<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.d_count, ntx, nty, counts, s.cell2);
-    k_sort_gather_all<<<blocks_for(n, 256), 256, 0, w.stream>>>(s.cell, s.off, s.vel, s.ms, s.d_count, s.cell2,
-                                                                 s.off2, s.vel2, w.d_err);
+    static bool carveout = false;
+    if (!carveout) { /* no shared memory: the whole of it as L1 */
+        cudaFuncSetAttribute(k_sort_gather_all, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        carveout = true;
+    }
+    k_sort_gather_all<<<blocks_for(n, GATHER_THREADS * GATHER_PER), GATHER_THREADS, 0, w.stream>>>(
+        s.cell, s.off, s.vel, s.ms, s.d_count, s.cell2, s.off2, s.vel2, w.d_err);
     w.nlaunch += 7;
     s.tiled = true;
     int32_t *tc = s.cell;
