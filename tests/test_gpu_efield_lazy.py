@@ -10,7 +10,8 @@ completed on demand, and World::getPE from the same pass.
 * The float64 field read back equals the oracle's computeEF of that
   potential bit for bit, also after the potential was overwritten (the
   reference's ef stays that of the last computeEF).
-* getPE agrees with the oracle within 1e-13.
+* getPE agrees with the oracle within 1e-13, also on thin grids where most
+  of the kernel's threads take face columns.
 """
 import numpy as np
 import pytest
@@ -147,3 +148,25 @@ def test_efield_after_a_solve_matches_float64(espic, po):
     pe_o = po.potential_energy(g, ef_o, po.node_volumes(g))
     assert abs(pe_pairs - pe_o) <= 1e-13 * abs(pe_o)
     assert abs(pe_full - pe_o) <= 1e-13 * abs(pe_o)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [(3, 3, 6), (4, 5, 9), (5, 3, 11), (70, 3, 10)])
+def test_thin_grids(espic, po, n):
+    """k_efield4 on grids with few interior columns (its threads take the
+    interior columns first and the face columns after them): getPE equals
+    the oracle's within 1e-13 and the float64 field read back is the
+    oracle's computeEF bit for bit"""
+    rng = np.random.default_rng(sum(n))
+    with espic.World(*n, X0, XM) as w:
+        espic.Species(w, "O+", 16 * AMU, QE, mpw0=1e3, capacity=64, form=espic.FORM_MIXED)
+        phi = rng.standard_normal(int(np.prod(n)))
+        w.write(espic.FIELD_PHI, phi)
+        espic.check(espic.lib().espic_efield(w.h))
+        pe = w.getPE()
+        ef = w.read(espic.FIELD_EF).copy()
+    g = po.grid(list(n), list(X0), list(XM))
+    ef_o = po.efield(g, phi).reshape(-1, 3)
+    assert np.array_equal(ef.reshape(-1, 3), ef_o)
+    pe_o = po.potential_energy(g, ef_o, po.node_volumes(g))
+    assert abs(pe - pe_o) <= 1e-13 * abs(pe_o)
