@@ -230,6 +230,26 @@ def timed_steps(E, torch, w, cfg, steps, warmup, flush):
                 solves=s1[0] - s0[0], newton=s1[1] - s0[1], inner=s1[2] - s0[2])
 
 
+def deposit_alone(E, torch, w, s, reps=3):
+    """The deposit outside the fused push: espic_deposit on the current ions
+    (the accumulator cleared, k_deposit_mixed, k_density), CUDA events on the
+    library's stream, after one untimed call.  The ions do not move, so the
+    density it leaves is the one the step's fused deposit left."""
+    stream = torch.cuda.ExternalStream(w.stream_handle())
+    s.computeNumberDensity()
+    w.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in ev:
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        s.computeNumberDensity()
+        with torch.cuda.stream(stream):
+            b.record(stream)
+    torch.cuda.synchronize()
+    w.sync()
+    return float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+
 def profiled_steps(E, w, cfg, steps):
     w.profile(True)
     for _ in range(steps):
@@ -1134,6 +1154,7 @@ def main():
     t = timed_steps(E, torch, w, cfg, args.steps, args.warmup, flush)
     ck = clocks.stop()
     ms_step, value, _ = aggregate(float(np.sum(t["ms"])) / args.steps, t["n"], dist, "cuda")
+    dep_ms = deposit_alone(E, torch, w, s)
     # one whole sort period, so the sort's share of a step is in the table
     phases, counts = profiled_steps(E, w, cfg, cfg["sort_every"] or max(3, min(args.steps, 10)))
     snap = {"den": s.den, "phi": w.phi.copy(), "ef": w.ef}
@@ -1211,6 +1232,16 @@ def main():
                           "traffic": push_traffic},
         "clocks": ck,
     }
+    # the step fuses the deposit into the push; alone, on the same ions: the
+    # key and offsets read (16 B an ion), the accumulator cleared, read, and
+    # turned into den with the node volumes (40 B a node)
+    nn_all = int(np.prod(cfg["n"]))
+    dep_bytes = 16.0 * t["n"] + 40.0 * nn_all
+    dep_gbs = dep_bytes / (dep_ms * 1e-3) / 1e9
+    line["roofline_deposit"] = {"bound": "hbm", "kernel": "k_deposit_mixed (espic_deposit: the clear, the deposit, "
+                                "k_density)", "achieved": dep_gbs, "peak": hbm, "unit": "GB/s",
+                                "frac": dep_gbs / hbm, "ms": dep_ms, "bytes_per_particle": 16,
+                                "bytes_per_node": 40}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         if big:
