@@ -1238,8 +1238,9 @@ def main():
     nn_all = int(np.prod(cfg["n"]))
     dep_bytes = 16.0 * t["n"] + 40.0 * nn_all
     dep_gbs = dep_bytes / (dep_ms * 1e-3) / 1e9
-    line["roofline_deposit"] = {"bound": "hbm", "kernel": "k_deposit_mixed (espic_deposit: the clear, the deposit, "
-                                "k_density)", "achieved": dep_gbs, "peak": hbm, "unit": "GB/s",
+    line["roofline_deposit"] = {"bound": "hbm", "kernel": "k_deposit_tiles (espic_deposit: the clear, "
+                                "k_deposit_tiles and k_deposit_tail, k_density)", "achieved": dep_gbs, "peak": hbm,
+                                "unit": "GB/s",
                                 "frac": dep_gbs / hbm, "ms": dep_ms, "bytes_per_particle": 16,
                                 "bytes_per_node": 40}
     if rank == 0 and not args.no_cpu:

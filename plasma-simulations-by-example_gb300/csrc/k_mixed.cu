@@ -452,6 +452,106 @@ __global__ void __launch_bounds__(256, 4) k_push_tiles(MixArgs a, const float4 *
     }
 }
 
+/* The deposit alone over tile segments (Species::computeNumberDensity of
+ * a sorted mixed species whose push did not deposit): one block per tile
+ * segment, the 2^-23 fixed-point corner weights of deposit_block summed in
+ * a shared TBW^3-node box placed as k_push_tiles places it (the per-axis
+ * median cell of 32 keys of the segment), ions outside the box through
+ * global atomics, the box added to the grid once.  The integer sums equal
+ * those of k_deposit_mixed bit for bit. */
+__global__ void __launch_bounds__(256) k_deposit_tiles(MixArgs a, const int32_t *__restrict__ cell,
+                                                       const float *__restrict__ off, int64_t stride,
+                                                       const int32_t *__restrict__ seg,
+                                                       const int64_t *__restrict__ d_count,
+                                                       unsigned long long *acc) {
+    constexpr int BV = TBW * TBW * TBW;
+    __shared__ unsigned int sD[BV];
+    __shared__ int s_lo[3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int64_t n = d_count[0];
+    const int p0 = seg[blockIdx.x];
+    const int p1 = (int)min((int64_t)seg[blockIdx.x + 1], n);
+    if (p1 <= p0) return; /* block-uniform */
+    if (warp == 0) {
+        const int q = p0 + (int)(((int64_t)(p1 - p0) * lane) >> 5);
+        int i, j, k;
+        unpack(cell[q], i, j, k);
+        const int c[3] = {warp_median(i), warp_median(j), warp_median(k)};
+        const int ncell[3] = {a.ni - 1, a.nj - 1, a.nk - 1};
+        if (lane < 3) {
+            int lo = c[lane] - (TBW - 1) / 2;
+            if (lo > ncell[lane] - (TBW - 1)) lo = ncell[lane] - (TBW - 1);
+            if (lo < 0) lo = 0;
+            s_lo[lane] = lo;
+        }
+    }
+    for (int t = threadIdx.x; t < BV; t += blockDim.x) sD[t] = 0u;
+    __syncthreads();
+    const int li = s_lo[0], lj = s_lo[1], lk = s_lo[2];
+    const int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+        int i, j, k;
+        unpack(cell[p], i, j, k);
+        float w[8];
+        cic_w(off[p], off[stride + p], off[2 * stride + p], w);
+        const int bi = i - li, bj = j - lj, bk = k - lk;
+        if ((unsigned)bi < TBW - 1 && (unsigned)bj < TBW - 1 && (unsigned)bk < TBW - 1) {
+            const int L = (bk * TBW + bj) * TBW + bi;
+            const int idx[8] = {L,           L + 1,           L + 1 + TBW,           L + TBW,
+                                L + TBW * TBW, L + 1 + TBW * TBW, L + 1 + TBW + TBW * TBW, L + TBW + TBW * TBW};
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                if (q) atomicAdd(&sD[idx[c]], q);
+            }
+        } else {
+            const int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+            const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                    n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+                if (q) atomicAdd(acc + idx[c], (unsigned long long)q);
+            }
+        }
+    }
+    __syncthreads();
+    for (int r = warp; r < TBW * TBW; r += nwarps) {
+        const int tk = r / TBW, tj = r - tk * TBW;
+        unsigned long long *dst = acc + ((int64_t)(lk + tk) * sz + (int64_t)(lj + tj) * sy + li);
+        for (int ti = lane; ti < TBW; ti += 32) {
+            const unsigned v = sD[r * TBW + ti];
+            if (v) atomicAdd(dst + ti, (unsigned long long)v);
+        }
+    }
+}
+
+/* the deposit alone of the particles appended since the sort: [first, n),
+ * grid-stride, global atomics */
+__global__ void __launch_bounds__(256) k_deposit_tail(MixArgs a, const int32_t *__restrict__ cell,
+                                                      const float *__restrict__ off, int64_t stride,
+                                                      const int32_t *__restrict__ first,
+                                                      const int64_t *__restrict__ d_count,
+                                                      unsigned long long *acc) {
+    const int64_t n = d_count[0];
+    const int64_t sy = a.ni, sz = (int64_t)a.ni * a.nj;
+    for (int64_t p = first[0] + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        unpack(cell[p], i, j, k);
+        float w[8];
+        cic_w(off[p], off[stride + p], off[2 * stride + p], w);
+        const int64_t n0 = ((int64_t)k * a.nj + j) * a.ni + i;
+        const int64_t idx[8] = {n0,      n0 + 1,      n0 + 1 + sy,      n0 + sy,
+                                n0 + sz, n0 + 1 + sz, n0 + 1 + sy + sz, n0 + sy + sz};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const unsigned q = __float2uint_rn(w[c] * MIX_Q);
+            if (q) atomicAdd(acc + idx[c], (unsigned long long)q);
+        }
+    }
+}
+
 /* particles appended since the sort: [seg[ntiles], n), grid-stride, the
  * particle step of push_particle_mixed and global-atomic deposits */
 template <int WALLS, bool DEPOSIT>
@@ -1000,6 +1100,14 @@ void launch_deposit_mixed(World &w, Species &s) {
     int64_t n = s.host_bound;
     if (n <= 0) return;
     MixArgs a = mix_args(w, s);
+    if (tiles_usable(w, s)) {
+        const int64_t ntiles = (int64_t)tile_count(w.g.ni - 1) * tile_count(w.g.nj - 1) * tile_count(w.g.nk - 1);
+        k_deposit_tiles<<<(unsigned)ntiles, 256, 0, w.stream>>>(a, s.cell, s.off, s.ms, s.seg, s.d_count, s.acc);
+        k_deposit_tail<<<2 * w.sm_count, 256, 0, w.stream>>>(a, s.cell, s.off, s.ms, s.seg + ntiles, s.d_count,
+                                                             s.acc);
+        w.nlaunch += 2;
+        return;
+    }
     k_deposit_mixed<<<blocks_for(n, 256), 256, 0, w.stream>>>(a, s.cell, s.off, s.ms, s.d_count, s.acc);
     w.nlaunch++;
 }
