@@ -1211,10 +1211,40 @@ __global__ void k_dsum_final(const double *__restrict__ dsum, int64_t nb, const 
     }
 }
 
+/* first stage of the row's sums: block b adds its contiguous range of the
+ * push's block sums (threads strided, then the warps in order), so that the
+ * final kernel adds DSUM_PARTS partials instead of one per tile */
+constexpr int DSUM_PARTS = 64;
+
+__global__ void __launch_bounds__(256) k_dsum_part(const double *__restrict__ dsum, int64_t nb, double *part) {
+    __shared__ double ws[8][4];
+    const int64_t per = (nb + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = (int64_t)blockIdx.x * per, b1 = b0 + per < nb ? b0 + per : nb;
+    double t[4] = {0, 0, 0, 0};
+    for (int64_t b = b0 + threadIdx.x; b < b1; b += blockDim.x)
+        for (int q = 0; q < 4; q++) t[q] += dsum[4 * b + q];
+    for (int q = 0; q < 4; q++)
+        for (int o = 16; o > 0; o >>= 1) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 4; q++) ws[threadIdx.x >> 5][q] = t[q];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double r = 0;
+        for (int w8 = 0; w8 < (int)(blockDim.x >> 5); w8++) r += ws[w8][threadIdx.x];
+        part[4 * (int64_t)blockIdx.x + threadIdx.x] = r;
+    }
+}
+
 void launch_diag_mixed(World &w, Species &s, double *d_out5) {
     if (s.dsum_valid) { /* the sums the last push left (no particle has changed since) */
-        k_dsum_final<<<1, 1024, 0, w.stream>>>(s.dsum, s.dsum_n, s.d_count, s.mass, s.mpw0, d_out5);
-        w.nlaunch++;
+        if (s.dsum_n > 4 * DSUM_PARTS && w.partial_slots >= 4 * DSUM_PARTS) {
+            k_dsum_part<<<DSUM_PARTS, 256, 0, w.stream>>>(s.dsum, s.dsum_n, w.d_partials);
+            k_dsum_final<<<1, 1024, 0, w.stream>>>(w.d_partials, DSUM_PARTS, s.d_count, s.mass, s.mpw0, d_out5);
+            w.nlaunch += 2;
+        } else {
+            k_dsum_final<<<1, 1024, 0, w.stream>>>(s.dsum, s.dsum_n, s.d_count, s.mass, s.mpw0, d_out5);
+            w.nlaunch++;
+        }
         return;
     }
     /* eight blocks of 256 per SM, within the partials buffer (5 per block) */
