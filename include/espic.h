@@ -205,9 +205,11 @@ int espic_solver_set_multigrid(espic_world *w, int levels, double scale);
 int espic_solver_set_launch(espic_world *w, int max_blocks);
 /* Newton predictor (default on): when exactly one charge density was
  * computed since the last solve (consecutive steps), the Newton-PCG solve
- * starts from 2 phi^n - phi^(n-1) on the unknowns instead of phi^n; the
- * converged solution and its test are unchanged.  No reference counterpart
- * (the reference starts from phi^n). */
+ * starts on the unknowns from 2 phi^n - phi^(n-1) instead of phi^n, and the
+ * float-inner solve, once the solve before was consecutive too, from
+ * 3 phi^n - 3 phi^(n-1) + phi^(n-2); the converged solution and its test
+ * are unchanged.  No reference counterpart (the reference starts from
+ * phi^n). */
 int espic_solver_set_predictor(espic_world *w, int enable);
 /* The reference's fallback when the inner linear PCG fails
  * (ch3/ver2/PotentialSolver.cpp:270-271): Gauss-Seidel with omega 1

@@ -695,7 +695,9 @@ class PotentialSolver:
         return bool(a.value), b.value, c.value, d.value, r.value
 
     def setPredictor(self, enable=True):
-        """Start Newton solves of consecutive steps from 2 phi^n - phi^(n-1)."""
+        """Start Newton solves of consecutive steps from 2 phi^n - phi^(n-1)
+        (the float-inner solve, after three consecutive solves, from
+        3 phi^n - 3 phi^(n-1) + phi^(n-2))."""
         check(lib().espic_solver_set_predictor(self.world.h, 1 if enable else 0))
 
     def setCoarse(self, block_nodes):
