@@ -276,3 +276,31 @@ def test_tile_segment_push_matches_oracle_over_steps(espic, po, walls):
             dead_total += int(dead.sum())
         if walls == "absorb":
             assert dead_total > 0
+
+
+def test_tile_deposit_with_appended_ions(espic):
+    """computeNumberDensity of a tile-sorted species whose ions were pushed
+    and then joined by injected ions (the tile segments plus the appended
+    tail): the same integer charge as the per-ion deposit of the same ions
+    in a species that was never sorted"""
+    geo = SPH
+    P = state(geo, 200_000, 11)
+    w, s = make(espic, geo, P, espic.WALLS_ABSORB, True)
+    with w:
+        # n v A dt / mpw0 = 4e9 * 7000 * 0.04 * 1e-7 / 40 = 2800 ions a
+        # sample, within the 4096 spare slots
+        src = espic.BeamSource(s, 7000.0, 4e9)
+        s.advance(deposit=False)
+        n_pushed = s.getNp()
+        src.sample()
+        cell, off, vel = s.get_mixed()
+        assert cell.size > n_pushed + 2000  # the injected tail is there
+        s.computeNumberDensity()
+        tiled = s.den
+    w2, s2 = make(espic, geo, P, espic.WALLS_ABSORB, False)
+    with w2:
+        s2.set_mixed(cell, off, vel)
+        s2.computeNumberDensity()
+        plain = s2.den
+    assert np.array_equal(tiled, plain)
+    assert np.sum(tiled) > 0
